@@ -1,0 +1,237 @@
+/*
+ * msplat_gb300.h -- C ABI of the GB300 (sm_103a) Gaussian-splatting rasteriser.
+ *
+ * Every entry point takes plain device pointers, sizes and a CUDA stream, and
+ * returns an msplat_status (0 = ok).  Nothing here allocates device memory:
+ * outputs and scratch ("workspace") are owned by the caller.  Work is only
+ * enqueued on `stream`; no function synchronises the host with the device.
+ *
+ * Each declaration names the reference interface it replaces
+ * (pointrix-project/msplat, paths relative to that project).  The reference
+ * exports these as a pybind11 module `msplat._C` (msplat/src/ext.cpp:13-26);
+ * here they are `extern "C"` so ctypes / cgo / JNI can bind them directly.
+ *
+ * Conventions shared by all entry points
+ *   - float tensors are fp32, contiguous, in the reference's layouts:
+ *     xyz [P,3], uv [P,2], depth [P], scales [P,3], uquats [P,4] (r,x,y,z),
+ *     cov3d [P,6] (upper triangle), conic [P,3], radius/tiles [P] int32,
+ *     intr [4] = (fx,fy,cx,cy), extr [3,4] (or the first 12 floats of [4,4])
+ *     row-major world-to-camera [R|t].
+ *   - `visible` is a bool (1 byte) mask [P]; NULL means "all visible".
+ *   - Tiles are 16x16 pixels; the tile grid is ceil(W/16) x ceil(H/16).
+ *   - Outputs are fully written (elements the reference leaves at zero are
+ *     written as zero), so callers may pass uninitialised buffers, except
+ *     where a comment says "accumulated".
+ */
+#ifndef MSPLAT_GB300_H
+#define MSPLAT_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(_WIN32)
+#define MSPLAT_API __declspec(dllexport)
+#else
+#define MSPLAT_API __attribute__((visibility("default")))
+#endif
+
+typedef struct CUstream_st *msplat_stream_t; /* == cudaStream_t */
+
+typedef enum {
+    MSPLAT_OK = 0,
+    MSPLAT_ERR_INVALID_ARGUMENT = 1, /* null pointer, negative size, bad shape */
+    MSPLAT_ERR_WORKSPACE = 2,        /* workspace too small or misaligned */
+    MSPLAT_ERR_LAUNCH = 3,           /* a kernel launch failed */
+    MSPLAT_ERR_CAPACITY = 4,         /* more intersections than int32 / capacity */
+    MSPLAT_ERR_UNSUPPORTED = 5,      /* e.g. SH degree > 10 */
+    MSPLAT_ERR_TIMEOUT = 6           /* a bounded device-side wait gave up */
+} msplat_status;
+
+/* Human-readable text for a status, and the detail message of the last
+ * failing call on this host thread. */
+MSPLAT_API const char *msplat_status_string(int status);
+MSPLAT_API const char *msplat_last_error(void);
+/* Library version, e.g. "0.1.0". */
+MSPLAT_API const char *msplat_version(void);
+
+/* ------------------------------------------------------------------------ */
+/* Projection: replaces projectPointsForward / projectPointsBackward
+ * (msplat/src/project_point.cu:147-179, :181-228; bound as
+ * _C.project_point_forward / _C.project_point_backward, ext.cpp:14-15).
+ * uv = (fx*tx/tz + cx - 0.5, fy*ty/tz + cy - 0.5), depth = tz with
+ * t = R*xyz + T.  Culled points (near / extent) get uv = 0, depth = 0.    */
+MSPLAT_API int msplat_project_point_forward(int P, const float *xyz, const float *intr,
+                                 const float *extr, int W, int H,
+                                 float nearest, float extent, float *uv,
+                                 float *depth, msplat_stream_t stream);
+
+/* Scratch needed by the backward passes that reduce camera gradients. */
+MSPLAT_API size_t msplat_camera_grad_workspace_size(int P);
+
+/* dL_dxyz is written.  dL_dintr [4] / dL_dextr [12] may be NULL (the
+ * reference skips them when intr/extr do not require grad); when given they
+ * are written (not accumulated), reduced in a fixed order (deterministic). */
+MSPLAT_API int msplat_project_point_backward(int P, const float *xyz, const float *intr,
+                                  const float *extr, int W, int H,
+                                  const float *uv, const float *depth,
+                                  const float *dL_duv, const float *dL_ddepth,
+                                  float *dL_dxyz, float *dL_dintr,
+                                  float *dL_dextr, void *workspace,
+                                  size_t workspace_bytes,
+                                  msplat_stream_t stream);
+
+/* ------------------------------------------------------------------------ */
+/* 3-D covariance: replaces computeCov3DForward / computeCov3DBackward
+ * (msplat/src/compute_cov3d.cu:149-170, :172-200; ext.cpp:16-17).
+ * Sigma = (S R)^T (S R) as [s00,s01,s02,s11,s12,s22].                      */
+MSPLAT_API int msplat_compute_cov3d_forward(int P, const float *scales,
+                                 const float *uquats, const uint8_t *visible,
+                                 float *cov3d, msplat_stream_t stream);
+MSPLAT_API int msplat_compute_cov3d_backward(int P, const float *scales,
+                                  const float *uquats, const uint8_t *visible,
+                                  const float *dL_dcov3d, float *dL_dscales,
+                                  float *dL_duquats, msplat_stream_t stream);
+
+/* ------------------------------------------------------------------------ */
+/* EWA splatting: replaces EWAProjectForward / EWAProjectBackward
+ * (msplat/src/ewa_project.cu:254-297, :299-345; ext.cpp:18-19).
+ * conic [P,3], radius [P], tiles [P] (tiles touched in the 16x16 grid).    */
+MSPLAT_API int msplat_ewa_project_forward(int P, const float *xyz, const float *cov3d,
+                               const float *intr, const float *extr,
+                               const float *uv, int W, int H,
+                               const uint8_t *visible, float *conic,
+                               int32_t *radius, int32_t *tiles,
+                               msplat_stream_t stream);
+MSPLAT_API int msplat_ewa_project_backward(int P, const float *xyz, const float *cov3d,
+                                const float *intr, const float *extr,
+                                const int32_t *radius, const float *dL_dconic,
+                                float *dL_dxyz, float *dL_dcov3d,
+                                float *dL_dintr, float *dL_dextr,
+                                void *workspace, size_t workspace_bytes,
+                                msplat_stream_t stream);
+
+/* ------------------------------------------------------------------------ */
+/* Spherical harmonics, degrees 0..10 (D = (deg+1)^2 <= 121): replaces
+ * computeSHForward / computeSHBackward (msplat/src/compute_sh.cu:1696-1753;
+ * ext.cpp:22-23).  shs [P,C,D] channel-major, dirs [P,3], value [P,C].     */
+MSPLAT_API int msplat_compute_sh_forward(int P, int C, int D, const float *shs,
+                              const float *dirs, const uint8_t *visible,
+                              float *value, msplat_stream_t stream);
+MSPLAT_API int msplat_compute_sh_backward(int P, int C, int D, const float *shs,
+                               const float *dirs, const uint8_t *visible,
+                               const float *dL_dvalue, float *dL_dshs,
+                               float *dL_ddirs, msplat_stream_t stream);
+
+/* ------------------------------------------------------------------------ */
+/* Sorting.  The reference sorts with torch.cumsum + its key kernel +
+ * torch.sort + torch.gather + its range kernel (msplat/sort_gaussian.py:
+ * 41-52).  The two native pieces are mirrored one-to-one:                  */
+
+/* Replaces computeGaussianKey (msplat/src/sort_gaussian.cu:74-113;
+ * ext.cpp:20).  `tiles_cumsum` is the inclusive int32 scan of tiles;
+ * `num_intersects` = tiles_cumsum[P-1] (the reference reads it with a
+ * blocking .item(); here the caller passes it).  key [I] int64 =
+ * (tile << 32) | sign-extended depth bits; idx [I] int32.  Slots that no
+ * Gaussian fills stay 0, like the reference's zero-initialised buffers.    */
+MSPLAT_API int msplat_compute_gaussian_key(int P, const float *uv, const float *depth,
+                                int W, int H, const int32_t *radius,
+                                const int32_t *tiles_cumsum,
+                                int64_t num_intersects, int64_t *key,
+                                int32_t *idx, msplat_stream_t stream);
+
+/* Replaces computeTileGaussianRange (msplat/src/sort_gaussian.cu:115-142;
+ * ext.cpp:21).  tile_range [ntiles,2] int32 = [start,end) per tile, [0,0]
+ * for empty tiles.  Keys whose tile id is outside the grid (negative-depth
+ * keys) are skipped where the reference writes out of bounds.              */
+MSPLAT_API int msplat_compute_tile_gaussian_range(int W, int H, int64_t num_intersects,
+                                       const int64_t *key_sorted,
+                                       int32_t *tile_range,
+                                       msplat_stream_t stream);
+
+/* Inclusive int32 scan (the reference's torch.cumsum(tiles, dtype=int32),
+ * msplat/sort_gaussian.py:42).  Also writes out[n-1] widened to int64 into
+ * *total (device pointer, may be NULL) for overflow-safe host reads.      */
+MSPLAT_API size_t msplat_scan_workspace_size(int n);
+MSPLAT_API int msplat_inclusive_scan_i32(int n, const int32_t *in, int32_t *out,
+                              int64_t *total, void *workspace,
+                              size_t workspace_bytes, msplat_stream_t stream);
+
+/* Stable LSD radix sort of (int64 key, int32 value) pairs in SIGNED int64
+ * order (torch.sort on int64, msplat/sort_gaussian.py:49) that carries the
+ * values along (the torch.gather of :50).  Only key bits [begin_bit,
+ * end_bit) are sorted, 8 per pass; callers that know all keys are
+ * non-negative pass end_bit < 64 to skip constant high digits, otherwise
+ * end_bit must be 64.  vals_in == NULL means value = input index.  The
+ * inputs are only read; outputs must not alias them.                      */
+MSPLAT_API size_t msplat_radix_sort_i64_workspace_size(int64_t n);
+MSPLAT_API int msplat_radix_sort_i64_pairs(int64_t n, const int64_t *keys_in,
+                                const int32_t *vals_in, int64_t *keys_out,
+                                int32_t *vals_out, int begin_bit,
+                                int end_bit, void *workspace,
+                                size_t workspace_bytes,
+                                msplat_stream_t stream);
+
+/* Fast drop-in for the whole of sort_gaussian (msplat/sort_gaussian.py:
+ * 8-54) in two calls with one host read in between:
+ *   1. _prepare: depth-sorts the Gaussians and scans their tile counts in
+ *      depth order; writes counts[0] = number of intersections I and
+ *      counts[1] = number of "filler" slots (tiles[i] larger than the
+ *      Gaussian's rectangle, or radius <= 0 with tiles > 0).
+ *   2. _finish (only valid when counts[1] == 0): emits (tile, id) pairs in
+ *      depth order, stable-sorts them by tile, writes idx_sorted [I] and
+ *      tile_range [ntiles,2].  Bit-identical to the reference's output.
+ * When counts[1] != 0 the caller uses the reference-layout path
+ * (compute_gaussian_key + radix_sort_i64_pairs + tile range), which
+ * reproduces the zero-filled slots exactly.                                */
+MSPLAT_API size_t msplat_sort_prepare_workspace_size(int P);
+MSPLAT_API size_t msplat_sort_finish_workspace_size(int P, int64_t num_intersects,
+                                         int W, int H);
+MSPLAT_API int msplat_sort_gaussian_prepare(int P, const float *depth,
+                                 const int32_t *radius, const int32_t *tiles,
+                                 const float *uv, int W, int H,
+                                 int64_t *counts, void *workspace,
+                                 size_t workspace_bytes,
+                                 msplat_stream_t stream);
+MSPLAT_API int msplat_sort_gaussian_finish(int P, const float *uv, const float *depth,
+                                const int32_t *radius, int W, int H,
+                                int64_t num_intersects,
+                                const void *prepare_workspace,
+                                int32_t *idx_sorted, int32_t *tile_range,
+                                void *workspace, size_t workspace_bytes,
+                                msplat_stream_t stream);
+
+/* ------------------------------------------------------------------------ */
+/* Alpha blending: replaces alphaBlendingForward / alphaBlendingBackward
+ * (msplat/src/alpha_blending.cu:248-394, :396-573; ext.cpp:24-25).
+ * feature [P,C] (any C >= 1, one pass, no chunking), out [C,H,W],
+ * final_T [H,W], ncontrib [H,W] int32.                                     */
+MSPLAT_API int msplat_alpha_blending_forward(int P, int C, const float *uv,
+                                  const float *conic, const float *opacity,
+                                  const float *feature,
+                                  const int32_t *idx_sorted,
+                                  const int32_t *tile_range, float bg, int W,
+                                  int H, float *out, float *final_T,
+                                  int32_t *ncontrib, msplat_stream_t stream);
+
+/* Gradients are ACCUMULATED into dL_duv [P,2], dL_dconic [P,3],
+ * dL_dopacity [P], dL_dfeature [P,C]: the caller zero-fills them. */
+MSPLAT_API int msplat_alpha_blending_backward(int P, int C, const float *uv,
+                                   const float *conic, const float *opacity,
+                                   const float *feature,
+                                   const int32_t *idx_sorted,
+                                   const int32_t *tile_range, float bg, int W,
+                                   int H, const float *final_T,
+                                   const int32_t *ncontrib,
+                                   const float *dL_dout, float *dL_duv,
+                                   float *dL_dconic, float *dL_dopacity,
+                                   float *dL_dfeature, msplat_stream_t stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MSPLAT_GB300_H */

@@ -1,0 +1,94 @@
+"""Builds the native library ``libmsplat_gb300.so`` in-tree with nvcc.
+
+Every translation unit in ``csrc/`` is compiled for sm_103a only
+(``-gencode arch=compute_103a,code=sm_103a``) with the same floating-point
+flags as the reference build (``-O3 --use_fast_math``, reference
+``setup.py:39``), in parallel, then linked into one shared object that
+exports the C ABI declared in ``include/msplat_gb300.h``.
+
+Run ``python -m msplat_gb300._build`` (or ``__graft_entry__.build()``).
+"""
+from __future__ import annotations
+
+import concurrent.futures as cf
+import os
+import shutil
+import subprocess
+import sys
+
+PKG_DIR = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(PKG_DIR)
+CSRC = os.path.join(PKG_DIR, "csrc")
+INCLUDE = os.path.join(ROOT, "include")
+BUILD_DIR = os.path.join(PKG_DIR, "_build")
+LIB_PATH = os.path.join(PKG_DIR, "libmsplat_gb300.so")
+
+ARCH_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a"]
+NVCC_FLAGS = ARCH_FLAGS + [
+    "-O3",
+    "--use_fast_math",
+    "-lineinfo",
+    "-std=c++17",
+    "-Xcompiler",
+    "-fPIC",
+    "-Xcompiler",
+    "-fvisibility=hidden",
+    "--expt-relaxed-constexpr",
+]
+
+
+def _nvcc() -> str:
+    cand = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    if not os.path.exists(cand):
+        raise RuntimeError("nvcc not found; the CUDA toolkit is required to build msplat_gb300")
+    return cand
+
+
+def sources() -> list[str]:
+    return sorted(os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(".cu"))
+
+
+def _needs_build(objs: list[str]) -> bool:
+    if not os.path.exists(LIB_PATH):
+        return True
+    lib_m = os.path.getmtime(LIB_PATH)
+    deps = [os.path.join(CSRC, f) for f in os.listdir(CSRC)]
+    deps.append(os.path.join(INCLUDE, "msplat_gb300.h"))
+    deps.append(os.path.abspath(__file__))
+    return any(os.path.getmtime(d) > lib_m for d in deps)
+
+
+def build(force: bool = False, verbose: bool = False, extra_flags: list[str] | None = None) -> str:
+    """Compiles and links the library; returns its path."""
+    srcs = sources()
+    os.makedirs(BUILD_DIR, exist_ok=True)
+    objs = [os.path.join(BUILD_DIR, os.path.basename(s)[:-3] + ".o") for s in srcs]
+    if not force and not _needs_build(objs):
+        return LIB_PATH
+    nvcc = _nvcc()
+    flags = NVCC_FLAGS + ["-I", INCLUDE, "-I", CSRC] + list(extra_flags or [])
+
+    def compile_one(pair):
+        src, obj = pair
+        cmd = [nvcc, *flags, "-c", src, "-o", obj]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"nvcc failed for {os.path.basename(src)}:\n{r.stderr}")
+        return r.stderr
+
+    workers = min(len(srcs), max(1, os.cpu_count() or 1))
+    with cf.ThreadPoolExecutor(max_workers=workers) as ex:
+        for msg in ex.map(compile_one, zip(srcs, objs)):
+            if verbose and msg:
+                print(msg, file=sys.stderr)
+    tmp = LIB_PATH + ".tmp"
+    cmd = [nvcc, *ARCH_FLAGS, "-shared", "-o", tmp, *objs]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"nvcc link failed:\n{r.stderr}")
+    os.replace(tmp, LIB_PATH)
+    return LIB_PATH
+
+
+if __name__ == "__main__":
+    print(build(force="--force" in sys.argv, verbose="-v" in sys.argv))

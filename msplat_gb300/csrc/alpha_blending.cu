@@ -1,0 +1,384 @@
+// Tile-based front-to-back alpha blending of depth-sorted 2-D Gaussians.
+//
+// Semantics follow msplat/src/alpha_blending.cu (forward :16-110, backward
+// :112-246): one 16x16 tile per CTA, pixel centres at integer coordinates,
+//   power = -0.5 (a dx^2 + c dy^2) - b dx dy        (skip if > 0)
+//   alpha = min(0.99, opacity * exp(power))          (skip if < 1/255)
+//   stop before a Gaussian that would take T below 1e-4,
+//   out = sum f alpha T + T bg, ncontrib = list index of the last blended.
+// The per-pair arithmetic is written as in the reference so T, ncontrib and
+// the colours agree to the last bit where the exponential does.
+//
+// What is different (results unchanged):
+//  * each batch of the tile's list is gathered once into shared memory
+//    (geometry and features), and Gaussians whose alpha >= 1/255 ellipse
+//    misses the whole tile are dropped there by a conservative box test;
+//    survivors keep their list index so ncontrib counts every entry;
+//  * per pair, exp is skipped when power is below a per-Gaussian bound that
+//    already implies alpha < 1/255;
+//  * any channel count runs in one pass up to 32 channels (the reference
+//    re-runs the whole blend per chunk of <= 32 and transposes features);
+//  * backward starts at the tile's largest ncontrib instead of the end of
+//    the list, and per-Gaussian gradients are summed over each warp with a
+//    reduce-scatter of shuffles before one atomic per value per warp (the
+//    reference issues C + 6 atomics per pixel-Gaussian pair).
+#include "common.cuh"
+
+namespace msplat {
+
+constexpr int kBlendThreads = kTilePixels;  // 256: one thread per pixel
+constexpr int kBatch = kBlendThreads;
+
+struct BlendRec {
+    float4 a;  // uv.x, uv.y, conic.x, conic.y
+    float4 b;  // conic.z, opacity, power bound, list index (as int bits)
+};
+
+// Conservative test: true only if no pixel centre of the tile box
+// [bx0, bx0 + 15] x [by0, by0 + 15] can reach alpha >= 1/255.
+__device__ __forceinline__ bool cull_tile(float gx, float gy, float a, float b, float c, float op,
+                                          float bx0, float by0) {
+    if (!(op > 0.0f)) return op <= 0.0f;           // NaN opacity is never culled
+    const float tau = 2.0f * logf(255.0f * op);    // q <= tau  <=>  op e^{-q/2} >= 1/255
+    const float det = a * c - b * b;
+    if (!(a > 0.0f) || !(c > 0.0f) || !(det > 0.0f)) return false;  // not an ellipse
+    const float bx1 = bx0 + (float)(kTile - 1), by1 = by0 + (float)(kTile - 1);
+    const float lx = bx0 - gx, hx = bx1 - gx, ly = by0 - gy, hy = by1 - gy;  // pixel - centre
+    const float DX = fmaxf(fabsf(lx), fabsf(hx)), DY = fmaxf(fabsf(ly), fabsf(hy));
+    // Bound on how far the blend's float evaluation of q at a pixel can sit
+    // below the exact value: product/sum rounding (relative to the term
+    // sizes), rounding of the coordinate differences (relative to the
+    // coordinates), and the approximate logarithm in tau.
+    const float coord_eps = 1e-6f * (fabsf(gx) + fabsf(gy) + fabsf(bx1) + fabsf(by1) + 1.0f);
+    const float err = 1e-5f * (a * DX * DX + c * DY * DY + 2.0f * fabsf(b) * DX * DY) +
+                      4.0f * coord_eps * (a * DX + c * DY + 2.0f * fabsf(b) * (DX + DY)) +
+                      1e-5f * fabsf(tau) + 1e-4f;
+    if (lx <= 0.0f && hx >= 0.0f && ly <= 0.0f && hy >= 0.0f) return tau + err < 0.0f;
+    // Minimum of q(dx, dy) = a dx^2 + 2 b dx dy + c dy^2 over the box edges.
+    float qmin = INFINITY;
+    {
+        const float xs[2] = {lx, hx};
+#pragma unroll
+        for (int e = 0; e < 2; ++e) {
+            const float dx = xs[e];
+            const float dy = fminf(fmaxf(-b * dx / c, ly), hy);
+            qmin = fminf(qmin, a * dx * dx + 2.0f * b * dx * dy + c * dy * dy);
+        }
+        const float ys[2] = {ly, hy};
+#pragma unroll
+        for (int e = 0; e < 2; ++e) {
+            const float dy = ys[e];
+            const float dx = fminf(fmaxf(-b * dy / a, lx), hx);
+            qmin = fminf(qmin, a * dx * dx + 2.0f * b * dx * dy + c * dy * dy);
+        }
+    }
+    return qmin > tau + err;
+}
+
+// power < bound  =>  opacity * exp(power) < 1/255 (with margin for the
+// approximate exponential); -inf disables the shortcut.
+__device__ __forceinline__ float power_bound(float op) {
+    if (!(op > 0.0f)) return -INFINITY;
+    const float h = -logf(255.0f * op);
+    return h - (1e-3f + 1e-5f * fabsf(h));
+}
+
+// Gathers entry `j` (when valid) and compacts the kept entries of the block
+// into shared memory in thread order.  Returns the number kept.
+template <int CMAX>
+__device__ __forceinline__ int gather_batch(bool valid, int j, const int32_t *__restrict__ idx_sorted,
+                                            const float2 *__restrict__ uv, const float *__restrict__ conic,
+                                            const float *__restrict__ opacity,
+                                            const float *__restrict__ feature, int C, int c0, int nc,
+                                            float bx0, float by0, BlendRec *srec, float *sfeat,
+                                            int *sgid, int *swarp) {
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    BlendRec r;
+    int g = 0;
+    bool keep = false;
+    if (valid) {
+        g = idx_sorted[j];
+        const float2 p = uv[g];
+        const float ca = conic[3 * g], cb = conic[3 * g + 1], cc = conic[3 * g + 2];
+        const float op = opacity[g];
+        keep = !cull_tile(p.x, p.y, ca, cb, cc, op, bx0, by0);
+        r.a = make_float4(p.x, p.y, ca, cb);
+        r.b = make_float4(cc, op, power_bound(op), __int_as_float(j));
+    }
+    const unsigned m = __ballot_sync(0xffffffffu, keep);
+    if (lane == 0) swarp[warp] = __popc(m);
+    __syncthreads();
+    int base = 0, total = 0;
+#pragma unroll
+    for (int w = 0; w < kBlendThreads / 32; ++w) {
+        const int cw = swarp[w];
+        base += (w < warp) ? cw : 0;
+        total += cw;
+    }
+    if (keep) {
+        const int pos = base + __popc(m & ((1u << lane) - 1u));
+        srec[pos] = r;
+        sgid[pos] = g;
+        const float *f = feature + (size_t)g * C + c0;
+#pragma unroll
+        for (int k = 0; k < CMAX; ++k)
+            if (k < nc) sfeat[k * kBatch + pos] = f[k];
+    }
+    __syncthreads();
+    return total;
+}
+
+template <int CMAX>
+__global__ void __launch_bounds__(kBlendThreads)
+blend_fwd_kernel(int P, int C, int c0, const float2 *__restrict__ uv, const float *__restrict__ conic,
+                 const float *__restrict__ opacity, const float *__restrict__ feature,
+                 const int32_t *__restrict__ idx_sorted, const int2 *__restrict__ tile_range, float bg,
+                 int W, int H, float *__restrict__ out, float *__restrict__ final_T,
+                 int32_t *__restrict__ ncontrib) {
+    __shared__ BlendRec srec[kBatch];
+    __shared__ float sfeat[CMAX * kBatch];
+    __shared__ int sgid[kBatch];
+    __shared__ int swarp[kBlendThreads / 32];
+    const int nc = min(CMAX, C - c0);
+    const int gxn = (W + kTile - 1) / kTile;
+    const int tile = blockIdx.y * gxn + blockIdx.x;
+    const int px = blockIdx.x * kTile + (threadIdx.x & (kTile - 1));
+    const int py = blockIdx.y * kTile + (threadIdx.x >> 4);
+    const bool inside = px < W && py < H;
+    const float fx = (float)px, fy = (float)py;
+    const float bx0 = (float)(blockIdx.x * kTile), by0 = (float)(blockIdx.y * kTile);
+    const int2 range = tile_range[tile];
+
+    bool done = !inside;
+    float T = 1.0f;
+    int last = 0;
+    float F[CMAX];
+#pragma unroll
+    for (int k = 0; k < CMAX; ++k) F[k] = 0.0f;
+
+    for (int start = range.x; start < range.y; start += kBatch) {
+        if (__syncthreads_count(done) == kBlendThreads) break;
+        const int j = start + (int)threadIdx.x;
+        const int n = gather_batch<CMAX>(j < range.y, j, idx_sorted, uv, conic, opacity, feature, C, c0,
+                                         nc, bx0, by0, srec, sfeat, sgid, swarp);
+        for (int k = 0; k < n && !done; ++k) {
+            const BlendRec r = srec[k];
+            const float dx = r.a.x - fx, dy = r.a.y - fy;
+            const float power = -0.5f * (r.a.z * dx * dx + r.b.x * dy * dy) - r.a.w * dx * dy;
+            if (power > 0.0f || power < r.b.z) continue;
+            const float alpha = fminf(0.99f, r.b.y * __expf(power));
+            if (alpha < 1.0f / 255.0f) continue;
+            const float nT = T * (1.0f - alpha);
+            if (nT < 0.0001f) {
+                done = true;
+                continue;
+            }
+#pragma unroll
+            for (int q = 0; q < CMAX; ++q)
+                if (q < nc) F[q] += sfeat[q * kBatch + k] * alpha * T;
+            T = nT;
+            last = __float_as_int(r.b.w) - range.x + 1;
+        }
+    }
+    if (inside) {
+        const int pix = py * W + px;
+        if (c0 == 0) {
+            final_T[pix] = T;
+            ncontrib[pix] = last;
+        }
+#pragma unroll
+        for (int q = 0; q < CMAX; ++q)
+            if (q < nc) out[(size_t)(c0 + q) * H * W + pix] = F[q] + T * bg;
+    }
+}
+
+// Reduce-scatter of 16 values over a warp: lane l returns the warp total of
+// value (l >> 1) (lanes 2i and 2i+1 hold the same total).
+__device__ __forceinline__ float warp_reduce_scatter16(float (&v)[16]) {
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int o = 16, n = 16; o >= 2; o >>= 1, n >>= 1) {
+        const bool up = (lane & o) != 0;
+        const int h = n >> 1;
+#pragma unroll
+        for (int k = 0; k < h; ++k) {
+            const float send = up ? v[k] : v[k + h];
+            const float keep = up ? v[k + h] : v[k];
+            v[k] = keep + __shfl_xor_sync(0xffffffffu, send, o);
+        }
+    }
+    return v[0] + __shfl_xor_sync(0xffffffffu, v[0], 1);
+}
+
+constexpr int kBwdC = 10;  // channels per backward pass (6 + 10 = 16 values)
+
+__global__ void __launch_bounds__(kBlendThreads)
+blend_bwd_kernel(int P, int C, int c0, const float2 *__restrict__ uv, const float *__restrict__ conic,
+                 const float *__restrict__ opacity, const float *__restrict__ feature,
+                 const int32_t *__restrict__ idx_sorted, const int2 *__restrict__ tile_range, float bg,
+                 int W, int H, const float *__restrict__ final_T, const int32_t *__restrict__ ncontrib,
+                 const float *__restrict__ dL_dout, float *__restrict__ dL_duv,
+                 float *__restrict__ dL_dconic, float *__restrict__ dL_dopacity,
+                 float *__restrict__ dL_dfeature) {
+    __shared__ BlendRec srec[kBatch];
+    __shared__ float sfeat[kBwdC * kBatch];
+    __shared__ int sgid[kBatch];
+    __shared__ int swarp[kBlendThreads / 32];
+    __shared__ int smax;
+    const int nc = min(kBwdC, C - c0);
+    const int gxn = (W + kTile - 1) / kTile;
+    const int tile = blockIdx.y * gxn + blockIdx.x;
+    const int px = blockIdx.x * kTile + (threadIdx.x & (kTile - 1));
+    const int py = blockIdx.y * kTile + (threadIdx.x >> 4);
+    const bool inside = px < W && py < H;
+    const float fx = (float)px, fy = (float)py;
+    const float bx0 = (float)(blockIdx.x * kTile), by0 = (float)(blockIdx.y * kTile);
+    const int2 range = tile_range[tile];
+    const int pix = py * W + px;
+    const int lane = threadIdx.x & 31;
+
+    const float T_final = inside ? final_T[pix] : 0.0f;
+    const int last = inside ? ncontrib[pix] : 0;
+    float T = T_final;
+    float dpix[kBwdC], accum[kBwdC], lastf[kBwdC];
+    float bg_dot = 0.0f;
+#pragma unroll
+    for (int q = 0; q < kBwdC; ++q) {
+        dpix[q] = (inside && q < nc) ? dL_dout[(size_t)(c0 + q) * H * W + pix] : 0.0f;
+        accum[q] = 0.0f;
+        lastf[q] = 0.0f;
+        bg_dot += bg * dpix[q];
+    }
+    float last_alpha = 0.0f;
+
+    // Nothing past the tile's largest ncontrib contributes.
+    if (threadIdx.x == 0) smax = 0;
+    __syncthreads();
+    int wmax = last;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) wmax = max(wmax, __shfl_xor_sync(0xffffffffu, wmax, o));
+    if (lane == 0) atomicMax(&smax, wmax);
+    __syncthreads();
+    const int end = range.x + min(smax, range.y - range.x);
+
+    for (int bend = end; bend > range.x; bend -= kBatch) {
+        const int bstart = max(range.x, bend - kBatch);
+        const int j = bend - 1 - (int)threadIdx.x;
+        const int n = gather_batch<kBwdC>(j >= bstart, j, idx_sorted, uv, conic, opacity, feature, C, c0,
+                                          nc, bx0, by0, srec, sfeat, sgid, swarp);
+        for (int k = 0; k < n; ++k) {
+            const BlendRec r = srec[k];
+            const int jl = __float_as_int(r.b.w) - range.x;  // list position
+            float v[16];
+#pragma unroll
+            for (int q = 0; q < 16; ++q) v[q] = 0.0f;
+            bool contrib = false;
+            if (jl < last) {
+                const float dx = r.a.x - fx, dy = r.a.y - fy;
+                const float ca = r.a.z, cb = r.a.w, cc = r.b.x, op = r.b.y;
+                const float power = -0.5f * (ca * dx * dx + cc * dy * dy) - cb * dx * dy;
+                if (power <= 0.0f && power >= r.b.z) {
+                    const float G = __expf(power);
+                    const float alpha = fminf(0.99f, op * G);
+                    if (alpha >= 1.0f / 255.0f) {
+                        contrib = true;
+                        T = T / (1.f - alpha);
+                        const float dcol = alpha * T;
+                        float dL_dalpha = 0.0f;
+#pragma unroll
+                        for (int q = 0; q < kBwdC; ++q) {
+                            if (q < nc) {
+                                const float f = sfeat[q * kBatch + k];
+                                accum[q] = last_alpha * lastf[q] + (1.f - last_alpha) * accum[q];
+                                lastf[q] = f;
+                                dL_dalpha += (f - accum[q]) * dpix[q];
+                                v[6 + q] = dcol * dpix[q];
+                            }
+                        }
+                        dL_dalpha *= T;
+                        last_alpha = alpha;
+                        dL_dalpha += (-T_final / (1.f - alpha)) * bg_dot;
+                        const float dL_dG = op * dL_dalpha;
+                        const float gdx = -G * dx * ca - G * dy * cb;
+                        const float gdy = -G * dy * cc - G * dx * cb;
+                        v[0] = dL_dG * gdx;
+                        v[1] = dL_dG * gdy;
+                        v[2] = -0.5f * G * dx * dx * dL_dG;
+                        v[3] = -G * dx * dy * dL_dG;
+                        v[4] = -0.5f * G * dy * dy * dL_dG;
+                        v[5] = G * dL_dalpha;
+                    }
+                }
+            }
+            if (__any_sync(0xffffffffu, contrib)) {
+                const float s = warp_reduce_scatter16(v);
+                const int vi = lane >> 1;
+                if ((lane & 1) == 0 && vi < 6 + nc) {
+                    const int g = sgid[k];
+                    float *dst;
+                    if (vi < 2) dst = dL_duv + 2 * g + vi;
+                    else if (vi < 5) dst = dL_dconic + 3 * g + (vi - 2);
+                    else if (vi == 5) dst = dL_dopacity + g;
+                    else dst = dL_dfeature + (size_t)g * C + c0 + (vi - 6);
+                    atomicAdd(dst, s);
+                }
+            }
+        }
+        __syncthreads();
+    }
+}
+
+}  // namespace msplat
+
+using namespace msplat;
+
+extern "C" int msplat_alpha_blending_forward(int P, int C, const float *uv, const float *conic,
+                                             const float *opacity, const float *feature,
+                                             const int32_t *idx_sorted, const int32_t *tile_range,
+                                             float bg, int W, int H, float *out, float *final_T,
+                                             int32_t *ncontrib, msplat_stream_t stream) {
+    if (P < 0 || C <= 0 || W <= 0 || H <= 0)
+        return set_error(MSPLAT_ERR_INVALID_ARGUMENT, "alpha_blending_forward: bad sizes P=%d C=%d W=%d H=%d",
+                         P, C, W, H);
+    if (!tile_range || !out || !final_T || !ncontrib || (P > 0 && (!uv || !conic || !opacity || !feature)))
+        return set_error(MSPLAT_ERR_INVALID_ARGUMENT, "alpha_blending_forward: null pointer");
+    const dim3 grid(ceil_div(W, kTile), ceil_div(H, kTile));
+    for (int c0 = 0; c0 < C; c0 += 32) {
+        const int nc = min(32, C - c0);
+        if (nc <= 4)
+            blend_fwd_kernel<4><<<grid, kBlendThreads, 0, stream>>>(P, C, c0, (const float2 *)uv, conic, opacity,
+                                                                    feature, idx_sorted, (const int2 *)tile_range,
+                                                                    bg, W, H, out, final_T, ncontrib);
+        else if (nc <= 16)
+            blend_fwd_kernel<16><<<grid, kBlendThreads, 0, stream>>>(P, C, c0, (const float2 *)uv, conic, opacity,
+                                                                     feature, idx_sorted, (const int2 *)tile_range,
+                                                                     bg, W, H, out, final_T, ncontrib);
+        else
+            blend_fwd_kernel<32><<<grid, kBlendThreads, 0, stream>>>(P, C, c0, (const float2 *)uv, conic, opacity,
+                                                                     feature, idx_sorted, (const int2 *)tile_range,
+                                                                     bg, W, H, out, final_T, ncontrib);
+    }
+    return check_launch("alpha_blending_forward");
+}
+
+extern "C" int msplat_alpha_blending_backward(int P, int C, const float *uv, const float *conic,
+                                              const float *opacity, const float *feature,
+                                              const int32_t *idx_sorted, const int32_t *tile_range,
+                                              float bg, int W, int H, const float *final_T,
+                                              const int32_t *ncontrib, const float *dL_dout,
+                                              float *dL_duv, float *dL_dconic, float *dL_dopacity,
+                                              float *dL_dfeature, msplat_stream_t stream) {
+    if (P < 0 || C <= 0 || W <= 0 || H <= 0)
+        return set_error(MSPLAT_ERR_INVALID_ARGUMENT, "alpha_blending_backward: bad sizes");
+    if (!tile_range || !final_T || !ncontrib || !dL_dout ||
+        (P > 0 && (!uv || !conic || !opacity || !feature || !dL_duv || !dL_dconic || !dL_dopacity || !dL_dfeature)))
+        return set_error(MSPLAT_ERR_INVALID_ARGUMENT, "alpha_blending_backward: null pointer");
+    if (P == 0) return MSPLAT_OK;
+    const dim3 grid(ceil_div(W, kTile), ceil_div(H, kTile));
+    for (int c0 = 0; c0 < C; c0 += kBwdC)
+        blend_bwd_kernel<<<grid, kBlendThreads, 0, stream>>>(P, C, c0, (const float2 *)uv, conic, opacity, feature,
+                                                             idx_sorted, (const int2 *)tile_range, bg, W, H, final_T,
+                                                             ncontrib, dL_dout, dL_duv, dL_dconic, dL_dopacity,
+                                                             dL_dfeature);
+    return check_launch("alpha_blending_backward");
+}

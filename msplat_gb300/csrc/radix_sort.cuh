@@ -1,0 +1,343 @@
+// LSD radix sort of (key, uint32 value) pairs and int32 scans, written for
+// sm_103a without library calls.
+//
+// One 8-bit pass = three launches with no device-side waiting:
+//   upsweep   per-tile digit histogram (warp-aggregated shared atomics via
+//             __match_any_sync), stored digit-major [256][tiles]
+//   row scan  one block per digit: exclusive scan of its row, offset by the
+//             totals of the smaller digits -> global start of every
+//             (digit, tile) bucket
+//   downsweep re-reads the tile, ranks each item among equal digits with a
+//             warp-level multisplit (stable: items are ranked in index
+//             order), reorders the tile in shared memory and writes each
+//             digit run contiguously (coalesced).
+// Tiles are 4096 items (256 threads x 16).
+#pragma once
+
+#include "block_scan.cuh"
+
+namespace msplat {
+
+constexpr int kRadixBits = 8;
+constexpr int kRadix = 1 << kRadixBits;
+constexpr int kSortThreads = 256;
+constexpr int kSortItems = 16;
+constexpr int kSortTile = kSortThreads * kSortItems;  // 4096
+constexpr int kSortWarps = kSortThreads / 32;
+
+template <typename K>
+__device__ __forceinline__ K sign_bit() { return K(1) << (sizeof(K) * 8 - 1); }
+
+template <typename K>
+__device__ __forceinline__ uint32_t digit_of(K k, int shift) {
+    return (uint32_t)(k >> shift) & (kRadix - 1);
+}
+
+inline int sort_tiles(int64_t n) { return (int)ceil_div64(n, kSortTile); }
+
+// ---------------------------------------------------------------- upsweep
+template <typename K, bool FLIP>
+__global__ void __launch_bounds__(kSortThreads)
+radix_upsweep_kernel(const K *__restrict__ keys, int64_t n, int shift, int ntiles,
+                     uint32_t *__restrict__ hist, uint32_t *__restrict__ totals) {
+    __shared__ uint32_t cnt[kRadix];
+    cnt[threadIdx.x] = 0;  // kSortThreads == kRadix
+    __syncthreads();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int64_t base = (int64_t)blockIdx.x * kSortTile;
+#pragma unroll 4
+    for (int r = 0; r < kSortItems; ++r) {
+        const int64_t idx = base + warp * (32 * kSortItems) + r * 32 + lane;
+        const bool valid = idx < n;
+        const unsigned vmask = __ballot_sync(0xffffffffu, valid);
+        if (valid) {
+            K k = keys[idx];
+            if (FLIP) k ^= sign_bit<K>();
+            const uint32_t d = digit_of(k, shift);
+            const unsigned peers = __match_any_sync(vmask, d);
+            if (lane == 31 - __clz(peers)) atomicAdd(&cnt[d], (uint32_t)__popc(peers));
+        }
+    }
+    __syncthreads();
+    const uint32_t c = cnt[threadIdx.x];
+    hist[(size_t)threadIdx.x * ntiles + blockIdx.x] = c;
+    if (c) atomicAdd(&totals[threadIdx.x], c);
+}
+
+// --------------------------------------------------------------- row scan
+// Block d turns row d of hist into global start offsets.
+__global__ void __launch_bounds__(1024)
+radix_rowscan_kernel(uint32_t *__restrict__ hist, const uint32_t *__restrict__ totals, int ntiles) {
+    __shared__ uint32_t scratch[33];
+    __shared__ uint32_t base_s;
+    const int d = blockIdx.x;
+    if (threadIdx.x < 32) {
+        uint32_t s = 0;
+        for (int q = threadIdx.x; q < d; q += 32) s += totals[q];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        if (threadIdx.x == 0) base_s = s;
+    }
+    __syncthreads();
+    uint32_t carry = base_s;
+    uint32_t *row = hist + (size_t)d * ntiles;
+    for (int c0 = 0; c0 < ntiles; c0 += blockDim.x) {
+        const int i = c0 + threadIdx.x;
+        const uint32_t v = i < ntiles ? row[i] : 0u;
+        uint32_t tot;
+        const uint32_t ex = block_exclusive_scan<uint32_t>(v, scratch, &tot);
+        if (i < ntiles) row[i] = carry + ex;
+        carry += tot;
+    }
+}
+
+// -------------------------------------------------------------- downsweep
+inline size_t radix_downsweep_smem(size_t key_bytes) {
+    return kSortTile * (key_bytes + 4) + (size_t)(kSortWarps * kRadix + 2 * kRadix) * 4;
+}
+
+// vals_in == nullptr means "value = input index".  FLIP_IN / FLIP_OUT xor
+// the key's sign bit on load / store (signed-integer order).
+template <typename K, bool FLIP_IN, bool FLIP_OUT>
+__global__ void __launch_bounds__(kSortThreads)
+radix_downsweep_kernel(const K *__restrict__ kin, const uint32_t *__restrict__ vin,
+                       K *__restrict__ kout, uint32_t *__restrict__ vout, int64_t n, int shift,
+                       int ntiles, const uint32_t *__restrict__ hist) {
+    extern __shared__ __align__(16) unsigned char sm_raw[];
+    K *skeys = reinterpret_cast<K *>(sm_raw);
+    uint32_t *svals = reinterpret_cast<uint32_t *>(skeys + kSortTile);
+    uint32_t *whist = svals + kSortTile;            // [warps][radix]
+    uint32_t *lstart = whist + kSortWarps * kRadix;  // [radix]
+    uint32_t *gstart = lstart + kRadix;              // [radix]
+    __shared__ uint32_t scan_scratch[33];
+
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int64_t base = (int64_t)blockIdx.x * kSortTile;
+    const int tile_n = (int)min((int64_t)kSortTile, n - base);
+    for (int i = tid; i < kSortWarps * kRadix; i += kSortThreads) whist[i] = 0;
+    gstart[tid] = hist[(size_t)tid * ntiles + blockIdx.x];
+    __syncthreads();
+
+    K key[kSortItems];
+    uint32_t val[kSortItems];
+    uint32_t rank[kSortItems];
+    uint32_t *my_hist = whist + warp * kRadix;
+#pragma unroll
+    for (int r = 0; r < kSortItems; ++r) {
+        const int li = warp * (32 * kSortItems) + r * 32 + lane;
+        const bool valid = li < tile_n;
+        K k = K(0);
+        uint32_t v = 0;
+        if (valid) {
+            k = kin[base + li];
+            if (FLIP_IN) k ^= sign_bit<K>();
+            v = vin ? vin[base + li] : (uint32_t)(base + li);
+        }
+        key[r] = k;
+        val[r] = v;
+        const unsigned vmask = __ballot_sync(0xffffffffu, valid);
+        const uint32_t d = digit_of(k, shift);
+        unsigned peers = 0;
+        uint32_t b0 = 0;
+        if (valid) {
+            peers = __match_any_sync(vmask, d);
+            b0 = my_hist[d];
+        }
+        __syncwarp();
+        if (valid) {
+            rank[r] = b0 + __popc(peers & ((1u << lane) - 1u));
+            if (lane == 31 - __clz(peers)) my_hist[d] = b0 + __popc(peers);
+        }
+        __syncwarp();
+    }
+    __syncthreads();
+    // Per digit (thread = digit): exclusive over warps, then over digits.
+    uint32_t tot = 0;
+#pragma unroll
+    for (int w = 0; w < kSortWarps; ++w) {
+        const uint32_t c = whist[w * kRadix + tid];
+        whist[w * kRadix + tid] = tot;
+        tot += c;
+    }
+    const uint32_t ex = block_exclusive_scan<uint32_t>(tot, scan_scratch, nullptr);
+    lstart[tid] = ex;
+    __syncthreads();
+#pragma unroll
+    for (int r = 0; r < kSortItems; ++r) {
+        const int li = warp * (32 * kSortItems) + r * 32 + lane;
+        if (li < tile_n) {
+            const uint32_t d = digit_of(key[r], shift);
+            const uint32_t pos = lstart[d] + my_hist[d] + rank[r];
+            skeys[pos] = key[r];
+            svals[pos] = val[r];
+        }
+    }
+    __syncthreads();
+    for (int i = tid; i < tile_n; i += kSortThreads) {
+        K k = skeys[i];
+        const uint32_t d = digit_of(k, shift);
+        const size_t o = (size_t)gstart[d] + (size_t)(i - (int)lstart[d]);
+        if (FLIP_OUT) k ^= sign_bit<K>();
+        if (kout) kout[o] = k;
+        vout[o] = svals[i];
+    }
+}
+
+// Workspace of one sort of n items over `passes` digits.
+struct RadixBuffers {
+    uint32_t *hist;    // [radix][tiles]
+    uint32_t *totals;  // [passes][radix]
+};
+
+inline void radix_size(WorkspaceSizer &s, int64_t n, int passes) {
+    s.take<uint32_t>((size_t)kRadix * sort_tiles(n));
+    s.take<uint32_t>((size_t)kRadix * passes);
+}
+
+inline bool radix_take(Workspace &w, int64_t n, int passes, RadixBuffers &b) {
+    b.hist = w.take<uint32_t>((size_t)kRadix * sort_tiles(n));
+    b.totals = w.take<uint32_t>((size_t)kRadix * passes);
+    return !w.overflow;
+}
+
+// Stable sort of n (key, value) pairs by key bits [begin_bit, begin_bit +
+// 8 * passes).  Pass p reads `src` and writes `dst`; the chain is
+//   in -> out -> tmp -> out ...   (odd pass count)
+//   in -> tmp -> out -> tmp -> out (even pass count)
+// so the result always lands in (kout, vout) and `in` is only read.
+// Aliasing allowed: for an even pass count `in` may alias `out`, for an odd
+// count `in` may alias `tmp`.  vin == nullptr means value = index.  kout may
+// not be null.  FLIP: keys are signed integers (sign bit flipped on the
+// first load and restored on the last store).
+template <typename K, bool FLIP>
+int radix_sort_pairs(int64_t n, int begin_bit, int passes, const K *kin, const uint32_t *vin,
+                     K *kout, uint32_t *vout, K *ktmp, uint32_t *vtmp, const RadixBuffers &b,
+                     cudaStream_t stream) {
+    if (n <= 0 || passes <= 0) return MSPLAT_OK;
+    const int nt = sort_tiles(n);
+    const size_t smem = radix_downsweep_smem(sizeof(K));
+    cudaMemsetAsync(b.totals, 0, sizeof(uint32_t) * kRadix * passes, stream);
+    const K *ksrc = kin;
+    const uint32_t *vsrc = vin;
+    for (int p = 0; p < passes; ++p) {
+        const int shift = begin_bit + p * kRadixBits;
+        const bool to_out = ((passes - 1 - p) & 1) == 0;
+        K *kdst = to_out ? kout : ktmp;
+        uint32_t *vdst = to_out ? vout : vtmp;
+        uint32_t *tot = b.totals + p * kRadix;
+        const bool first = p == 0, last = p == passes - 1;
+        if (FLIP && first)
+            radix_upsweep_kernel<K, true><<<nt, kSortThreads, 0, stream>>>(ksrc, n, shift, nt, b.hist, tot);
+        else
+            radix_upsweep_kernel<K, false><<<nt, kSortThreads, 0, stream>>>(ksrc, n, shift, nt, b.hist, tot);
+        radix_rowscan_kernel<<<kRadix, 1024, 0, stream>>>(b.hist, tot, nt);
+#define MSPLAT_DOWNSWEEP(FI, FO)                                                                \
+    do {                                                                                        \
+        auto kern = radix_downsweep_kernel<K, FI, FO>;                                          \
+        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);     \
+        kern<<<nt, kSortThreads, smem, stream>>>(ksrc, vsrc, kdst, vdst, n, shift, nt, b.hist); \
+    } while (0)
+        if (FLIP && first && last) MSPLAT_DOWNSWEEP(true, true);
+        else if (FLIP && first) MSPLAT_DOWNSWEEP(true, false);
+        else if (FLIP && last) MSPLAT_DOWNSWEEP(false, true);
+        else MSPLAT_DOWNSWEEP(false, false);
+#undef MSPLAT_DOWNSWEEP
+        ksrc = kdst;
+        vsrc = vdst;
+    }
+    return check_launch("radix_sort_pairs");
+}
+
+// ------------------------------------------------------------------- scan
+constexpr int kScanThreads = 256;
+constexpr int kScanItems = 16;
+constexpr int kScanTile = kScanThreads * kScanItems;
+
+__global__ void __launch_bounds__(kScanThreads)
+scan_reduce_kernel(const int32_t *__restrict__ in, int n, int64_t *__restrict__ partials) {
+    const int64_t base = (int64_t)blockIdx.x * kScanTile;
+    int64_t s = 0;
+    for (int i = threadIdx.x; i < kScanTile; i += kScanThreads) {
+        const int64_t idx = base + i;
+        if (idx < n) s += in[idx];
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    __shared__ int64_t ws[kScanThreads / 32];
+    if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int64_t t = 0;
+        for (int w = 0; w < kScanThreads / 32; ++w) t += ws[w];
+        partials[blockIdx.x] = t;
+    }
+}
+
+// One block: exclusive scan of the tile sums (in place), total -> *total.
+__global__ void __launch_bounds__(1024)
+scan_partials_kernel(int64_t *__restrict__ partials, int nparts, int64_t *__restrict__ total) {
+    __shared__ int64_t scratch[33];
+    int64_t carry = 0;
+    for (int c0 = 0; c0 < nparts; c0 += blockDim.x) {
+        const int i = c0 + threadIdx.x;
+        const int64_t v = i < nparts ? partials[i] : 0;
+        int64_t tot;
+        const int64_t ex = block_exclusive_scan<int64_t>(v, scratch, &tot);
+        if (i < nparts) partials[i] = carry + ex;
+        carry += tot;
+    }
+    if (threadIdx.x == 0 && total) *total = carry;
+}
+
+// Rescans each tile with its carry-in; writes inclusive or exclusive sums.
+// Items are blocked per thread (16 consecutive) for a thread-local prefix.
+__global__ void __launch_bounds__(kScanThreads)
+scan_apply_kernel(const int32_t *__restrict__ in, int n, const int64_t *__restrict__ partials,
+                  int32_t *__restrict__ out, bool inclusive) {
+    __shared__ int64_t scratch[33];
+    __shared__ int32_t tile[kScanTile];
+    const int64_t base = (int64_t)blockIdx.x * kScanTile;
+    for (int i = threadIdx.x; i < kScanTile; i += kScanThreads) {
+        const int64_t idx = base + i;
+        tile[i] = idx < n ? in[idx] : 0;
+    }
+    __syncthreads();
+    int64_t local = 0;
+    const int t0 = threadIdx.x * kScanItems;
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) local += tile[t0 + k];
+    const int64_t ex = block_exclusive_scan<int64_t>(local, scratch, nullptr);
+    int64_t run = partials[blockIdx.x] + ex;
+    int32_t res[kScanItems];
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) {
+        const int32_t v = tile[t0 + k];
+        res[k] = (int32_t)(inclusive ? run + v : run);
+        run += v;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) tile[t0 + k] = res[k];
+    __syncthreads();
+    for (int i = threadIdx.x; i < kScanTile; i += kScanThreads) {
+        const int64_t idx = base + i;
+        if (idx < n) out[idx] = tile[i];
+    }
+}
+
+inline void scan_size(WorkspaceSizer &s, int n) { s.take<int64_t>((size_t)ceil_div(n, kScanTile) + 1); }
+
+inline int scan_i32(int n, const int32_t *in, int32_t *out, bool inclusive, int64_t *total,
+                    int64_t *partials, cudaStream_t stream) {
+    if (n <= 0) {
+        if (total) cudaMemsetAsync(total, 0, sizeof(int64_t), stream);
+        return check_launch("scan");
+    }
+    const int nb = ceil_div(n, kScanTile);
+    scan_reduce_kernel<<<nb, kScanThreads, 0, stream>>>(in, n, partials);
+    scan_partials_kernel<<<1, 1024, 0, stream>>>(partials, nb, total);
+    scan_apply_kernel<<<nb, kScanThreads, 0, stream>>>(in, n, partials, out, inclusive);
+    return check_launch("scan");
+}
+
+}  // namespace msplat

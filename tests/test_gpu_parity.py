@@ -1,0 +1,377 @@
+"""GPU parity of every stage against the CPU oracle (float32 emulation of the
+reference's arithmetic for forward passes, float64 for adjoints).
+
+Bars (from the rasteriser's specification):
+  * radius, tiles_touched, idx_sorted, tile_range: bit-exact (radius may
+    differ only where the oracle flags the value as within rounding reach of
+    an integer boundary -- the GPU divides / square-roots approximately,
+    exactly like the reference's fast-math build);
+  * uv, depth, cov3d: bit-exact (same operations, same FMA contractions);
+  * rendered features: within 1e-5 absolute;
+  * gradients: within 1e-4 relative (to the largest magnitude of the output).
+"""
+import numpy as np
+import pytest
+import torch
+
+import oracle
+from _golden import load
+from _scenes import camera, scene
+
+pytestmark = pytest.mark.gpu
+DEV = "cuda"
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _built():
+    from msplat_gb300 import _build, _lib
+    _build.build()
+    _lib.load()
+    oracle.set_fma_mode(oracle.FMA_MODE)
+    yield
+
+
+def T(x, dtype=None):
+    t = torch.as_tensor(np.asarray(x))
+    if dtype is not None:
+        t = t.to(dtype)
+    return t.to(DEV).contiguous()
+
+
+def N(x):
+    return x.detach().cpu().numpy()
+
+
+def rel_close(got, ref, rtol=1e-4, what=""):
+    got = np.asarray(got, np.float64)
+    ref = np.asarray(ref, np.float64)
+    scale = max(np.abs(ref).max(), 1e-30)
+    err = np.abs(got - ref).max() if got.size else 0.0
+    assert err <= rtol * scale, f"{what}: max abs err {err:.3e} > {rtol} * {scale:.3e}"
+
+
+import msplat_gb300 as ms  # noqa: E402
+
+
+def projected_scene(n=20000, W=640, H=480, seed=0, front=False):
+    s = scene(n, seed)
+    intr, extr = camera(W, H, seed=seed, front=front)
+    return s, intr, extr
+
+
+# ------------------------------------------------------------ projection
+@pytest.mark.parametrize("seed,front", [(0, False), (1, False), (2, True)])
+def test_project_point_forward_bit_exact(seed, front):
+    s, intr, extr = projected_scene(seed=seed, front=front)
+    uv, depth = ms.project_point(T(s["xyz"]), T(intr), T(extr), 640, 480)
+    ouv, od = oracle.project_point_forward(s["xyz"].numpy(), intr, extr, 640, 480)
+    np.testing.assert_array_equal(N(uv), ouv)
+    np.testing.assert_array_equal(N(depth), od)
+
+
+def test_fma_mode_is_the_compilers():
+    """The oracle's contraction pattern is the one nvcc produces: with any
+    other pattern the projection is no longer bit-identical."""
+    s, intr, extr = projected_scene(seed=5)
+    uv, depth = ms.project_point(T(s["xyz"]), T(intr), T(extr), 640, 480)
+    hits = {}
+    for m in (0, 1, 2):
+        oracle.set_fma_mode(m)
+        ouv, od = oracle.project_point_forward(s["xyz"].numpy(), intr, extr, 640, 480)
+        hits[m] = bool(np.array_equal(N(uv), ouv) and np.array_equal(N(depth), od))
+    oracle.set_fma_mode(oracle.FMA_MODE)
+    assert hits[oracle.FMA_MODE], hits
+
+
+def test_project_point_golden_and_culling():
+    g = load("project_point")
+    uv, depth = ms.project_point(T(g["xyz"]), T(g["intr"]), T(g["extr"]), g["W"], g["H"])
+    ouv, od = oracle.project_point_forward(g["xyz"], g["intr"], g["extr"], g["W"], g["H"])
+    np.testing.assert_array_equal(N(uv), ouv)
+    np.testing.assert_array_equal(N(depth), od)
+    # near culling and a [4,4] extrinsic
+    s, intr, extr = projected_scene(seed=3, front=True)
+    e44 = np.eye(4, dtype=np.float32)
+    e44[:3] = extr
+    uv, depth = ms.project_point(T(s["xyz"]), T(intr), T(e44), 640, 480, nearest=4.0, extent=0.5)
+    ouv, od = oracle.project_point_forward(s["xyz"].numpy(), intr, extr, 640, 480, 4.0, 0.5)
+    np.testing.assert_array_equal(N(uv), ouv)
+    np.testing.assert_array_equal(N(depth), od)
+    assert (od == 0).any() and (od != 0).any()
+
+
+def test_project_point_backward():
+    s, intr, extr = projected_scene(seed=4)
+    xyz = T(s["xyz"]).requires_grad_()
+    ti, te = T(intr).requires_grad_(), T(extr).requires_grad_()
+    uv, depth = ms.project_point(xyz, ti, te, 640, 480)
+    g = torch.Generator().manual_seed(0)
+    wu, wd = torch.randn(uv.shape, generator=g), torch.randn(depth.shape, generator=g)
+    ((uv * T(wu)).sum() + (depth * T(wd)).sum()).backward()
+    dx, di, de = oracle.project_point_backward(s["xyz"].numpy(), intr, extr, N(depth), wu.numpy(), wd.numpy())
+    rel_close(N(xyz.grad), dx, what="dL/dxyz")
+    rel_close(N(ti.grad), di, what="dL/dintr")
+    rel_close(N(te.grad), de, what="dL/dextr")
+    # no camera grads requested -> None, as the reference
+    xyz2 = T(s["xyz"]).requires_grad_()
+    uv2, d2 = ms.project_point(xyz2, T(intr), T(extr), 640, 480)
+    (uv2.sum() + d2.sum()).backward()
+    assert xyz2.grad is not None
+
+
+# ----------------------------------------------------------------- cov3d
+def test_compute_cov3d_bit_exact_and_backward():
+    g = load("compute_cov3d")
+    s, q = g["scales"], g["uquats"]
+    vis = np.random.default_rng(0).random(s.shape[0]) > 0.2
+    ts, tq = T(s).requires_grad_(), T(q).requires_grad_()
+    cov = ms.compute_cov3d(ts, tq, T(vis))
+    ocov = oracle.compute_cov3d_forward(s, q, vis)
+    np.testing.assert_array_equal(N(cov), ocov)
+    w = np.random.default_rng(1).normal(size=cov.shape).astype(np.float32)
+    (cov * T(w)).sum().backward()
+    ds, dq = oracle.compute_cov3d_backward(s, q, vis, w)
+    rel_close(N(ts.grad), ds, what="dL/dscale")
+    rel_close(N(tq.grad), dq, what="dL/dquat")
+
+
+# ------------------------------------------------------------------- EWA
+def ewa_inputs(n=30000, W=800, H=600, seed=0):
+    s, intr, extr = projected_scene(n, W, H, seed)
+    uv, d = oracle.project_point_forward(s["xyz"].numpy(), intr, extr, W, H)
+    vis = (d != 0).reshape(-1)
+    cov = oracle.compute_cov3d_forward(s["scale"].numpy(), s["rot"].numpy(), vis)
+    return s, intr, extr, uv, vis, cov, W, H
+
+
+@pytest.mark.parametrize("seed", [0, 1])
+def test_ewa_project_forward(seed):
+    s, intr, extr, uv, vis, cov, W, H = ewa_inputs(seed=seed)
+    conic, radius, tiles = ms.ewa_project(T(s["xyz"]), T(cov), T(intr), T(extr), T(uv), W, H, T(vis))
+    oc, orad, otil, amb = oracle.ewa_project_forward(s["xyz"].numpy(), cov, intr, extr, uv, W, H, vis)
+    mism = (N(radius) != orad) | (N(tiles) != otil)
+    assert not (mism & ~amb).any(), f"{(mism & ~amb).sum()} unflagged radius/tiles mismatches"
+    assert mism.sum() <= max(2, int(1e-4 * mism.size))
+    ok = ~mism
+    np.testing.assert_allclose(N(conic)[ok], oc[ok], rtol=2e-5, atol=1e-7)
+    assert (orad > 0).sum() > 1000
+
+
+def test_ewa_project_golden():
+    g = load("ewa_project")
+    conic, radius, tiles = ms.ewa_project(T(g["xyz"]), T(g["cov3d"]), T(g["intr"]), T(g["extr"]), T(g["uv"]),
+                                          g["W"], g["H"], T(g["visible"]))
+    oc, orad, otil, amb = oracle.ewa_project_forward(g["xyz"], g["cov3d"], g["intr"], g["extr"], g["uv"],
+                                                     g["W"], g["H"], g["visible"])
+    mism = (N(radius) != orad) | (N(tiles) != otil)
+    assert not (mism & ~amb).any()
+    # and against the reference's own PyTorch restatement, as its test does
+    mism_ref = (N(radius) != g["radius"]) | (N(tiles) != g["tiles"])
+    assert mism_ref.sum() <= 2
+
+
+def test_ewa_project_backward():
+    s, intr, extr, uv, vis, cov, W, H = ewa_inputs(n=20000, seed=2)
+    xyz = T(s["xyz"]).requires_grad_()
+    tc = T(cov).requires_grad_()
+    ti, te = T(intr).requires_grad_(), T(extr).requires_grad_()
+    conic, radius, tiles = ms.ewa_project(xyz, tc, ti, te, T(uv), W, H, T(vis))
+    w = np.random.default_rng(3).normal(size=conic.shape).astype(np.float32)
+    (conic * T(w)).sum().backward()
+    dx, dc, di, de = oracle.ewa_project_backward(s["xyz"].numpy(), cov, intr, extr, N(radius), w)
+    rel_close(N(xyz.grad), dx, what="dL/dxyz")
+    rel_close(N(tc.grad), dc, what="dL/dcov3d")
+    rel_close(N(ti.grad), di, what="dL/dintr")
+    rel_close(N(te.grad), de, what="dL/dextr")
+
+
+# -------------------------------------------------------------------- SH
+@pytest.mark.parametrize("deg", list(range(11)))
+@pytest.mark.parametrize("C", [1, 3, 5])
+def test_compute_sh(deg, C):
+    rng = np.random.default_rng(deg * 10 + C)
+    P = 3000
+    D = (deg + 1) ** 2
+    shs = rng.normal(scale=0.3, size=(P, C, D)).astype(np.float32)
+    d = rng.normal(size=(P, 3))
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    d = d.astype(np.float32)
+    vis = rng.random(P) > 0.1
+    tsh, td = T(shs).requires_grad_(), T(d).requires_grad_()
+    val = ms.compute_sh(tsh, td, T(vis))
+    oval = oracle.compute_sh_forward(shs, d, vis)
+    rel_close(N(val), oval, rtol=2e-6, what="value")
+    w = rng.normal(size=(P, C)).astype(np.float32)
+    (val * T(w)).sum().backward()
+    dsh, dd = oracle.compute_sh_backward(shs, d, vis, w)
+    rel_close(N(tsh.grad), dsh, rtol=2e-6, what="dL/dsh")
+    rel_close(N(td.grad), dd, rtol=1e-4, what="dL/ddir")
+
+
+def test_compute_sh_golden():
+    g = load("compute_sh")
+    val = ms.compute_sh(T(g["sh_coeffs"]), T(g["viewdirs"]))
+    np.testing.assert_allclose(N(val), g["value"], rtol=1e-5, atol=5e-4)
+
+
+# ------------------------------------------------------------------ sort
+def sort_inputs(n=50000, W=640, H=480, seed=0):
+    s, intr, extr, uv, vis, cov, W, H = ewa_inputs(n, W, H, seed)
+    conic, radius, tiles, _ = oracle.ewa_project_forward(s["xyz"].numpy(), cov, intr, extr, uv, W, H, vis)
+    d, = [oracle.project_point_forward(s["xyz"].numpy(), intr, extr, W, H)[1]]
+    return uv, d, radius, tiles, W, H
+
+
+def check_sort(uv, d, radius, tiles, W, H):
+    idx, tr = ms.sort_gaussian(T(uv), T(d), W, H, T(radius, torch.int32), T(tiles, torch.int32))
+    oidx, otr = oracle.sort_gaussian(uv, d, W, H, radius, tiles)
+    np.testing.assert_array_equal(N(tr), otr)
+    np.testing.assert_array_equal(N(idx), oidx)
+    return oidx
+
+
+def test_sort_known_answer():
+    g = load("sort_known_answer")
+    idx, tr = ms.sort_gaussian(T(g["uv"]), T(g["depth"]), g["W"], g["H"], T(g["radius"]), T(g["tiles"]))
+    np.testing.assert_array_equal(N(idx), g["idx_sorted"])
+    np.testing.assert_array_equal(N(tr), g["tile_range"])
+
+
+@pytest.mark.parametrize("seed", [0, 1])
+def test_sort_random(seed):
+    oidx = check_sort(*sort_inputs(seed=seed))
+    assert oidx.size > 100000
+
+
+def test_sort_depth_ties_follow_gaussian_id():
+    uv, d, radius, tiles, W, H = sort_inputs(20000, seed=3)
+    d = np.round(d * 8) / 8  # heavy depth-bit collisions
+    check_sort(uv, d.astype(np.float32), radius, tiles, W, H)
+
+
+def test_sort_negative_depths_lead_and_stay_out_of_ranges():
+    uv, d, radius, tiles, W, H = sort_inputs(20000, seed=4)
+    d = d.copy()
+    d[::7] *= -1.0
+    d[::11] = -0.0
+    oidx = check_sort(uv, d, radius, tiles, W, H)
+    assert oidx.size > 0
+
+
+def test_sort_filler_slots_use_reference_layout():
+    g = load("alpha_blending")  # radius 0 with tiles > 0: zero-filled slots
+    idx, tr = ms.sort_gaussian(T(g["uv"]), T(g["depth"]), g["W"], g["H"], T(g["radius"]),
+                               T(g["tiles"], torch.int32))
+    np.testing.assert_array_equal(N(idx), g["idx_sorted"])
+    np.testing.assert_array_equal(N(tr), g["tile_range"])
+
+
+def test_sort_empty():
+    z = np.zeros((0, 2), np.float32)
+    idx, tr = ms.sort_gaussian(T(z), T(np.zeros((0, 1), np.float32)), 64, 48, T(np.zeros(0, np.int32)),
+                               T(np.zeros(0, np.int32)))
+    assert idx.numel() == 0 and tr.shape == (12, 2) and int(tr.abs().sum()) == 0
+    uv, d, radius, tiles, W, H = sort_inputs(1000, seed=5)
+    idx, tr = ms.sort_gaussian(T(uv), T(d), W, H, T(np.zeros_like(radius)), T(np.zeros_like(tiles)))
+    assert idx.numel() == 0 and int(tr.abs().sum()) == 0
+
+
+def test_radix_sort_i64_matches_stable_sort():
+    from msplat_gb300 import _lib
+    lib = _lib.load()
+    rng = np.random.default_rng(0)
+    n = 300000
+    keys = rng.integers(-2**40, 2**40, size=n, dtype=np.int64)
+    keys[::3] = keys[1::3][: len(keys[::3])]  # duplicates
+    vals = np.arange(n, dtype=np.int32)
+    tk, tv = T(keys), T(vals)
+    ko, vo = torch.empty_like(tk), torch.empty_like(tv)
+    ws = _lib.workspace(lib.msplat_radix_sort_i64_workspace_size(n), tk.device)
+    _lib.check(lib.msplat_radix_sort_i64_pairs(n, tk.data_ptr(), tv.data_ptr(), ko.data_ptr(), vo.data_ptr(), 0, 64,
+                                               ws.data_ptr(), ws.numel(), _lib.stream()), "sort")
+    order = np.argsort(keys, kind="stable")
+    np.testing.assert_array_equal(N(ko), keys[order])
+    np.testing.assert_array_equal(N(vo), vals[order])
+
+
+# ----------------------------------------------------------------- blend
+def blend_inputs(n=10000, W=256, H=256, C=3, seed=0):
+    s = scene(n, seed, C=C)
+    intr, extr = camera(W, H, front=True)
+    out, inter = oracle.rasterization_forward(s["xyz"].numpy(), s["scale"].numpy(), s["rot"].numpy(),
+                                              s["opacity"].numpy(), s["feat"].numpy(), intr, extr, W, H, 0.0)
+    return s, inter, W, H
+
+
+@pytest.mark.parametrize("C", [1, 3, 4, 5, 16, 33, 40])
+def test_alpha_blending_forward(C):
+    s, it, W, H = blend_inputs(C=C, seed=C)
+    bg = 0.25
+    args = (T(it["uv"]), T(it["conic"]), T(s["opacity"]), T(s["feat"]), T(it["idx_sorted"]), T(it["tile_range"]))
+    out = ms.alpha_blending(*args, bg, W, H)
+    oout, oT, onc, amb = oracle.alpha_blending_forward(it["uv"], it["conic"], s["opacity"].numpy(),
+                                                       s["feat"].numpy(), it["idx_sorted"], it["tile_range"], bg, W, H)
+    ok = ~amb
+    assert ok.mean() > 0.99
+    err = np.abs(N(out) - oout)[:, ok].max()
+    assert err <= 1e-5, err
+
+
+def test_alpha_blending_final_T_and_ncontrib():
+    from msplat_gb300 import _lib
+    s, it, W, H = blend_inputs(C=3, seed=11)
+    lib = _lib.load()
+    P = s["feat"].shape[0]
+    outs = [torch.empty(3, H, W, device=DEV), torch.empty(H, W, device=DEV),
+            torch.empty(H, W, dtype=torch.int32, device=DEV)]
+    ins = [T(it["uv"]), T(it["conic"]), T(s["opacity"]), T(s["feat"]), T(it["idx_sorted"]), T(it["tile_range"])]
+    _lib.check(lib.msplat_alpha_blending_forward(P, 3, *[x.data_ptr() for x in ins], 0.0, W, H,
+                                                 *[x.data_ptr() for x in outs], _lib.stream()), "blend")
+    oout, oT, onc, amb = oracle.alpha_blending_forward(it["uv"], it["conic"], s["opacity"].numpy(),
+                                                       s["feat"].numpy(), it["idx_sorted"], it["tile_range"], 0.0, W, H)
+    ok = ~amb
+    assert (N(outs[2])[ok] == onc[ok]).mean() > 0.9999
+    np.testing.assert_allclose(N(outs[1])[ok], oT[ok], rtol=1e-5, atol=1e-7)
+
+
+def test_alpha_blending_golden():
+    g = load("alpha_blending")
+    args = [T(g["uv"]), T(g["conic"]), T(g["opacity"]), T(g["feature"]), T(g["idx_sorted"]), T(g["tile_range"])]
+    for a in args[:4]:
+        a.requires_grad_()
+    out = ms.alpha_blending(*args, float(g["bg"]), g["W"], g["H"])
+    np.testing.assert_allclose(N(out), g["out"], rtol=1.3e-6, atol=1e-5)
+    out.sum().backward()
+    for a, key in zip(args[:4], ["dL_duv", "dL_dconic", "dL_dopacity", "dL_dfeature"]):
+        np.testing.assert_allclose(N(a.grad), g[key].reshape(a.shape), rtol=1e-4,
+                                   atol=1e-5 * max(1.0, np.abs(g[key]).max()))
+
+
+@pytest.mark.parametrize("C,bg", [(3, 0.0), (3, 0.7), (13, 0.3), (33, 1.0)])
+def test_alpha_blending_backward(C, bg):
+    s, it, W, H = blend_inputs(n=6000, C=C, seed=20 + C)
+    ins = [T(it["uv"]), T(it["conic"]), T(s["opacity"]), T(s["feat"])]
+    for a in ins:
+        a.requires_grad_()
+    out = ms.alpha_blending(*ins, T(it["idx_sorted"]), T(it["tile_range"]), bg, W, H)
+    w = np.random.default_rng(C).normal(size=out.shape).astype(np.float32)
+    (out * T(w)).sum().backward()
+    oout, oT, onc, amb = oracle.alpha_blending_forward(it["uv"], it["conic"], s["opacity"].numpy(),
+                                                       s["feat"].numpy(), it["idx_sorted"], it["tile_range"], bg, W, H)
+    grads = oracle.alpha_blending_backward(it["uv"], it["conic"], s["opacity"].numpy(), s["feat"].numpy(),
+                                           it["idx_sorted"], it["tile_range"], bg, W, H, oT, onc, w)
+    for a, ref, name in zip(ins, grads, ["uv", "conic", "opacity", "feature"]):
+        rel_close(N(a.grad).reshape(ref.shape), ref, rtol=1e-4, what=f"dL/d{name}")
+
+
+# ------------------------------------------------------------- pipeline
+def test_rasterization_matches_oracle_pipeline():
+    s, it, W, H = blend_inputs(n=10000, seed=3)
+    intr, extr = camera(W, H, front=True)
+    img = ms.rasterization(T(s["xyz"]), T(s["scale"]), T(s["rot"]), T(s["opacity"]), T(s["feat"]), T(intr),
+                           T(extr), W, H, 0.0)
+    ref = oracle.rasterization_forward(s["xyz"].numpy(), s["scale"].numpy(), s["rot"].numpy(),
+                                       s["opacity"].numpy(), s["feat"].numpy(), intr, extr, W, H, 0.0)[0]
+    amb = it["blend_ambiguous"]
+    err = np.abs(N(img) - ref)[:, ~amb].max()
+    assert err <= 1e-5, err
