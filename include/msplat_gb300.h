@@ -187,7 +187,7 @@ MSPLAT_API int msplat_radix_sort_i64_pairs(int64_t n, const int64_t *keys_in,
  * When counts[1] != 0 the caller uses the reference-layout path
  * (compute_gaussian_key + radix_sort_i64_pairs + tile range), which
  * reproduces the zero-filled slots exactly.                                */
-MSPLAT_API size_t msplat_sort_prepare_workspace_size(int P);
+MSPLAT_API size_t msplat_sort_prepare_workspace_size(int P, int W, int H);
 MSPLAT_API size_t msplat_sort_finish_workspace_size(int P, int64_t num_intersects,
                                          int W, int H);
 MSPLAT_API int msplat_sort_gaussian_prepare(int P, const float *depth,

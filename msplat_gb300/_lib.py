@@ -42,7 +42,7 @@ _SIGNATURES = {
     "msplat_inclusive_scan_i32": (_I, [_I, _P, _P, _P, _P, _SZ, _P]),
     "msplat_radix_sort_i64_workspace_size": (_SZ, [_I64]),
     "msplat_radix_sort_i64_pairs": (_I, [_I64, _P, _P, _P, _P, _I, _I, _P, _SZ, _P]),
-    "msplat_sort_prepare_workspace_size": (_SZ, [_I]),
+    "msplat_sort_prepare_workspace_size": (_SZ, [_I, _I, _I]),
     "msplat_sort_finish_workspace_size": (_SZ, [_I, _I64, _I, _I]),
     "msplat_sort_gaussian_prepare": (_I, [_I, _P, _P, _P, _P, _I, _I, _P, _P, _SZ, _P]),
     "msplat_sort_gaussian_finish": (

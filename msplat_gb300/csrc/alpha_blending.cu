@@ -328,6 +328,384 @@ blend_bwd_kernel(int P, int C, int c0, const float2 *__restrict__ uv, const floa
     }
 }
 
+
+// ===================================================================
+// Several pixels per thread, C <= 4 channels (the common RGB case).
+//
+// A thread owns NPIX pixels of one tile column (rows ly, ly + 16/NPIX, ...),
+// so each gathered Gaussian is read from shared memory once per NPIX pixels
+// and, in the backward, the per-Gaussian sums over a warp cover 32 * NPIX
+// pixels per reduction.  Pairs of pixels are evaluated with packed f32x2
+// arithmetic.  The reference's per-pair expression
+//   power = -0.5f * (a*dx*dx + c*dy*dy) - b*dx*dy
+// is spelled out with the FMA contractions the compiler gives it in the
+// one-pixel kernels above (the product a*dx*dx fused into the sum, b*dx*dy
+// fused into the scaling), so every pixel sees bit-identical powers,
+// alphas, transmittances and contributor counts.
+// ===================================================================
+
+template <int NPIX>
+struct PixPow {
+    float v[NPIX];
+};
+
+template <int NPIX>
+__device__ __forceinline__ PixPow<NPIX> blend_power_n(float a, float b, float c, float dx,
+                                                      const float (&dy)[NPIX]) {
+    PixPow<NPIX> out;
+    const float adx = __fmul_rn(a, dx), bdx = __fmul_rn(b, dx);
+#pragma unroll
+    for (int i = 0; i < NPIX; i += 2) {
+        if (i + 1 < NPIX) {
+            const float2 d = make_float2(dy[i], dy[i + 1]);
+            const float2 cdd = __fmul2_rn(__fmul2_rn(make_float2(c, c), d), d);
+            const float2 s = __ffma2_rn(make_float2(adx, adx), make_float2(dx, dx), cdd);
+            const float2 bdd = __fmul2_rn(make_float2(bdx, bdx), d);
+            const float2 pw = __ffma2_rn(make_float2(-0.5f, -0.5f), s, make_float2(-bdd.x, -bdd.y));
+            out.v[i] = pw.x;
+            out.v[i + 1] = pw.y;
+        } else {
+            const float s = __fmaf_rn(adx, dx, __fmul_rn(__fmul_rn(c, dy[i]), dy[i]));
+            out.v[i] = __fmaf_rn(-0.5f, s, -__fmul_rn(bdx, dy[i]));
+        }
+    }
+    return out;
+}
+
+// Gathers NPIX entries per thread (thread t owns list positions
+// base + dir * (t * NPIX + r)) and compacts the kept ones into shared
+// memory in list order.  Returns the number kept.
+template <int C, int NPIX, bool WITH_ID>
+__device__ __forceinline__ int gather_small(int base, int dir, int lo, int hi,
+                                            const int32_t *__restrict__ idx_sorted,
+                                            const float2 *__restrict__ uv, const float *__restrict__ conic,
+                                            const float *__restrict__ opacity,
+                                            const float *__restrict__ feature, float bx0, float by0,
+                                            float4 *sA, float4 *sB, float4 *sF, int *sG, int *scan) {
+    constexpr int NT = kTilePixels / NPIX;
+    float4 A[NPIX], B[NPIX], F[NPIX];
+    int G[NPIX];
+    bool keep[NPIX];
+    int nk = 0;
+#pragma unroll
+    for (int r = 0; r < NPIX; ++r) {
+        const int j = base + dir * ((int)threadIdx.x * NPIX + r);
+        keep[r] = false;
+        if (j >= lo && j < hi) {
+            const int g = idx_sorted[j];
+            const float2 p = uv[g];
+            const float ca = conic[3 * g], cb = conic[3 * g + 1], cc = conic[3 * g + 2];
+            const float op = opacity[g];
+            keep[r] = !cull_tile(p.x, p.y, ca, cb, cc, op, bx0, by0);
+            A[r] = make_float4(p.x, p.y, ca, cb);
+            B[r] = make_float4(cc, op, power_bound(op), __int_as_float(j));
+            float f[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+            for (int q = 0; q < C; ++q) f[q] = feature[(size_t)g * C + q];
+            F[r] = make_float4(f[0], f[1], f[2], f[3]);
+            G[r] = g;
+        }
+        nk += keep[r];
+    }
+    // Block exclusive scan of the per-thread counts (NT <= 256 threads).
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    int inc = nk;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int n = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= o) inc += n;
+    }
+    if (lane == 31) scan[warp] = inc;
+    __syncthreads();
+    int wbase = 0, total = 0;
+#pragma unroll
+    for (int w = 0; w < NT / 32; ++w) {
+        const int c = scan[w];
+        wbase += (w < warp) ? c : 0;
+        total += c;
+    }
+    int pos = wbase + inc - nk;
+#pragma unroll
+    for (int r = 0; r < NPIX; ++r) {
+        if (keep[r]) {
+            sA[pos] = A[r];
+            sB[pos] = B[r];
+            sF[pos] = F[r];
+            if (WITH_ID) sG[pos] = G[r];
+            ++pos;
+        }
+    }
+    __syncthreads();
+    return total;
+}
+
+template <int C, int NPIX>
+__global__ void __launch_bounds__(kTilePixels / NPIX)
+blend_fwd_small_kernel(int P, const float2 *__restrict__ uv, const float *__restrict__ conic,
+                       const float *__restrict__ opacity, const float *__restrict__ feature,
+                       const int32_t *__restrict__ idx_sorted, const int2 *__restrict__ tile_range, float bg,
+                       int W, int H, float *__restrict__ out, float *__restrict__ final_T,
+                       int32_t *__restrict__ ncontrib) {
+    constexpr int NT = kTilePixels / NPIX, RS = kTile / NPIX;
+    __shared__ float4 sA[kBatch], sB[kBatch], sF[kBatch];
+    __shared__ int scan[NT / 32];
+    const int gxn = (W + kTile - 1) / kTile;
+    const int2 range = tile_range[blockIdx.y * gxn + blockIdx.x];
+    const int px = blockIdx.x * kTile + (threadIdx.x & (kTile - 1));
+    const int py0 = blockIdx.y * kTile + (threadIdx.x >> 4);
+    const float fx = (float)px;
+    const float bx0 = (float)(blockIdx.x * kTile), by0 = (float)(blockIdx.y * kTile);
+    float fy[NPIX], T[NPIX], F[NPIX][4];
+    int last[NPIX];
+    bool done[NPIX];
+#pragma unroll
+    for (int i = 0; i < NPIX; ++i) {
+        const int py = py0 + i * RS;
+        fy[i] = (float)py;
+        T[i] = 1.0f;
+        last[i] = 0;
+        done[i] = !(px < W && py < H);
+#pragma unroll
+        for (int q = 0; q < 4; ++q) F[i][q] = 0.0f;
+    }
+    for (int start = range.x; start < range.y; start += kBatch) {
+        bool all_done = true;
+#pragma unroll
+        for (int i = 0; i < NPIX; ++i) all_done &= done[i];
+        if (__syncthreads_count(all_done) == NT) break;
+        const int n = gather_small<C, NPIX, false>(start, 1, range.x, range.y, idx_sorted, uv, conic, opacity,
+                                                   feature, bx0, by0, sA, sB, sF, nullptr, scan);
+        for (int k = 0; k < n; ++k) {
+            bool ad = true;
+#pragma unroll
+            for (int i = 0; i < NPIX; ++i) ad &= done[i];
+            if (ad) break;
+            const float4 A = sA[k], B = sB[k];
+            const float dx = A.x - fx;
+            float dy[NPIX];
+#pragma unroll
+            for (int i = 0; i < NPIX; ++i) dy[i] = A.y - fy[i];
+            const PixPow<NPIX> pw = blend_power_n<NPIX>(A.z, A.w, B.x, dx, dy);
+            const float4 f = sF[k];
+            const float fv[4] = {f.x, f.y, f.z, f.w};
+#pragma unroll
+            for (int i = 0; i < NPIX; ++i) {
+                const float power = pw.v[i];
+                if (done[i] || power > 0.0f || power < B.z) continue;
+                const float alpha = fminf(0.99f, B.y * __expf(power));
+                if (alpha < 1.0f / 255.0f) continue;
+                const float nT = T[i] * (1.0f - alpha);
+                if (nT < 0.0001f) {
+                    done[i] = true;
+                    continue;
+                }
+#pragma unroll
+                for (int q = 0; q < C; ++q) F[i][q] += fv[q] * alpha * T[i];
+                T[i] = nT;
+                last[i] = __float_as_int(B.w) - range.x + 1;
+            }
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < NPIX; ++i) {
+        const int py = py0 + i * RS;
+        if (px < W && py < H) {
+            const int pix = py * W + px;
+            final_T[pix] = T[i];
+            ncontrib[pix] = last[i];
+#pragma unroll
+            for (int q = 0; q < C; ++q) out[(size_t)q * H * W + pix] = F[i][q] + T[i] * bg;
+        }
+    }
+}
+
+// Reduce-scatter of NV (power of two, 8 or 16) values over a warp: lane l
+// returns the warp total of value (l >> (5 - log2 NV)).
+template <int NV>
+__device__ __forceinline__ float warp_reduce_scatter(float (&v)[NV]) {
+    const int lane = threadIdx.x & 31;
+    constexpr int LOG = NV == 16 ? 4 : 3;
+    constexpr int OMIN = 32 >> LOG;  // smallest halving offset
+#pragma unroll
+    for (int o = 16, n = NV; o >= OMIN; o >>= 1, n >>= 1) {
+        const bool up = (lane & o) != 0;
+        const int h = n >> 1;
+#pragma unroll
+        for (int k = 0; k < h; ++k) {
+            const float send = up ? v[k] : v[k + h];
+            const float keep = up ? v[k + h] : v[k];
+            v[k] = keep + __shfl_xor_sync(0xffffffffu, send, o);
+        }
+    }
+    float r = v[0];
+#pragma unroll
+    for (int o = OMIN >> 1; o > 0; o >>= 1) r += __shfl_xor_sync(0xffffffffu, r, o);
+    return r;
+}
+
+template <int C, int NPIX>
+__global__ void __launch_bounds__(kTilePixels / NPIX)
+blend_bwd_small_kernel(int P, const float2 *__restrict__ uv, const float *__restrict__ conic,
+                       const float *__restrict__ opacity, const float *__restrict__ feature,
+                       const int32_t *__restrict__ idx_sorted, const int2 *__restrict__ tile_range, float bg,
+                       int W, int H, const float *__restrict__ final_T, const int32_t *__restrict__ ncontrib,
+                       const float *__restrict__ dL_dout, float *__restrict__ dL_duv,
+                       float *__restrict__ dL_dconic, float *__restrict__ dL_dopacity,
+                       float *__restrict__ dL_dfeature) {
+    constexpr int NT = kTilePixels / NPIX, RS = kTile / NPIX;
+    constexpr int NV = (6 + C) <= 8 ? 8 : 16;
+    constexpr int LOG = NV == 16 ? 4 : 3;
+    __shared__ float4 sA[kBatch], sB[kBatch], sF[kBatch];
+    __shared__ int sG[kBatch];
+    __shared__ int scan[NT / 32];
+    __shared__ int smax;
+    const int gxn = (W + kTile - 1) / kTile;
+    const int2 range = tile_range[blockIdx.y * gxn + blockIdx.x];
+    const int px = blockIdx.x * kTile + (threadIdx.x & (kTile - 1));
+    const int py0 = blockIdx.y * kTile + (threadIdx.x >> 4);
+    const float fx = (float)px;
+    const float bx0 = (float)(blockIdx.x * kTile), by0 = (float)(blockIdx.y * kTile);
+    const int lane = threadIdx.x & 31;
+
+    float fy[NPIX], T[NPIX], Tf[NPIX], la[NPIX], bgd[NPIX];
+    float dp[NPIX][4], acc[NPIX][4], lf[NPIX][4];
+    int last[NPIX];
+    int mylast = 0;
+#pragma unroll
+    for (int i = 0; i < NPIX; ++i) {
+        const int py = py0 + i * RS;
+        const bool in = px < W && py < H;
+        const int pix = py * W + px;
+        fy[i] = (float)py;
+        Tf[i] = in ? final_T[pix] : 0.0f;
+        T[i] = Tf[i];
+        last[i] = in ? ncontrib[pix] : 0;
+        mylast = max(mylast, last[i]);
+        la[i] = 0.0f;
+        bgd[i] = 0.0f;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            dp[i][q] = (in && q < C) ? dL_dout[(size_t)q * H * W + pix] : 0.0f;
+            acc[i][q] = 0.0f;
+            lf[i][q] = 0.0f;
+            if (q < C) bgd[i] += bg * dp[i][q];
+        }
+    }
+    if (threadIdx.x == 0) smax = 0;
+    __syncthreads();
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) mylast = max(mylast, __shfl_xor_sync(0xffffffffu, mylast, o));
+    if (lane == 0) atomicMax(&smax, mylast);
+    __syncthreads();
+    const int end = range.x + min(smax, range.y - range.x);
+
+    for (int bend = end; bend > range.x; bend -= kBatch) {
+        const int bstart = max(range.x, bend - kBatch);
+        const int n = gather_small<C, NPIX, true>(bend - 1, -1, bstart, bend, idx_sorted, uv, conic, opacity,
+                                                  feature, bx0, by0, sA, sB, sF, sG, scan);
+        for (int k = 0; k < n; ++k) {
+            const float4 A = sA[k], B = sB[k];
+            const int jl = __float_as_int(B.w) - range.x;
+            const float dx = A.x - fx;
+            float dy[NPIX];
+#pragma unroll
+            for (int i = 0; i < NPIX; ++i) dy[i] = A.y - fy[i];
+            const PixPow<NPIX> pw = blend_power_n<NPIX>(A.z, A.w, B.x, dx, dy);
+            const float4 f = sF[k];
+            const float fv[4] = {f.x, f.y, f.z, f.w};
+            const float ca = A.z, cb = A.w, cc = B.x, op = B.y;
+            float v[NV];
+#pragma unroll
+            for (int q = 0; q < NV; ++q) v[q] = 0.0f;
+            bool any = false;
+#pragma unroll
+            for (int i = 0; i < NPIX; ++i) {
+                const float power = pw.v[i];
+                if (jl >= last[i] || power > 0.0f || power < B.z) continue;
+                const float G = __expf(power);
+                const float alpha = fminf(0.99f, op * G);
+                if (alpha < 1.0f / 255.0f) continue;
+                any = true;
+                T[i] = T[i] / (1.f - alpha);
+                const float dcol = alpha * T[i];
+                float dL_dalpha = 0.0f;
+#pragma unroll
+                for (int q = 0; q < C; ++q) {
+                    acc[i][q] = la[i] * lf[i][q] + (1.f - la[i]) * acc[i][q];
+                    lf[i][q] = fv[q];
+                    dL_dalpha += (fv[q] - acc[i][q]) * dp[i][q];
+                    v[6 + q] += dcol * dp[i][q];
+                }
+                dL_dalpha *= T[i];
+                la[i] = alpha;
+                dL_dalpha += (-Tf[i] / (1.f - alpha)) * bgd[i];
+                const float dL_dG = op * dL_dalpha;
+                const float ddx = dx, ddy = dy[i];
+                v[0] += dL_dG * (-G * ddx * ca - G * ddy * cb);
+                v[1] += dL_dG * (-G * ddy * cc - G * ddx * cb);
+                v[2] += -0.5f * G * ddx * ddx * dL_dG;
+                v[3] += -G * ddx * ddy * dL_dG;
+                v[4] += -0.5f * G * ddy * ddy * dL_dG;
+                v[5] += G * dL_dalpha;
+            }
+            if (__any_sync(0xffffffffu, any)) {
+                const float s = warp_reduce_scatter<NV>(v);
+                const int vi = lane >> (5 - LOG);
+                if ((lane & ((1 << (5 - LOG)) - 1)) == 0 && vi < 6 + C) {
+                    const int g = sG[k];
+                    float *dst;
+                    if (vi < 2) dst = dL_duv + 2 * g + vi;
+                    else if (vi < 5) dst = dL_dconic + 3 * g + (vi - 2);
+                    else if (vi == 5) dst = dL_dopacity + g;
+                    else dst = dL_dfeature + (size_t)g * C + (vi - 6);
+                    atomicAdd(dst, s);
+                }
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// Pixels per thread of the C <= 4 kernels (compile-time tunables).
+#ifndef MSPLAT_BLEND_NPIX_FWD
+#define MSPLAT_BLEND_NPIX_FWD 2
+#endif
+#ifndef MSPLAT_BLEND_NPIX_BWD
+#define MSPLAT_BLEND_NPIX_BWD 2
+#endif
+constexpr int kBlendNpixFwd = MSPLAT_BLEND_NPIX_FWD;
+constexpr int kBlendNpixBwd = MSPLAT_BLEND_NPIX_BWD;
+
+template <int C>
+void launch_small(bool bwd, dim3 grid, cudaStream_t stream, int P, const float2 *uv, const float *conic,
+                  const float *opacity, const float *feature, const int32_t *idx, const int2 *tr, float bg, int W,
+                  int H, float *out, float *final_T, int32_t *nc, const float *fT, const int32_t *nci,
+                  const float *dout, float *duv, float *dcon, float *dop, float *dfeat) {
+    if (!bwd)
+        blend_fwd_small_kernel<C, kBlendNpixFwd><<<grid, kTilePixels / kBlendNpixFwd, 0, stream>>>(
+            P, uv, conic, opacity, feature, idx, tr, bg, W, H, out, final_T, nc);
+    else
+        blend_bwd_small_kernel<C, kBlendNpixBwd><<<grid, kTilePixels / kBlendNpixBwd, 0, stream>>>(
+            P, uv, conic, opacity, feature, idx, tr, bg, W, H, fT, nci, dout, duv, dcon, dop, dfeat);
+}
+
+inline void dispatch_small(bool bwd, int C, dim3 grid, cudaStream_t stream, int P, const float2 *uv,
+                           const float *conic, const float *opacity, const float *feature, const int32_t *idx,
+                           const int2 *tr, float bg, int W, int H, float *out, float *final_T, int32_t *nc,
+                           const float *fT, const int32_t *nci, const float *dout, float *duv, float *dcon,
+                           float *dop, float *dfeat) {
+    switch (C) {
+#define MSPLAT_SMALL(CC)                                                                                       \
+    case CC:                                                                                                   \
+        launch_small<CC>(bwd, grid, stream, P, uv, conic, opacity, feature, idx, tr, bg, W, H, out, final_T,   \
+                         nc, fT, nci, dout, duv, dcon, dop, dfeat);                                           \
+        break;
+        MSPLAT_SMALL(1) MSPLAT_SMALL(2) MSPLAT_SMALL(3) MSPLAT_SMALL(4)
+#undef MSPLAT_SMALL
+        default: break;
+    }
+}
+
 }  // namespace msplat
 
 using namespace msplat;
@@ -343,6 +721,12 @@ extern "C" int msplat_alpha_blending_forward(int P, int C, const float *uv, cons
     if (!tile_range || !out || !final_T || !ncontrib || (P > 0 && (!uv || !conic || !opacity || !feature)))
         return set_error(MSPLAT_ERR_INVALID_ARGUMENT, "alpha_blending_forward: null pointer");
     const dim3 grid(ceil_div(W, kTile), ceil_div(H, kTile));
+    if (C <= 4) {
+        dispatch_small(false, C, grid, stream, P, (const float2 *)uv, conic, opacity, feature, idx_sorted,
+                       (const int2 *)tile_range, bg, W, H, out, final_T, ncontrib, nullptr, nullptr, nullptr,
+                       nullptr, nullptr, nullptr, nullptr);
+        return check_launch("alpha_blending_forward");
+    }
     for (int c0 = 0; c0 < C; c0 += 32) {
         const int nc = min(32, C - c0);
         if (nc <= 4)
@@ -375,6 +759,12 @@ extern "C" int msplat_alpha_blending_backward(int P, int C, const float *uv, con
         return set_error(MSPLAT_ERR_INVALID_ARGUMENT, "alpha_blending_backward: null pointer");
     if (P == 0) return MSPLAT_OK;
     const dim3 grid(ceil_div(W, kTile), ceil_div(H, kTile));
+    if (C <= 4) {
+        dispatch_small(true, C, grid, stream, P, (const float2 *)uv, conic, opacity, feature, idx_sorted,
+                       (const int2 *)tile_range, bg, W, H, nullptr, nullptr, nullptr, final_T, ncontrib, dL_dout,
+                       dL_duv, dL_dconic, dL_dopacity, dL_dfeature);
+        return check_launch("alpha_blending_backward");
+    }
     for (int c0 = 0; c0 < C; c0 += kBwdC)
         blend_bwd_kernel<<<grid, kBlendThreads, 0, stream>>>(P, C, c0, (const float2 *)uv, conic, opacity, feature,
                                                              idx_sorted, (const int2 *)tile_range, bg, W, H, final_T,

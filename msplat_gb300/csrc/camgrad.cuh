@@ -38,15 +38,18 @@ __device__ __forceinline__ void block_partial_16(float (&vals)[kCamGradVals],
 }
 
 // Fixed-order sum of `nblocks` partial rows; writes (does not accumulate)
-// dL_dintr[4] and dL_dextr[12], either of which may be null.
-static __global__ void cam_grad_finalize_kernel(int nblocks,
-                                                const float *__restrict__ partials,
-                                                float *__restrict__ dL_dintr,
-                                                float *__restrict__ dL_dextr) {
-    const int k = threadIdx.x;
-    if (k >= kCamGradVals) return;
+// dL_dintr[4] and dL_dextr[12], either of which may be null.  Launched with
+// 16 warps: warp k sums column k, each lane a strided subset in double, then
+// a fixed shuffle tree -- deterministic and latency-parallel.
+static __global__ void __launch_bounds__(32 * kCamGradVals)
+cam_grad_finalize_kernel(int nblocks, const float *__restrict__ partials,
+                         float *__restrict__ dL_dintr, float *__restrict__ dL_dextr) {
+    const int k = threadIdx.x >> 5, lane = threadIdx.x & 31;
     double s = 0.0;
-    for (int b = 0; b < nblocks; ++b) s += (double)partials[b * kCamGradVals + k];
+    for (int b = lane; b < nblocks; b += 32) s += (double)partials[b * kCamGradVals + k];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane != 0) return;
     if (k < 4) {
         if (dL_dintr) dL_dintr[k] = (float)s;
     } else if (dL_dextr) {

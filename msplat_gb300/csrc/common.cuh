@@ -22,8 +22,8 @@ inline int check_launch(const char *what) {
     return MSPLAT_OK;
 }
 
-inline int ceil_div(int a, int b) { return (a + b - 1) / b; }
-inline int64_t ceil_div64(int64_t a, int64_t b) { return (a + b - 1) / b; }
+__host__ __device__ inline int ceil_div(int a, int b) { return (a + b - 1) / b; }
+__host__ __device__ inline int64_t ceil_div64(int64_t a, int64_t b) { return (a + b - 1) / b; }
 
 // Number of SMs of the current device (cached per device).
 int num_sms();

@@ -94,7 +94,6 @@ __device__ __forceinline__ void sh_basis(float x, float y, float z, Emit &&emit)
                 qu = (float)(2 * m + 1) * z * qu1;
                 zu = (float)(2 * m + 1) * qu1;
             } else {
-                constexpr float dummy = 0.f; (void)dummy;
                 const float a = (float)(2 * l - 1), b = (float)(l + m - 1), ic = 1.0f / (float)(l - m);
                 qu = (a * z * qu1 - b * qu2) * ic;
                 zu = (a * (qu1 + z * zu1) - b * zu2) * ic;
@@ -146,25 +145,61 @@ __device__ __forceinline__ void sh_basis(float x, float y, float z, Emit &&emit)
 
 constexpr int kShChanBlock = 4;
 
-// Copies rows [p0, p0 + n) of a [*, CD] array into shared memory rows of
-// `stride` floats, one warp per row (coalesced).
+// Copies n contiguous rows of CD floats from global memory into shared
+// memory rows of `stride` floats (odd, against bank conflicts).  The chunk is
+// read as a flat, coalesced stream -- 16-byte vectors when aligned -- with
+// many loads in flight per thread.
 __device__ __forceinline__ void stage_rows(float *dst, const float *__restrict__ src, int n, int CD,
                                            int stride) {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    for (int p = warp; p < n; p += nw) {
-        const float *s = src + (size_t)p * CD;
-        float *d = dst + p * stride;
-        for (int k = lane; k < CD; k += 32) d[k] = __ldcs(s + k);
+    const int total = n * CD;
+    int done = 0;
+    if ((((uintptr_t)src) & 15) == 0) {
+        const int nv = total >> 2;
+        const float4 *s4 = reinterpret_cast<const float4 *>(src);
+#pragma unroll 4
+        for (int v = threadIdx.x; v < nv; v += blockDim.x) {
+            const float4 q = __ldcs(s4 + v);
+            int e = v << 2;
+            int p = e / CD, k = e - p * CD;
+            const float vals[4] = {q.x, q.y, q.z, q.w};
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                dst[p * stride + k] = vals[u];
+                if (++k == CD) { k = 0; ++p; }
+            }
+        }
+        done = nv << 2;
+    }
+    for (int e = done + threadIdx.x; e < total; e += blockDim.x) {
+        const int p = e / CD;
+        dst[p * stride + (e - p * CD)] = __ldcs(src + e);
     }
 }
 
 __device__ __forceinline__ void unstage_rows(float *__restrict__ dst, const float *src, int n, int CD,
                                              int stride) {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    for (int p = warp; p < n; p += nw) {
-        float *d = dst + (size_t)p * CD;
-        const float *s = src + p * stride;
-        for (int k = lane; k < CD; k += 32) __stcs(d + k, s[k]);
+    const int total = n * CD;
+    int done = 0;
+    if ((((uintptr_t)dst) & 15) == 0) {
+        const int nv = total >> 2;
+        float4 *d4 = reinterpret_cast<float4 *>(dst);
+#pragma unroll 4
+        for (int v = threadIdx.x; v < nv; v += blockDim.x) {
+            int e = v << 2;
+            int p = e / CD, k = e - p * CD;
+            float vals[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                vals[u] = src[p * stride + k];
+                if (++k == CD) { k = 0; ++p; }
+            }
+            __stcs(d4 + v, make_float4(vals[0], vals[1], vals[2], vals[3]));
+        }
+        done = nv << 2;
+    }
+    for (int e = done + threadIdx.x; e < total; e += blockDim.x) {
+        const int p = e / CD;
+        __stcs(dst + e, src[p * stride + (e - p * CD)]);
     }
 }
 

@@ -166,6 +166,6 @@ extern "C" int msplat_project_point_backward(
     project_point_bwd_kernel<<<blocks, 256, 0, stream>>>(
         P, xyz, intr, extr, depth, (const float2 *)dL_duv, dL_ddepth, dL_dxyz, cam, partials);
     if (cam)
-        cam_grad_finalize_kernel<<<1, 32, 0, stream>>>(blocks, partials, dL_dintr, dL_dextr);
+        cam_grad_finalize_kernel<<<1, 32 * kCamGradVals, 0, stream>>>(blocks, partials, dL_dintr, dL_dextr);
     return check_launch("project_point_backward");
 }

@@ -2,8 +2,9 @@
 // sm_103a without library calls.
 //
 // One 8-bit pass = three launches with no device-side waiting:
-//   upsweep   per-tile digit histogram (warp-aggregated shared atomics via
-//             __match_any_sync), stored digit-major [256][tiles]
+//   upsweep   per-tile digit histogram (warp-aggregated shared atomics; the
+//             lanes sharing a digit are found with ballots), stored
+//             digit-major [256][tiles]
 //   row scan  one block per digit: exclusive scan of its row, offset by the
 //             totals of the smaller digits -> global start of every
 //             (digit, tile) bucket
@@ -35,31 +36,52 @@ __device__ __forceinline__ uint32_t digit_of(K k, int shift) {
 
 inline int sort_tiles(int64_t n) { return (int)ceil_div64(n, kSortTile); }
 
+// Lanes of `valid` holding the same 8-bit digit as this lane, from eight
+// ballots (much cheaper than __match_any_sync, whose throughput limits a
+// ranking loop).  Every lane of the warp must call it.
+__device__ __forceinline__ unsigned digit_peers(uint32_t d, unsigned valid) {
+    unsigned peers = valid;
+#pragma unroll
+    for (int b = 0; b < kRadixBits; ++b) {
+        const bool bit = (d >> b) & 1u;
+        const unsigned bb = __ballot_sync(0xffffffffu, bit);
+        peers &= bit ? bb : ~bb;
+    }
+    return peers;
+}
+
 // ---------------------------------------------------------------- upsweep
+// All of a thread's keys are loaded before any counting so that the loads
+// are in flight together; counts go to per-warp shared histograms through
+// one atomic per distinct digit per warp.
 template <typename K, bool FLIP>
 __global__ void __launch_bounds__(kSortThreads)
 radix_upsweep_kernel(const K *__restrict__ keys, int64_t n, int shift, int ntiles,
                      uint32_t *__restrict__ hist, uint32_t *__restrict__ totals) {
-    __shared__ uint32_t cnt[kRadix];
-    cnt[threadIdx.x] = 0;  // kSortThreads == kRadix
+    __shared__ uint32_t cnt[kSortWarps][kRadix];
+    for (int i = threadIdx.x; i < kSortWarps * kRadix; i += kSortThreads) (&cnt[0][0])[i] = 0;
     __syncthreads();
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int64_t base = (int64_t)blockIdx.x * kSortTile;
-#pragma unroll 4
+    const int64_t base = (int64_t)blockIdx.x * kSortTile + warp * (32 * kSortItems) + lane;
+    uint32_t dig[kSortItems];
+#pragma unroll
     for (int r = 0; r < kSortItems; ++r) {
-        const int64_t idx = base + warp * (32 * kSortItems) + r * 32 + lane;
-        const bool valid = idx < n;
+        const int64_t idx = base + r * 32;
+        K k = idx < n ? __ldcs(keys + idx) : K(0);
+        if (FLIP) k ^= sign_bit<K>();
+        dig[r] = idx < n ? digit_of(k, shift) : 0xffffffffu;
+    }
+#pragma unroll
+    for (int r = 0; r < kSortItems; ++r) {
+        const bool valid = dig[r] != 0xffffffffu;
         const unsigned vmask = __ballot_sync(0xffffffffu, valid);
-        if (valid) {
-            K k = keys[idx];
-            if (FLIP) k ^= sign_bit<K>();
-            const uint32_t d = digit_of(k, shift);
-            const unsigned peers = __match_any_sync(vmask, d);
-            if (lane == 31 - __clz(peers)) atomicAdd(&cnt[d], (uint32_t)__popc(peers));
-        }
+        const unsigned peers = digit_peers(dig[r] & (kRadix - 1), vmask);
+        if (valid && lane == 31 - __clz(peers)) atomicAdd(&cnt[warp][dig[r]], (uint32_t)__popc(peers));
     }
     __syncthreads();
-    const uint32_t c = cnt[threadIdx.x];
+    uint32_t c = 0;
+#pragma unroll
+    for (int w = 0; w < kSortWarps; ++w) c += cnt[w][threadIdx.x];
     hist[(size_t)threadIdx.x * ntiles + blockIdx.x] = c;
     if (c) atomicAdd(&totals[threadIdx.x], c);
 }
@@ -122,6 +144,8 @@ radix_downsweep_kernel(const K *__restrict__ kin, const uint32_t *__restrict__ v
     uint32_t val[kSortItems];
     uint32_t rank[kSortItems];
     uint32_t *my_hist = whist + warp * kRadix;
+    // Issue every load of the tile before ranking (the ranking loop's warp
+    // barriers would otherwise serialise them).
 #pragma unroll
     for (int r = 0; r < kSortItems; ++r) {
         const int li = warp * (32 * kSortItems) + r * 32 + lane;
@@ -129,20 +153,23 @@ radix_downsweep_kernel(const K *__restrict__ kin, const uint32_t *__restrict__ v
         K k = K(0);
         uint32_t v = 0;
         if (valid) {
-            k = kin[base + li];
+            k = __ldcs(kin + base + li);
             if (FLIP_IN) k ^= sign_bit<K>();
-            v = vin ? vin[base + li] : (uint32_t)(base + li);
+            v = vin ? __ldcs(vin + base + li) : (uint32_t)(base + li);
         }
         key[r] = k;
         val[r] = v;
+    }
+#pragma unroll
+    for (int r = 0; r < kSortItems; ++r) {
+        const int li = warp * (32 * kSortItems) + r * 32 + lane;
+        const bool valid = li < tile_n;
+        const K k = key[r];
         const unsigned vmask = __ballot_sync(0xffffffffu, valid);
         const uint32_t d = digit_of(k, shift);
-        unsigned peers = 0;
+        const unsigned peers = digit_peers(d, vmask);
         uint32_t b0 = 0;
-        if (valid) {
-            peers = __match_any_sync(vmask, d);
-            b0 = my_hist[d];
-        }
+        if (valid) b0 = my_hist[d];
         __syncwarp();
         if (valid) {
             rank[r] = b0 + __popc(peers & ((1u << lane) - 1u));

@@ -12,15 +12,16 @@
 //   detection.  Mirrors the reference step by step; used when the caller's
 //   tiles[] disagree with the rectangles (zero slots exist).
 //
-// * fast path -- since a stable sort by (tile, depth) equals a stable sort
-//   by tile of a list already in depth order, Gaussians are first sorted by
-//   depth (P keys, 32 bits), their intersections emitted in that order, and
-//   the I intersections sorted by tile only (ceil(log2(tiles + 1)) bits,
-//   2 passes at 1080p instead of 6-8 over 64-bit keys).  Depth keys are the
-//   float bits with the sign bit flipped, i.e. signed-int32 order, matching
-//   the reference's sign-extended keys; negative-depth Gaussians get tile
-//   key 0 so they lead idx_sorted and stay out of every tile's range, as in
-//   the reference (which writes their range out of bounds; we skip that).
+// * fast path -- a stable sort by (tile, depth) equals a stable sort by
+//   tile of a list already in depth order.  So the P Gaussians are sorted by
+//   depth once (32-bit keys: the float bits with the sign flipped, i.e. the
+//   reference's signed order; ties keep id order), their intersections are
+//   emitted in that order with coalesced writes, and the I intersections are
+//   stable-sorted by tile only: ceil(log2(tiles + 1)) bits, 2 passes at
+//   1080p instead of 6-8 over 64-bit keys.  Negative-depth Gaussians, whose
+//   sign-extended keys the reference sorts first and keeps out of every
+//   range, get tile key 0 so they lead idx_sorted in depth order as there
+//   (the reference writes their range out of bounds; we skip that write).
 #include "radix_sort.cuh"
 
 namespace msplat {
@@ -74,14 +75,17 @@ depth_key_kernel(int P, const float *__restrict__ depth, const int32_t *__restri
     keys[g] = radius[g] > 0 ? (__float_as_uint(depth[g]) ^ 0x80000000u) : 0xffffffffu;
 }
 
-// Tile count of each Gaussian, in depth order; counts Gaussians whose tiles[]
-// entry disagrees with the rectangle (these need the reference layout).
+// Tile count of each Gaussian in depth order.  Also counts Gaussians whose
+// tiles[] entry disagrees with their rectangle (those need the reference
+// layout), the negative-depth emitters (they come first in depth order) and
+// their intersections.
 __global__ void __launch_bounds__(256)
 depth_order_count_kernel(int P, const uint32_t *__restrict__ order, const float2 *__restrict__ uv,
-                         const int32_t *__restrict__ radius, const int32_t *__restrict__ tiles,
-                         int gx, int gy, int32_t *__restrict__ cnt, int64_t *__restrict__ counts) {
+                         const float *__restrict__ depth, const int32_t *__restrict__ radius,
+                         const int32_t *__restrict__ tiles, int gx, int gy, int32_t *__restrict__ cnt,
+                         int64_t *__restrict__ counts, unsigned long long *__restrict__ neg) {
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
-    bool bad = false;
+    bool bad = false, isneg = false;
     if (j < P) {
         const int g = (int)order[j];
         int c = 0;
@@ -90,16 +94,37 @@ depth_order_count_kernel(int P, const uint32_t *__restrict__ order, const float2
             const float2 p = uv[g];
             tile_rect(p.x, p.y, radius[g], gx, gy, x0, y0, x1, y1);
             c = (x1 - x0) * (y1 - y0);
+            // Sign-bit-set depths sort before all others (signed order).
+            isneg = (__float_as_uint(depth[g]) >> 31) != 0;
+            if (isneg && c > 0) atomicAdd(neg + 1, (unsigned long long)c);
         }
         bad = c != tiles[g];
         cnt[j] = c;
     }
-    const unsigned m = __ballot_sync(0xffffffffu, bad);
-    if ((threadIdx.x & 31) == 0 && m) atomicAdd((unsigned long long *)&counts[1], (unsigned long long)__popc(m));
+    const unsigned mb = __ballot_sync(0xffffffffu, bad), mn = __ballot_sync(0xffffffffu, isneg);
+    if ((threadIdx.x & 31) == 0) {
+        if (mb) atomicAdd((unsigned long long *)&counts[1], (unsigned long long)__popc(mb));
+        if (mn) atomicAdd(neg, (unsigned long long)__popc(mn));
+    }
 }
 
-// Emits the intersections of 32 depth-ordered Gaussians per warp; each
-// Gaussian's run is written by all lanes (coalesced).
+// Calls f(tile) for every tile of the rectangle of depth-ordered Gaussian j.
+template <typename F>
+__device__ __forceinline__ void for_rect_tiles(int g, const float2 *__restrict__ uv,
+                                               const int32_t *__restrict__ radius, int gx, int gy, F &&f) {
+    const int r = radius[g];
+    if (r <= 0) return;
+    int x0, y0, x1, y1;
+    const float2 p = uv[g];
+    tile_rect(p.x, p.y, r, gx, gy, x0, y0, x1, y1);
+    for (int ty = y0; ty < y1; ++ty)
+        for (int tx = x0; tx < x1; ++tx) f(ty * gx + tx);
+}
+
+// Emits the intersections of 32 depth-ordered Gaussians per warp: each lane
+// loads one Gaussian, then the whole warp writes each Gaussian's run of
+// (tile key, id) pairs with the lanes spread over its tiles (coalesced).
+// Tile key 0 marks negative-depth Gaussians, t + 1 tile t.
 __global__ void __launch_bounds__(256)
 emit_kernel(int P, const uint32_t *__restrict__ order, const int32_t *__restrict__ offs,
             const float2 *__restrict__ uv, const float *__restrict__ depth,
@@ -116,28 +141,30 @@ emit_kernel(int P, const uint32_t *__restrict__ order, const int32_t *__restrict
             tile_rect(p.x, p.y, radius[g], gx, gy, x0, y0, x1, y1);
             start = offs[j];
             neg = (__float_as_uint(depth[g]) >> 31) != 0;
-        } else {
-            x1 = x0;  // empty
         }
     }
-    for (int s = 0; s < 32; ++s) {
-        const int sg = __shfl_sync(0xffffffffu, g, s);
-        const int sx0 = __shfl_sync(0xffffffffu, x0, s), sy0 = __shfl_sync(0xffffffffu, y0, s);
-        const int sx1 = __shfl_sync(0xffffffffu, x1, s), sy1 = __shfl_sync(0xffffffffu, y1, s);
-        const int sstart = __shfl_sync(0xffffffffu, start, s);
-        const bool sneg = __shfl_sync(0xffffffffu, (int)neg, s) != 0;
-        if (sg < 0) continue;
-        const int w = sx1 - sx0;
-        const int count = w * (sy1 - sy0);
-        for (int k = lane; k < count; k += 32) {
-            const int ty = sy0 + k / w, tx = sx0 + k % w;
-            tkeys[sstart + k] = sneg ? 0u : (uint32_t)(ty * gx + tx + 1);
+    const int w = x1 - x0, n = w * (y1 - y0);
+    unsigned todo = __ballot_sync(0xffffffffu, n > 0);
+    while (todo) {
+        const int sl = __ffs(todo) - 1;
+        todo &= todo - 1;
+        const int sg = __shfl_sync(0xffffffffu, g, sl);
+        const int sx0 = __shfl_sync(0xffffffffu, x0, sl), sy0 = __shfl_sync(0xffffffffu, y0, sl);
+        const int sw = __shfl_sync(0xffffffffu, w, sl), sn = __shfl_sync(0xffffffffu, n, sl);
+        const int sstart = __shfl_sync(0xffffffffu, start, sl);
+        const bool sneg = __shfl_sync(0xffffffffu, (int)neg, sl) != 0;
+        const float inv = 1.0f / (float)sw;
+        for (int k = lane; k < sn; k += 32) {
+            int ry = (int)(((float)k + 0.5f) * inv);  // k / sw, corrected below
+            ry -= (ry * sw > k);
+            ry += ((ry + 1) * sw <= k);
+            tkeys[sstart + k] = sneg ? 0u : (uint32_t)((sy0 + ry) * gx + sx0 + (k - ry * sw) + 1);
             tvals[sstart + k] = (uint32_t)sg;
         }
     }
 }
 
-// Ranges from tile keys (key 0 = no tile, key t + 1 = tile t).
+// Ranges from the sorted tile keys (key 0 = no tile, key t + 1 = tile t).
 __global__ void __launch_bounds__(256)
 range_from_tilekey_kernel(int64_t I, const uint32_t *__restrict__ keys, int2 *__restrict__ range) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -157,35 +184,43 @@ inline int bits_for(uint32_t maxval) {
 
 constexpr int kDepthPasses = 4;
 
-// Prepare-step workspace.  `order` and `offs` come first and are read again
-// by the finish step (which re-derives their addresses from P).
+// Prepare-step workspace.  `order`, `offs`, `cnt` and the negative-depth
+// counters come first and are read again by the finish step (which
+// re-derives their addresses from P).
 struct PrepareWs {
     uint32_t *order = nullptr;  // [P] Gaussian ids in depth order
     int32_t *offs = nullptr;    // [P] exclusive scan of tile counts, depth order
-    int32_t *cnt = nullptr;     // [P]
+    int32_t *cnt = nullptr;     // [P] tile counts, depth order
+    unsigned long long *neg = nullptr;  // [0] negative emitters, [1] their intersections
     uint32_t *ka = nullptr, *kb = nullptr, *vt = nullptr;
     int64_t *scan_parts = nullptr;
     RadixBuffers rb{};
 };
 
-inline void prepare_carve(Workspace &w, int P, PrepareWs &ws) {
-    ws.order = w.take<uint32_t>(P);
-    ws.offs = w.take<int32_t>(P);
-    ws.cnt = w.take<int32_t>(P);
-    ws.ka = w.take<uint32_t>(P);
-    ws.kb = w.take<uint32_t>(P);
-    ws.vt = w.take<uint32_t>(P);
-    ws.scan_parts = w.take<int64_t>((size_t)ceil_div(P, kScanTile) + 1);
-    radix_take(w, P, kDepthPasses, ws.rb);
+template <typename WS>
+inline void prepare_carve(WS &w, int P, PrepareWs &ws) {
+    ws.order = w.template take<uint32_t>(P);
+    ws.offs = w.template take<int32_t>(P);
+    ws.cnt = w.template take<int32_t>(P);
+    ws.neg = w.template take<unsigned long long>(2);
+    ws.ka = w.template take<uint32_t>(P);
+    ws.kb = w.template take<uint32_t>(P);
+    ws.vt = w.template take<uint32_t>(P);
+    ws.scan_parts = w.template take<int64_t>((size_t)ceil_div(P, kScanTile) + 1);
+    ws.rb.hist = w.template take<uint32_t>((size_t)kRadix * sort_tiles(P));
+    ws.rb.totals = w.template take<uint32_t>((size_t)kRadix * kDepthPasses);
 }
 
-inline size_t prepare_bytes(int P) {
+struct SizeOnly {
     WorkspaceSizer s;
-    s.take<uint32_t>(P); s.take<int32_t>(P); s.take<int32_t>(P);
-    s.take<uint32_t>(P); s.take<uint32_t>(P); s.take<uint32_t>(P);
-    s.take<int64_t>((size_t)ceil_div(P, kScanTile) + 1);
-    radix_size(s, P, kDepthPasses);
-    return s.used;
+    template <typename T> T *take(size_t n) { s.take<T>(n); return nullptr; }
+};
+
+inline size_t prepare_bytes(int P) {
+    SizeOnly z;
+    PrepareWs ws;
+    prepare_carve(z, P, ws);
+    return z.s.used;
 }
 
 inline int tile_key_passes(int W, int H) {
@@ -194,11 +229,25 @@ inline int tile_key_passes(int W, int H) {
     return ceil_div(bits > 0 ? bits : 1, kRadixBits);
 }
 
+struct FinishWs {
+    uint32_t *ka = nullptr, *kb = nullptr, *vt = nullptr;
+    RadixBuffers rb{};
+};
+
+template <typename WS>
+inline void finish_carve(WS &w, int64_t I, int passes, FinishWs &f) {
+    f.ka = w.template take<uint32_t>(I);
+    f.kb = w.template take<uint32_t>(I);
+    f.vt = w.template take<uint32_t>(I);
+    f.rb.hist = w.template take<uint32_t>((size_t)kRadix * sort_tiles(I));
+    f.rb.totals = w.template take<uint32_t>((size_t)kRadix * passes);
+}
+
 inline size_t finish_bytes(int64_t I, int W, int H) {
-    WorkspaceSizer s;
-    s.take<uint32_t>(I); s.take<uint32_t>(I); s.take<uint32_t>(I);
-    radix_size(s, I, tile_key_passes(W, H));
-    return s.used;
+    SizeOnly z;
+    FinishWs f;
+    finish_carve(z, I, tile_key_passes(W, H), f);
+    return z.s.used;
 }
 
 inline size_t radix_i64_bytes(int64_t n) {
@@ -304,7 +353,10 @@ extern "C" int msplat_radix_sort_i64_pairs(int64_t n, const int64_t *keys_in, co
                                             (uint32_t *)vals_out, kt, vt, rb, stream);
 }
 
-extern "C" size_t msplat_sort_prepare_workspace_size(int P) { return prepare_bytes(P < 0 ? 0 : P); }
+extern "C" size_t msplat_sort_prepare_workspace_size(int P, int W, int H) {
+    (void)W; (void)H;
+    return prepare_bytes(P < 0 ? 0 : P);
+}
 
 extern "C" int msplat_sort_gaussian_prepare(int P, const float *depth, const int32_t *radius,
                                             const int32_t *tiles, const float *uv, int W, int H,
@@ -313,16 +365,17 @@ extern "C" int msplat_sort_gaussian_prepare(int P, const float *depth, const int
     if (P < 0 || W <= 0 || H <= 0)
         return set_error(MSPLAT_ERR_INVALID_ARGUMENT, "sort_gaussian_prepare: bad sizes");
     if (!counts) return set_error(MSPLAT_ERR_INVALID_ARGUMENT, "sort_gaussian_prepare: null counts");
-    cudaMemsetAsync(counts, 0, 2 * sizeof(int64_t), stream);
-    if (P == 0) return check_launch("sort_gaussian_prepare");
-    if (!depth || !radius || !tiles || !uv)
-        return set_error(MSPLAT_ERR_INVALID_ARGUMENT, "sort_gaussian_prepare: null pointer");
     Workspace w(workspace, workspace_bytes);
     PrepareWs ws;
     prepare_carve(w, P, ws);
     if (w.overflow)
         return set_error(MSPLAT_ERR_WORKSPACE, "sort_gaussian_prepare: workspace of %zu bytes < %zu",
                          workspace_bytes, prepare_bytes(P));
+    cudaMemsetAsync(counts, 0, 2 * sizeof(int64_t), stream);
+    cudaMemsetAsync(ws.neg, 0, 2 * sizeof(unsigned long long), stream);
+    if (P == 0) return check_launch("sort_gaussian_prepare");
+    if (!depth || !radius || !tiles || !uv)
+        return set_error(MSPLAT_ERR_INVALID_ARGUMENT, "sort_gaussian_prepare: null pointer");
     const int gx = ceil_div(W, kTile), gy = ceil_div(H, kTile);
     depth_key_kernel<<<ceil_div(P, 256), 256, 0, stream>>>(P, depth, radius, ws.ka);
     // Even pass count: the input keys may alias the output keys.
@@ -330,7 +383,7 @@ extern "C" int msplat_sort_gaussian_prepare(int P, const float *depth, const int
                                                ws.kb, ws.vt, ws.rb, stream);
     if (st) return st;
     depth_order_count_kernel<<<ceil_div(P, 256), 256, 0, stream>>>(
-        P, ws.order, (const float2 *)uv, radius, tiles, gx, gy, ws.cnt, counts);
+        P, ws.order, (const float2 *)uv, depth, radius, tiles, gx, gy, ws.cnt, counts, ws.neg);
     return scan_i32(P, ws.cnt, ws.offs, false, counts, ws.scan_parts, stream);
 }
 
@@ -350,9 +403,9 @@ extern "C" int msplat_sort_gaussian_finish(int P, const float *uv, const float *
     if (num_intersects > INT32_MAX)
         return set_error(MSPLAT_ERR_CAPACITY, "sort_gaussian_finish: %lld intersections exceed int32",
                          (long long)num_intersects);
-    const int gx = ceil_div(W, kTile), gy = ceil_div(H, kTile), ntiles = gx * gy;
+    const int gx = ceil_div(W, kTile), gy = ceil_div(H, kTile), nt = gx * gy;
     if (!tile_range) return set_error(MSPLAT_ERR_INVALID_ARGUMENT, "sort_gaussian_finish: null tile_range");
-    cudaMemsetAsync(tile_range, 0, sizeof(int32_t) * 2 * ntiles, stream);
+    cudaMemsetAsync(tile_range, 0, sizeof(int32_t) * 2 * nt, stream);
     if (P == 0 || num_intersects == 0) return check_launch("sort_gaussian_finish");
     if (!uv || !depth || !radius || !prepare_workspace || !idx_sorted)
         return set_error(MSPLAT_ERR_INVALID_ARGUMENT, "sort_gaussian_finish: null pointer");
@@ -362,23 +415,22 @@ extern "C" int msplat_sort_gaussian_finish(int P, const float *uv, const float *
     const int64_t I = num_intersects;
     const int passes = tile_key_passes(W, H);
     Workspace w(workspace, workspace_bytes);
-    uint32_t *ka = w.take<uint32_t>(I), *kb = w.take<uint32_t>(I), *vt = w.take<uint32_t>(I);
-    RadixBuffers rb;
-    radix_take(w, I, passes, rb);
+    FinishWs f;
+    finish_carve(w, I, passes, f);
     if (w.overflow)
         return set_error(MSPLAT_ERR_WORKSPACE, "sort_gaussian_finish: workspace of %zu bytes < %zu",
                          workspace_bytes, finish_bytes(I, W, H));
-    // Even pass count: emit the ids straight into idx_sorted (input may alias
-    // output); odd: emit into the temporary (input may alias tmp).
+    // Even pass count: emit the ids straight into idx_sorted (the input may
+    // alias the output); odd: into the temporary (the input may alias tmp).
     uint32_t *out = (uint32_t *)idx_sorted;
-    uint32_t *vemit = (passes % 2 == 0) ? out : vt;
-    emit_kernel<<<ceil_div(P, 256), 256, 0, stream>>>(P, prep.order, prep.offs, (const float2 *)uv,
-                                                      depth, radius, gx, gy, ka, vemit);
-    int st = radix_sort_pairs<uint32_t, false>(I, 0, passes, ka, vemit, (passes % 2 == 0) ? ka : kb, out,
-                                               (passes % 2 == 0) ? kb : ka, vt, rb, stream);
+    const bool even = passes % 2 == 0;
+    uint32_t *vemit = even ? out : f.vt;
+    emit_kernel<<<ceil_div(P, 256), 256, 0, stream>>>(P, prep.order, prep.offs, (const float2 *)uv, depth,
+                                                      radius, gx, gy, f.ka, vemit);
+    uint32_t *kout = even ? f.ka : f.kb;
+    int st = radix_sort_pairs<uint32_t, false>(I, 0, passes, f.ka, vemit, kout, out, even ? f.kb : f.ka, f.vt,
+                                               f.rb, stream);
     if (st) return st;
-    const uint32_t *sorted_keys = (passes % 2 == 0) ? ka : kb;
-    range_from_tilekey_kernel<<<(unsigned)ceil_div64(I, 256), 256, 0, stream>>>(I, sorted_keys,
-                                                                               (int2 *)tile_range);
+    range_from_tilekey_kernel<<<(unsigned)ceil_div64(I, 256), 256, 0, stream>>>(I, kout, (int2 *)tile_range);
     return check_launch("sort_gaussian_finish");
 }

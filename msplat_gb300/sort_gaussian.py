@@ -46,7 +46,7 @@ def sort_gaussian(
     lib = _lib.load()
     st = _lib.stream(dev)
     counts = torch.empty(2, dtype=torch.int64, device=dev)
-    ws_prep = _lib.workspace(lib.msplat_sort_prepare_workspace_size(P), dev)
+    ws_prep = _lib.workspace(lib.msplat_sort_prepare_workspace_size(P, W, H), dev)
     with _lib.stage("sort_gaussian_prepare"):
         _lib.check(lib.msplat_sort_gaussian_prepare(
             P, _lib.ptr(d), _lib.ptr(r), _lib.ptr(t), _lib.ptr(u), W, H, _lib.ptr(counts),

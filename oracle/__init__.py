@@ -23,6 +23,8 @@ _P = ctypes.c_void_p
 # FMA contraction pattern of the GPU build (see oracle.c); pinned by
 # tests/test_gpu_parity.py::test_fma_mode_is_the_compilers.
 FMA_MODE = 0
+# Pairing choices inside the covariance code (see oracle.c).
+COV_VARIANT = 0
 
 
 def _load():
@@ -34,6 +36,7 @@ def _load():
         sig = {
             "oracle_set_fma_mode": (None, [i]),
             "oracle_get_fma_mode": (i, []),
+            "oracle_set_cov_variant": (None, [i]),
             "oracle_project_point_forward": (None, [i, _P, _P, _P, i, i, f, f, _P, _P]),
             "oracle_project_point_backward": (None, [i, _P, _P, _P, _P, _P, _P, _P, _P, _P]),
             "oracle_compute_cov3d_forward": (None, [i, _P, _P, _P, _P]),
@@ -55,6 +58,7 @@ def _load():
             fn.restype = res
             fn.argtypes = args
         lib.oracle_set_fma_mode(FMA_MODE)
+        lib.oracle_set_cov_variant(COV_VARIANT)
         _lib = lib
     return _lib
 
@@ -76,6 +80,10 @@ def _mask(v, P):
 def set_fma_mode(mode: int) -> None:
     """0: a*b + c*d -> fma(a, b, c*d); 1: fma(c, d, a*b); 2: no FMAs."""
     _load().oracle_set_fma_mode(int(mode))
+
+
+def set_cov_variant(v: int) -> None:
+    _load().oracle_set_cov_variant(int(v))
 
 
 def get_fma_mode() -> int:

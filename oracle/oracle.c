@@ -148,10 +148,51 @@ void oracle_project_point_backward(int P, const float *xyz, const float *intr, c
 }
 
 /* --------------------------------------------------------------- cov3d */
+/* Contraction choices of the covariance code, where products are shared
+ * between entries and the compiler's pairing can differ from the global
+ * mode: bit 0 flips the pairing of the rotation's sums, bit 1 of its
+ * differences, bit 2 of the Sigma = M^T M products.  Pinned by the GPU
+ * parity tests. */
+static int g_cov_variant = 0;
+
+void oracle_set_cov_variant(int v) { g_cov_variant = v; }
+
+static inline float sum2_v(float a, float b, float c, float d, int flip) {
+    if (g_mode == 2) return a * b + c * d;
+    return (flip ^ (g_mode == 1)) ? fmaf(c, d, a * b) : fmaf(a, b, c * d);
+}
+
+static inline float msub_v(float a, float b, float c, float d, int flip) {
+    if (g_mode == 2) return a * b - c * d;
+    return (flip ^ (g_mode == 1)) ? fmaf(-c, d, a * b) : fmaf(a, b, -(c * d));
+}
+
+/* bit 3: products shared between a sum and a difference (x*y, r*z, ...)
+ * are not fused at all; bit 4: the same for the squares. */
+static inline float osum(float a, float b, float c, float d, int flip, int nofuse) {
+    return nofuse ? a * b + c * d : sum2_v(a, b, c, d, flip);
+}
+
+static inline float odif(float a, float b, float c, float d, int flip, int nofuse) {
+    return nofuse ? a * b - c * d : msub_v(a, b, c, d, flip);
+}
+
 static mat3f quat_rot_cols(float r, float x, float y, float z) {
-    return m3_cols(1.f - 2.f * sum2(y, y, z, z), 2.f * msub(x, y, r, z), 2.f * sum2(x, z, r, y),
-                   2.f * sum2(x, y, r, z), 1.f - 2.f * sum2(x, x, z, z), 2.f * msub(y, z, r, x),
-                   2.f * msub(x, z, r, y), 2.f * sum2(y, z, r, x), 1.f - 2.f * sum2(x, x, y, y));
+    const int fs = g_cov_variant & 1, fd = (g_cov_variant >> 1) & 1;
+    const int no = (g_cov_variant >> 3) & 1, nq = (g_cov_variant >> 4) & 1;
+    return m3_cols(1.f - 2.f * osum(y, y, z, z, fs, nq), 2.f * odif(x, y, r, z, fd, no), 2.f * osum(x, z, r, y, fs, no),
+                   2.f * osum(x, y, r, z, fs, no), 1.f - 2.f * osum(x, x, z, z, fs, nq), 2.f * odif(y, z, r, x, fd, no),
+                   2.f * odif(x, z, r, y, fd, no), 2.f * osum(y, z, r, x, fs, no), 1.f - 2.f * osum(x, x, y, y, fs, nq));
+}
+
+static mat3f m3_mul_v(mat3f A, mat3f B, int flip) {
+    mat3f R;
+    for (int j = 0; j < 3; ++j)
+        for (int i = 0; i < 3; ++i) {
+            const float p = sum2_v(A.m[0][i], B.m[j][0], A.m[1][i], B.m[j][1], flip);
+            R.m[j][i] = g_mode == 2 ? p + A.m[2][i] * B.m[j][2] : fmaf(A.m[2][i], B.m[j][2], p);
+        }
+    return R;
 }
 
 /* msplat/src/compute_cov3d.cu:14-58, 119-129 */
@@ -167,7 +208,7 @@ void oracle_compute_cov3d_forward(int P, const float *scales, const float *q, co
         const mat3f S = m3_cols(s[0], 0.f, 0.f, 0.f, s[1], 0.f, 0.f, 0.f, s[2]);
         const mat3f R = quat_rot_cols(q[4 * i], q[4 * i + 1], q[4 * i + 2], q[4 * i + 3]);
         const mat3f M = m3_mul(S, R);
-        const mat3f Sig = m3_mul(m3_t(M), M);
+        const mat3f Sig = m3_mul_v(m3_t(M), M, (g_cov_variant >> 2) & 1);
         o[0] = Sig.m[0][0]; o[1] = Sig.m[0][1]; o[2] = Sig.m[0][2];
         o[3] = Sig.m[1][1]; o[4] = Sig.m[1][2]; o[5] = Sig.m[2][2];
     }
