@@ -160,6 +160,26 @@ MSPLAT_API int msplat_inclusive_scan_i32(int n, const int32_t *in, int32_t *out,
                               int64_t *total, void *workspace,
                               size_t workspace_bytes, msplat_stream_t stream);
 
+/* Allocation-free variant of msplat_inclusive_scan_i32 (no counterpart in
+ * the reference).  For callers that cannot allocate device memory where they
+ * call the scan -- code running inside a CUDA stream capture, a host
+ * application or plugin framework that owns every device allocation, or a
+ * real-time loop that may not call an allocator -- and so cannot provide a
+ * workspace.  Its scratch (the per-4096-element partial sums) is a fixed
+ * array inside the library: every GPU that loads the library keeps those
+ * 131 KB until the process exits.  n may not exceed
+ * MSPLAT_SCAN_NOALLOC_MAX_N; larger n is rejected with MSPLAT_ERR_CAPACITY
+ * before any work is enqueued.  All calls share the one array, so calls
+ * that overlap on the GPU (different streams, or different host threads
+ * without ordering) race and give wrong sums; serialise them.  The first
+ * call on each device looks up the array's device address (with that device
+ * current); make that first call before any stream capture.  It never calls
+ * cudaMalloc / cudaFree or any allocating routine.                         */
+#define MSPLAT_SCAN_NOALLOC_MAX_N (64 * 1024 * 1024)
+MSPLAT_API int msplat_inclusive_scan_i32_noalloc(int n, const int32_t *in,
+                                                 int32_t *out, int64_t *total,
+                                                 msplat_stream_t stream);
+
 /* Stable LSD radix sort of (int64 key, int32 value) pairs in SIGNED int64
  * order (torch.sort on int64, msplat/sort_gaussian.py:49) that carries the
  * values along (the torch.gather of :50).  Only key bits [begin_bit,

@@ -40,6 +40,7 @@ _SIGNATURES = {
     "msplat_compute_tile_gaussian_range": (_I, [_I, _I, _I64, _P, _P, _P]),
     "msplat_scan_workspace_size": (_SZ, [_I]),
     "msplat_inclusive_scan_i32": (_I, [_I, _P, _P, _P, _P, _SZ, _P]),
+    "msplat_inclusive_scan_i32_noalloc": (_I, [_I, _P, _P, _P, _P]),
     "msplat_radix_sort_i64_workspace_size": (_SZ, [_I64]),
     "msplat_radix_sort_i64_pairs": (_I, [_I64, _P, _P, _P, _P, _I, _I, _P, _SZ, _P]),
     "msplat_sort_prepare_workspace_size": (_SZ, [_I, _I, _I]),

@@ -22,6 +22,8 @@
 //   sign-extended keys the reference sorts first and keeps out of every
 //   range, get tile key 0 so they lead idx_sorted in depth order as there
 //   (the reference writes their range out of bounds; we skip that write).
+#include <mutex>
+
 #include "radix_sort.cuh"
 
 namespace msplat {
@@ -319,6 +321,56 @@ extern "C" int msplat_inclusive_scan_i32(int n, const int32_t *in, int32_t *out,
     if (w.overflow)
         return set_error(MSPLAT_ERR_WORKSPACE, "inclusive_scan_i32: workspace of %zu bytes < %zu",
                          workspace_bytes, msplat_scan_workspace_size(n));
+    return scan_i32(n, in, out, true, total, parts, stream);
+}
+
+// ---------------------------------------------------- allocation-free scan
+// Scratch of msplat_inclusive_scan_i32_noalloc: the partial sums of a scan of
+// up to MSPLAT_SCAN_NOALLOC_MAX_N elements, one int64 per 4096-element tile
+// plus one (131 KB).  Host code cannot use the symbol as a device address;
+// noalloc_scan_parts() looks the address up once per device.
+constexpr int kNoAllocScanParts = MSPLAT_SCAN_NOALLOC_MAX_N / kScanTile + 1;
+static __device__ __align__(256) int64_t g_noalloc_scan_parts[kNoAllocScanParts];
+
+// Device address of g_noalloc_scan_parts on the current device (looked up
+// with cudaGetSymbolAddress the first time each device is seen).
+static int64_t *noalloc_scan_parts(cudaError_t *err) {
+    static std::mutex mu;
+    static int64_t *addr[128] = {nullptr};
+    int dev = 0;
+    *err = cudaGetDevice(&dev);
+    if (*err != cudaSuccess) return nullptr;
+    if (dev < 0 || dev >= 128) {
+        *err = cudaErrorInvalidDevice;
+        return nullptr;
+    }
+    std::lock_guard<std::mutex> lock(mu);
+    if (!addr[dev]) {
+        void *p = nullptr;
+        *err = cudaGetSymbolAddress(&p, g_noalloc_scan_parts);
+        if (*err != cudaSuccess) return nullptr;
+        addr[dev] = static_cast<int64_t *>(p);
+    }
+    return addr[dev];
+}
+
+extern "C" int msplat_inclusive_scan_i32_noalloc(int n, const int32_t *in, int32_t *out, int64_t *total,
+                                                 msplat_stream_t stream) {
+    if (n < 0) return set_error(MSPLAT_ERR_INVALID_ARGUMENT, "inclusive_scan_i32_noalloc: n < 0");
+    if (n > MSPLAT_SCAN_NOALLOC_MAX_N)
+        return set_error(MSPLAT_ERR_CAPACITY,
+                         "inclusive_scan_i32_noalloc: n = %d exceeds the maximum of %d elements of its "
+                         "built-in scratch; use msplat_inclusive_scan_i32 with a workspace",
+                         n, MSPLAT_SCAN_NOALLOC_MAX_N);
+    if (n > 0 && (!in || !out))
+        return set_error(MSPLAT_ERR_INVALID_ARGUMENT, "inclusive_scan_i32_noalloc: null pointer");
+    cudaError_t err = cudaSuccess;
+    int64_t *parts = noalloc_scan_parts(&err);
+    if (!parts)
+        return set_error(MSPLAT_ERR_LAUNCH, "inclusive_scan_i32_noalloc: device address of the scratch: %s",
+                         cudaGetErrorString(err));
+    // Every partial sum is written by scan_reduce_kernel before it is read,
+    // so the shared scratch needs no clearing between calls.
     return scan_i32(n, in, out, true, total, parts, stream);
 }
 
