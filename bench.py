@@ -10,11 +10,9 @@ the scene and loss weights copied from pinned host memory every step and the
 loss read back.  Inputs (236 MB of parameters + 25 MB of loss weights) are
 larger than L2, so no explicit flush is done between steps.
 
-`--impl reference` times the reference algorithm on the host CPU (the CPU
-oracle port of the reference, all host threads) on a bounded sample of the
-same frame: the full projection / covariance / SH / EWA / sort for all
-Gaussians plus the forward and backward blend of a band of tile rows, the
-band's time scaled to the whole frame.
+`--impl reference` times the reference algorithm on the host CPU: the CPU
+oracle (a C restatement of the reference's kernels) on all host threads,
+one full forward + backward frame per step.
 """
 from __future__ import annotations
 
@@ -38,6 +36,7 @@ N_GAUSS = 1_000_000
 W_IMG, H_IMG = 1920, 1080
 FOCAL = 1500.0
 SH_DEG = 3
+WORKLOAD = "1M Gaussians, 1920x1080, SH deg 3, fwd+bwd, loss sum(W*img)"
 
 
 # ------------------------------------------------------------------ scene
@@ -86,54 +85,113 @@ def train_step(ms, p, weights):
 
 
 # ------------------------------------------------------------------ clocks
+# NVML clock-event reason bits (nvml.h, nvmlClocksEventReason*).
+_NVML_REASONS = {0x4: "sw_power_cap", 0x8: "hw_slowdown", 0x20: "sw_thermal_slowdown",
+                 0x40: "hw_thermal_slowdown", 0x80: "hw_power_brake_slowdown"}
+
+
 class ClockSampler:
+    """Samples the SM clock and the clock-event reasons of this process's GPU
+    every 10 ms while the timed region runs (NVML through ctypes; falls back
+    to `nvidia-smi -lms 100`).  Read-only: no GPU setting is touched."""
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
-    def __init__(self, gpu_index: int):
-        self.gpu = gpu_index
+    def __init__(self, device: int):
+        self.device = device
+        self.sm: list[float] = []
+        self.reasons: set[str] = set()
+        self.max_mhz = None
+        self.source = None
+        self._stop = threading.Event()
+        self._t = None
         self.proc = None
-        self.lines: list[str] = []
+
+    def _nvml_handle(self):
+        import ctypes
+        nv = ctypes.CDLL("libnvidia-ml.so.1")
+        if nv.nvmlInit_v2() != 0:
+            return None, None
+        h = ctypes.c_void_p()
+        bus = None
+        try:
+            pr = torch.cuda.get_device_properties(self.device)
+            bus = "%08x:%02x:%02x.0" % (pr.pci_domain_id, pr.pci_bus_id, pr.pci_device_id)
+        except AttributeError:
+            pass
+        if bus is None or nv.nvmlDeviceGetHandleByPciBusId_v2(bus.encode(), ctypes.byref(h)) != 0:
+            if nv.nvmlDeviceGetHandleByIndex_v2(self.device, ctypes.byref(h)) != 0:
+                return None, None
+        return nv, h
+
+    def _nvml_loop(self, nv, h):
+        import ctypes
+        mhz = ctypes.c_uint()
+        rs = ctypes.c_ulonglong()
+        while not self._stop.is_set():
+            if nv.nvmlDeviceGetClockInfo(h, 1, ctypes.byref(mhz)) == 0:  # NVML_CLOCK_SM
+                self.sm.append(float(mhz.value))
+            if nv.nvmlDeviceGetCurrentClocksEventReasons(h, ctypes.byref(rs)) == 0:
+                for bit, name in _NVML_REASONS.items():
+                    if rs.value & bit:
+                        self.reasons.add(name)
+            self._stop.wait(0.01)
 
     def start(self):
         try:
+            import ctypes
+            nv, h = self._nvml_handle()
+            if nv is not None:
+                mx = ctypes.c_uint()
+                if nv.nvmlDeviceGetMaxClockInfo(h, 1, ctypes.byref(mx)) == 0:
+                    self.max_mhz = float(mx.value)
+                self.source = "nvml 10 ms"
+                self._t = threading.Thread(target=self._nvml_loop, args=(nv, h), daemon=True)
+                self._t.start()
+                return
+        except OSError:
+            pass
+        try:
+            idx = int(os.environ.get("LOCAL_RANK", self.device))
             self.proc = subprocess.Popen(
-                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
-                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
-            self._t = threading.Thread(target=self._read, daemon=True)
+                ["nvidia-smi", f"--id={idx}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.source = "nvidia-smi 100 ms"
+            self._t = threading.Thread(target=self._smi_loop, daemon=True)
             self._t.start()
-        except (OSError, FileNotFoundError):
+        except OSError:
             self.proc = None
 
-    def _read(self):
-        for line in self.proc.stdout:
-            self.lines.append(line.strip())
-
-    def stop(self) -> dict:
-        if self.proc is None:
-            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
-        self.proc.terminate()
-        try:
-            self.proc.wait(timeout=5)
-        except subprocess.TimeoutExpired:
-            self.proc.kill()
-        sm, mx, reasons = [], [], set()
+    def _smi_loop(self):
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for ln in self.lines:
+        for ln in self.proc.stdout:
             f = [x.strip() for x in ln.split(",")]
             if len(f) < 9:
                 continue
             try:
-                sm.append(float(f[1]))
-                mx.append(float(f[2]))
+                self.sm.append(float(f[1]))
+                self.max_mhz = float(f[2])
             except ValueError:
                 continue
             for name, val in zip(names, f[5:9]):
                 if val.lower().startswith("active"):
-                    reasons.add(name)
-        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
-                "reasons": sorted(reasons), "samples": len(sm)}
+                    self.reasons.add(name)
+
+    def stop(self) -> dict:
+        if self.source is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["clock sampling unavailable"]}
+        self._stop.set()
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+        if self._t is not None:
+            self._t.join(timeout=5)
+        return {"sm_mhz": float(np.median(self.sm)) if self.sm else None, "sm_max_mhz": self.max_mhz,
+                "reasons": sorted(self.reasons), "samples": len(self.sm), "source": self.source}
 
 
 # ---------------------------------------------------------------- roofline
@@ -229,19 +287,20 @@ def run_ours(args, rank, world, device):
         train_step(ms, p, weights)
     barrier()
 
-    clocks = ClockSampler(torch.cuda.current_device() if "CUDA_VISIBLE_DEVICES" not in os.environ
-                          else int(os.environ.get("LOCAL_RANK", 0)))
+    clocks = ClockSampler(torch.cuda.current_device())
     clocks.start()
     stream = torch.cuda.current_stream()
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     _lib.profile_start()
     barrier()
+    n_launch0 = _lib.kernel_launches()
     ev0.record(stream)
     for _ in range(args.steps):
         for t in p.values():
             t.grad = None
         train_step(ms, p, weights)
     ev1.record(stream)
+    n_launch = _lib.kernel_launches() - n_launch0
     barrier()
     stages = _lib.profile_stop()
     clk = clocks.stop()
@@ -253,7 +312,7 @@ def run_ours(args, rank, world, device):
 
     # e2e: the same step with host inputs copied in and the loss read back.
     if args.no_e2e:
-        return _finish(args, rank, world, ms, p, stages, clk, ms_step, None, 0)
+        return _finish(args, rank, world, ms, p, stages, clk, ms_step, None, 0, n_launch)
     host = {k: scene[k].pin_memory() for k in PARAMS}
     host_w = scene["weights"].pin_memory()
     h2d = sum(v.numel() * v.element_size() for v in host.values()) + host_w.numel() * host_w.element_size()
@@ -274,10 +333,10 @@ def run_ours(args, rank, world, device):
     if world > 1:
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
     e2e_ms = float(t.item())
-    return _finish(args, rank, world, ms, p, stages, clk, ms_step, e2e_ms, h2d)
+    return _finish(args, rank, world, ms, p, stages, clk, ms_step, e2e_ms, h2d, n_launch)
 
 
-def _finish(args, rank, world, ms, p, stages, clk, ms_step, e2e_ms, h2d):
+def _finish(args, rank, world, ms, p, stages, clk, ms_step, e2e_ms, h2d, n_launch):
     if rank != 0:
         return None
     pairs, inter, nvis = blend_pairs(ms, p)
@@ -297,98 +356,102 @@ def _finish(args, rank, world, ms, p, stages, clk, ms_step, e2e_ms, h2d):
         "vs_baseline": None,
         "dtype": "f32",
         "data": "synthetic (seeded; config distributions, random look-at camera on a radius-4 sphere)",
-        "config": {"workload": "1M Gaussians, 1920x1080, SH deg 3, fwd+bwd, loss sum(W*img)",
+        "config": {"workload": WORKLOAD,
                    "n_gaussians": N_GAUSS, "width": W_IMG, "height": H_IMG, "sh_degree": SH_DEG,
                    "focal": FOCAL, "intersections": inter, "visible_gaussians": nvis, "blend_pairs": pairs,
                    "parallelism": "replicas" if world > 1 else "single",
                    "l2": "inputs (261 MB) larger than L2; no flush"},
         "e2e": None if e2e_ms is None else {"value": round(e2e_ms / world, 4), "unit": "ms/frame",
                                             "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": 4},
-        "gpu_launches": None,
+        "gpu_launches": int(n_launch),
         "stage_ms_per_step": stage_ms,
         "roofline": roof,
         "clocks": clk,
     }
-    out["gpu_launches"] = int(launches_per_step(stages, args.steps) * args.steps)
     if not args.no_cpu:
-        out["cpu_baseline"] = cpu_baseline(threads=1)
+        out["cpu_baseline"] = cpu_baseline(host_threads())
     return out
 
 
-# Native kernels each native call launches (counted from the C sources).
-KERNELS_PER_CALL = {
-    "project_point_forward": 1, "project_point_backward": 2, "compute_cov3d_forward": 1,
-    "compute_cov3d_backward": 1, "compute_sh_forward": 1, "compute_sh_backward": 1,
-    "ewa_project_forward": 1, "ewa_project_backward": 2, "sort_gaussian_prepare": 1 + 4 * 3 + 1 + 3,
-    "sort_gaussian_finish": 1 + 2 * 3 + 1, "alpha_blending_forward": 1, "alpha_blending_backward": 1,
-}
-
-
-def launches_per_step(stages, steps):
-    return sum(KERNELS_PER_CALL.get(k, 1) * c for k, (c, _) in stages.items()) / steps
-
-
 # ------------------------------------------------------------- CPU (oracle)
-def cpu_frame(scene, band_rows=8, threads=1):
-    """Wall time of one frame of the reference algorithm on the CPU oracle,
-    with the blend measured on `band_rows` tile rows and scaled."""
+def host_threads() -> int:
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+def cpu_frame(scene, threads):
+    """Wall time (ms) of one fwd+bwd frame of the reference algorithm on the
+    CPU oracle with `threads` host threads: SH, projection, covariance, EWA,
+    tile sort, blend forward and backward over the full image, and every
+    adjoint."""
     import oracle
-    os.environ["OMP_NUM_THREADS"] = str(threads)
-    s = {k: v.numpy() for k, v in scene.items()}
-    W, H = W_IMG, H_IMG
-    t0 = time.perf_counter()
-    dirs = s["xyz"] - (-(s["extr"][:, :3].T @ s["extr"][:, 3]))
-    dirs = (dirs / np.linalg.norm(dirs, axis=1, keepdims=True)).astype(np.float32)
-    color = oracle.compute_sh_forward(s["shs"], dirs).astype(np.float32)
-    uv, depth = oracle.project_point_forward(s["xyz"], s["intr"], s["extr"], W, H)
-    vis = (depth != 0).reshape(-1)
-    cov = oracle.compute_cov3d_forward(s["scale"], s["rot"], vis)
-    conic, radius, tiles, _ = oracle.ewa_project_forward(s["xyz"], cov, s["intr"], s["extr"], uv, W, H, vis)
-    idx, tr = oracle.sort_gaussian(uv, depth, W, H, radius, tiles)
-    t_pre = time.perf_counter() - t0
-    # band of tile rows in the middle of the image
-    gx, gy = (W + 15) // 16, (H + 15) // 16
-    r0 = gy // 2 - band_rows // 2
-    h = band_rows * 16
-    uvb = uv.copy()
-    uvb[:, 1] -= r0 * 16
-    trb = tr.reshape(gy, gx, 2)[r0:r0 + band_rows].reshape(-1, 2)
-    wb = s["weights"][:, r0 * 16:r0 * 16 + h]
-    t1 = time.perf_counter()
-    out, T, nc, _ = oracle.alpha_blending_forward(uvb, conic, s["opacity"], color, idx, trb, 0.0, W, h)
-    grads = oracle.alpha_blending_backward(uvb, conic, s["opacity"], color, idx, trb, 0.0, W, h, T, nc, wb)
-    t_blend = (time.perf_counter() - t1) * gy / band_rows
-    t2 = time.perf_counter()
-    duv, dcon, dop, dcol = grads
-    dcol = dcol.astype(np.float32)
-    oracle.ewa_project_backward(s["xyz"], cov, s["intr"], s["extr"], radius, dcon.astype(np.float32))
-    oracle.compute_cov3d_backward(s["scale"], s["rot"], vis, np.zeros_like(cov))
-    oracle.project_point_backward(s["xyz"], s["intr"], s["extr"], depth, duv.astype(np.float32),
-                                  np.zeros_like(depth))
-    oracle.compute_sh_backward(s["shs"], dirs, None, dcol)
-    t_post = time.perf_counter() - t2
-    return (t_pre + t_blend + t_post) * 1e3, band_rows, gy
+    oracle.set_threads(threads)
+    used = oracle.get_threads()
+    try:
+        s = {k: v.numpy() for k, v in scene.items()}
+        W, H = W_IMG, H_IMG
+        t0 = time.perf_counter()
+        dirs = s["xyz"] - (-(s["extr"][:, :3].T @ s["extr"][:, 3]))
+        dirs = (dirs / np.linalg.norm(dirs, axis=1, keepdims=True)).astype(np.float32)
+        color = oracle.compute_sh_forward(s["shs"], dirs).astype(np.float32)
+        uv, depth = oracle.project_point_forward(s["xyz"], s["intr"], s["extr"], W, H)
+        vis = (depth != 0).reshape(-1)
+        cov = oracle.compute_cov3d_forward(s["scale"], s["rot"], vis)
+        conic, radius, tiles, _ = oracle.ewa_project_forward(s["xyz"], cov, s["intr"], s["extr"], uv, W, H, vis)
+        idx, tr = oracle.sort_gaussian(uv, depth, W, H, radius, tiles)
+        out, T, nc, _ = oracle.alpha_blending_forward(uv, conic, s["opacity"], color, idx, tr, 0.0, W, H)
+        grads = oracle.alpha_blending_backward(uv, conic, s["opacity"], color, idx, tr, 0.0, W, H, T, nc,
+                                               s["weights"])
+        duv, dcon, dop, dcol = grads
+        dcol = dcol.astype(np.float32)
+        _, dcov, _, _ = oracle.ewa_project_backward(s["xyz"], cov, s["intr"], s["extr"], radius,
+                                                    dcon.astype(np.float32))
+        oracle.compute_cov3d_backward(s["scale"], s["rot"], vis, dcov.astype(np.float32))
+        oracle.project_point_backward(s["xyz"], s["intr"], s["extr"], depth, duv.astype(np.float32),
+                                      np.zeros_like(depth))
+        oracle.compute_sh_backward(s["shs"], dirs, None, dcol)
+        return (time.perf_counter() - t0) * 1e3, used
+    finally:
+        oracle.set_threads(1)
 
 
-def cpu_baseline(threads=1):
+CPU_SAMPLE = ("one full fwd+bwd frame of the same scene on the CPU oracle (C restatement of the reference "
+              "kernels, OpenMP over Gaussians and pixel rows): SH, projection, covariance, EWA, tile sort, "
+              "blend forward and backward over 1920x1080, and every adjoint")
+
+
+def cpu_baseline(threads):
     scene = make_scene(0)
-    ms_frame, band, gy = cpu_frame(scene, threads=threads)
-    return {"value": round(ms_frame, 1), "unit": "ms/frame", "cores": threads, "kind": "port",
-            "sample": f"all 1M Gaussians through projection/cov3d/SH/EWA/sort and their adjoints; blend fwd+bwd "
-                      f"on {band} of {gy} tile rows (1920x{band * 16} band), scaled to the frame"}
+    ms_frame, used = cpu_frame(scene, threads)
+    return {"value": round(ms_frame, 1), "unit": "ms/frame", "cores": used, "kind": "port", "sample": CPU_SAMPLE}
 
 
 # ------------------------------------------------------------- reference arm
 def run_reference(args):
-    threads = os.cpu_count() or 1
-    base = cpu_baseline(threads=threads)
+    """The reference arm: the reference algorithm (CPU oracle, the C
+    restatement of the reference's kernels) on all host threads, W untimed
+    frames then K timed frames."""
+    threads = host_threads()
+    scene = make_scene(0)
+    for _ in range(args.warmup):
+        cpu_frame(scene, threads)
+    times, used = [], 1
+    for _ in range(args.steps):
+        t, used = cpu_frame(scene, threads)
+        times.append(t)
+    ms_frame = round(float(np.mean(times)), 1)
+    base = {"value": ms_frame, "unit": "ms/frame", "cores": used, "kind": "port", "sample": CPU_SAMPLE}
     return {
-        "impl": "reference", "metric": METRIC, "value": base["value"], "unit": "ms/frame", "n_gpus": args.gpus,
-        "steps": 1, "warmup": 0, "ms_per_step": base["value"], "higher_is_better": False, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
-        "config": {"workload": "1M Gaussians, 1920x1080, SH deg 3, fwd+bwd, loss sum(W*img)"},
+        "impl": "reference", "metric": METRIC, "value": ms_frame, "unit": "ms/frame", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_frame, "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded; config distributions, random look-at camera on a radius-4 sphere)",
+        "config": {"workload": WORKLOAD, "n_gaussians": N_GAUSS, "width": W_IMG, "height": H_IMG,
+                   "sh_degree": SH_DEG, "focal": FOCAL},
         "cpu_baseline": base,
-        "e2e": {"value": base["value"], "unit": "ms/frame", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "e2e": {"value": ms_frame, "unit": "ms/frame", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
 
 

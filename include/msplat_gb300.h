@@ -57,6 +57,11 @@ MSPLAT_API const char *msplat_status_string(int status);
 MSPLAT_API const char *msplat_last_error(void);
 /* Library version, e.g. "0.1.0". */
 MSPLAT_API const char *msplat_version(void);
+/* Number of kernels this library has launched in the process so far (all
+ * host threads, all devices).  Instrumentation with no counterpart in the
+ * reference: a caller reads it around a region to count the launches
+ * inside. */
+MSPLAT_API unsigned long long msplat_kernel_launches(void);
 
 /* ------------------------------------------------------------------------ */
 /* Projection: replaces projectPointsForward / projectPointsBackward
@@ -237,8 +242,8 @@ MSPLAT_API int msplat_alpha_blending_forward(int P, int C, const float *uv,
                                   int H, float *out, float *final_T,
                                   int32_t *ncontrib, msplat_stream_t stream);
 
-/* Gradients are ACCUMULATED into dL_duv [P,2], dL_dconic [P,3],
- * dL_dopacity [P], dL_dfeature [P,C]: the caller zero-fills them. */
+/* dL_duv [P,2], dL_dconic [P,3], dL_dopacity [P], dL_dfeature [P,C] must be
+ * zero on entry (the kernels accumulate into them with atomics). */
 MSPLAT_API int msplat_alpha_blending_backward(int P, int C, const float *uv,
                                    const float *conic, const float *opacity,
                                    const float *feature,

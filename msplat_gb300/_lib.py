@@ -25,6 +25,7 @@ _SIGNATURES = {
     "msplat_status_string": (ctypes.c_char_p, [_I]),
     "msplat_last_error": (ctypes.c_char_p, []),
     "msplat_version": (ctypes.c_char_p, []),
+    "msplat_kernel_launches": (ctypes.c_ulonglong, []),
     "msplat_project_point_forward": (_I, [_I, _P, _P, _P, _I, _I, _F, _F, _P, _P, _P]),
     "msplat_camera_grad_workspace_size": (_SZ, [_I]),
     "msplat_project_point_backward": (
@@ -83,6 +84,11 @@ def load(path: str | None = None):
         if path is None:
             _lib = lib
         return lib
+
+
+def kernel_launches() -> int:
+    """Kernels the native library has launched in this process so far."""
+    return int(load().msplat_kernel_launches())
 
 
 def check(status: int, what: str) -> None:

@@ -5,6 +5,8 @@
 #include <stdint.h>
 #include <stdio.h>
 
+#include <utility>
+
 #include "msplat_gb300.h"
 
 namespace msplat {
@@ -24,6 +26,18 @@ inline int check_launch(const char *what) {
 
 __host__ __device__ inline int ceil_div(int a, int b) { return (a + b - 1) / b; }
 __host__ __device__ inline int64_t ceil_div64(int64_t a, int64_t b) { return (a + b - 1) / b; }
+
+// Counts one kernel launch (read back by msplat_kernel_launches()).
+void note_launch();
+
+// Every kernel of the library is launched through here so that the launch
+// count is exact.
+template <typename... KArgs, typename... Args>
+inline void launch(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t stream,
+                   Args &&...args) {
+    note_launch();
+    kernel<<<grid, block, smem, stream>>>(std::forward<Args>(args)...);
+}
 
 // Number of SMs of the current device (cached per device).
 int num_sms();

@@ -120,7 +120,7 @@ extern "C" int msplat_compute_cov3d_forward(int P, const float *scales,
         return set_error(MSPLAT_ERR_INVALID_ARGUMENT, "compute_cov3d_forward: null pointer");
     if (((uintptr_t)uquats & 15) != 0)
         return set_error(MSPLAT_ERR_INVALID_ARGUMENT, "compute_cov3d_forward: uquats not 16-byte aligned");
-    cov3d_fwd_kernel<<<ceil_div(P, 256), 256, 0, stream>>>(P, scales, (const float4 *)uquats,
+    launch(cov3d_fwd_kernel, ceil_div(P, 256), 256, 0, stream, P, scales, (const float4 *)uquats,
                                                            visible, cov3d);
     return check_launch("compute_cov3d_forward");
 }
@@ -137,7 +137,7 @@ extern "C" int msplat_compute_cov3d_backward(int P, const float *scales,
         return set_error(MSPLAT_ERR_INVALID_ARGUMENT, "compute_cov3d_backward: null pointer");
     if ((((uintptr_t)uquats | (uintptr_t)dL_duquats) & 15) != 0)
         return set_error(MSPLAT_ERR_INVALID_ARGUMENT, "compute_cov3d_backward: quaternion buffers not 16-byte aligned");
-    cov3d_bwd_kernel<<<ceil_div(P, 256), 256, 0, stream>>>(P, scales, (const float4 *)uquats, visible,
+    launch(cov3d_bwd_kernel, ceil_div(P, 256), 256, 0, stream, P, scales, (const float4 *)uquats, visible,
                                                            dL_dcov3d, dL_dscales, (float4 *)dL_duquats);
     return check_launch("compute_cov3d_backward");
 }

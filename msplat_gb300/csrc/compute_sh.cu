@@ -305,10 +305,10 @@ int sh_launch(bool backward, int P, int C, const float *shs, const float *dirs,
     const int blocks = ceil_div(P, nt);
     if (!backward) {
         cudaFuncSetAttribute(sh_fwd_kernel<DEG>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        sh_fwd_kernel<DEG><<<blocks, nt, smem, stream>>>(P, C, shs, dirs, visible, out);
+        launch(sh_fwd_kernel<DEG>, blocks, nt, smem, stream, P, C, shs, dirs, visible, out);
     } else {
         cudaFuncSetAttribute(sh_bwd_kernel<DEG>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        sh_bwd_kernel<DEG><<<blocks, nt, smem, stream>>>(P, C, shs, dirs, visible, dval, out, ddirs);
+        launch(sh_bwd_kernel<DEG>, blocks, nt, smem, stream, P, C, shs, dirs, visible, dval, out, ddirs);
     }
     return check_launch(backward ? "compute_sh_backward" : "compute_sh_forward");
 }

@@ -217,7 +217,7 @@ extern "C" int msplat_ewa_project_forward(int P, const float *xyz, const float *
     if (!xyz || !cov3d || !intr || !extr || !uv || !conic || !radius || !tiles)
         return set_error(MSPLAT_ERR_INVALID_ARGUMENT, "ewa_project_forward: null pointer");
     const int gx = ceil_div(W, kTile), gy = ceil_div(H, kTile);
-    ewa_fwd_kernel<<<ceil_div(P, 256), 256, 0, stream>>>(P, xyz, cov3d, intr, extr, (const float2 *)uv,
+    launch(ewa_fwd_kernel, ceil_div(P, 256), 256, 0, stream, P, xyz, cov3d, intr, extr, (const float2 *)uv,
                                                          gx, gy, visible, conic, radius, tiles);
     return check_launch("ewa_project_forward");
 }
@@ -242,8 +242,8 @@ extern "C" int msplat_ewa_project_backward(int P, const float *xyz, const float 
                          workspace_bytes, cam_grad_workspace_bytes());
     const int blocks = min(ceil_div(P, 256), kCamGradBlocks);
     float *partials = (float *)workspace;
-    ewa_bwd_kernel<<<blocks, 256, 0, stream>>>(P, xyz, cov3d, intr, extr, radius, dL_dconic,
+    launch(ewa_bwd_kernel, blocks, 256, 0, stream, P, xyz, cov3d, intr, extr, radius, dL_dconic,
                                                dL_dxyz, dL_dcov3d, cam, partials);
-    if (cam) cam_grad_finalize_kernel<<<1, 32 * kCamGradVals, 0, stream>>>(blocks, partials, dL_dintr, dL_dextr);
+    if (cam) launch(cam_grad_finalize_kernel, 1, 32 * kCamGradVals, 0, stream, blocks, partials, dL_dintr, dL_dextr);
     return check_launch("ewa_project_backward");
 }

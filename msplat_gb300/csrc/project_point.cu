@@ -131,7 +131,7 @@ extern "C" int msplat_project_point_forward(int P, const float *xyz,
     if (P == 0) return MSPLAT_OK;
     if (!xyz || !intr || !extr || !uv || !depth)
         return set_error(MSPLAT_ERR_INVALID_ARGUMENT, "project_point_forward: null pointer");
-    project_point_fwd_kernel<<<ceil_div(P, 256), 256, 0, stream>>>(
+    launch(project_point_fwd_kernel, ceil_div(P, 256), 256, 0, stream,
         P, xyz, intr, extr, W, H, nearest, extent, (float2 *)uv, depth);
     return check_launch("project_point_forward");
 }
@@ -163,9 +163,9 @@ extern "C" int msplat_project_point_backward(
         return set_error(MSPLAT_ERR_WORKSPACE, "project_point_backward: workspace of %zu bytes < %zu",
                          workspace_bytes, msplat_camera_grad_workspace_size(P));
     float *partials = (float *)workspace;
-    project_point_bwd_kernel<<<blocks, 256, 0, stream>>>(
+    launch(project_point_bwd_kernel, blocks, 256, 0, stream,
         P, xyz, intr, extr, depth, (const float2 *)dL_duv, dL_ddepth, dL_dxyz, cam, partials);
     if (cam)
-        cam_grad_finalize_kernel<<<1, 32 * kCamGradVals, 0, stream>>>(blocks, partials, dL_dintr, dL_dextr);
+        launch(cam_grad_finalize_kernel, 1, 32 * kCamGradVals, 0, stream, blocks, partials, dL_dintr, dL_dextr);
     return check_launch("project_point_backward");
 }

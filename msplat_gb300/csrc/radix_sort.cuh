@@ -2,8 +2,7 @@
 // sm_103a without library calls.
 //
 // One 8-bit pass = three launches with no device-side waiting:
-//   upsweep   per-tile digit histogram (warp-aggregated shared atomics; the
-//             lanes sharing a digit are found with ballots), stored
+//   upsweep   per-tile digit histogram (per-warp shared atomics), stored
 //             digit-major [256][tiles]
 //   row scan  one block per digit: exclusive scan of its row, offset by the
 //             totals of the smaller digits -> global start of every
@@ -12,7 +11,7 @@
 //             warp-level multisplit (stable: items are ranked in index
 //             order), reorders the tile in shared memory and writes each
 //             digit run contiguously (coalesced).
-// Tiles are 4096 items (256 threads x 16).
+// Tiles are 3072 items (256 threads x 12).
 #pragma once
 
 #include "block_scan.cuh"
@@ -22,8 +21,11 @@ namespace msplat {
 constexpr int kRadixBits = 8;
 constexpr int kRadix = 1 << kRadixBits;
 constexpr int kSortThreads = 256;
-constexpr int kSortItems = 16;
-constexpr int kSortTile = kSortThreads * kSortItems;  // 4096
+#ifndef MSPLAT_SORT_ITEMS
+#define MSPLAT_SORT_ITEMS 12
+#endif
+constexpr int kSortItems = MSPLAT_SORT_ITEMS;
+constexpr int kSortTile = kSortThreads * kSortItems;
 constexpr int kSortWarps = kSortThreads / 32;
 
 template <typename K>
@@ -52,8 +54,8 @@ __device__ __forceinline__ unsigned digit_peers(uint32_t d, unsigned valid) {
 
 // ---------------------------------------------------------------- upsweep
 // All of a thread's keys are loaded before any counting so that the loads
-// are in flight together; counts go to per-warp shared histograms through
-// one atomic per distinct digit per warp.
+// are in flight together; counts go to per-warp shared histograms with plain
+// shared atomics (cheaper than aggregating equal digits first).
 template <typename K, bool FLIP>
 __global__ void __launch_bounds__(kSortThreads)
 radix_upsweep_kernel(const K *__restrict__ keys, int64_t n, int shift, int ntiles,
@@ -72,12 +74,8 @@ radix_upsweep_kernel(const K *__restrict__ keys, int64_t n, int shift, int ntile
         dig[r] = idx < n ? digit_of(k, shift) : 0xffffffffu;
     }
 #pragma unroll
-    for (int r = 0; r < kSortItems; ++r) {
-        const bool valid = dig[r] != 0xffffffffu;
-        const unsigned vmask = __ballot_sync(0xffffffffu, valid);
-        const unsigned peers = digit_peers(dig[r] & (kRadix - 1), vmask);
-        if (valid && lane == 31 - __clz(peers)) atomicAdd(&cnt[warp][dig[r]], (uint32_t)__popc(peers));
-    }
+    for (int r = 0; r < kSortItems; ++r)
+        if (dig[r] != 0xffffffffu) atomicAdd(&cnt[warp][dig[r]], 1u);
     __syncthreads();
     uint32_t c = 0;
 #pragma unroll
@@ -254,15 +252,15 @@ int radix_sort_pairs(int64_t n, int begin_bit, int passes, const K *kin, const u
         uint32_t *tot = b.totals + p * kRadix;
         const bool first = p == 0, last = p == passes - 1;
         if (FLIP && first)
-            radix_upsweep_kernel<K, true><<<nt, kSortThreads, 0, stream>>>(ksrc, n, shift, nt, b.hist, tot);
+            launch(radix_upsweep_kernel<K, true>, nt, kSortThreads, 0, stream, ksrc, n, shift, nt, b.hist, tot);
         else
-            radix_upsweep_kernel<K, false><<<nt, kSortThreads, 0, stream>>>(ksrc, n, shift, nt, b.hist, tot);
-        radix_rowscan_kernel<<<kRadix, 1024, 0, stream>>>(b.hist, tot, nt);
-#define MSPLAT_DOWNSWEEP(FI, FO)                                                                \
-    do {                                                                                        \
-        auto kern = radix_downsweep_kernel<K, FI, FO>;                                          \
-        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);     \
-        kern<<<nt, kSortThreads, smem, stream>>>(ksrc, vsrc, kdst, vdst, n, shift, nt, b.hist); \
+            launch(radix_upsweep_kernel<K, false>, nt, kSortThreads, 0, stream, ksrc, n, shift, nt, b.hist, tot);
+        launch(radix_rowscan_kernel, kRadix, 1024, 0, stream, b.hist, tot, nt);
+#define MSPLAT_DOWNSWEEP(FI, FO)                                                                    \
+    do {                                                                                            \
+        auto kern = radix_downsweep_kernel<K, FI, FO>;                                              \
+        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);         \
+        launch(kern, nt, kSortThreads, smem, stream, ksrc, vsrc, kdst, vdst, n, shift, nt, b.hist); \
     } while (0)
         if (FLIP && first && last) MSPLAT_DOWNSWEEP(true, true);
         else if (FLIP && first) MSPLAT_DOWNSWEEP(true, false);
@@ -361,9 +359,9 @@ inline int scan_i32(int n, const int32_t *in, int32_t *out, bool inclusive, int6
         return check_launch("scan");
     }
     const int nb = ceil_div(n, kScanTile);
-    scan_reduce_kernel<<<nb, kScanThreads, 0, stream>>>(in, n, partials);
-    scan_partials_kernel<<<1, 1024, 0, stream>>>(partials, nb, total);
-    scan_apply_kernel<<<nb, kScanThreads, 0, stream>>>(in, n, partials, out, inclusive);
+    launch(scan_reduce_kernel, nb, kScanThreads, 0, stream, in, n, partials);
+    launch(scan_partials_kernel, 1, 1024, 0, stream, partials, nb, total);
+    launch(scan_apply_kernel, nb, kScanThreads, 0, stream, in, n, partials, out, inclusive);
     return check_launch("scan");
 }
 

@@ -280,7 +280,7 @@ extern "C" int msplat_compute_gaussian_key(int P, const float *uv, const float *
     if (!uv || !depth || !radius || !tiles_cumsum)
         return set_error(MSPLAT_ERR_INVALID_ARGUMENT, "compute_gaussian_key: null pointer");
     const int gx = ceil_div(W, kTile), gy = ceil_div(H, kTile);
-    gaussian_key_kernel<<<ceil_div(P, 256), 256, 0, stream>>>(P, (const float2 *)uv, depth, radius,
+    launch(gaussian_key_kernel, ceil_div(P, 256), 256, 0, stream, P, (const float2 *)uv, depth, radius,
                                                               tiles_cumsum, gx, gy, num_intersects,
                                                               key, idx);
     return check_launch("compute_gaussian_key");
@@ -298,7 +298,7 @@ extern "C" int msplat_compute_tile_gaussian_range(int W, int H, int64_t num_inte
     if (num_intersects > 0) {
         if (!key_sorted)
             return set_error(MSPLAT_ERR_INVALID_ARGUMENT, "compute_tile_gaussian_range: null keys");
-        range_from_i64_kernel<<<(unsigned)ceil_div64(num_intersects, 256), 256, 0, stream>>>(
+        launch(range_from_i64_kernel, (unsigned)ceil_div64(num_intersects, 256), 256, 0, stream,
             num_intersects, key_sorted, ntiles, (int2 *)tile_range);
     }
     return check_launch("compute_tile_gaussian_range");
@@ -429,12 +429,12 @@ extern "C" int msplat_sort_gaussian_prepare(int P, const float *depth, const int
     if (!depth || !radius || !tiles || !uv)
         return set_error(MSPLAT_ERR_INVALID_ARGUMENT, "sort_gaussian_prepare: null pointer");
     const int gx = ceil_div(W, kTile), gy = ceil_div(H, kTile);
-    depth_key_kernel<<<ceil_div(P, 256), 256, 0, stream>>>(P, depth, radius, ws.ka);
+    launch(depth_key_kernel, ceil_div(P, 256), 256, 0, stream, P, depth, radius, ws.ka);
     // Even pass count: the input keys may alias the output keys.
     int st = radix_sort_pairs<uint32_t, false>(P, 0, kDepthPasses, ws.ka, nullptr, ws.ka, ws.order,
                                                ws.kb, ws.vt, ws.rb, stream);
     if (st) return st;
-    depth_order_count_kernel<<<ceil_div(P, 256), 256, 0, stream>>>(
+    launch(depth_order_count_kernel, ceil_div(P, 256), 256, 0, stream,
         P, ws.order, (const float2 *)uv, depth, radius, tiles, gx, gy, ws.cnt, counts, ws.neg);
     return scan_i32(P, ws.cnt, ws.offs, false, counts, ws.scan_parts, stream);
 }
@@ -477,12 +477,12 @@ extern "C" int msplat_sort_gaussian_finish(int P, const float *uv, const float *
     uint32_t *out = (uint32_t *)idx_sorted;
     const bool even = passes % 2 == 0;
     uint32_t *vemit = even ? out : f.vt;
-    emit_kernel<<<ceil_div(P, 256), 256, 0, stream>>>(P, prep.order, prep.offs, (const float2 *)uv, depth,
+    launch(emit_kernel, ceil_div(P, 256), 256, 0, stream, P, prep.order, prep.offs, (const float2 *)uv, depth,
                                                       radius, gx, gy, f.ka, vemit);
     uint32_t *kout = even ? f.ka : f.kb;
     int st = radix_sort_pairs<uint32_t, false>(I, 0, passes, f.ka, vemit, kout, out, even ? f.kb : f.ka, f.vt,
                                                f.rb, stream);
     if (st) return st;
-    range_from_tilekey_kernel<<<(unsigned)ceil_div64(I, 256), 256, 0, stream>>>(I, kout, (int2 *)tile_range);
+    launch(range_from_tilekey_kernel, (unsigned)ceil_div64(I, 256), 256, 0, stream, I, kout, (int2 *)tile_range);
     return check_launch("sort_gaussian_finish");
 }

@@ -1,6 +1,8 @@
 // Status strings, last-error detail and device queries for the C ABI.
 #include <stdarg.h>
 
+#include <atomic>
+
 #include "common.cuh"
 
 namespace msplat {
@@ -14,6 +16,10 @@ int set_error(int code, const char *fmt, ...) {
     va_end(ap);
     return code;
 }
+
+static std::atomic<unsigned long long> g_launches{0};
+
+void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 
 int num_sms() {
     static int cached[64] = {0};
@@ -46,3 +52,7 @@ extern "C" const char *msplat_status_string(int status) {
 extern "C" const char *msplat_last_error(void) { return msplat::g_last_error; }
 
 extern "C" const char *msplat_version(void) { return "0.1.0"; }
+
+extern "C" unsigned long long msplat_kernel_launches(void) {
+    return msplat::g_launches.load(std::memory_order_relaxed);
+}

@@ -37,6 +37,8 @@ def _load():
             "oracle_set_fma_mode": (None, [i]),
             "oracle_get_fma_mode": (i, []),
             "oracle_set_cov_variant": (None, [i]),
+            "oracle_set_threads": (None, [i]),
+            "oracle_get_threads": (i, []),
             "oracle_project_point_forward": (None, [i, _P, _P, _P, i, i, f, f, _P, _P]),
             "oracle_project_point_backward": (None, [i, _P, _P, _P, _P, _P, _P, _P, _P, _P]),
             "oracle_compute_cov3d_forward": (None, [i, _P, _P, _P, _P]),
@@ -84,6 +86,17 @@ def set_fma_mode(mode: int) -> None:
 
 def set_cov_variant(v: int) -> None:
     _load().oracle_set_cov_variant(int(v))
+
+
+def set_threads(n: int) -> None:
+    """Host threads for the oracle's loops (1, the default, is what every
+    parity check uses)."""
+    _load().oracle_set_threads(int(n))
+
+
+def get_threads() -> int:
+    """Threads the oracle actually uses (1 when it was built without OpenMP)."""
+    return int(_load().oracle_get_threads())
 
 
 def get_fma_mode() -> int:

@@ -32,6 +32,31 @@ static int g_mode = 0;
 void oracle_set_fma_mode(int m) { g_mode = m; }
 int oracle_get_fma_mode(void) { return g_mode; }
 
+/* Host threads for the timed CPU baseline.  1 (the default, used by every
+ * parity check) runs each loop serially in index order; n > 1 splits the
+ * per-Gaussian loops into n static chunks and the pixel loops into
+ * interleaved rows.  Outputs are identical except for the order in which
+ * the double-precision camera and per-Gaussian blend gradients are summed. */
+static int g_threads = 1;
+void oracle_set_threads(int n) { g_threads = n < 1 ? 1 : n; }
+int oracle_get_threads(void) {
+#ifdef _OPENMP
+    return g_threads;
+#else
+    return 1;
+#endif
+}
+#ifdef _OPENMP
+#include <omp.h>
+#define PARFOR _Pragma("omp parallel for schedule(static) num_threads(g_threads)")
+static int thread_id(void) { return omp_get_thread_num(); }
+static int team_size(void) { return omp_get_num_threads(); }
+#else
+#define PARFOR
+static int thread_id(void) { return 0; }
+static int team_size(void) { return 1; }
+#endif
+
 static inline float madd(float a, float b, float c) { return g_mode == 2 ? a * b + c : fmaf(a, b, c); }
 
 static inline float sum2(float a, float b, float c, float d) {
@@ -93,6 +118,7 @@ static inline void cam_point(const float *e, float x, float y, float z, float *t
 /* msplat/src/project_point.cu:13-57 */
 void oracle_project_point_forward(int P, const float *xyz, const float *intr, const float *extr, int W,
                                   int H, float nearest, float extent, float *uv, float *depth) {
+    PARFOR
     for (int i = 0; i < P; ++i) {
         float t[3];
         cam_point(extr, xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2], t);
@@ -118,31 +144,44 @@ void oracle_project_point_forward(int P, const float *xyz, const float *intr, co
 void oracle_project_point_backward(int P, const float *xyz, const float *intr, const float *extr,
                                    const float *depth, const float *dL_duv, const float *dL_ddepth,
                                    double *dL_dxyz, double *dL_dintr, double *dL_dextr) {
-    const double *dummy = 0; (void)dummy;
     double gi[4] = {0, 0, 0, 0}, ge[12];
     memset(ge, 0, sizeof(ge));
     const double fx = intr[0], fy = intr[1];
-    for (int i = 0; i < P; ++i) {
-        dL_dxyz[3 * i] = dL_dxyz[3 * i + 1] = dL_dxyz[3 * i + 2] = 0.0;
-        if (depth[i] == 0.0f) continue;
-        const double p[3] = {xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2]};
-        double t[3];
-        for (int r = 0; r < 3; ++r)
-            t[r] = extr[4 * r] * p[0] + extr[4 * r + 1] * p[1] + extr[4 * r + 2] * p[2] + extr[4 * r + 3];
-        const double gu = dL_duv[2 * i], gv = dL_duv[2 * i + 1], gd = dL_ddepth[i];
-        const double dt[3] = {fx * gu / t[2], fy * gv / t[2],
-                              -(fx * t[0] * gu + fy * t[1] * gv) / (t[2] * t[2]) + gd};
-        for (int c = 0; c < 3; ++c)
-            dL_dxyz[3 * i + c] = extr[c] * dt[0] + extr[4 + c] * dt[1] + extr[8 + c] * dt[2];
-        gi[0] += t[0] / t[2] * gu;
-        gi[1] += t[1] / t[2] * gv;
-        gi[2] += gu;
-        gi[3] += gv;
-        for (int r = 0; r < 3; ++r) {
-            for (int c = 0; c < 3; ++c) ge[4 * r + c] += dt[r] * p[c];
-            ge[4 * r + 3] += dt[r];
+    double *part = (double *)calloc((size_t)g_threads * 16, sizeof(double));
+#ifdef _OPENMP
+#pragma omp parallel num_threads(g_threads)
+#endif
+    {
+        const int tid = thread_id(), nth = team_size();
+        const int i0 = (int)((int64_t)P * tid / nth), i1 = (int)((int64_t)P * (tid + 1) / nth);
+        double *pi = part + 16 * tid, *pe = pi + 4;
+        for (int i = i0; i < i1; ++i) {
+            dL_dxyz[3 * i] = dL_dxyz[3 * i + 1] = dL_dxyz[3 * i + 2] = 0.0;
+            if (depth[i] == 0.0f) continue;
+            const double p[3] = {xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2]};
+            double t[3];
+            for (int r = 0; r < 3; ++r)
+                t[r] = extr[4 * r] * p[0] + extr[4 * r + 1] * p[1] + extr[4 * r + 2] * p[2] + extr[4 * r + 3];
+            const double gu = dL_duv[2 * i], gv = dL_duv[2 * i + 1], gd = dL_ddepth[i];
+            const double dt[3] = {fx * gu / t[2], fy * gv / t[2],
+                                  -(fx * t[0] * gu + fy * t[1] * gv) / (t[2] * t[2]) + gd};
+            for (int c = 0; c < 3; ++c)
+                dL_dxyz[3 * i + c] = extr[c] * dt[0] + extr[4 + c] * dt[1] + extr[8 + c] * dt[2];
+            pi[0] += t[0] / t[2] * gu;
+            pi[1] += t[1] / t[2] * gv;
+            pi[2] += gu;
+            pi[3] += gv;
+            for (int r = 0; r < 3; ++r) {
+                for (int c = 0; c < 3; ++c) pe[4 * r + c] += dt[r] * p[c];
+                pe[4 * r + 3] += dt[r];
+            }
         }
     }
+    for (int t = 0; t < g_threads; ++t) {
+        for (int k = 0; k < 4; ++k) gi[k] += part[16 * t + k];
+        for (int k = 0; k < 12; ++k) ge[k] += part[16 * t + 4 + k];
+    }
+    free(part);
     if (dL_dintr) memcpy(dL_dintr, gi, sizeof(gi));
     if (dL_dextr) memcpy(dL_dextr, ge, sizeof(ge));
 }
@@ -198,6 +237,7 @@ static mat3f m3_mul_v(mat3f A, mat3f B, int flip) {
 /* msplat/src/compute_cov3d.cu:14-58, 119-129 */
 void oracle_compute_cov3d_forward(int P, const float *scales, const float *q, const uint8_t *visible,
                                   float *cov3d) {
+    PARFOR
     for (int i = 0; i < P; ++i) {
         float *o = cov3d + 6 * i;
         if (visible && !visible[i]) {
@@ -218,6 +258,7 @@ void oracle_compute_cov3d_forward(int P, const float *scales, const float *q, co
  * A = Rs diag(s), Rs the standard rotation of q = (r, x, y, z). */
 void oracle_compute_cov3d_backward(int P, const float *scales, const float *q, const uint8_t *visible,
                                    const float *dL_dcov, double *dL_ds, double *dL_dq) {
+    PARFOR
     for (int i = 0; i < P; ++i) {
         double *ds = dL_ds + 3 * i, *dq = dL_dq + 4 * i;
         ds[0] = ds[1] = ds[2] = 0;
@@ -278,6 +319,7 @@ void oracle_ewa_project_forward(int P, const float *xyz, const float *cov3d, con
                                 float *conic, int32_t *radius, int32_t *tiles, uint8_t *ambiguous) {
     const int gx = (W + TILE - 1) / TILE, gy = (H + TILE - 1) / TILE;
     const float fx = intr[0], fy = intr[1];
+    PARFOR
     for (int i = 0; i < P; ++i) {
         conic[3 * i] = conic[3 * i + 1] = conic[3 * i + 2] = 0.f;
         radius[i] = 0;
@@ -329,69 +371,83 @@ void oracle_ewa_project_backward(int P, const float *xyz, const float *cov3d, co
     double R[3][3];
     for (int r = 0; r < 3; ++r)
         for (int c = 0; c < 3; ++c) R[r][c] = extr[4 * r + c];
-    for (int i = 0; i < P; ++i) {
-        double *dx = dL_dxyz + 3 * i, *dv = dL_dcov3d + 6 * i;
-        memset(dx, 0, 3 * sizeof(double));
-        memset(dv, 0, 6 * sizeof(double));
-        if (!(radius[i] > 0)) continue;
-        const double p[3] = {xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2]};
-        double t[3];
-        for (int r = 0; r < 3; ++r) t[r] = R[r][0] * p[0] + R[r][1] * p[1] + R[r][2] * p[2] + extr[4 * r + 3];
-        const double J00 = fx / t[2], J11 = fy / t[2];
-        const double J02 = -fx * t[0] / (t[2] * t[2]), J12 = -fy * t[1] / (t[2] * t[2]);
-        double T0[3], T1[3];
-        for (int k = 0; k < 3; ++k) {
-            T0[k] = J00 * R[0][k] + J02 * R[2][k];
-            T1[k] = J11 * R[1][k] + J12 * R[2][k];
+    double *part = (double *)calloc((size_t)g_threads * 16, sizeof(double));
+#ifdef _OPENMP
+#pragma omp parallel num_threads(g_threads)
+#endif
+    {
+        const int tid = thread_id(), nth = team_size();
+        const int i0 = (int)((int64_t)P * tid / nth), i1 = (int)((int64_t)P * (tid + 1) / nth);
+        double *pi = part + 16 * tid, *pe = pi + 4;
+        for (int i = i0; i < i1; ++i) {
+            double *dx = dL_dxyz + 3 * i, *dv = dL_dcov3d + 6 * i;
+            memset(dx, 0, 3 * sizeof(double));
+            memset(dv, 0, 6 * sizeof(double));
+            if (!(radius[i] > 0)) continue;
+            const double p[3] = {xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2]};
+            double t[3];
+            for (int r = 0; r < 3; ++r) t[r] = R[r][0] * p[0] + R[r][1] * p[1] + R[r][2] * p[2] + extr[4 * r + 3];
+            const double J00 = fx / t[2], J11 = fy / t[2];
+            const double J02 = -fx * t[0] / (t[2] * t[2]), J12 = -fy * t[1] / (t[2] * t[2]);
+            double T0[3], T1[3];
+            for (int k = 0; k < 3; ++k) {
+                T0[k] = J00 * R[0][k] + J02 * R[2][k];
+                T1[k] = J11 * R[1][k] + J12 * R[2][k];
+            }
+            const float *vf = cov3d + 6 * i;
+            const double V[3][3] = {{vf[0], vf[1], vf[2]}, {vf[1], vf[3], vf[4]}, {vf[2], vf[4], vf[5]}};
+            double VT0[3], VT1[3];
+            for (int k = 0; k < 3; ++k) {
+                VT0[k] = V[k][0] * T0[0] + V[k][1] * T0[1] + V[k][2] * T0[2];
+                VT1[k] = V[k][0] * T1[0] + V[k][1] * T1[1] + V[k][2] * T1[2];
+            }
+            const double a = T0[0] * VT0[0] + T0[1] * VT0[1] + T0[2] * VT0[2] + 0.3;
+            const double b = T0[0] * VT1[0] + T0[1] * VT1[1] + T0[2] * VT1[2];
+            const double c = T1[0] * VT1[0] + T1[1] * VT1[1] + T1[2] * VT1[2] + 0.3;
+            const double det = a * c - b * b;
+            if (det == 0.0) continue;
+            const double g0 = dL_dconic[3 * i], g1 = dL_dconic[3 * i + 1], g2 = dL_dconic[3 * i + 2];
+            const double inv2 = 1.0 / (det * det);
+            const double da = inv2 * (-c * c * g0 + b * c * g1 + (det - a * c) * g2);
+            const double db = inv2 * (2 * b * c * g0 - (det + 2 * b * b) * g1 + 2 * a * b * g2);
+            const double dc = inv2 * ((det - a * c) * g0 + a * b * g1 - a * a * g2);
+            dv[0] = T0[0] * T0[0] * da + T0[0] * T1[0] * db + T1[0] * T1[0] * dc;
+            dv[3] = T0[1] * T0[1] * da + T0[1] * T1[1] * db + T1[1] * T1[1] * dc;
+            dv[5] = T0[2] * T0[2] * da + T0[2] * T1[2] * db + T1[2] * T1[2] * dc;
+            dv[1] = 2 * T0[0] * T0[1] * da + (T0[0] * T1[1] + T0[1] * T1[0]) * db + 2 * T1[0] * T1[1] * dc;
+            dv[2] = 2 * T0[0] * T0[2] * da + (T0[0] * T1[2] + T0[2] * T1[0]) * db + 2 * T1[0] * T1[2] * dc;
+            dv[4] = 2 * T0[1] * T0[2] * da + (T0[1] * T1[2] + T0[2] * T1[1]) * db + 2 * T1[1] * T1[2] * dc;
+            double dT0[3], dT1[3];
+            for (int k = 0; k < 3; ++k) {
+                dT0[k] = 2 * VT0[k] * da + VT1[k] * db;
+                dT1[k] = VT0[k] * db + 2 * VT1[k] * dc;
+            }
+            const double dJ00 = R[0][0] * dT0[0] + R[0][1] * dT0[1] + R[0][2] * dT0[2];
+            const double dJ02 = R[2][0] * dT0[0] + R[2][1] * dT0[1] + R[2][2] * dT0[2];
+            const double dJ11 = R[1][0] * dT1[0] + R[1][1] * dT1[1] + R[1][2] * dT1[2];
+            const double dJ12 = R[2][0] * dT1[0] + R[2][1] * dT1[1] + R[2][2] * dT1[2];
+            const double iz = 1.0 / t[2], iz2 = iz * iz, iz3 = iz2 * iz;
+            const double dt[3] = {-fx * iz2 * dJ02, -fy * iz2 * dJ12,
+                                  -fx * iz2 * dJ00 - fy * iz2 * dJ11 + 2 * fx * t[0] * iz3 * dJ02 +
+                                      2 * fy * t[1] * iz3 * dJ12};
+            for (int k = 0; k < 3; ++k) dx[k] = R[0][k] * dt[0] + R[1][k] * dt[1] + R[2][k] * dt[2];
+            pi[0] += iz * dJ00 - t[0] * iz2 * dJ02;
+            pi[1] += iz * dJ11 - t[1] * iz2 * dJ12;
+            for (int k = 0; k < 3; ++k) {
+                pe[k] += J00 * dT0[k] + p[k] * dt[0];
+                pe[4 + k] += J11 * dT1[k] + p[k] * dt[1];
+                pe[8 + k] += J02 * dT0[k] + J12 * dT1[k] + p[k] * dt[2];
+            }
+            pe[3] += dt[0];
+            pe[7] += dt[1];
+            pe[11] += dt[2];
         }
-        const float *vf = cov3d + 6 * i;
-        const double V[3][3] = {{vf[0], vf[1], vf[2]}, {vf[1], vf[3], vf[4]}, {vf[2], vf[4], vf[5]}};
-        double VT0[3], VT1[3];
-        for (int k = 0; k < 3; ++k) {
-            VT0[k] = V[k][0] * T0[0] + V[k][1] * T0[1] + V[k][2] * T0[2];
-            VT1[k] = V[k][0] * T1[0] + V[k][1] * T1[1] + V[k][2] * T1[2];
-        }
-        const double a = T0[0] * VT0[0] + T0[1] * VT0[1] + T0[2] * VT0[2] + 0.3;
-        const double b = T0[0] * VT1[0] + T0[1] * VT1[1] + T0[2] * VT1[2];
-        const double c = T1[0] * VT1[0] + T1[1] * VT1[1] + T1[2] * VT1[2] + 0.3;
-        const double det = a * c - b * b;
-        if (det == 0.0) continue;
-        const double g0 = dL_dconic[3 * i], g1 = dL_dconic[3 * i + 1], g2 = dL_dconic[3 * i + 2];
-        const double inv2 = 1.0 / (det * det);
-        const double da = inv2 * (-c * c * g0 + b * c * g1 + (det - a * c) * g2);
-        const double db = inv2 * (2 * b * c * g0 - (det + 2 * b * b) * g1 + 2 * a * b * g2);
-        const double dc = inv2 * ((det - a * c) * g0 + a * b * g1 - a * a * g2);
-        dv[0] = T0[0] * T0[0] * da + T0[0] * T1[0] * db + T1[0] * T1[0] * dc;
-        dv[3] = T0[1] * T0[1] * da + T0[1] * T1[1] * db + T1[1] * T1[1] * dc;
-        dv[5] = T0[2] * T0[2] * da + T0[2] * T1[2] * db + T1[2] * T1[2] * dc;
-        dv[1] = 2 * T0[0] * T0[1] * da + (T0[0] * T1[1] + T0[1] * T1[0]) * db + 2 * T1[0] * T1[1] * dc;
-        dv[2] = 2 * T0[0] * T0[2] * da + (T0[0] * T1[2] + T0[2] * T1[0]) * db + 2 * T1[0] * T1[2] * dc;
-        dv[4] = 2 * T0[1] * T0[2] * da + (T0[1] * T1[2] + T0[2] * T1[1]) * db + 2 * T1[1] * T1[2] * dc;
-        double dT0[3], dT1[3];
-        for (int k = 0; k < 3; ++k) {
-            dT0[k] = 2 * VT0[k] * da + VT1[k] * db;
-            dT1[k] = VT0[k] * db + 2 * VT1[k] * dc;
-        }
-        const double dJ00 = R[0][0] * dT0[0] + R[0][1] * dT0[1] + R[0][2] * dT0[2];
-        const double dJ02 = R[2][0] * dT0[0] + R[2][1] * dT0[1] + R[2][2] * dT0[2];
-        const double dJ11 = R[1][0] * dT1[0] + R[1][1] * dT1[1] + R[1][2] * dT1[2];
-        const double dJ12 = R[2][0] * dT1[0] + R[2][1] * dT1[1] + R[2][2] * dT1[2];
-        const double iz = 1.0 / t[2], iz2 = iz * iz, iz3 = iz2 * iz;
-        const double dt[3] = {-fx * iz2 * dJ02, -fy * iz2 * dJ12,
-                              -fx * iz2 * dJ00 - fy * iz2 * dJ11 + 2 * fx * t[0] * iz3 * dJ02 +
-                                  2 * fy * t[1] * iz3 * dJ12};
-        for (int k = 0; k < 3; ++k) dx[k] = R[0][k] * dt[0] + R[1][k] * dt[1] + R[2][k] * dt[2];
-        gi[0] += iz * dJ00 - t[0] * iz2 * dJ02;
-        gi[1] += iz * dJ11 - t[1] * iz2 * dJ12;
-        for (int k = 0; k < 3; ++k) {
-            ge[k] += J00 * dT0[k] + p[k] * dt[0];
-            ge[4 + k] += J11 * dT1[k] + p[k] * dt[1];
-            ge[8 + k] += J02 * dT0[k] + J12 * dT1[k] + p[k] * dt[2];
-        }
-        ge[3] += dt[0];
-        ge[7] += dt[1];
-        ge[11] += dt[2];
     }
+    for (int t = 0; t < g_threads; ++t) {
+        for (int k = 0; k < 4; ++k) gi[k] += part[16 * t + k];
+        for (int k = 0; k < 12; ++k) ge[k] += part[16 * t + 4 + k];
+    }
+    free(part);
     if (dL_dintr) memcpy(dL_dintr, gi, sizeof(gi));
     if (dL_dextr) memcpy(dL_dextr, ge, sizeof(ge));
 }
@@ -485,8 +541,9 @@ int oracle_compute_sh_forward(int P, int C, int D, const float *shs, const float
                               double *value) {
     const int deg = sh_deg_of(D);
     if (deg < 0) return 1;
-    double y[121], gx[121], gy[121], gz[121];
+    PARFOR
     for (int i = 0; i < P; ++i) {
+        double y[121], gx[121], gy[121], gz[121];
         for (int c = 0; c < C; ++c) value[(size_t)i * C + c] = 0;
         if (visible && !visible[i]) continue;
         sh_basis_d(deg, dirs[3 * i], dirs[3 * i + 1], dirs[3 * i + 2], y, gx, gy, gz);
@@ -505,8 +562,9 @@ int oracle_compute_sh_backward(int P, int C, int D, const float *shs, const floa
                                const float *dL_dval, double *dL_dshs, double *dL_ddirs) {
     const int deg = sh_deg_of(D);
     if (deg < 0) return 1;
-    double y[121], gx[121], gy[121], gz[121];
+    PARFOR
     for (int i = 0; i < P; ++i) {
+        double y[121], gx[121], gy[121], gz[121];
         double *dd = dL_ddirs + 3 * i;
         dd[0] = dd[1] = dd[2] = 0;
         for (int k = 0; k < C * D; ++k) dL_dshs[(size_t)i * C * D + k] = 0;
@@ -554,17 +612,24 @@ int64_t oracle_sort_gaussian(int P, const float *uv, const float *depth, int W, 
     memset(tile_range, 0, sizeof(int32_t) * 2 * (size_t)nt);
     if (I <= 0) return I < 0 ? 0 : I;
     kv_t *kv = (kv_t *)calloc((size_t)I, sizeof(kv_t));
+    PARFOR
     for (int64_t k = 0; k < I; ++k) kv[k].pos = k;
+    /* start offsets: exclusive int32 scan of tiles (wrapping like the
+     * reference's int32 cumsum) */
+    int32_t *start = (int32_t *)malloc(sizeof(int32_t) * (P > 0 ? P : 1));
     int32_t cum = 0;
     for (int g = 0; g < P; ++g) {
-        const int32_t prev = cum;
+        start[g] = cum;
         cum = (int32_t)((uint32_t)cum + (uint32_t)tiles[g]);
+    }
+    PARFOR
+    for (int g = 0; g < P; ++g) {
         if (radius[g] <= 0) continue;
         int x0, y0, x1, y1;
         get_rect(uv[2 * g], uv[2 * g + 1], radius[g], gx, gy, &x0, &y0, &x1, &y1);
         int32_t d;
         memcpy(&d, &depth[g], 4);
-        int64_t cur = prev;
+        int64_t cur = start[g];
         for (int ty = y0; ty < y1; ++ty)
             for (int tx = x0; tx < x1; ++tx) {
                 if (cur >= 0 && cur < I) {
@@ -574,11 +639,67 @@ int64_t oracle_sort_gaussian(int P, const float *uv, const float *depth, int W, 
                 ++cur;
             }
     }
-    qsort(kv, (size_t)I, sizeof(kv_t), kv_cmp);
+    free(start);
+    /* Sort by (key, position): a stable sort by key.  When every key's high
+     * word is a tile index, a stable counting pass by tile followed by a
+     * sort of each tile's run gives the same order as one global sort. */
+    int64_t bad = 0;
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static) num_threads(g_threads) reduction(+ : bad)
+#endif
+    for (int64_t k = 0; k < I; ++k) {
+        const int64_t t = kv[k].key >> 32;
+        bad += (t < 0 || t >= nt);
+    }
+    if (bad == 0) {
+        int64_t *off = (int64_t *)calloc((size_t)nt + 1, sizeof(int64_t));
+        int64_t *hist = (int64_t *)calloc((size_t)g_threads * nt, sizeof(int64_t));  /* [thread][tile] */
+        kv_t *tmp = (kv_t *)malloc((size_t)I * sizeof(kv_t));
+#ifdef _OPENMP
+#pragma omp parallel num_threads(g_threads)
+#endif
+        {
+            const int tid = thread_id(), nth = team_size();
+            const int64_t k0 = I * tid / nth, k1 = I * (tid + 1) / nth;
+            int64_t *h = hist + (size_t)tid * nt;
+            for (int64_t k = k0; k < k1; ++k) h[kv[k].key >> 32]++;
+#ifdef _OPENMP
+#pragma omp barrier
+#pragma omp single
+#endif
+            {
+                /* exclusive offsets in (tile, thread) order keep the scatter stable */
+                int64_t run = 0;
+                for (int t = 0; t < nt; ++t) {
+                    off[t] = run;
+                    for (int q = 0; q < nth; ++q) {
+                        const int64_t c = hist[(size_t)q * nt + t];
+                        hist[(size_t)q * nt + t] = run;
+                        run += c;
+                    }
+                }
+                off[nt] = run;
+            }
+            for (int64_t k = k0; k < k1; ++k) tmp[h[kv[k].key >> 32]++] = kv[k];
+        }
+        free(kv);
+        kv = tmp;
+        free(hist);
+#ifdef _OPENMP
+#pragma omp parallel for schedule(dynamic, 1) num_threads(g_threads)
+#endif
+        for (int t = 0; t < nt; ++t)
+            qsort(kv + off[t], (size_t)(off[t + 1] - off[t]), sizeof(kv_t), kv_cmp);
+        free(off);
+    } else {
+        qsort(kv, (size_t)I, sizeof(kv_t), kv_cmp);
+    }
+    PARFOR
     for (int64_t k = 0; k < I; ++k) {
         idx_sorted[k] = kv[k].val;
         if (keys_sorted) keys_sorted[k] = kv[k].key;
     }
+    PARFOR
     for (int64_t k = 0; k < I; ++k) {
         const int t = (int)(kv[k].key >> 32);
         if (t < 0 || t >= nt) continue;
@@ -611,7 +732,14 @@ void oracle_alpha_blending_forward(int P, int C, const float *uv, const float *c
                                    uint8_t *ambiguous) {
     (void)P;
     const int gx = (W + TILE - 1) / TILE;
+#ifdef _OPENMP
+#pragma omp parallel num_threads(g_threads)
+#endif
+    {
     float *F = (float *)malloc(sizeof(float) * (C > 0 ? C : 1));
+#ifdef _OPENMP
+#pragma omp for schedule(static, 1)
+#endif
     for (int py = 0; py < H; ++py)
         for (int px = 0; px < W; ++px) {
             const int tile = (py / TILE) * gx + px / TILE;
@@ -642,6 +770,7 @@ void oracle_alpha_blending_forward(int P, int C, const float *uv, const float *c
             for (int c = 0; c < C; ++c) out[(size_t)c * H * W + pix] = F[c] + T * bg;
         }
     free(F);
+    }
 }
 
 /* msplat/src/alpha_blending.cu:112-246, in double given the forward's
@@ -656,8 +785,30 @@ void oracle_alpha_blending_backward(int P, int C, const float *uv, const float *
     memset(dL_dconic, 0, sizeof(double) * 3 * (size_t)P);
     memset(dL_dop, 0, sizeof(double) * (size_t)P);
     memset(dL_dfeat, 0, sizeof(double) * (size_t)P * C);
+    /* Thread 0 accumulates into the outputs; threads 1.. into private
+     * buffers that are added afterwards in thread order. */
+    const size_t per = (size_t)P * (6 + C);
+    double *priv = g_threads > 1 ? (double *)calloc(per * (size_t)(g_threads - 1), sizeof(double)) : NULL;
+    int nteam = 1;
+#ifdef _OPENMP
+#pragma omp parallel num_threads(g_threads)
+#endif
+    {
+    const int tid = thread_id();
+    if (tid == 0) nteam = team_size();
+    double *dL_duv_t = dL_duv, *dL_dconic_t = dL_dconic, *dL_dop_t = dL_dop, *dL_dfeat_t = dL_dfeat;
+    if (tid > 0) {
+        double *b = priv + per * (size_t)(tid - 1);
+        dL_duv_t = b;
+        dL_dconic_t = b + 2 * (size_t)P;
+        dL_dop_t = b + 5 * (size_t)P;
+        dL_dfeat_t = b + 6 * (size_t)P;
+    }
     double *acc = (double *)malloc(sizeof(double) * 3 * (C > 0 ? C : 1));
     double *lastf = acc + C, *dpix = acc + 2 * C;
+#ifdef _OPENMP
+#pragma omp for schedule(static, 1)
+#endif
     for (int py = 0; py < H; ++py)
         for (int px = 0; px < W; ++px) {
             const int tile = (py / TILE) * gx + px / TILE;
@@ -690,19 +841,33 @@ void oracle_alpha_blending_backward(int P, int C, const float *uv, const float *
                     acc[c] = last_alpha * lastf[c] + (1.0 - last_alpha) * acc[c];
                     lastf[c] = f;
                     dL_dalpha += (f - acc[c]) * dpix[c];
-                    dL_dfeat[(size_t)g * C + c] += dcol * dpix[c];
+                    dL_dfeat_t[(size_t)g * C + c] += dcol * dpix[c];
                 }
                 dL_dalpha *= T;
                 last_alpha = alpha;
                 dL_dalpha += (-Tf / (1.0 - alpha)) * bg_dot;
                 const double dG = op * dL_dalpha;
-                dL_duv[2 * g] += dG * (-G * dx * a - G * dy * b);
-                dL_duv[2 * g + 1] += dG * (-G * dy * c_ - G * dx * b);
-                dL_dconic[3 * g] += -0.5 * G * dx * dx * dG;
-                dL_dconic[3 * g + 1] += -G * dx * dy * dG;
-                dL_dconic[3 * g + 2] += -0.5 * G * dy * dy * dG;
-                dL_dop[g] += G * dL_dalpha;
+                dL_duv_t[2 * g] += dG * (-G * dx * a - G * dy * b);
+                dL_duv_t[2 * g + 1] += dG * (-G * dy * c_ - G * dx * b);
+                dL_dconic_t[3 * g] += -0.5 * G * dx * dx * dG;
+                dL_dconic_t[3 * g + 1] += -G * dx * dy * dG;
+                dL_dconic_t[3 * g + 2] += -0.5 * G * dy * dy * dG;
+                dL_dop_t[g] += G * dL_dalpha;
             }
         }
     free(acc);
+    }
+    if (priv) {
+        PARFOR
+        for (int g = 0; g < P; ++g)
+            for (int t = 1; t < nteam; ++t) {
+                const double *b = priv + per * (size_t)(t - 1);
+                dL_duv[2 * g] += b[2 * (size_t)g];
+                dL_duv[2 * g + 1] += b[2 * (size_t)g + 1];
+                for (int k = 0; k < 3; ++k) dL_dconic[3 * g + k] += b[2 * (size_t)P + 3 * (size_t)g + k];
+                dL_dop[g] += b[5 * (size_t)P + g];
+                for (int c = 0; c < C; ++c) dL_dfeat[(size_t)g * C + c] += b[6 * (size_t)P + (size_t)g * C + c];
+            }
+        free(priv);
+    }
 }

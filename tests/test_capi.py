@@ -12,7 +12,7 @@ HEADER = os.path.join(ROOT, "include", "msplat_gb300.h")
 
 def declared_names():
     text = open(HEADER).read()
-    return sorted(set(re.findall(r"MSPLAT_API\s+(?:const\s+char\s*\*|int|size_t)\s*(msplat_\w+)\s*\(", text)))
+    return sorted(set(re.findall(r"MSPLAT_API\s+(?:const\s+char\s*\*|int|size_t|unsigned\s+long\s+long)\s*(msplat_\w+)\s*\(", text)))
 
 
 @pytest.fixture(scope="module")
@@ -83,3 +83,7 @@ def test_ops_require_cuda_tensors():
         ms.project_point(torch.zeros(4, 3), torch.ones(4), torch.eye(4)[:3], 8, 8)
     with pytest.raises(RuntimeError, match="must be a CUDA tensor"):
         ms.compute_cov3d(torch.zeros(4, 3), torch.zeros(4, 4))
+
+
+def test_launch_counter_starts_at_zero_without_gpu_work(lib):
+    assert lib.msplat_kernel_launches() == 0
