@@ -85,8 +85,19 @@ def view_dirs(xyz, extr):
 
 
 def train_step(ms, p, weights):
-    """One fwd+bwd frame through the public API (reference call sequence:
-    compute_sh -> rasterization -> loss -> backward)."""
+    """One fwd+bwd frame through the fused public call: SH colour on the
+    camera's view directions, projection, covariance and EWA in one kernel,
+    tile sort, blend, loss, backward."""
+    img = ms.rasterization_sh(p["xyz"], p["scale"], p["rot"], p["opacity"], p["shs"], p["intr"], p["extr"],
+                              W_IMG, H_IMG, 0.0)
+    loss = (img * weights).sum()
+    loss.backward()
+    return loss
+
+
+def dropin_step(ms, p, weights):
+    """The same frame in the reference's call sequence: compute_sh on view
+    directions computed in PyTorch, then rasterization."""
     color = ms.compute_sh(p["shs"], view_dirs(p["xyz"], p["extr"]))
     img = ms.rasterization(p["xyz"], p["scale"], p["rot"], p["opacity"], color, p["intr"], p["extr"],
                            W_IMG, H_IMG, 0.0)
@@ -270,6 +281,11 @@ def roofline(stages, steps, pairs, inter, nvis, sm_mhz, peaks, peak_kind):
         "compute_cov3d_backward": N_GAUSS * 81.0,
         "project_point_forward": N_GAUSS * 24.0,
         "project_point_backward": N_GAUSS * 48.0,
+        # fused: geometry 40 B in + 32 B out; SH 192 B coefficients + 12 B
+        # xyz + 4 B depth in, 12 B colour out
+        "rasterize_preprocess_forward": N_GAUSS * (72.0 + 4 * 3 * 16 + 16 + 12),
+        # SH adjoint 220 B in, 204 B out; geometry adjoint 92 B in, 40 B out
+        "rasterize_preprocess_backward": N_GAUSS * (424.0 + 132.0),
     }.get(name, 0.0)
     ach = bytes_per / (per_launch_ms * 1e-3) / 1e9
     peak = peaks.get("hbm_gbs", 6800.0)
@@ -321,9 +337,32 @@ def run_ours(args, rank, world, device):
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
     ms_step = float(t.item())
 
+    # the reference's call sequence (compute_sh + rasterization), same clock
+    dropin_ms = None
+    if not args.no_dropin:
+        for _ in range(args.warmup):
+            for t in p.values():
+                t.grad = None
+            dropin_step(ms, p, weights)
+        barrier()
+        d0, d1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        d0.record(stream)
+        for _ in range(args.steps):
+            for t in p.values():
+                t.grad = None
+            dropin_step(ms, p, weights)
+        d1.record(stream)
+        barrier()
+        dropin_ms = d0.elapsed_time(d1) / args.steps
+        t = torch.tensor([dropin_ms], device=device)
+        if world > 1:
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        dropin_ms = float(t.item())
+    extra = {"launches": n_launch, "dropin_ms": dropin_ms}
+
     # e2e: the same step with host inputs copied in and the loss read back.
     if args.no_e2e:
-        return _finish(args, rank, world, ms, p, stages, clk, ms_step, None, 0, n_launch)
+        return _finish(args, rank, world, ms, p, stages, clk, ms_step, None, 0, extra)
     host = {k: scene[k].pin_memory() for k in PARAMS}
     host_w = scene["weights"].pin_memory()
     h2d = sum(v.numel() * v.element_size() for v in host.values()) + host_w.numel() * host_w.element_size()
@@ -344,10 +383,10 @@ def run_ours(args, rank, world, device):
     if world > 1:
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
     e2e_ms = float(t.item())
-    return _finish(args, rank, world, ms, p, stages, clk, ms_step, e2e_ms, h2d, n_launch)
+    return _finish(args, rank, world, ms, p, stages, clk, ms_step, e2e_ms, h2d, extra)
 
 
-def _finish(args, rank, world, ms, p, stages, clk, ms_step, e2e_ms, h2d, n_launch):
+def _finish(args, rank, world, ms, p, stages, clk, ms_step, e2e_ms, h2d, extra):
     if rank != 0:
         return None
     pairs, inter, nvis = blend_pairs(ms, p)
@@ -376,7 +415,8 @@ def _finish(args, rank, world, ms, p, stages, clk, ms_step, e2e_ms, h2d, n_launc
                          if in_mb > 129 else f"inputs ({in_mb:.0f} MB) fit in L2; no flush (profiling case)"},
         "e2e": None if e2e_ms is None else {"value": round(e2e_ms / world, 4), "unit": "ms/frame",
                                             "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": 4},
-        "gpu_launches": int(n_launch),
+        "gpu_launches": int(extra["launches"]),
+        "dropin_ms_per_step": None if extra["dropin_ms"] is None else round(extra["dropin_ms"], 4),
         "stage_ms_per_step": stage_ms,
         "roofline": roof,
         "clocks": clk,
@@ -476,6 +516,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer (e2e) loop")
+    ap.add_argument("--no-dropin", action="store_true",
+                    help="skip timing the reference call sequence (compute_sh + rasterization)")
     ap.add_argument("--gaussians", type=int, default=N_GAUSS,
                     help="scene size (a smaller case for profiling; the benchmark is 1M)")
     ap.add_argument("--width", type=int, default=W_IMG)

@@ -255,6 +255,39 @@ MSPLAT_API int msplat_alpha_blending_backward(int P, int C, const float *uv,
                                    float *dL_dconic, float *dL_dopacity,
                                    float *dL_dfeature, msplat_stream_t stream);
 
+/* ------------------------------------------------------------------------ */
+/* Fused preprocess of a rasterisation.  No single counterpart in the
+ * reference: it is the composite project_point -> compute_cov3d ->
+ * ewa_project of msplat/__init__.py:70-93 (visible = depth != 0), optionally
+ * followed by compute_sh (msplat/compute_sh.py:8-64) on the view directions
+ * d = (xyz - c) / |xyz - c|, c = -R^T T the camera centre of extr.  uv,
+ * depth, conic, radius and tiles are bit-identical to the three stage calls.
+ * shs [P,C,D] may be NULL (C = 0); color [P,C] is written when it is not. */
+MSPLAT_API int msplat_rasterize_preprocess_forward(int P, const float *xyz, const float *scales,
+                                  const float *uquats, const float *intr, const float *extr,
+                                  int W, int H, float nearest, float extent, int C, int D,
+                                  const float *shs, float *uv, float *depth, float *conic,
+                                  int32_t *radius, int32_t *tiles, float *color,
+                                  msplat_stream_t stream);
+
+/* Scratch for the camera gradients of the backward (0 when P == 0). */
+MSPLAT_API size_t msplat_rasterize_preprocess_workspace_size(int P, int C, int D);
+
+/* Adjoint of the fused forward: from dL_duv [P,2] and dL_dconic [P,3] of
+ * the blend (and dL_dcolor [P,C] when shs is given) writes dL_dxyz [P,3]
+ * (projection + EWA + view direction), dL_dscales [P,3], dL_duquats [P,4],
+ * dL_dshs [P,C,D], and dL_dintr [4] / dL_dextr [12] when not NULL (then
+ * the workspace is required).  The covariance is recomputed, not stored. */
+MSPLAT_API int msplat_rasterize_preprocess_backward(int P, const float *xyz, const float *scales,
+                                  const float *uquats, const float *intr, const float *extr,
+                                  int C, int D, const float *shs, const float *depth,
+                                  const int32_t *radius, const float *dL_duv,
+                                  const float *dL_dconic, const float *dL_dcolor,
+                                  float *dL_dxyz, float *dL_dscales, float *dL_duquats,
+                                  float *dL_dshs, float *dL_dintr, float *dL_dextr,
+                                  void *workspace, size_t workspace_bytes,
+                                  msplat_stream_t stream);
+
 #ifdef __cplusplus
 }
 #endif

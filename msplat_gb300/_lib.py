@@ -53,6 +53,11 @@ _SIGNATURES = {
         _I, [_I, _I, _P, _P, _P, _P, _P, _P, _F, _I, _I, _P, _P, _P, _P]),
     "msplat_alpha_blending_backward": (
         _I, [_I, _I, _P, _P, _P, _P, _P, _P, _F, _I, _I, _P, _P, _P, _P, _P, _P, _P, _P]),
+    "msplat_rasterize_preprocess_forward": (
+        _I, [_I, _P, _P, _P, _P, _P, _I, _I, _F, _F, _I, _I, _P, _P, _P, _P, _P, _P, _P, _P]),
+    "msplat_rasterize_preprocess_workspace_size": (_SZ, [_I, _I, _I]),
+    "msplat_rasterize_preprocess_backward": (
+        _I, [_I, _P, _P, _P, _P, _P, _I, _I, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _SZ, _P]),
 }
 
 _lock = threading.Lock()

@@ -5,8 +5,8 @@
 // same 16 addresses (msplat/src/project_point.cu:107-144,
 // msplat/src/ewa_project.cu:206-246): heavily contended and
 // order-nondeterministic.  Here each block reduces its points with warp
-// shuffles, writes one partial row to scratch, and a single-warp kernel sums
-// the rows in a fixed order in double.
+// shuffles, writes one partial row to scratch, and one block sums the rows
+// in a fixed order in double.
 #pragma once
 
 #include "common.cuh"
@@ -38,22 +38,34 @@ __device__ __forceinline__ void block_partial_16(float (&vals)[kCamGradVals],
 }
 
 // Fixed-order sum of `nblocks` partial rows; writes (does not accumulate)
-// dL_dintr[4] and dL_dextr[12], either of which may be null.  Launched with
-// 16 warps: warp k sums column k, each lane a strided subset in double, then
-// a fixed shuffle tree -- deterministic and latency-parallel.
-static __global__ void __launch_bounds__(32 * kCamGradVals)
+// dL_dintr[4] and dL_dextr[12], either of which may be null.  Thread t sums
+// column t % 16 over rows t / 16, t / 16 + 32, ... in double with four
+// independent accumulators (so the row loads overlap); the 32 group sums
+// of a column are then added in group order.  Deterministic.
+constexpr int kCamGradGroups = 32;
+constexpr int kCamGradFinalizeThreads = kCamGradGroups * kCamGradVals;
+
+static __global__ void __launch_bounds__(kCamGradFinalizeThreads)
 cam_grad_finalize_kernel(int nblocks, const float *__restrict__ partials,
                          float *__restrict__ dL_dintr, float *__restrict__ dL_dextr) {
-    const int k = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    double s = 0.0;
-    for (int b = lane; b < nblocks; b += 32) s += (double)partials[b * kCamGradVals + k];
+    __shared__ double part[kCamGradGroups][kCamGradVals];
+    const int k = threadIdx.x % kCamGradVals, grp = threadIdx.x / kCamGradVals;
+    double s[4] = {0.0, 0.0, 0.0, 0.0};
+    int b = grp;
+    for (; b + 3 * kCamGradGroups < nblocks; b += 4 * kCamGradGroups) {
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-    if (lane != 0) return;
-    if (k < 4) {
-        if (dL_dintr) dL_dintr[k] = (float)s;
+        for (int u = 0; u < 4; ++u) s[u] += (double)partials[(b + u * kCamGradGroups) * kCamGradVals + k];
+    }
+    for (; b < nblocks; b += kCamGradGroups) s[0] += (double)partials[b * kCamGradVals + k];
+    part[grp][k] = (s[0] + s[1]) + (s[2] + s[3]);
+    __syncthreads();
+    if (threadIdx.x >= kCamGradVals) return;
+    double t = 0.0;
+    for (int g = 0; g < kCamGradGroups; ++g) t += part[g][threadIdx.x];
+    if (threadIdx.x < 4) {
+        if (dL_dintr) dL_dintr[threadIdx.x] = (float)t;
     } else if (dL_dextr) {
-        dL_dextr[k - 4] = (float)s;
+        dL_dextr[threadIdx.x - 4] = (float)t;
     }
 }
 

@@ -7,20 +7,9 @@
 // shape so Sigma is bit-identical.  Backward follows :60-117 (no
 // normalisation adjoint: the quaternion is taken as already unit length).
 // Points with visible == 0 produce zeros.
-#include "common.cuh"
-#include "mat3.cuh"
+#include "geometry.cuh"
 
 namespace msplat {
-
-__device__ __forceinline__ Mat3 quat_to_rot_cols(float r, float x, float y, float z) {
-    return Mat3::cols(1.f - 2.f * (y * y + z * z), 2.f * (x * y - r * z), 2.f * (x * z + r * y),
-                      2.f * (x * y + r * z), 1.f - 2.f * (x * x + z * z), 2.f * (y * z - r * x),
-                      2.f * (x * z - r * y), 2.f * (y * z + r * x), 1.f - 2.f * (x * x + y * y));
-}
-
-__device__ __forceinline__ Mat3 diag_scale(float sx, float sy, float sz) {
-    return Mat3::cols(sx, 0.f, 0.f, 0.f, sy, 0.f, 0.f, 0.f, sz);
-}
 
 __global__ void __launch_bounds__(256)
 cov3d_fwd_kernel(int P, const float *__restrict__ scales,
@@ -29,19 +18,7 @@ cov3d_fwd_kernel(int P, const float *__restrict__ scales,
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= P) return;
     float out[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-    if (!visible || visible[i]) {
-        const float4 q = quats[i];
-        const Mat3 S = diag_scale(scales[3 * i], scales[3 * i + 1], scales[3 * i + 2]);
-        const Mat3 R = quat_to_rot_cols(q.x, q.y, q.z, q.w);
-        const Mat3 M = S * R;
-        const Mat3 Sig = M.transposed() * M;
-        out[0] = Sig.c[0][0];
-        out[1] = Sig.c[0][1];
-        out[2] = Sig.c[0][2];
-        out[3] = Sig.c[1][1];
-        out[4] = Sig.c[1][2];
-        out[5] = Sig.c[2][2];
-    }
+    if (!visible || visible[i]) cov3d_fwd_one(scales[3 * i], scales[3 * i + 1], scales[3 * i + 2], quats[i], out);
 #pragma unroll
     for (int k = 0; k < 6; ++k) cov3d[6 * i + k] = out[k];
 }
@@ -56,49 +33,8 @@ cov3d_bwd_kernel(int P, const float *__restrict__ scales,
     float ds[3] = {0.f, 0.f, 0.f};
     float4 dq = make_float4(0.f, 0.f, 0.f, 0.f);
     if (!visible || visible[i]) {
-        const float4 q = quats[i];
-        const float r = q.x, x = q.y, y = q.z, z = q.w;
         const float s[3] = {scales[3 * i], scales[3 * i + 1], scales[3 * i + 2]};
-        // Standard rotation Rs(i,j); the glm matrix of the forward is its
-        // transpose, so M(i,j) = s_i * Rs(j,i) and Sigma = Rs S^2 Rs^T.
-        float Rs[3][3];
-        Rs[0][0] = 1.f - 2.f * (y * y + z * z); Rs[0][1] = 2.f * (x * y - r * z); Rs[0][2] = 2.f * (x * z + r * y);
-        Rs[1][0] = 2.f * (x * y + r * z); Rs[1][1] = 1.f - 2.f * (x * x + z * z); Rs[1][2] = 2.f * (y * z - r * x);
-        Rs[2][0] = 2.f * (x * z - r * y); Rs[2][1] = 2.f * (y * z + r * x); Rs[2][2] = 1.f - 2.f * (x * x + y * y);
-        const float *g = dL_dcov + 6 * i;
-        // Symmetric dL/dSigma: off-diagonal entries of the 6-vector stand for
-        // both (i,j) and (j,i).
-        const float G[3][3] = {{g[0], 0.5f * g[1], 0.5f * g[2]},
-                               {0.5f * g[1], g[3], 0.5f * g[4]},
-                               {0.5f * g[2], 0.5f * g[4], g[5]}};
-        // Sigma = A A^T with A = Rs S: dL/dA = 2 G A.
-        float A[3][3], dA[3][3];
-#pragma unroll
-        for (int a = 0; a < 3; ++a)
-#pragma unroll
-            for (int b = 0; b < 3; ++b) A[a][b] = Rs[a][b] * s[b];
-#pragma unroll
-        for (int a = 0; a < 3; ++a)
-#pragma unroll
-            for (int b = 0; b < 3; ++b)
-                dA[a][b] = 2.f * (G[a][0] * A[0][b] + G[a][1] * A[1][b] + G[a][2] * A[2][b]);
-        // A(a,b) = Rs(a,b) s_b.
-        float Gr[3][3];
-#pragma unroll
-        for (int b = 0; b < 3; ++b) {
-            ds[b] = dA[0][b] * Rs[0][b] + dA[1][b] * Rs[1][b] + dA[2][b] * Rs[2][b];
-#pragma unroll
-            for (int a = 0; a < 3; ++a) Gr[a][b] = dA[a][b] * s[b];
-        }
-        // Quaternion adjoint of the standard rotation matrix.
-        dq.x = 2.f * z * (Gr[1][0] - Gr[0][1]) + 2.f * y * (Gr[0][2] - Gr[2][0]) +
-               2.f * x * (Gr[2][1] - Gr[1][2]);
-        dq.y = 2.f * y * (Gr[0][1] + Gr[1][0]) + 2.f * z * (Gr[0][2] + Gr[2][0]) +
-               2.f * r * (Gr[2][1] - Gr[1][2]) - 4.f * x * (Gr[1][1] + Gr[2][2]);
-        dq.z = 2.f * x * (Gr[0][1] + Gr[1][0]) + 2.f * r * (Gr[0][2] - Gr[2][0]) +
-               2.f * z * (Gr[1][2] + Gr[2][1]) - 4.f * y * (Gr[0][0] + Gr[2][2]);
-        dq.w = 2.f * r * (Gr[1][0] - Gr[0][1]) + 2.f * x * (Gr[0][2] + Gr[2][0]) +
-               2.f * y * (Gr[1][2] + Gr[2][1]) - 4.f * z * (Gr[0][0] + Gr[1][1]);
+        cov3d_bwd_one(s, quats[i], dL_dcov + 6 * i, ds, dq);
     }
     dL_dscales[3 * i + 0] = ds[0];
     dL_dscales[3 * i + 1] = ds[1];

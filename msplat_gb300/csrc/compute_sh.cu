@@ -21,7 +21,7 @@
 // Coefficients are staged per block into shared memory with coalesced
 // loads (rows padded to an odd stride against bank conflicts); the
 // backward overwrites each row in place with dL/dsh and streams it out.
-#include "common.cuh"
+#include "sh_dispatch.cuh"
 
 namespace msplat {
 
@@ -203,9 +203,35 @@ __device__ __forceinline__ void unstage_rows(float *__restrict__ dst, const floa
     }
 }
 
-template <int DEG>
-__global__ void sh_fwd_kernel(int P, int C, const float *__restrict__ shs,
-                              const float *__restrict__ dirs, const uint8_t *__restrict__ visible,
+__device__ __forceinline__ void camera_centre(const float *__restrict__ e, float (&c)[3]) {
+#pragma unroll
+    for (int j = 0; j < 3; ++j) c[j] = -(__ldg(e + j) * __ldg(e + 3) + __ldg(e + 4 + j) * __ldg(e + 7) +
+                                         __ldg(e + 8 + j) * __ldg(e + 11));
+}
+
+// Direction of point p and whether it is visible; n = |x - c| in camera mode.
+template <bool CAM>
+__device__ __forceinline__ bool sh_direction(const ShDirs &in, int p, const float (&cc)[3], float (&d)[3],
+                                             float &n) {
+    if (CAM) {
+        if (in.depth[p] == 0.0f) return false;
+        const float dx = in.xyz[3 * p] - cc[0], dy = in.xyz[3 * p + 1] - cc[1], dz = in.xyz[3 * p + 2] - cc[2];
+        n = sqrtf(dx * dx + dy * dy + dz * dz);
+        d[0] = dx / n;
+        d[1] = dy / n;
+        d[2] = dz / n;
+        return true;
+    }
+    if (in.visible && !in.visible[p]) return false;
+    d[0] = in.dirs[3 * p];
+    d[1] = in.dirs[3 * p + 1];
+    d[2] = in.dirs[3 * p + 2];
+    n = 1.0f;
+    return true;
+}
+
+template <int DEG, bool CAM>
+__global__ void sh_fwd_kernel(int P, int C, const float *__restrict__ shs, ShDirs in,
                               float *__restrict__ value) {
     constexpr int D = (DEG + 1) * (DEG + 1);
     extern __shared__ float smem[];
@@ -219,15 +245,16 @@ __global__ void sh_fwd_kernel(int P, int C, const float *__restrict__ shs,
     const int p = p0 + t;
     const float *row = smem + t * stride;
     float *out = value + (size_t)p * C;
-    if (visible && !visible[p]) {
+    float cc[3] = {0.f, 0.f, 0.f}, d[3], len;
+    if (CAM) camera_centre(in.extr, cc);
+    if (!sh_direction<CAM>(in, p, cc, d, len)) {
         for (int c = 0; c < C; ++c) out[c] = 0.f;
         return;
     }
-    const float x = dirs[3 * p], y = dirs[3 * p + 1], z = dirs[3 * p + 2];
     for (int c0 = 0; c0 < C; c0 += kShChanBlock) {
         float acc[kShChanBlock] = {0.f, 0.f, 0.f, 0.f};
         const int nc = min(kShChanBlock, C - c0);
-        sh_basis<DEG, false>(x, y, z, [&](int i, float Y) {
+        sh_basis<DEG, false>(d[0], d[1], d[2], [&](int i, float Y) {
 #pragma unroll
             for (int cb = 0; cb < kShChanBlock; ++cb)
                 if (cb < nc) acc[cb] += Y * row[(c0 + cb) * D + i];
@@ -236,9 +263,8 @@ __global__ void sh_fwd_kernel(int P, int C, const float *__restrict__ shs,
     }
 }
 
-template <int DEG>
-__global__ void sh_bwd_kernel(int P, int C, const float *__restrict__ shs,
-                              const float *__restrict__ dirs, const uint8_t *__restrict__ visible,
+template <int DEG, bool CAM>
+__global__ void sh_bwd_kernel(int P, int C, const float *__restrict__ shs, ShDirs in,
                               const float *__restrict__ dL_dval, float *__restrict__ dL_dshs,
                               float *__restrict__ dL_ddirs) {
     constexpr int D = (DEG + 1) * (DEG + 1);
@@ -253,15 +279,17 @@ __global__ void sh_bwd_kernel(int P, int C, const float *__restrict__ shs,
         const int p = p0 + t;
         float *row = smem + t * stride;
         float gdx = 0.f, gdy = 0.f, gdz = 0.f;
-        if (visible && !visible[p]) {
+        float cc[3] = {0.f, 0.f, 0.f}, d[3], len = 1.f;
+        if (CAM) camera_centre(in.extr, cc);
+        const bool vis = sh_direction<CAM>(in, p, cc, d, len);
+        if (!vis) {
             for (int k = 0; k < CD; ++k) row[k] = 0.f;
         } else {
-            const float x = dirs[3 * p], y = dirs[3 * p + 1], z = dirs[3 * p + 2];
             for (int c0 = 0; c0 < C; c0 += kShChanBlock) {
                 float g[kShChanBlock] = {0.f, 0.f, 0.f, 0.f};
                 const int nc = min(kShChanBlock, C - c0);
                 for (int cb = 0; cb < nc; ++cb) g[cb] = dL_dval[(size_t)p * C + c0 + cb];
-                sh_basis<DEG, true>(x, y, z, [&](int i, float Y, float yx, float yy, float yz) {
+                sh_basis<DEG, true>(d[0], d[1], d[2], [&](int i, float Y, float yx, float yy, float yz) {
 #pragma unroll
                     for (int cb = 0; cb < kShChanBlock; ++cb) {
                         if (cb < nc) {
@@ -276,9 +304,25 @@ __global__ void sh_bwd_kernel(int P, int C, const float *__restrict__ shs,
                 });
             }
         }
-        dL_ddirs[3 * p + 0] = gdx;
-        dL_ddirs[3 * p + 1] = gdy;
-        dL_ddirs[3 * p + 2] = gdz;
+        if (!CAM) {
+            dL_ddirs[3 * p + 0] = gdx;
+            dL_ddirs[3 * p + 1] = gdy;
+            dL_ddirs[3 * p + 2] = gdz;
+        } else {
+            // d = v / |v| with v = x - c: dL/dv = (g - d (d . g)) / |v|,
+            // which is dL/dx; the camera centre's share (dL/dc = -dL/dv) is
+            // folded into the extrinsics by the fused geometry backward.
+            float gv[3] = {0.f, 0.f, 0.f};
+            if (vis) {
+                const float dg = d[0] * gdx + d[1] * gdy + d[2] * gdz;
+                gv[0] = (gdx - d[0] * dg) / len;
+                gv[1] = (gdy - d[1] * dg) / len;
+                gv[2] = (gdz - d[2] * dg) / len;
+            }
+            in.dxyz[3 * p + 0] = gv[0];
+            in.dxyz[3 * p + 1] = gv[1];
+            in.dxyz[3 * p + 2] = gv[2];
+        }
     }
     __syncthreads();
     unstage_rows(dL_dshs + (size_t)p0 * CD, smem, n, CD, stride);
@@ -293,9 +337,8 @@ inline int sh_block_points(int CD) {
 }
 
 template <int DEG>
-int sh_launch(bool backward, int P, int C, const float *shs, const float *dirs,
-              const uint8_t *visible, const float *dval, float *out, float *ddirs,
-              cudaStream_t stream) {
+int sh_launch(bool backward, int P, int C, const float *shs, const ShDirs &in, const float *dval, float *out,
+              float *ddirs, cudaStream_t stream) {
     constexpr int D = (DEG + 1) * (DEG + 1);
     const int CD = C * D;
     const int nt = sh_block_points(CD);
@@ -303,19 +346,25 @@ int sh_launch(bool backward, int P, int C, const float *shs, const float *dirs,
     if (smem > 200 * 1024)
         return set_error(MSPLAT_ERR_UNSUPPORTED, "compute_sh: C*D = %d too large", CD);
     const int blocks = ceil_div(P, nt);
-    if (!backward) {
-        cudaFuncSetAttribute(sh_fwd_kernel<DEG>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        launch(sh_fwd_kernel<DEG>, blocks, nt, smem, stream, P, C, shs, dirs, visible, out);
-    } else {
-        cudaFuncSetAttribute(sh_bwd_kernel<DEG>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        launch(sh_bwd_kernel<DEG>, blocks, nt, smem, stream, P, C, shs, dirs, visible, dval, out, ddirs);
+#define MSPLAT_SH_GO(CAM)                                                                                     \
+    if (!backward) {                                                                                          \
+        cudaFuncSetAttribute(sh_fwd_kernel<DEG, CAM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); \
+        launch(sh_fwd_kernel<DEG, CAM>, blocks, nt, smem, stream, P, C, shs, in, out);                        \
+    } else {                                                                                                  \
+        cudaFuncSetAttribute(sh_bwd_kernel<DEG, CAM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); \
+        launch(sh_bwd_kernel<DEG, CAM>, blocks, nt, smem, stream, P, C, shs, in, dval, out, ddirs);           \
     }
+    if (in.xyz) {
+        MSPLAT_SH_GO(true)
+    } else {
+        MSPLAT_SH_GO(false)
+    }
+#undef MSPLAT_SH_GO
     return check_launch(backward ? "compute_sh_backward" : "compute_sh_forward");
 }
 
-int sh_dispatch(bool backward, int P, int C, int D, const float *shs, const float *dirs,
-                const uint8_t *visible, const float *dval, float *out, float *ddirs,
-                cudaStream_t stream) {
+int sh_dispatch(bool backward, int P, int C, int D, const float *shs, const ShDirs &in, const float *dval,
+                float *out, float *ddirs, cudaStream_t stream) {
     int deg = -1;
     for (int l = 0; l <= kMaxShDeg; ++l)
         if ((l + 1) * (l + 1) == D) deg = l;
@@ -324,7 +373,7 @@ int sh_dispatch(bool backward, int P, int C, int D, const float *shs, const floa
                          "compute_sh: D = %d is not (deg+1)^2 for a degree in 0..10", D);
     switch (deg) {
 #define MSPLAT_SH_CASE(L) \
-    case L: return sh_launch<L>(backward, P, C, shs, dirs, visible, dval, out, ddirs, stream);
+    case L: return sh_launch<L>(backward, P, C, shs, in, dval, out, ddirs, stream);
         MSPLAT_SH_CASE(0) MSPLAT_SH_CASE(1) MSPLAT_SH_CASE(2) MSPLAT_SH_CASE(3)
         MSPLAT_SH_CASE(4) MSPLAT_SH_CASE(5) MSPLAT_SH_CASE(6) MSPLAT_SH_CASE(7)
         MSPLAT_SH_CASE(8) MSPLAT_SH_CASE(9) MSPLAT_SH_CASE(10)
@@ -345,7 +394,8 @@ extern "C" int msplat_compute_sh_forward(int P, int C, int D, const float *shs,
     if (P == 0 || C == 0) return MSPLAT_OK;
     if (!shs || !dirs || !value)
         return set_error(MSPLAT_ERR_INVALID_ARGUMENT, "compute_sh_forward: null pointer");
-    return sh_dispatch(false, P, C, D, shs, dirs, visible, nullptr, value, nullptr, stream);
+    const ShDirs in{dirs, visible, nullptr, nullptr, nullptr, nullptr};
+    return sh_dispatch(false, P, C, D, shs, in, nullptr, value, nullptr, stream);
 }
 
 extern "C" int msplat_compute_sh_backward(int P, int C, int D, const float *shs,
@@ -359,5 +409,6 @@ extern "C" int msplat_compute_sh_backward(int P, int C, int D, const float *shs,
                            ? MSPLAT_OK : set_error(MSPLAT_ERR_LAUNCH, "compute_sh_backward: memset failed");
     if (!shs || !dirs || !dL_dvalue || !dL_dshs || !dL_ddirs)
         return set_error(MSPLAT_ERR_INVALID_ARGUMENT, "compute_sh_backward: null pointer");
-    return sh_dispatch(true, P, C, D, shs, dirs, visible, dL_dvalue, dL_dshs, dL_ddirs, stream);
+    const ShDirs in{dirs, visible, nullptr, nullptr, nullptr, nullptr};
+    return sh_dispatch(true, P, C, D, shs, in, dL_dvalue, dL_dshs, dL_ddirs, stream);
 }

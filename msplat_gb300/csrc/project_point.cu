@@ -9,25 +9,9 @@
 // camera gradients, but reduces the camera terms per block (warp shuffles,
 // then a fixed-order pass over block partials) instead of issuing 20 global
 // atomics per point onto 16 addresses.
-#include "camgrad.cuh"
+#include "geometry.cuh"
 
 namespace msplat {
-
-struct Cam {
-    float e[12];
-    float fx, fy, cx, cy;
-};
-
-__device__ __forceinline__ Cam load_cam(const float *intr, const float *extr) {
-    Cam c;
-#pragma unroll
-    for (int k = 0; k < 12; ++k) c.e[k] = __ldg(extr + k);
-    c.fx = __ldg(intr + 0);
-    c.fy = __ldg(intr + 1);
-    c.cx = __ldg(intr + 2);
-    c.cy = __ldg(intr + 3);
-    return c;
-}
 
 __global__ void __launch_bounds__(256)
 project_point_fwd_kernel(int P, const float *__restrict__ xyz,
@@ -38,28 +22,11 @@ project_point_fwd_kernel(int P, const float *__restrict__ xyz,
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= P) return;
     const Cam c = load_cam(intr, extr);
-    const float px = xyz[3 * i + 0], py = xyz[3 * i + 1], pz = xyz[3 * i + 2];
-
-    // Same expression shape as the reference so the compiler contracts the
-    // same products into FMAs.
-    const float tx = c.e[0] * px + c.e[1] * py + c.e[2] * pz + c.e[3];
-    const float ty = c.e[4] * px + c.e[5] * py + c.e[6] * pz + c.e[7];
-    const float tz = c.e[8] * px + c.e[9] * py + c.e[10] * pz + c.e[11];
-    const float inv_z = (float)(1.0 / ((double)tz + 1e-7));
-    const float u = (float)((double)(c.fx * tx * inv_z + c.cx) - 0.5);
-    const float v = (float)((double)(c.fy * ty * inv_z + c.cy) - 0.5);
-
-    bool culled = (nearest > 0.0f) && (tz <= nearest);
-    if (extent > 0.0f) {
-        // (1 - extent) * W in float, then * 0.5 in double, as the reference.
-        const float xlo = (float)((double)((1.0f - extent) * (float)W) * 0.5);
-        const float xhi = (float)((double)((1.0f + extent) * (float)W) * 0.5);
-        const float ylo = (float)((double)((1.0f - extent) * (float)H) * 0.5);
-        const float yhi = (float)((double)((1.0f + extent) * (float)H) * 0.5);
-        culled |= (u < xlo) || (u > xhi) || (v < ylo) || (v > yhi);
-    }
-    uv[i] = culled ? make_float2(0.0f, 0.0f) : make_float2(u, v);
-    depth[i] = culled ? 0.0f : tz;
+    float2 u;
+    float d;
+    project_fwd_one(c, xyz[3 * i + 0], xyz[3 * i + 1], xyz[3 * i + 2], W, H, nearest, extent, u, d);
+    uv[i] = u;
+    depth[i] = d;
 }
 
 __global__ void __launch_bounds__(256)
@@ -78,39 +45,13 @@ project_point_bwd_kernel(int P, const float *__restrict__ xyz,
 
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < P;
          i += gridDim.x * blockDim.x) {
-        const float px = xyz[3 * i + 0], py = xyz[3 * i + 1], pz = xyz[3 * i + 2];
-        float gx = 0.0f, gy = 0.0f, gz = 0.0f;
-        if (depth[i] != 0.0f) {  // depth == 0 marks a culled point
-            const float tx = c.e[0] * px + c.e[1] * py + c.e[2] * pz + c.e[3];
-            const float ty = c.e[4] * px + c.e[5] * py + c.e[6] * pz + c.e[7];
-            const float tz = c.e[8] * px + c.e[9] * py + c.e[10] * pz + c.e[11];
-            const float iz = (float)(1.0 / (double)tz);
-            const float iz2 = (float)(1.0 / (double)(tz * tz));
-            const float2 g = dL_duv[i];
-            const float gd = dL_ddepth[i];
-            // dL/dt for t = R x + T.
-            const float dtx = c.fx * iz * g.x;
-            const float dty = c.fy * iz * g.y;
-            const float dtz = -(c.fx * tx * g.x + c.fy * ty * g.y) * iz2 + gd;
-            gx = c.e[0] * dtx + c.e[4] * dty + c.e[8] * dtz;
-            gy = c.e[1] * dtx + c.e[5] * dty + c.e[9] * dtz;
-            gz = c.e[2] * dtx + c.e[6] * dty + c.e[10] * dtz;
-            if (cam_grads) {
-                acc[0] += tx * iz * g.x;
-                acc[1] += ty * iz * g.y;
-                acc[2] += g.x;
-                acc[3] += g.y;
-                const float pt[4] = {px, py, pz, 1.0f};
-                const float dt[3] = {dtx, dty, dtz};
-#pragma unroll
-                for (int r = 0; r < 3; ++r)
-#pragma unroll
-                    for (int q = 0; q < 4; ++q) acc[4 + 4 * r + q] += dt[r] * pt[q];
-            }
-        }
-        dL_dxyz[3 * i + 0] = gx;
-        dL_dxyz[3 * i + 1] = gy;
-        dL_dxyz[3 * i + 2] = gz;
+        float g[3] = {0.0f, 0.0f, 0.0f};
+        if (depth[i] != 0.0f)  // depth == 0 marks a culled point
+            project_bwd_one(c, xyz[3 * i + 0], xyz[3 * i + 1], xyz[3 * i + 2], dL_duv[i], dL_ddepth[i], g,
+                            cam_grads, acc);
+        dL_dxyz[3 * i + 0] = g[0];
+        dL_dxyz[3 * i + 1] = g[1];
+        dL_dxyz[3 * i + 2] = g[2];
     }
     if (cam_grads) block_partial_16(acc, partials);
 }
@@ -166,6 +107,6 @@ extern "C" int msplat_project_point_backward(
     launch(project_point_bwd_kernel, blocks, 256, 0, stream,
         P, xyz, intr, extr, depth, (const float2 *)dL_duv, dL_ddepth, dL_dxyz, cam, partials);
     if (cam)
-        launch(cam_grad_finalize_kernel, 1, 32 * kCamGradVals, 0, stream, blocks, partials, dL_dintr, dL_dextr);
+        launch(cam_grad_finalize_kernel, 1, kCamGradFinalizeThreads, 0, stream, blocks, partials, dL_dintr, dL_dextr);
     return check_launch("project_point_backward");
 }

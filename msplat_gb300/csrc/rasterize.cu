@@ -1,0 +1,186 @@
+// Fused per-Gaussian preprocessing of a rasterisation: projection, 3-D
+// covariance, EWA splat (and optionally SH colour from view directions) in
+// one forward kernel, and all of their adjoints -- including the camera
+// (intrinsics / extrinsics) gradients -- in one backward kernel.
+//
+// This is the composite of msplat/__init__.py:70-93 (project_point ->
+// compute_cov3d -> ewa_project) plus the view-direction SH colour that the
+// reference's training loops evaluate before calling it.  Every quantity
+// comes from the same device functions as the single-stage kernels
+// (geometry.cuh), so uv, depth, conic, radius and tiles are bit-identical
+// to the stage-by-stage path; the covariance is recomputed in the backward
+// instead of being stored.
+#include "geometry.cuh"
+#include "sh_dispatch.cuh"
+
+namespace msplat {
+
+__global__ void __launch_bounds__(256)
+preprocess_fwd_kernel(int P, const float *__restrict__ xyz, const float *__restrict__ scales,
+                      const float4 *__restrict__ quats, const float *__restrict__ intr,
+                      const float *__restrict__ extr, int W, int H, float nearest, float extent, int gx, int gy,
+                      float2 *__restrict__ uv, float *__restrict__ depth, float *__restrict__ conic,
+                      int32_t *__restrict__ radius, int32_t *__restrict__ tiles) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P) return;
+    const Cam c = load_cam(intr, extr);
+    const float px = xyz[3 * i], py = xyz[3 * i + 1], pz = xyz[3 * i + 2];
+    float2 u;
+    float d;
+    project_fwd_one(c, px, py, pz, W, H, nearest, extent, u, d);
+    uv[i] = u;
+    depth[i] = d;
+    float o[3] = {0.f, 0.f, 0.f};
+    int rad = 0, nt = 0;
+    if (d != 0.0f) {  // visible = depth != 0, as the reference's rasterization
+        float cov[6];
+        cov3d_fwd_one(scales[3 * i], scales[3 * i + 1], scales[3 * i + 2], quats[i], cov);
+        ewa_fwd_one(c, px, py, pz, cov, u, gx, gy, o, rad, nt);
+    }
+    conic[3 * i + 0] = o[0];
+    conic[3 * i + 1] = o[1];
+    conic[3 * i + 2] = o[2];
+    radius[i] = rad;
+    tiles[i] = nt;
+}
+
+// dL/dxyz accumulates (projection + EWA) onto what the SH backward wrote
+// there when add_xyz is set.  That value gv is the adjoint of the view
+// direction's v = x - c, so the camera centre c = -R^T T receives -gv:
+// dL/dR(r,j) += T_r gv_j and dL/dT_r += sum_j R(r,j) gv_j.
+// 3 blocks per SM: 80 registers (a 24-byte spill) instead of 120.
+__global__ void __launch_bounds__(256, 3)
+preprocess_bwd_kernel(int P, const float *__restrict__ xyz, const float *__restrict__ scales,
+                      const float4 *__restrict__ quats, const float *__restrict__ intr,
+                      const float *__restrict__ extr, const float *__restrict__ depth,
+                      const int32_t *__restrict__ radius, const float2 *__restrict__ dL_duv,
+                      const float *__restrict__ dL_dconic, bool add_xyz, float *dL_dxyz,
+                      float *__restrict__ dL_dscales, float4 *__restrict__ dL_dquats, bool cam_grads,
+                      float *__restrict__ partials) {
+    const Cam c = load_cam(intr, extr);
+    float acc[kCamGradVals];
+#pragma unroll
+    for (int k = 0; k < kCamGradVals; ++k) acc[k] = 0.0f;
+
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < P; i += gridDim.x * blockDim.x) {
+        float g[3] = {0.f, 0.f, 0.f};
+        float ds[3] = {0.f, 0.f, 0.f};
+        float4 dq = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (depth[i] != 0.0f) {
+            const float px = xyz[3 * i], py = xyz[3 * i + 1], pz = xyz[3 * i + 2];
+            project_bwd_one(c, px, py, pz, dL_duv[i], 0.0f, g, cam_grads, acc);
+            if (radius[i] > 0) {
+                const float s[3] = {scales[3 * i], scales[3 * i + 1], scales[3 * i + 2]};
+                const float4 q = quats[i];
+                float cov[6], ge[3], dV[6];
+                cov3d_fwd_one(s[0], s[1], s[2], q, cov);
+                if (ewa_bwd_one(c, px, py, pz, cov, dL_dconic[3 * i], dL_dconic[3 * i + 1], dL_dconic[3 * i + 2],
+                                ge, dV, cam_grads, acc)) {
+                    cov3d_bwd_one(s, q, dV, ds, dq);
+#pragma unroll
+                    for (int k = 0; k < 3; ++k) g[k] += ge[k];
+                }
+            }
+        }
+        if (add_xyz) {
+            const float gv[3] = {dL_dxyz[3 * i], dL_dxyz[3 * i + 1], dL_dxyz[3 * i + 2]};
+#pragma unroll
+            for (int k = 0; k < 3; ++k) g[k] += gv[k];
+            if (cam_grads) {
+#pragma unroll
+                for (int r = 0; r < 3; ++r) {
+#pragma unroll
+                    for (int j = 0; j < 3; ++j) acc[4 + 4 * r + j] += c.e[4 * r + 3] * gv[j];
+                    acc[4 + 4 * r + 3] += c.e[4 * r] * gv[0] + c.e[4 * r + 1] * gv[1] + c.e[4 * r + 2] * gv[2];
+                }
+            }
+        }
+        dL_dxyz[3 * i + 0] = g[0];
+        dL_dxyz[3 * i + 1] = g[1];
+        dL_dxyz[3 * i + 2] = g[2];
+        dL_dscales[3 * i + 0] = ds[0];
+        dL_dscales[3 * i + 1] = ds[1];
+        dL_dscales[3 * i + 2] = ds[2];
+        dL_dquats[i] = dq;
+    }
+    if (cam_grads) block_partial_16(acc, partials);
+}
+
+inline int preprocess_bwd_blocks(int P) { return min(ceil_div(P, 256), kCamGradBlocks); }
+
+}  // namespace msplat
+
+using namespace msplat;
+
+extern "C" size_t msplat_rasterize_preprocess_workspace_size(int P, int C, int D) {
+    (void)C;
+    (void)D;
+    if (P <= 0) return 0;
+    return (size_t)preprocess_bwd_blocks(P) * kCamGradVals * sizeof(float);
+}
+
+extern "C" int msplat_rasterize_preprocess_forward(int P, const float *xyz, const float *scales,
+                                                   const float *uquats, const float *intr, const float *extr,
+                                                   int W, int H, float nearest, float extent, int C, int D,
+                                                   const float *shs, float *uv, float *depth, float *conic,
+                                                   int32_t *radius, int32_t *tiles, float *color,
+                                                   msplat_stream_t stream) {
+    if (P < 0 || W <= 0 || H <= 0 || C < 0)
+        return set_error(MSPLAT_ERR_INVALID_ARGUMENT, "rasterize_preprocess_forward: bad sizes P=%d W=%d H=%d C=%d",
+                         P, W, H, C);
+    if (P == 0) return MSPLAT_OK;
+    if (!xyz || !scales || !uquats || !intr || !extr || !uv || !depth || !conic || !radius || !tiles)
+        return set_error(MSPLAT_ERR_INVALID_ARGUMENT, "rasterize_preprocess_forward: null pointer");
+    if (((uintptr_t)uquats & 15) != 0 || ((uintptr_t)uv & 7) != 0)
+        return set_error(MSPLAT_ERR_INVALID_ARGUMENT, "rasterize_preprocess_forward: misaligned uquats / uv");
+    const bool sh = shs != nullptr && C > 0;
+    if (sh && !color)
+        return set_error(MSPLAT_ERR_INVALID_ARGUMENT, "rasterize_preprocess_forward: shs given without color");
+    const int gx = ceil_div(W, kTile), gy = ceil_div(H, kTile);
+    launch(preprocess_fwd_kernel, ceil_div(P, 256), 256, 0, stream, P, xyz, scales, (const float4 *)uquats, intr,
+           extr, W, H, nearest, extent, gx, gy, (float2 *)uv, depth, conic, radius, tiles);
+    int st = check_launch("rasterize_preprocess_forward");
+    if (st || !sh) return st;
+    const ShDirs in{nullptr, nullptr, xyz, extr, depth, nullptr};
+    return sh_dispatch(false, P, C, D, shs, in, nullptr, color, nullptr, stream);
+}
+
+extern "C" int msplat_rasterize_preprocess_backward(
+    int P, const float *xyz, const float *scales, const float *uquats, const float *intr, const float *extr,
+    int C, int D, const float *shs, const float *depth, const int32_t *radius, const float *dL_duv,
+    const float *dL_dconic, const float *dL_dcolor, float *dL_dxyz, float *dL_dscales, float *dL_duquats,
+    float *dL_dshs, float *dL_dintr, float *dL_dextr, void *workspace, size_t workspace_bytes,
+    msplat_stream_t stream) {
+    if (P < 0 || C < 0) return set_error(MSPLAT_ERR_INVALID_ARGUMENT, "rasterize_preprocess_backward: bad sizes");
+    const bool cam = dL_dintr || dL_dextr;
+    if (P == 0) {
+        if (dL_dintr) cudaMemsetAsync(dL_dintr, 0, 4 * sizeof(float), stream);
+        if (dL_dextr) cudaMemsetAsync(dL_dextr, 0, 12 * sizeof(float), stream);
+        return check_launch("rasterize_preprocess_backward");
+    }
+    if (!xyz || !scales || !uquats || !intr || !extr || !depth || !radius || !dL_duv || !dL_dconic || !dL_dxyz ||
+        !dL_dscales || !dL_duquats)
+        return set_error(MSPLAT_ERR_INVALID_ARGUMENT, "rasterize_preprocess_backward: null pointer");
+    if ((((uintptr_t)uquats | (uintptr_t)dL_duquats) & 15) != 0 || ((uintptr_t)dL_duv & 7) != 0)
+        return set_error(MSPLAT_ERR_INVALID_ARGUMENT, "rasterize_preprocess_backward: misaligned buffers");
+    const bool sh = shs != nullptr && C > 0;
+    if (sh && (!dL_dcolor || !dL_dshs))
+        return set_error(MSPLAT_ERR_INVALID_ARGUMENT, "rasterize_preprocess_backward: shs without dL_dcolor / dL_dshs");
+    const size_t need = msplat_rasterize_preprocess_workspace_size(P, sh ? C : 0, sh ? D : 0);
+    if (cam && (!workspace || workspace_bytes < need))
+        return set_error(MSPLAT_ERR_WORKSPACE, "rasterize_preprocess_backward: workspace of %zu bytes < %zu",
+                         workspace_bytes, need);
+    const int gblocks = preprocess_bwd_blocks(P);
+    float *partials = (float *)workspace;
+    if (sh) {
+        // writes dL/dxyz (view-direction part) first; the geometry kernel adds
+        const ShDirs in{nullptr, nullptr, xyz, extr, depth, dL_dxyz};
+        const int st = sh_dispatch(true, P, C, D, shs, in, dL_dcolor, dL_dshs, nullptr, stream);
+        if (st) return st;
+    }
+    launch(preprocess_bwd_kernel, gblocks, 256, 0, stream, P, xyz, scales, (const float4 *)uquats, intr, extr, depth,
+           radius, (const float2 *)dL_duv, dL_dconic, sh, dL_dxyz, dL_dscales, (float4 *)dL_duquats, cam, partials);
+    if (cam) launch(cam_grad_finalize_kernel, 1, kCamGradFinalizeThreads, 0, stream, gblocks, partials, dL_dintr,
+                    dL_dextr);
+    return check_launch("rasterize_preprocess_backward");
+}
