@@ -363,21 +363,41 @@ def run_ours(args, rank, world, device):
     # e2e: the same step with host inputs copied in and the loss read back.
     if args.no_e2e:
         return _finish(args, rank, world, ms, p, stages, clk, ms_step, None, 0, extra)
+    # Inputs (parameters and loss weights) are copied from pinned host memory
+    # every step, double-buffered: step k + 1's copy runs on a second stream
+    # while step k computes; each step's loss is copied back to pinned host
+    # memory and read after the timed region.
+    from msplat_gb300.pipeline import HostStager
     host = {k: scene[k].pin_memory() for k in PARAMS}
-    host_w = scene["weights"].pin_memory()
-    h2d = sum(v.numel() * v.element_size() for v in host.values()) + host_w.numel() * host_w.element_size()
-    for _ in range(max(1, args.warmup // 2)):
-        pe = {k: v.to(device, non_blocking=True).requires_grad_() for k, v in host.items()}
-        train_step(ms, pe, host_w.to(device, non_blocking=True)).item()
+    host["weights"] = scene["weights"].pin_memory()
+    stager = HostStager(host, device)
+    h2d = stager.nbytes()
+    loss_host = torch.empty(args.steps + args.warmup, dtype=torch.float32).pin_memory()
+
+    def e2e_loop(n, base):
+        stager.prefetch(0)
+        for j in range(n):
+            if j + 1 < n:
+                stager.prefetch(j + 1)
+            d = stager.get(j)
+            pe = {}
+            for k in PARAMS:
+                d[k].grad = None
+                pe[k] = d[k].requires_grad_()
+            loss = train_step(ms, pe, d["weights"])
+            loss_host[base + j].copy_(loss.detach(), non_blocking=True)
+            stager.release(j)
+
+    e2e_loop(max(1, args.warmup), 0)
     barrier()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(stream)
-    for _ in range(args.steps):
-        pe = {k: v.to(device, non_blocking=True).requires_grad_() for k, v in host.items()}
-        loss = train_step(ms, pe, host_w.to(device, non_blocking=True))
-        loss.item()
+    e2e_loop(args.steps, args.warmup)
     e1.record(stream)
     barrier()
+    losses = loss_host[args.warmup:].tolist()
+    if not all(math.isfinite(x) for x in losses):
+        raise RuntimeError(f"non-finite loss in the e2e loop: {losses}")
     e2e_ms = e0.elapsed_time(e1) / args.steps
     t = torch.tensor([e2e_ms], device=device)
     if world > 1:
@@ -414,7 +434,9 @@ def _finish(args, rank, world, ms, p, stages, clk, ms_step, e2e_ms, h2d, extra):
                    "l2": f"inputs ({in_mb:.0f} MB) larger than L2 (129 MB); no flush"
                          if in_mb > 129 else f"inputs ({in_mb:.0f} MB) fit in L2; no flush (profiling case)"},
         "e2e": None if e2e_ms is None else {"value": round(e2e_ms / world, 4), "unit": "ms/frame",
-                                            "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": 4},
+                                            "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": 4,
+                                            "copies": "double-buffered on a second stream, overlapping the "
+                                                      "previous step's compute"},
         "gpu_launches": int(extra["launches"]),
         "dropin_ms_per_step": None if extra["dropin_ms"] is None else round(extra["dropin_ms"], 4),
         "stage_ms_per_step": stage_ms,
