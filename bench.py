@@ -530,6 +530,110 @@ def run_reference(args):
     }
 
 
+# ------------------------------------------------------ multi-camera batch
+BATCH_SIZES = [(256, 256), (512, 512), (1280, 720), (1920, 1080)]
+
+
+def batch_scene(n, n_cams, seed=0):
+    """One scene with the config-0 distributions (SH degree 3, N(0, 0.3)
+    coefficients) and n_cams sphere cameras, resolutions drawn uniformly
+    from BATCH_SIZES, focal length keeping the 1080p field of view."""
+    g = torch.Generator().manual_seed(seed)
+    xyz = torch.rand(n, 3, generator=g) * 2 - 1
+    scale = torch.exp(torch.rand(n, 3, generator=g) * 2 - 5)
+    rot = torch.randn(n, 4, generator=g)
+    rot = rot / rot.norm(dim=-1, keepdim=True)
+    opacity = torch.sigmoid(torch.randn(n, 1, generator=g))
+    shs = torch.randn(n, 3, 16, generator=g) * 0.3
+    pick = torch.randint(0, len(BATCH_SIZES), (n_cams,), generator=g).tolist()
+    sizes = [BATCH_SIZES[i] for i in pick]
+    intrs, extrs = [], []
+    for w, h in sizes:
+        f = 1500.0 * w / 1920.0
+        intrs.append([f, f, w / 2, h / 2])
+        v = torch.randn(3, generator=g, dtype=torch.float64)
+        eye = (v / v.norm() * 4.0).numpy()
+        fw = -eye / np.linalg.norm(eye)
+        r = np.cross(fw, [0.0, 1.0, 0.0])
+        r /= np.linalg.norm(r)
+        d = np.cross(fw, r)
+        R = np.stack([r, d, fw])
+        extrs.append(np.concatenate([R, (-R @ eye)[:, None]], 1))
+    weights = [torch.randn(3, h, w, generator=g) for w, h in sizes]
+    return dict(xyz=xyz, scale=scale, rot=rot, opacity=opacity, shs=shs,
+                intrs=torch.tensor(intrs, dtype=torch.float32),
+                extrs=torch.tensor(np.stack(extrs), dtype=torch.float32)), sizes, weights
+
+
+def run_batch(args, device):
+    """Config 3: 64 cameras of one 2M-Gaussian scene, fwd+bwd, through one
+    rasterization_sh_batch call against 64 rasterization_sh calls."""
+    import msplat_gb300 as ms
+    n, n_cams = args.gaussians if args.gaussians != 1_000_000 else 2_000_000, args.cameras
+    sc, sizes, weights = batch_scene(n, n_cams)
+    p = {k: v.to(device).contiguous().requires_grad_() for k, v in sc.items()}
+    ws = [w.to(device) for w in weights]
+
+    def batched():
+        imgs = ms.rasterization_sh_batch(p["xyz"], p["scale"], p["rot"], p["opacity"], p["shs"], p["intrs"],
+                                         p["extrs"], sizes, 0.0)
+        sum((i * w).sum() for i, w in zip(imgs, ws)).backward()
+
+    def sequential():
+        for b, (w, h) in enumerate(sizes):
+            img = ms.rasterization_sh(p["xyz"], p["scale"], p["rot"], p["opacity"], p["shs"], p["intrs"][b],
+                                      p["extrs"][b], w, h, 0.0)
+            (img * ws[b]).sum().backward()
+
+    def timed(fn):
+        for _ in range(args.warmup):
+            for t in p.values():
+                t.grad = None
+            fn()
+        torch.cuda.synchronize()
+        out = []
+        for _ in range(args.steps):
+            for t in p.values():
+                t.grad = None
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            fn()
+            e1.record()
+            torch.cuda.synchronize()
+            out.append(e0.elapsed_time(e1))
+        return out
+
+    clocks = ClockSampler(torch.cuda.current_device())
+    clocks.start()
+    tb = timed(batched)
+    ts = timed(sequential)
+    clk = clocks.stop()
+    from msplat_gb300 import _lib
+    stage = {}
+    for name, fn in (("batched", batched), ("sequential", sequential)):
+        for t in p.values():
+            t.grad = None
+        _lib.profile_start()
+        fn()
+        stage[name] = {k: round(v[1], 3) for k, v in sorted(_lib.profile_stop().items(), key=lambda kv: -kv[1][1])}
+    mb, msq = float(np.median(tb)), float(np.median(ts))
+    return {
+        "metric": "batched renders/s (fwd+bwd), 64 cameras of one 2M-Gaussian scene",
+        "value": round(n_cams / (mb * 1e-3), 2), "unit": "renders/s", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(mb, 3), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded; config distributions)",
+        "config": {"workload": f"{n} Gaussians, SH deg 3, {n_cams} sphere cameras at "
+                               f"{sorted(set(sizes))}, fwd+bwd, loss sum_b sum(W_b*img_b)",
+                   "cameras": n_cams, "n_gaussians": n,
+                   "pixels": int(sum(w * h for w, h in sizes))},
+        "batched_ms": [round(x, 3) for x in tb], "sequential_ms": [round(x, 3) for x in ts],
+        "sequential_renders_per_s": round(n_cams / (msq * 1e-3), 2),
+        "speedup_vs_one_by_one": round(msq / mb, 3),
+        "stage_ms_per_batch": stage,
+        "clocks": clk,
+    }
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -544,6 +648,9 @@ def main():
                     help="scene size (a smaller case for profiling; the benchmark is 1M)")
     ap.add_argument("--width", type=int, default=W_IMG)
     ap.add_argument("--height", type=int, default=H_IMG)
+    ap.add_argument("--workload", default="frame", choices=["frame", "batch"],
+                    help="frame: the 1M / 1080p training frame (default); batch: 64 cameras of a 2M scene")
+    ap.add_argument("--cameras", type=int, default=64)
     args = ap.parse_args()
     set_workload(args.gaussians, args.width, args.height)
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -559,6 +666,10 @@ def main():
         torch.distributed.init_process_group("nccl", device_id=device)
     from msplat_gb300 import _build
     _build.build()
+    if args.workload == "batch":
+        if rank == 0:
+            print(json.dumps(run_batch(args, device)), flush=True)
+        return
     out = run_ours(args, rank, world, device)
     if rank == 0:
         print(json.dumps(out), flush=True)

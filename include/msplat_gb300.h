@@ -288,6 +288,39 @@ MSPLAT_API int msplat_rasterize_preprocess_backward(int P, const float *xyz, con
                                   void *workspace, size_t workspace_bytes,
                                   msplat_stream_t stream);
 
+/* ------------------------------------------------------------------------ */
+/* Batched preprocess of one scene for B cameras.  No counterpart in the
+ * reference (one camera per call).  cams [B,16] = intr (fx, fy, cx, cy)
+ * then extr (3x4 row-major); dims [B,2] int32 = (W, H).  Outputs are
+ * camera-major: uv [B,P,2], depth [B,P,1], conic [B,P,3], radius [B,P],
+ * tiles [B,P], color [B,P,C] (when shs [P,C,D] is given; C = 0 otherwise);
+ * each camera's slice equals msplat_rasterize_preprocess_forward for that
+ * camera bit for bit.  Each Gaussian and its SH rows are read once. */
+MSPLAT_API int msplat_batch_preprocess_forward(int P, int B, const float *xyz, const float *scales,
+                                  const float *uquats, const float *cams, const int32_t *dims,
+                                  float nearest, float extent, int C, int D, const float *shs,
+                                  float *uv, float *depth, float *conic, int32_t *radius,
+                                  int32_t *tiles, float *color, msplat_stream_t stream);
+
+/* Scratch of the backward's camera gradients (B x blocks x 16 floats). */
+MSPLAT_API size_t msplat_batch_preprocess_workspace_size(int P, int B, int C, int D);
+
+/* Adjoint: from the per-camera blend gradients dL_duv [B,P,2], dL_dconic
+ * [B,P,3], dL_dcolor [B,P,C] (with shs) and dL_dopacity_cam [B,P] (may be
+ * NULL) writes the gradients summed over the cameras -- dL_dxyz [P,3],
+ * dL_dscales [P,3], dL_duquats [P,4], dL_dshs [P,C,D], dL_dopacity [P]
+ * (may be NULL) -- and, when dL_dcams [B,16] is not NULL, each camera's
+ * (intr, extr) gradient (then the workspace is required). */
+MSPLAT_API int msplat_batch_preprocess_backward(int P, int B, const float *xyz, const float *scales,
+                                  const float *uquats, const float *cams, int C, int D,
+                                  const float *shs, const float *depth, const int32_t *radius,
+                                  const float *dL_duv, const float *dL_dconic,
+                                  const float *dL_dcolor, const float *dL_dopacity_cam,
+                                  float *dL_dxyz, float *dL_dscales, float *dL_duquats,
+                                  float *dL_dshs, float *dL_dopacity, float *dL_dcams,
+                                  void *workspace, size_t workspace_bytes,
+                                  msplat_stream_t stream);
+
 #ifdef __cplusplus
 }
 #endif

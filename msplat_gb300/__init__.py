@@ -11,6 +11,7 @@ from .compute_sh import compute_sh
 from .sort_gaussian import sort_gaussian
 from .alpha_blending import alpha_blending
 from .rasterize import preprocess, rasterization, rasterization_sh
+from .batch import rasterization_batch, rasterization_sh_batch
 
 __all__ = [
     "project_point",
@@ -22,6 +23,8 @@ __all__ = [
     "rasterization",
     "rasterization_sh",
     "preprocess",
+    "rasterization_batch",
+    "rasterization_sh_batch",
 ]
 
 __version__ = "0.1.0"

@@ -45,10 +45,15 @@ __device__ __forceinline__ void block_partial_16(float (&vals)[kCamGradVals],
 constexpr int kCamGradGroups = 32;
 constexpr int kCamGradFinalizeThreads = kCamGradGroups * kCamGradVals;
 
+// Launched with one block per camera: block b reads rows
+// [b * nblocks, (b + 1) * nblocks) and writes at out_stride * b.
 static __global__ void __launch_bounds__(kCamGradFinalizeThreads)
 cam_grad_finalize_kernel(int nblocks, const float *__restrict__ partials,
-                         float *__restrict__ dL_dintr, float *__restrict__ dL_dextr) {
+                         float *__restrict__ dL_dintr, float *__restrict__ dL_dextr, int out_stride) {
     __shared__ double part[kCamGradGroups][kCamGradVals];
+    partials += (size_t)blockIdx.x * nblocks * kCamGradVals;
+    if (dL_dintr) dL_dintr += (size_t)blockIdx.x * out_stride;
+    if (dL_dextr) dL_dextr += (size_t)blockIdx.x * out_stride;
     const int k = threadIdx.x % kCamGradVals, grp = threadIdx.x / kCamGradVals;
     double s[4] = {0.0, 0.0, 0.0, 0.0};
     int b = grp;

@@ -112,6 +112,7 @@ extern "C" int msplat_ewa_project_backward(int P, const float *xyz, const float 
     float *partials = (float *)workspace;
     launch(ewa_bwd_kernel, blocks, 256, 0, stream, P, xyz, cov3d, intr, extr, radius, dL_dconic,
                                                dL_dxyz, dL_dcov3d, cam, partials);
-    if (cam) launch(cam_grad_finalize_kernel, 1, kCamGradFinalizeThreads, 0, stream, blocks, partials, dL_dintr, dL_dextr);
+    if (cam) launch(cam_grad_finalize_kernel, 1, kCamGradFinalizeThreads, 0, stream, blocks, partials, dL_dintr,
+               dL_dextr, 0);
     return check_launch("ewa_project_backward");
 }

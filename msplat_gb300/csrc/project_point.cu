@@ -107,6 +107,7 @@ extern "C" int msplat_project_point_backward(
     launch(project_point_bwd_kernel, blocks, 256, 0, stream,
         P, xyz, intr, extr, depth, (const float2 *)dL_duv, dL_ddepth, dL_dxyz, cam, partials);
     if (cam)
-        launch(cam_grad_finalize_kernel, 1, kCamGradFinalizeThreads, 0, stream, blocks, partials, dL_dintr, dL_dextr);
+        launch(cam_grad_finalize_kernel, 1, kCamGradFinalizeThreads, 0, stream, blocks, partials, dL_dintr,
+               dL_dextr, 0);
     return check_launch("project_point_backward");
 }

@@ -181,6 +181,6 @@ extern "C" int msplat_rasterize_preprocess_backward(
     launch(preprocess_bwd_kernel, gblocks, 256, 0, stream, P, xyz, scales, (const float4 *)uquats, intr, extr, depth,
            radius, (const float2 *)dL_duv, dL_dconic, sh, dL_dxyz, dL_dscales, (float4 *)dL_duquats, cam, partials);
     if (cam) launch(cam_grad_finalize_kernel, 1, kCamGradFinalizeThreads, 0, stream, gblocks, partials, dL_dintr,
-                    dL_dextr);
+                    dL_dextr, 0);
     return check_launch("rasterize_preprocess_backward");
 }
