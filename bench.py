@@ -634,6 +634,94 @@ def run_batch(args, device):
     }
 
 
+# --------------------------------------------------------------- serving
+SERVE_SIZES = [(512, 512), (1280, 720), (1920, 1080)]
+
+
+def serve_workload(rate, duration, seed=0, n_scenes=8):
+    """Config 4: n_scenes resident scenes, N log-uniform in [1e5, 3e6]
+    (config-0 distributions, SH degree 3); Poisson arrivals at `rate`
+    requests/s for `duration` s, each a random sphere camera at one of
+    SERVE_SIZES, 80 % forward-only, 20 % forward + backward."""
+    from msplat_gb300.serve import Request
+    g = torch.Generator().manual_seed(seed)
+    rng = np.random.default_rng(seed)
+    scenes = []
+    for _ in range(n_scenes):
+        n = int(round(10 ** rng.uniform(5, np.log10(3e6))))
+        xyz = torch.rand(n, 3, generator=g) * 2 - 1
+        scale = torch.exp(torch.rand(n, 3, generator=g) * 2 - 5)
+        rot = torch.randn(n, 4, generator=g)
+        rot = rot / rot.norm(dim=-1, keepdim=True)
+        scenes.append({"xyz": xyz.cuda(), "scale": scale.cuda(), "rot": rot.cuda(),
+                       "opacity": torch.sigmoid(torch.randn(n, 1, generator=g)).cuda(),
+                       "shs": (torch.randn(n, 3, 16, generator=g) * 0.3).cuda()})
+    weights = {sz: torch.randn(3, sz[1], sz[0], generator=g).cuda() for sz in SERVE_SIZES}
+    t, reqs = 0.0, []
+    while True:
+        t += rng.exponential(1.0 / rate)
+        if t > duration:
+            break
+        w, h = SERVE_SIZES[rng.integers(len(SERVE_SIZES))]
+        f = 1500.0 * w / 1920.0
+        v = rng.normal(size=3)
+        eye = v / np.linalg.norm(v) * 4.0
+        fw = -eye / np.linalg.norm(eye)
+        r = np.cross(fw, [0.0, 1.0, 0.0])
+        r /= np.linalg.norm(r)
+        R = np.stack([r, np.cross(fw, r), fw])
+        extr = torch.tensor(np.concatenate([R, (-R @ eye)[:, None]], 1), dtype=torch.float32).cuda()
+        bwd = bool(rng.random() < 0.2)
+        reqs.append(Request(scene=int(rng.integers(n_scenes)), intr=torch.tensor([f, f, w / 2, h / 2]).cuda(),
+                            extr=extr, W=w, H=h, backward=bwd, weights=weights[(w, h)] if bwd else None,
+                            arrival=t))
+    return scenes, reqs
+
+
+def run_serve(args):
+    from msplat_gb300.serve import Server, serve_one_by_one
+    scenes, reqs = serve_workload(args.rate, args.duration)
+    srv = Server(scenes, hbm_budget=120 << 30, streams=args.streams, max_batch=16)
+    # warm-up: every scene and size once, through both paths
+    warm = [copy_request(r, 0.0) for r in reqs[:24]]
+    srv.serve(warm)
+    serve_one_by_one(scenes, [copy_request(r, 0.0) for r in reqs[:8]])
+    torch.cuda.synchronize()
+
+    def stats(done):
+        lat = np.array([r.latency for r in done]) * 1e3
+        span = max(r.done for r in done) - min(r.arrival for r in done)
+        return {"renders_per_s": round(len(done) / span, 2), "p50_ms": round(float(np.percentile(lat, 50)), 2),
+                "p99_ms": round(float(np.percentile(lat, 99)), 2), "makespan_s": round(span, 3)}
+
+    clocks = ClockSampler(torch.cuda.current_device())
+    clocks.start()
+    served = stats(srv.serve([copy_request(r, r.arrival) for r in reqs]))
+    torch.cuda.synchronize()
+    single = stats(serve_one_by_one(scenes, [copy_request(r, r.arrival) for r in reqs]))
+    clk = clocks.stop()
+    sizes = [s["xyz"].shape[0] for s in scenes]
+    return {
+        "metric": "served renders/s and p99 latency (continuous batching) vs one request at a time",
+        "value": served["renders_per_s"], "unit": "renders/s", "n_gpus": 1, "steps": len(reqs), "warmup": 32,
+        "ms_per_step": round(1e3 / served["renders_per_s"], 3), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded; config distributions, Poisson arrivals)",
+        "config": {"workload": f"{len(scenes)} resident scenes (N = {sizes}), SH deg 3, Poisson {args.rate} req/s "
+                               f"for {args.duration} s, sizes {SERVE_SIZES}, 80% fwd / 20% fwd+bwd, "
+                               f"120 GB budget, {args.streams} streams, batches up to 16",
+                   "requests": len(reqs), "backward_requests": sum(r.backward for r in reqs)},
+        "served": served, "one_by_one": single,
+        "throughput_ratio": round(served["renders_per_s"] / single["renders_per_s"], 3),
+        "clocks": clk,
+    }
+
+
+def copy_request(r, arrival):
+    from msplat_gb300.serve import Request
+    return Request(scene=r.scene, intr=r.intr, extr=r.extr, W=r.W, H=r.H, backward=r.backward, weights=r.weights,
+                   arrival=arrival, bg=r.bg)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -648,9 +736,13 @@ def main():
                     help="scene size (a smaller case for profiling; the benchmark is 1M)")
     ap.add_argument("--width", type=int, default=W_IMG)
     ap.add_argument("--height", type=int, default=H_IMG)
-    ap.add_argument("--workload", default="frame", choices=["frame", "batch"],
-                    help="frame: the 1M / 1080p training frame (default); batch: 64 cameras of a 2M scene")
+    ap.add_argument("--workload", default="frame", choices=["frame", "batch", "serve"],
+                    help="frame: the 1M / 1080p training frame (default); batch: 64 cameras of a 2M scene; "
+                         "serve: the request server over 8 resident scenes")
     ap.add_argument("--cameras", type=int, default=64)
+    ap.add_argument("--rate", type=float, default=500.0, help="serve: Poisson arrival rate (requests/s)")
+    ap.add_argument("--duration", type=float, default=1.0, help="serve: seconds of arrivals")
+    ap.add_argument("--streams", type=int, default=4, help="serve: worker streams")
     args = ap.parse_args()
     set_workload(args.gaussians, args.width, args.height)
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -666,9 +758,10 @@ def main():
         torch.distributed.init_process_group("nccl", device_id=device)
     from msplat_gb300 import _build
     _build.build()
-    if args.workload == "batch":
+    if args.workload in ("batch", "serve"):
         if rank == 0:
-            print(json.dumps(run_batch(args, device)), flush=True)
+            out = run_batch(args, device) if args.workload == "batch" else run_serve(args)
+            print(json.dumps(out), flush=True)
         return
     out = run_ours(args, rank, world, device)
     if rank == 0:

@@ -321,6 +321,16 @@ MSPLAT_API int msplat_batch_preprocess_backward(int P, int B, const float *xyz, 
                                   void *workspace, size_t workspace_bytes,
                                   msplat_stream_t stream);
 
+/* ------------------------------------------------------------------------ */
+/* Density-control statistics after a backward pass.  No kernel counterpart
+ * in the reference; accumulates the screen-space gradient that its
+ * alpha_blending returns for `ndc` (msplat/alpha_blending.py:107-110).
+ * For every Gaussian with radius > 0: grad_accum += |dL_dndc| (2-norm of
+ * the [P,2] row), count += 1, max_radius = max(max_radius, radius). */
+MSPLAT_API int msplat_density_stats_update(int P, const float *dL_dndc, const int32_t *radius,
+                                  float *grad_accum, int32_t *count, int32_t *max_radius,
+                                  msplat_stream_t stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -12,6 +12,7 @@ from .sort_gaussian import sort_gaussian
 from .alpha_blending import alpha_blending
 from .rasterize import preprocess, rasterization, rasterization_sh
 from .batch import rasterization_batch, rasterization_sh_batch
+from .density import DensityStats, prune_and_densify
 
 __all__ = [
     "project_point",
@@ -25,6 +26,8 @@ __all__ = [
     "preprocess",
     "rasterization_batch",
     "rasterization_sh_batch",
+    "DensityStats",
+    "prune_and_densify",
 ]
 
 __version__ = "0.1.0"

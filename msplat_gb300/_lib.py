@@ -56,6 +56,7 @@ _SIGNATURES = {
     "msplat_rasterize_preprocess_forward": (
         _I, [_I, _P, _P, _P, _P, _P, _I, _I, _F, _F, _I, _I, _P, _P, _P, _P, _P, _P, _P, _P]),
     "msplat_rasterize_preprocess_workspace_size": (_SZ, [_I, _I, _I]),
+    "msplat_density_stats_update": (_I, [_I, _P, _P, _P, _P, _P, _P]),
     "msplat_batch_preprocess_workspace_size": (_SZ, [_I, _I, _I, _I]),
     "msplat_batch_preprocess_forward": (
         _I, [_I, _I, _P, _P, _P, _P, _P, _F, _F, _I, _I, _P, _P, _P, _P, _P, _P, _P, _P]),

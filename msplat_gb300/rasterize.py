@@ -105,26 +105,31 @@ def preprocess(xyz: Tensor, scale: Tensor, rotate: Tensor, intr: Tensor, extr: T
 
 
 def rasterization(xyz: Tensor, scale: Tensor, rotate: Tensor, opacity: Tensor, feature: Tensor, intr: Tensor,
-                  extr: Tensor, W: int, H: int, bg: float, ndc: Tensor = None) -> Tensor:
+                  extr: Tensor, W: int, H: int, bg: float, ndc: Tensor = None, *, return_radius: bool = False):
     """3-D Gaussian splatting of `feature` (msplat/__init__.py:22-93).
 
     xyz [P,3], scale [P,3], rotate [P,4] unit quaternions (r,x,y,z),
     opacity [P,1], feature [P,C], intr [4] = (fx,fy,cx,cy), extr [3,4]
     world-to-camera, image W x H, scalar background `bg`; `ndc` [P,2]
-    optionally receives dL/duv * (W/2, H/2).  Returns [C, H, W].
+    optionally receives dL/duv * (W/2, H/2).  Returns [C, H, W], and with
+    return_radius=True also the screen radius [P] int32 (0 = not drawn),
+    for density statistics.
     """
     uv, depth, conic, radius, tiles, _ = preprocess(xyz, scale, rotate, intr, extr, W, H)
     idx_sorted, tile_range = sort_gaussian(uv, depth, W, H, radius, tiles)
-    return alpha_blending(uv, conic, opacity, feature, idx_sorted, tile_range, bg, W, H, ndc)
+    img = alpha_blending(uv, conic, opacity, feature, idx_sorted, tile_range, bg, W, H, ndc)
+    return (img, radius) if return_radius else img
 
 
 def rasterization_sh(xyz: Tensor, scale: Tensor, rotate: Tensor, opacity: Tensor, shs: Tensor, intr: Tensor,
-                     extr: Tensor, W: int, H: int, bg: float, ndc: Tensor = None) -> Tensor:
+                     extr: Tensor, W: int, H: int, bg: float, ndc: Tensor = None, *, return_radius: bool = False):
     """`rasterization` of the colour compute_sh(shs, view directions) with
     the view directions d = (xyz - c) / |xyz - c| of the camera centre
     c = -R^T t, evaluated inside the preprocess kernel; gradients flow into
     shs and, through d, into xyz and extr.  shs is [P, C, D] with
-    D = (degree + 1)^2, degree <= 10.  Returns [C, H, W]."""
+    D = (degree + 1)^2, degree <= 10.  Returns [C, H, W] (and the radius
+    [P] with return_radius=True)."""
     uv, depth, conic, radius, tiles, color = preprocess(xyz, scale, rotate, intr, extr, W, H, shs=shs)
     idx_sorted, tile_range = sort_gaussian(uv, depth, W, H, radius, tiles)
-    return alpha_blending(uv, conic, opacity, color, idx_sorted, tile_range, bg, W, H, ndc)
+    img = alpha_blending(uv, conic, opacity, color, idx_sorted, tile_range, bg, W, H, ndc)
+    return (img, radius) if return_radius else img
