@@ -167,17 +167,38 @@ emit_kernel(int P, const uint32_t *__restrict__ order, const int32_t *__restrict
 }
 
 // Ranges from the sorted tile keys (key 0 = no tile, key t + 1 = tile t).
+// Each thread reads 8 consecutive keys with two 16-byte loads (keys is
+// 16-byte aligned) plus one neighbour on each side; a boundary between
+// different keys writes the end of one tile's range and the start of the
+// next.  0xffffffff (never a key) stands for "outside the array".
+constexpr int kRangeKeys = 8;
+
 __global__ void __launch_bounds__(256)
 range_from_tilekey_kernel(int64_t I, const uint32_t *__restrict__ keys, int2 *__restrict__ range) {
-    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= I) return;
-    const uint32_t k = keys[i];
-    if (k == 0) return;
-    const int t = (int)k - 1;
-    if (i == 0 || keys[i - 1] != k) range[t].x = (int)i;
-    if (i == I - 1 || keys[i + 1] != k) range[t].y = (int)(i + 1);
+    const int64_t i0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) * kRangeKeys;
+    if (i0 >= I) return;
+    constexpr uint32_t kOut = 0xffffffffu;
+    uint32_t k[kRangeKeys + 2];
+    k[0] = i0 > 0 ? keys[i0 - 1] : kOut;
+    if (i0 + kRangeKeys <= I) {
+        const uint4 a = reinterpret_cast<const uint4 *>(keys + i0)[0];
+        const uint4 b = reinterpret_cast<const uint4 *>(keys + i0)[1];
+        k[1] = a.x; k[2] = a.y; k[3] = a.z; k[4] = a.w;
+        k[5] = b.x; k[6] = b.y; k[7] = b.z; k[8] = b.w;
+    } else {
+#pragma unroll
+        for (int u = 0; u < kRangeKeys; ++u) k[u + 1] = i0 + u < I ? keys[i0 + u] : kOut;
+    }
+    k[kRangeKeys + 1] = i0 + kRangeKeys < I ? keys[i0 + kRangeKeys] : kOut;
+#pragma unroll
+    for (int u = 1; u <= kRangeKeys; ++u) {
+        const uint32_t key = k[u];
+        if (key == 0 || key == kOut) continue;
+        const int64_t i = i0 + u - 1;
+        if (k[u - 1] != key) range[key - 1].x = (int)i;
+        if (k[u + 1] != key) range[key - 1].y = (int)(i + 1);
+    }
 }
-
 inline int bits_for(uint32_t maxval) {
     int b = 0;
     while (b < 32 && (maxval >> b) != 0) ++b;
@@ -483,6 +504,7 @@ extern "C" int msplat_sort_gaussian_finish(int P, const float *uv, const float *
     int st = radix_sort_pairs<uint32_t, false>(I, 0, passes, f.ka, vemit, kout, out, even ? f.kb : f.ka, f.vt,
                                                f.rb, stream);
     if (st) return st;
-    launch(range_from_tilekey_kernel, (unsigned)ceil_div64(I, 256), 256, 0, stream, I, kout, (int2 *)tile_range);
+    launch(range_from_tilekey_kernel, (unsigned)ceil_div64(ceil_div64(I, kRangeKeys), 256), 256, 0, stream, I, kout,
+           (int2 *)tile_range);
     return check_launch("sort_gaussian_finish");
 }
