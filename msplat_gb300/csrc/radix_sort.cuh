@@ -118,8 +118,10 @@ inline size_t radix_downsweep_smem(size_t key_bytes) {
 
 // vals_in == nullptr means "value = input index".  FLIP_IN / FLIP_OUT xor
 // the key's sign bit on load / store (signed-integer order).
+// 32-bit keys: capped at 64 registers for 4 blocks per SM (no spill); the
+// 64-bit keys of the reference-layout sort would spill there and keep 3.
 template <typename K, bool FLIP_IN, bool FLIP_OUT>
-__global__ void __launch_bounds__(kSortThreads)
+__global__ void __launch_bounds__(kSortThreads, sizeof(K) == 4 ? 4 : 3)
 radix_downsweep_kernel(const K *__restrict__ kin, const uint32_t *__restrict__ vin,
                        K *__restrict__ kout, uint32_t *__restrict__ vout, int64_t n, int shift,
                        int ntiles, const uint32_t *__restrict__ hist) {
