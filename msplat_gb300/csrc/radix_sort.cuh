@@ -4,10 +4,11 @@
 // One 8-bit pass = three launches with no device-side waiting:
 //   upsweep   per-tile digit histogram (per-warp shared atomics), stored
 //             digit-major [256][tiles]
-//   row scan  one block per digit: exclusive scan of its row, offset by the
-//             totals of the smaller digits -> global start of every
-//             (digit, tile) bucket
-//   downsweep re-reads the tile, ranks each item among equal digits with a
+//   row scan  one block per digit: exclusive scan of its row (the start of
+//             each (digit, tile) bucket among the digit's items) and the
+//             digit's total
+//   downsweep adds the exclusive scan of the 256 totals (the start of each
+//             digit), re-reads the tile, ranks each item among equal digits with a
 //             warp-level multisplit (stable: items are ranked in index
 //             order), reorders the tile in shared memory and writes each
 //             digit run contiguously (coalesced).
@@ -59,7 +60,7 @@ __device__ __forceinline__ unsigned digit_peers(uint32_t d, unsigned valid) {
 template <typename K, bool FLIP>
 __global__ void __launch_bounds__(kSortThreads)
 radix_upsweep_kernel(const K *__restrict__ keys, int64_t n, int shift, int ntiles,
-                     uint32_t *__restrict__ hist, uint32_t *__restrict__ totals) {
+                     uint32_t *__restrict__ hist) {
     __shared__ uint32_t cnt[kSortWarps][kRadix];
     for (int i = threadIdx.x; i < kSortWarps * kRadix; i += kSortThreads) (&cnt[0][0])[i] = 0;
     __syncthreads();
@@ -81,25 +82,17 @@ radix_upsweep_kernel(const K *__restrict__ keys, int64_t n, int shift, int ntile
 #pragma unroll
     for (int w = 0; w < kSortWarps; ++w) c += cnt[w][threadIdx.x];
     hist[(size_t)threadIdx.x * ntiles + blockIdx.x] = c;
-    if (c) atomicAdd(&totals[threadIdx.x], c);
 }
 
 // --------------------------------------------------------------- row scan
-// Block d turns row d of hist into global start offsets.
+// Block d: exclusive scan of row d of hist in place, and the row's total.
+// (A total per digit written once replaces atomics from every upsweep tile
+// onto 256 addresses, which serialised when the digits were diverse.)
 __global__ void __launch_bounds__(1024)
-radix_rowscan_kernel(uint32_t *__restrict__ hist, const uint32_t *__restrict__ totals, int ntiles) {
+radix_rowscan_kernel(uint32_t *__restrict__ hist, uint32_t *__restrict__ totals, int ntiles) {
     __shared__ uint32_t scratch[33];
-    __shared__ uint32_t base_s;
     const int d = blockIdx.x;
-    if (threadIdx.x < 32) {
-        uint32_t s = 0;
-        for (int q = threadIdx.x; q < d; q += 32) s += totals[q];
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-        if (threadIdx.x == 0) base_s = s;
-    }
-    __syncthreads();
-    uint32_t carry = base_s;
+    uint32_t carry = 0;
     uint32_t *row = hist + (size_t)d * ntiles;
     for (int c0 = 0; c0 < ntiles; c0 += blockDim.x) {
         const int i = c0 + threadIdx.x;
@@ -109,6 +102,7 @@ radix_rowscan_kernel(uint32_t *__restrict__ hist, const uint32_t *__restrict__ t
         if (i < ntiles) row[i] = carry + ex;
         carry += tot;
     }
+    if (threadIdx.x == 0) totals[d] = carry;
 }
 
 // -------------------------------------------------------------- downsweep
@@ -124,7 +118,7 @@ template <typename K, bool FLIP_IN, bool FLIP_OUT>
 __global__ void __launch_bounds__(kSortThreads, sizeof(K) == 4 ? 4 : 3)
 radix_downsweep_kernel(const K *__restrict__ kin, const uint32_t *__restrict__ vin,
                        K *__restrict__ kout, uint32_t *__restrict__ vout, int64_t n, int shift,
-                       int ntiles, const uint32_t *__restrict__ hist) {
+                       int ntiles, const uint32_t *__restrict__ hist, const uint32_t *__restrict__ totals) {
     extern __shared__ __align__(16) unsigned char sm_raw[];
     K *skeys = reinterpret_cast<K *>(sm_raw);
     uint32_t *svals = reinterpret_cast<uint32_t *>(skeys + kSortTile);
@@ -137,7 +131,10 @@ radix_downsweep_kernel(const K *__restrict__ kin, const uint32_t *__restrict__ v
     const int64_t base = (int64_t)blockIdx.x * kSortTile;
     const int tile_n = (int)min((int64_t)kSortTile, n - base);
     for (int i = tid; i < kSortWarps * kRadix; i += kSortThreads) whist[i] = 0;
-    gstart[tid] = hist[(size_t)tid * ntiles + blockIdx.x];
+    // start of this tile's bucket of digit tid: the digit's start (scan of
+    // the totals of the smaller digits) + the tile's offset within the digit
+    const uint32_t dbase = block_exclusive_scan<uint32_t>(totals[tid], scan_scratch, nullptr);
+    gstart[tid] = dbase + hist[(size_t)tid * ntiles + blockIdx.x];
     __syncthreads();
 
     K key[kSortItems];
@@ -243,7 +240,6 @@ int radix_sort_pairs(int64_t n, int begin_bit, int passes, const K *kin, const u
     if (n <= 0 || passes <= 0) return MSPLAT_OK;
     const int nt = sort_tiles(n);
     const size_t smem = radix_downsweep_smem(sizeof(K));
-    cudaMemsetAsync(b.totals, 0, sizeof(uint32_t) * kRadix * passes, stream);
     const K *ksrc = kin;
     const uint32_t *vsrc = vin;
     for (int p = 0; p < passes; ++p) {
@@ -254,15 +250,15 @@ int radix_sort_pairs(int64_t n, int begin_bit, int passes, const K *kin, const u
         uint32_t *tot = b.totals + p * kRadix;
         const bool first = p == 0, last = p == passes - 1;
         if (FLIP && first)
-            launch(radix_upsweep_kernel<K, true>, nt, kSortThreads, 0, stream, ksrc, n, shift, nt, b.hist, tot);
+            launch(radix_upsweep_kernel<K, true>, nt, kSortThreads, 0, stream, ksrc, n, shift, nt, b.hist);
         else
-            launch(radix_upsweep_kernel<K, false>, nt, kSortThreads, 0, stream, ksrc, n, shift, nt, b.hist, tot);
+            launch(radix_upsweep_kernel<K, false>, nt, kSortThreads, 0, stream, ksrc, n, shift, nt, b.hist);
         launch(radix_rowscan_kernel, kRadix, 1024, 0, stream, b.hist, tot, nt);
-#define MSPLAT_DOWNSWEEP(FI, FO)                                                                    \
-    do {                                                                                            \
-        auto kern = radix_downsweep_kernel<K, FI, FO>;                                              \
-        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);         \
-        launch(kern, nt, kSortThreads, smem, stream, ksrc, vsrc, kdst, vdst, n, shift, nt, b.hist); \
+#define MSPLAT_DOWNSWEEP(FI, FO)                                                                         \
+    do {                                                                                                 \
+        auto kern = radix_downsweep_kernel<K, FI, FO>;                                                   \
+        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);              \
+        launch(kern, nt, kSortThreads, smem, stream, ksrc, vsrc, kdst, vdst, n, shift, nt, b.hist, tot); \
     } while (0)
         if (FLIP && first && last) MSPLAT_DOWNSWEEP(true, true);
         else if (FLIP && first) MSPLAT_DOWNSWEEP(true, false);
