@@ -256,6 +256,12 @@ def blend_pairs(ms, p, color_dim=3):
         return int(nc.sum().item()), int(idx.numel()), int((radius > 0).sum().item())
 
 
+# DRAM bytes per launch (read + write) of the blend kernels at the benchmark
+# size, from one ncu capture (profiles/dram_traffic_1M_1080p.md).
+NCU_TRAFFIC_1M_1080P = {"alpha_blending_backward": 101.09e6 + 1.37e6,
+                        "alpha_blending_forward": 42.72e6 + 7.37e6}
+
+
 def roofline(stages, steps, pairs, inter, nvis, sm_mhz, peaks, peak_kind):
     """Roofline entry for the stage with the largest share of the step."""
     name, (calls, total) = max(stages.items(), key=lambda kv: kv[1][1])
@@ -266,10 +272,20 @@ def roofline(stages, steps, pairs, inter, nvis, sm_mhz, peaks, peak_kind):
         flops = pairs * (fl + 1)  # + one exponential per pair
         ach = flops / (per_launch_ms * 1e-3) / 1e12
         peak = fp32_peak_tflops(sm_mhz)
-        return name, {"bound": "fp32", "achieved": round(ach, 3), "peak": round(peak, 2), "unit": "TFLOP/s",
-                      "frac": round(ach / peak, 4), "traffic": None,
-                      "peak_source": "nominal FP32 lanes x sampled SM clock (not measured)",
-                      "kernel": name, "per_launch_ms": round(per_launch_ms, 4)}
+        full = (N_GAUSS, W_IMG, H_IMG) == (1_000_000, 1920, 1080)
+        traffic = NCU_TRAFFIC_1M_1080P.get(name) if full else None
+        hbm = peaks.get("hbm_gbs", 6800.0)
+        out = {"bound": "fp32", "achieved": round(ach, 3), "peak": round(peak, 2), "unit": "TFLOP/s",
+               "frac": round(ach / peak, 4), "traffic": traffic,
+               "peak_source": "nominal FP32 lanes x sampled SM clock (not measured)",
+               "kernel": name, "per_launch_ms": round(per_launch_ms, 4)}
+        if traffic:
+            # the same kernel against the memory roof: DRAM bytes per launch
+            # (ncu) over the live launch time
+            gbs = traffic / (per_launch_ms * 1e-3) / 1e9
+            out["dram"] = {"achieved_gbs": round(gbs, 1), "peak_gbs": hbm, "frac": round(gbs / hbm, 4),
+                           "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum, one launch"}
+        return name, out
     bytes_per = {
         "sort_gaussian_finish": inter * 52.0,
         "sort_gaussian_prepare": N_GAUSS * 100.0,
