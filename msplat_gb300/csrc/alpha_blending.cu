@@ -551,7 +551,9 @@ __device__ __forceinline__ float warp_reduce_scatter(float (&v)[NV]) {
 // the reduction always and 2.98 ms with atomics always).
 constexpr int kFewLanes = 12;
 
-template <int C, int NPIX>
+// BG: the background is nonzero, so dL/dalpha has the term
+// -T_final / (1 - alpha) * sum_c bg dL/dpix_c (compiled out for bg == 0).
+template <int C, int NPIX, bool BG>
 __global__ void __launch_bounds__(kTilePixels / NPIX)
 blend_bwd_small_kernel(int P, const float2 *__restrict__ uv, const float *__restrict__ conic,
                        const float *__restrict__ opacity, const float *__restrict__ feature,
@@ -651,7 +653,7 @@ blend_bwd_small_kernel(int P, const float2 *__restrict__ uv, const float *__rest
                 }
                 dL_dalpha *= T[i];
                 la[i] = alpha;
-                dL_dalpha += (-Tf[i] * inv1m) * bgd[i];
+                if (BG) dL_dalpha += (-Tf[i] * inv1m) * bgd[i];
                 // Moments of h = G dL/dalpha over the pixels; the uv, conic
                 // and opacity gradients are linear in them (finished per
                 // Gaussian by blend_grad_finish_kernel).
@@ -738,8 +740,11 @@ void launch_small(bool bwd, dim3 grid, cudaStream_t stream, int P, const float2 
     if (!bwd)
         launch(blend_fwd_small_kernel<C, kBlendNpixFwd>, grid, kTilePixels / kBlendNpixFwd, 0, stream,
             P, uv, conic, opacity, feature, idx, tr, bg, W, H, out, final_T, nc);
+    else if (bg != 0.0f)
+        launch(blend_bwd_small_kernel<C, kBlendNpixBwd, true>, grid, kTilePixels / kBlendNpixBwd, 0, stream,
+            P, uv, conic, opacity, feature, idx, tr, bg, W, H, fT, nci, dout, duv, dcon, dop, dfeat);
     else
-        launch(blend_bwd_small_kernel<C, kBlendNpixBwd>, grid, kTilePixels / kBlendNpixBwd, 0, stream,
+        launch(blend_bwd_small_kernel<C, kBlendNpixBwd, false>, grid, kTilePixels / kBlendNpixBwd, 0, stream,
             P, uv, conic, opacity, feature, idx, tr, bg, W, H, fT, nci, dout, duv, dcon, dop, dfeat);
 }
 
