@@ -577,8 +577,13 @@ blend_bwd_small_kernel(int P, const float2 *__restrict__ uv, const float *__rest
     const float bx0 = (float)(blockIdx.x * kTile), by0 = (float)(blockIdx.y * kTile);
     const int lane = threadIdx.x & 31;
 
-    float fy[NPIX], T[NPIX], Tf[NPIX], la[NPIX], bgd[NPIX];
-    float dp[NPIX][4], acc[NPIX][4], lf[NPIX][4];
+    // Per pixel: the colour recursion of the reference (accum_rec =
+    // last_alpha * last_color + (1 - last_alpha) * accum_rec per channel)
+    // enters dL/dalpha only through its dot product with dL/dpix, so it is
+    // carried as that scalar: ad = accum_rec . dL/dpix and lfd = last_color
+    // . dL/dpix.
+    float fy[NPIX], T[NPIX], Tf[NPIX], la[NPIX], bgd[NPIX], ad[NPIX], lfd[NPIX];
+    float dp[NPIX][4];
     int last[NPIX];
     int mylast = 0;
     __shared__ int wmax[NT / 32];
@@ -594,11 +599,11 @@ blend_bwd_small_kernel(int P, const float2 *__restrict__ uv, const float *__rest
         mylast = max(mylast, last[i]);
         la[i] = 0.0f;
         bgd[i] = 0.0f;
+        ad[i] = 0.0f;
+        lfd[i] = 0.0f;
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
             dp[i][q] = (in && q < C) ? dL_dout[(size_t)q * H * W + pix] : 0.0f;
-            acc[i][q] = 0.0f;
-            lf[i][q] = 0.0f;
             if (q < C) bgd[i] += bg * dp[i][q];
         }
     }
@@ -643,14 +648,15 @@ blend_bwd_small_kernel(int P, const float2 *__restrict__ uv, const float *__rest
                 const float inv1m = __fdividef(1.f, 1.f - alpha);
                 T[i] = T[i] * inv1m;
                 const float dcol = alpha * T[i];
-                float dL_dalpha = 0.0f;
+                float fd = 0.0f;  // colour . dL/dpix
 #pragma unroll
                 for (int q = 0; q < C; ++q) {
-                    acc[i][q] = la[i] * lf[i][q] + (1.f - la[i]) * acc[i][q];
-                    lf[i][q] = fv[q];
-                    dL_dalpha += (fv[q] - acc[i][q]) * dp[i][q];
+                    fd += fv[q] * dp[i][q];
                     v[6 + q] += dcol * dp[i][q];
                 }
+                ad[i] = la[i] * lfd[i] + (1.f - la[i]) * ad[i];
+                lfd[i] = fd;
+                float dL_dalpha = fd - ad[i];
                 dL_dalpha *= T[i];
                 la[i] = alpha;
                 if (BG) dL_dalpha += (-Tf[i] * inv1m) * bgd[i];
