@@ -52,26 +52,8 @@ def set_workload(n: int, w: int, h: int) -> None:
 
 
 def make_scene(seed: int = 0):
-    g = torch.Generator().manual_seed(seed)
-    n = N_GAUSS
-    xyz = torch.rand(n, 3, generator=g) * 2 - 1
-    scale = torch.exp(torch.rand(n, 3, generator=g) * 2 - 5)
-    rot = torch.randn(n, 4, generator=g)
-    rot = rot / rot.norm(dim=-1, keepdim=True)
-    opacity = torch.sigmoid(torch.randn(n, 1, generator=g))
-    shs = torch.randn(n, 3, (SH_DEG + 1) ** 2, generator=g) * 0.3
-    # random look-at camera on a radius-4 sphere (OpenCV: right, down, forward)
-    v = torch.randn(3, generator=g, dtype=torch.float64)
-    eye = (v / v.norm() * 4.0).numpy()
-    f = -eye / np.linalg.norm(eye)
-    r = np.cross(f, [0.0, 1.0, 0.0])
-    r /= np.linalg.norm(r)
-    d = np.cross(f, r)
-    R = np.stack([r, d, f])
-    extr = torch.tensor(np.concatenate([R, (-R @ eye)[:, None]], 1), dtype=torch.float32)
-    intr = torch.tensor([FOCAL, FOCAL, W_IMG / 2, H_IMG / 2], dtype=torch.float32)
-    weights = torch.randn(3, H_IMG, W_IMG, generator=g)
-    return dict(xyz=xyz, scale=scale, rot=rot, opacity=opacity, shs=shs, intr=intr, extr=extr, weights=weights)
+    from msplat_gb300.synthetic import training_scene
+    return training_scene(N_GAUSS, W_IMG, H_IMG, FOCAL, seed=seed, sh_degree=SH_DEG)
 
 
 PARAMS = ["xyz", "scale", "rot", "opacity", "shs", "intr", "extr"]

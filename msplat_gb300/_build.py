@@ -6,11 +6,16 @@ flags as the reference build (``-O3 --use_fast_math``, reference
 ``setup.py:39``), in parallel, then linked into one shared object that
 exports the C ABI declared in ``include/msplat_gb300.h``.
 
+Kernel shape parameters chosen by the autotuner (``msplat_gb300/autotune.py``)
+are read from ``msplat_gb300/tuning.json`` when it exists and passed as -D
+flags; without it the sources' defaults apply.
+
 Run ``python -m msplat_gb300._build`` (or ``__graft_entry__.build()``).
 """
 from __future__ import annotations
 
 import concurrent.futures as cf
+import json
 import os
 import shutil
 import subprocess
@@ -22,6 +27,7 @@ CSRC = os.path.join(PKG_DIR, "csrc")
 INCLUDE = os.path.join(ROOT, "include")
 BUILD_DIR = os.path.join(PKG_DIR, "_build")
 LIB_PATH = os.path.join(PKG_DIR, "libmsplat_gb300.so")
+TUNING_PATH = os.path.join(PKG_DIR, "tuning.json")
 
 ARCH_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH_FLAGS + [
@@ -48,25 +54,45 @@ def sources() -> list[str]:
     return sorted(os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(".cu"))
 
 
-def _needs_build(objs: list[str]) -> bool:
-    if not os.path.exists(LIB_PATH):
+def tuned_defines(path: str = TUNING_PATH) -> dict:
+    """The autotuner's choices {macro: value}, or {} without a tuning file."""
+    if not os.path.exists(path):
+        return {}
+    with open(path) as f:
+        return {str(k): int(v) for k, v in json.load(f).get("defines", {}).items()}
+
+
+def define_flags(defines: dict) -> list[str]:
+    return [f"-D{k}={v}" for k, v in sorted(defines.items())]
+
+
+def _needs_build(lib_path: str) -> bool:
+    if not os.path.exists(lib_path):
         return True
-    lib_m = os.path.getmtime(LIB_PATH)
+    lib_m = os.path.getmtime(lib_path)
     deps = [os.path.join(CSRC, f) for f in os.listdir(CSRC)]
     deps.append(os.path.join(INCLUDE, "msplat_gb300.h"))
     deps.append(os.path.abspath(__file__))
+    if os.path.exists(TUNING_PATH):
+        deps.append(TUNING_PATH)
     return any(os.path.getmtime(d) > lib_m for d in deps)
 
 
-def build(force: bool = False, verbose: bool = False, extra_flags: list[str] | None = None) -> str:
-    """Compiles and links the library; returns its path."""
+def build(force: bool = False, verbose: bool = False, extra_flags: list[str] | None = None,
+          defines: dict | None = None, lib_path: str | None = None, build_dir: str | None = None) -> str:
+    """Compiles and links the library; returns its path.  `defines`
+    replaces the tuning file's macros (the autotuner builds its variants this
+    way, into their own `lib_path` / `build_dir`)."""
+    lib_path = lib_path or LIB_PATH
+    build_dir = build_dir or BUILD_DIR
     srcs = sources()
-    os.makedirs(BUILD_DIR, exist_ok=True)
-    objs = [os.path.join(BUILD_DIR, os.path.basename(s)[:-3] + ".o") for s in srcs]
-    if not force and not _needs_build(objs):
-        return LIB_PATH
+    os.makedirs(build_dir, exist_ok=True)
+    objs = [os.path.join(build_dir, os.path.basename(s)[:-3] + ".o") for s in srcs]
+    if not force and not _needs_build(lib_path):
+        return lib_path
     nvcc = _nvcc()
-    flags = NVCC_FLAGS + ["-I", INCLUDE, "-I", CSRC] + list(extra_flags or [])
+    macros = tuned_defines() if defines is None else dict(defines)
+    flags = NVCC_FLAGS + ["-I", INCLUDE, "-I", CSRC] + define_flags(macros) + list(extra_flags or [])
 
     def compile_one(pair):
         src, obj = pair
@@ -81,13 +107,13 @@ def build(force: bool = False, verbose: bool = False, extra_flags: list[str] | N
         for msg in ex.map(compile_one, zip(srcs, objs)):
             if verbose and msg:
                 print(msg, file=sys.stderr)
-    tmp = LIB_PATH + ".tmp"
+    tmp = lib_path + ".tmp"
     cmd = [nvcc, *ARCH_FLAGS, "-shared", "-o", tmp, *objs]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"nvcc link failed:\n{r.stderr}")
-    os.replace(tmp, LIB_PATH)
-    return LIB_PATH
+    os.replace(tmp, lib_path)
+    return lib_path
 
 
 if __name__ == "__main__":

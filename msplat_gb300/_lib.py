@@ -82,7 +82,7 @@ def load(path: str | None = None):
     with _lock:
         if _lib is not None and path is None:
             return _lib
-        p = path or LIB_PATH
+        p = path or os.environ.get("MSPLAT_GB300_LIB") or LIB_PATH
         if not os.path.exists(p):
             raise RuntimeError(
                 f"msplat_gb300 native library not found at {p}; build it with "

@@ -549,7 +549,10 @@ __device__ __forceinline__ float warp_reduce_scatter(float (&v)[NV]) {
 // costs a fixed ~16 shuffles per value set: the measured optimum of the two at
 // 1M Gaussians / 1080p is 12-16 lanes (blend backward 0.90 ms vs 1.00 ms with
 // the reduction always and 2.98 ms with atomics always).
-constexpr int kFewLanes = 12;
+#ifndef MSPLAT_FEW_LANES
+#define MSPLAT_FEW_LANES 12
+#endif
+constexpr int kFewLanes = MSPLAT_FEW_LANES;
 
 // BG: the background is nonzero, so dL/dalpha has the term
 // -T_final / (1 - alpha) * sum_c bg dL/dpix_c (compiled out for bg == 0).
