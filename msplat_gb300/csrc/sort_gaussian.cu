@@ -77,20 +77,22 @@ depth_key_kernel(int P, const float *__restrict__ depth, const int32_t *__restri
     keys[g] = radius[g] > 0 ? (__float_as_uint(depth[g]) ^ 0x80000000u) : 0xffffffffu;
 }
 
-// Tile count of each Gaussian in depth order.  Also counts Gaussians whose
-// tiles[] entry disagrees with their rectangle (those need the reference
-// layout), the negative-depth emitters (they come first in depth order) and
-// their intersections.
+// Tile counts of the Gaussians in depth order, summed per block of 256
+// (the block layout emit_kernel uses): bsum[block].  Also counts Gaussians
+// whose tiles[] entry disagrees with their rectangle (those need the
+// reference layout), the negative-depth emitters (they come first in depth
+// order) and their intersections.
 __global__ void __launch_bounds__(256)
 depth_order_count_kernel(int P, const uint32_t *__restrict__ order, const float2 *__restrict__ uv,
                          const float *__restrict__ depth, const int32_t *__restrict__ radius,
-                         const int32_t *__restrict__ tiles, int gx, int gy, int32_t *__restrict__ cnt,
+                         const int32_t *__restrict__ tiles, int gx, int gy, int64_t *__restrict__ bsum,
                          int64_t *__restrict__ counts, unsigned long long *__restrict__ neg) {
+    __shared__ int64_t scratch[33];
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     bool bad = false, isneg = false;
+    int c = 0;
     if (j < P) {
         const int g = (int)order[j];
-        int c = 0;
         if (radius[g] > 0) {
             int x0, y0, x1, y1;
             const float2 p = uv[g];
@@ -101,13 +103,32 @@ depth_order_count_kernel(int P, const uint32_t *__restrict__ order, const float2
             if (isneg && c > 0) atomicAdd(neg + 1, (unsigned long long)c);
         }
         bad = c != tiles[g];
-        cnt[j] = c;
     }
     const unsigned mb = __ballot_sync(0xffffffffu, bad), mn = __ballot_sync(0xffffffffu, isneg);
     if ((threadIdx.x & 31) == 0) {
         if (mb) atomicAdd((unsigned long long *)&counts[1], (unsigned long long)__popc(mb));
         if (mn) atomicAdd(neg, (unsigned long long)__popc(mn));
     }
+    int64_t total;
+    block_exclusive_scan<int64_t>((int64_t)c, scratch, &total);
+    if (threadIdx.x == 0) bsum[blockIdx.x] = total;
+}
+
+// Exclusive scan of the nb block sums in place (one block), and the total:
+// the number of intersections, written to counts[0].
+__global__ void __launch_bounds__(1024)
+block_offsets_kernel(int nb, int64_t *__restrict__ bsum, int64_t *__restrict__ counts) {
+    __shared__ int64_t scratch[33];
+    int64_t carry = 0;
+    for (int c0 = 0; c0 < nb; c0 += blockDim.x) {
+        const int i = c0 + threadIdx.x;
+        const int64_t v = i < nb ? bsum[i] : 0;
+        int64_t tot;
+        const int64_t ex = block_exclusive_scan<int64_t>(v, scratch, &tot);
+        if (i < nb) bsum[i] = carry + ex;
+        carry += tot;
+    }
+    if (threadIdx.x == 0) counts[0] = carry;
 }
 
 // Calls f(tile) for every tile of the rectangle of depth-ordered Gaussian j.
@@ -127,25 +148,28 @@ __device__ __forceinline__ void for_rect_tiles(int g, const float2 *__restrict__
 // loads one Gaussian, then the whole warp writes each Gaussian's run of
 // (tile key, id) pairs with the lanes spread over its tiles (coalesced).
 // Tile key 0 marks negative-depth Gaussians, t + 1 tile t.
+// A Gaussian's first slot is its block's base (boff, from the block sums)
+// plus the exclusive scan of the tile counts within the block.
 __global__ void __launch_bounds__(256)
-emit_kernel(int P, const uint32_t *__restrict__ order, const int32_t *__restrict__ offs,
+emit_kernel(int P, const uint32_t *__restrict__ order, const int64_t *__restrict__ boff,
             const float2 *__restrict__ uv, const float *__restrict__ depth,
             const int32_t *__restrict__ radius, int gx, int gy, uint32_t *__restrict__ tkeys,
             uint32_t *__restrict__ tvals) {
+    __shared__ int scratch[33];
     const int lane = threadIdx.x & 31;
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
-    int g = -1, x0 = 0, y0 = 0, x1 = 0, y1 = 0, start = 0;
+    int g = -1, x0 = 0, y0 = 0, x1 = 0, y1 = 0;
     bool neg = false;
     if (j < P) {
         g = (int)order[j];
         if (radius[g] > 0) {
             const float2 p = uv[g];
             tile_rect(p.x, p.y, radius[g], gx, gy, x0, y0, x1, y1);
-            start = offs[j];
             neg = (__float_as_uint(depth[g]) >> 31) != 0;
         }
     }
     const int w = x1 - x0, n = w * (y1 - y0);
+    const int start = (int)boff[blockIdx.x] + block_exclusive_scan<int>(n, scratch, nullptr);
     unsigned todo = __ballot_sync(0xffffffffu, n > 0);
     while (todo) {
         const int sl = __ffs(todo) - 1;
@@ -212,24 +236,20 @@ constexpr int kDepthPasses = 4;
 // re-derives their addresses from P).
 struct PrepareWs {
     uint32_t *order = nullptr;  // [P] Gaussian ids in depth order
-    int32_t *offs = nullptr;    // [P] exclusive scan of tile counts, depth order
-    int32_t *cnt = nullptr;     // [P] tile counts, depth order
+    int64_t *bsum = nullptr;    // [P/256] tile counts per block of 256 in depth order, then their scan
     unsigned long long *neg = nullptr;  // [0] negative emitters, [1] their intersections
     uint32_t *ka = nullptr, *kb = nullptr, *vt = nullptr;
-    int64_t *scan_parts = nullptr;
     RadixBuffers rb{};
 };
 
 template <typename WS>
 inline void prepare_carve(WS &w, int P, PrepareWs &ws) {
     ws.order = w.template take<uint32_t>(P);
-    ws.offs = w.template take<int32_t>(P);
-    ws.cnt = w.template take<int32_t>(P);
+    ws.bsum = w.template take<int64_t>((size_t)ceil_div(P, 256));
     ws.neg = w.template take<unsigned long long>(2);
     ws.ka = w.template take<uint32_t>(P);
     ws.kb = w.template take<uint32_t>(P);
     ws.vt = w.template take<uint32_t>(P);
-    ws.scan_parts = w.template take<int64_t>((size_t)ceil_div(P, kScanTile) + 1);
     ws.rb.hist = w.template take<uint32_t>((size_t)kRadix * sort_tiles(P));
     ws.rb.totals = w.template take<uint32_t>((size_t)kRadix * kDepthPasses);
 }
@@ -455,9 +475,11 @@ extern "C" int msplat_sort_gaussian_prepare(int P, const float *depth, const int
     int st = radix_sort_pairs<uint32_t, false>(P, 0, kDepthPasses, ws.ka, nullptr, ws.ka, ws.order,
                                                ws.kb, ws.vt, ws.rb, stream);
     if (st) return st;
-    launch(depth_order_count_kernel, ceil_div(P, 256), 256, 0, stream,
-        P, ws.order, (const float2 *)uv, depth, radius, tiles, gx, gy, ws.cnt, counts, ws.neg);
-    return scan_i32(P, ws.cnt, ws.offs, false, counts, ws.scan_parts, stream);
+    const int nb = ceil_div(P, 256);
+    launch(depth_order_count_kernel, nb, 256, 0, stream,
+        P, ws.order, (const float2 *)uv, depth, radius, tiles, gx, gy, ws.bsum, counts, ws.neg);
+    launch(block_offsets_kernel, 1, 1024, 0, stream, nb, ws.bsum, counts);
+    return check_launch("sort_gaussian_prepare");
 }
 
 extern "C" size_t msplat_sort_finish_workspace_size(int P, int64_t num_intersects, int W, int H) {
@@ -498,7 +520,7 @@ extern "C" int msplat_sort_gaussian_finish(int P, const float *uv, const float *
     uint32_t *out = (uint32_t *)idx_sorted;
     const bool even = passes % 2 == 0;
     uint32_t *vemit = even ? out : f.vt;
-    launch(emit_kernel, ceil_div(P, 256), 256, 0, stream, P, prep.order, prep.offs, (const float2 *)uv, depth,
+    launch(emit_kernel, ceil_div(P, 256), 256, 0, stream, P, prep.order, prep.bsum, (const float2 *)uv, depth,
                                                       radius, gx, gy, f.ka, vemit);
     uint32_t *kout = even ? f.ka : f.kb;
     int st = radix_sort_pairs<uint32_t, false>(I, 0, passes, f.ka, vemit, kout, out, even ? f.kb : f.ka, f.vt,
