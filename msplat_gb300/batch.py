@@ -11,10 +11,12 @@ Gaussian (and its SH rows) once and projects it into every camera
 (msplat_batch_preprocess_forward); one adjoint kernel sums the per-camera
 gradients per Gaussian (msplat_batch_preprocess_backward); the B tile
 sorts read their intersection counts with one host synchronisation.  The
-sort and blend of each camera run as in the single-camera path.
+sort and blend of each camera run as in the single-camera path, spread over
+four side streams so that small cameras overlap on the device.
 """
 from __future__ import annotations
 
+import threading
 from typing import Sequence
 
 import torch
@@ -23,6 +25,38 @@ from torch import Tensor
 from . import _lib
 from . import _tensors as tt
 from .sort_gaussian import sort_gaussian_many
+
+
+_TLS = threading.local()
+N_SIDE_STREAMS = 4
+
+
+def side_streams(dev: torch.device) -> list:
+    """Streams on which the cameras' sorts and blends overlap (camera b on
+    stream b % N_SIDE_STREAMS); one set per device and host thread, so
+    concurrent callers (the server's workers) do not wait on each other."""
+    key = dev.index if dev.index is not None else torch.cuda.current_device()
+    cache = getattr(_TLS, "streams", None)
+    if cache is None:
+        cache = _TLS.streams = {}
+    if key not in cache:
+        cache[key] = [torch.cuda.Stream(device=dev) for _ in range(N_SIDE_STREAMS)]
+    return cache[key]
+
+
+def _fork(streams: list, dev) -> torch.cuda.Stream:
+    """Makes every side stream wait for the work so far on the current one."""
+    main = torch.cuda.current_stream(dev)
+    ev = torch.cuda.Event()
+    ev.record(main)
+    for s in streams:
+        s.wait_event(ev)
+    return main
+
+
+def _join(main: torch.cuda.Stream, streams: list) -> None:
+    for s in streams:
+        main.wait_stream(s)
 
 
 def _cameras(intrs: Tensor, extrs: Tensor, B: int):
@@ -74,24 +108,30 @@ class _RasterizeBatch(torch.autograd.Function):
                 0.0, 1.3, C if shs_c is not None else 0, D, _lib.ptr(shs_c), _lib.ptr(uv), _lib.ptr(depth),
                 _lib.ptr(conic), _lib.ptr(radius), _lib.ptr(tiles), _lib.ptr(color), st),
                 "batch_preprocess_forward")
+        streams = side_streams(dev)
         sorted_ = sort_gaussian_many([(uv[b], depth[b], int(w), int(h), radius[b], tiles[b])
-                                      for b, (w, h) in enumerate(sizes)])
+                                      for b, (w, h) in enumerate(sizes)], streams)
         outs, finals = [], []
+        main = _fork(streams, dev)
         with _lib.stage("alpha_blending_forward"):
             for b, (w, h) in enumerate(sizes):
                 w, h = int(w), int(h)
                 feat_b = color[b] if color is not None else feat_c
-                out = torch.empty((C, h, w), dtype=torch.float32, device=dev)
-                final_T = torch.empty((h, w), dtype=torch.float32, device=dev)
-                ncontrib = torch.empty((h, w), dtype=torch.int32, device=dev)
                 idx, tr = sorted_[b]
-                if C > 0:
-                    _lib.check(lib.msplat_alpha_blending_forward(
-                        P, C, _lib.ptr(uv[b]), _lib.ptr(conic[b]), _lib.ptr(op_c), _lib.ptr(feat_b), _lib.ptr(idx),
-                        _lib.ptr(tr), float(bg), w, h, _lib.ptr(out), _lib.ptr(final_T), _lib.ptr(ncontrib), st),
-                        "alpha_blending_forward")
+                with torch.cuda.stream(streams[b % len(streams)]):
+                    out = torch.empty((C, h, w), dtype=torch.float32, device=dev)
+                    final_T = torch.empty((h, w), dtype=torch.float32, device=dev)
+                    ncontrib = torch.empty((h, w), dtype=torch.int32, device=dev)
+                    if C > 0:
+                        _lib.check(lib.msplat_alpha_blending_forward(
+                            P, C, _lib.ptr(uv[b]), _lib.ptr(conic[b]), _lib.ptr(op_c), _lib.ptr(feat_b),
+                            _lib.ptr(idx), _lib.ptr(tr), float(bg), w, h, _lib.ptr(out), _lib.ptr(final_T),
+                            _lib.ptr(ncontrib), _lib.stream(dev)), "alpha_blending_forward")
+                    for x in (out, final_T, ncontrib):
+                        x.record_stream(main)
                 outs.append(out)
                 finals.append((final_T, ncontrib))
+        _join(main, streams)
         ctx.sizes, ctx.bg, ctx.C, ctx.D = [(int(w), int(h)) for w, h in sizes], float(bg), C, D
         ctx.sorted, ctx.finals = sorted_, finals
         ctx.intr_shape, ctx.extr_shape, ctx.op_shape = intrs.shape, extrs.shape, opacity.shape
@@ -109,20 +149,24 @@ class _RasterizeBatch(torch.autograd.Function):
         dL_dconic = torch.zeros((B, P, 3), dtype=torch.float32, device=dev)
         dL_dop = torch.zeros((B, P), dtype=torch.float32, device=dev)
         dL_dcol = torch.zeros((B, P, C), dtype=torch.float32, device=dev)
+        streams = side_streams(dev)
+        main = _fork(streams, dev)
         with _lib.stage("alpha_blending_backward"):
             for b, (w, h) in enumerate(ctx.sizes):
                 g = grads[b]
                 if g is None or C == 0:
                     continue
-                g = g.float().contiguous()
                 idx, tr = ctx.sorted[b]
                 final_T, ncontrib = ctx.finals[b]
                 feat_b = color[b] if color is not None else feat
-                _lib.check(lib.msplat_alpha_blending_backward(
-                    P, C, _lib.ptr(uv[b]), _lib.ptr(conic[b]), _lib.ptr(op), _lib.ptr(feat_b), _lib.ptr(idx),
-                    _lib.ptr(tr), ctx.bg, w, h, _lib.ptr(final_T), _lib.ptr(ncontrib), _lib.ptr(g),
-                    _lib.ptr(dL_duv[b]), _lib.ptr(dL_dconic[b]), _lib.ptr(dL_dop[b]), _lib.ptr(dL_dcol[b]), st),
-                    "alpha_blending_backward")
+                with torch.cuda.stream(streams[b % len(streams)]):
+                    g = g.float().contiguous()
+                    _lib.check(lib.msplat_alpha_blending_backward(
+                        P, C, _lib.ptr(uv[b]), _lib.ptr(conic[b]), _lib.ptr(op), _lib.ptr(feat_b), _lib.ptr(idx),
+                        _lib.ptr(tr), ctx.bg, w, h, _lib.ptr(final_T), _lib.ptr(ncontrib), _lib.ptr(g),
+                        _lib.ptr(dL_duv[b]), _lib.ptr(dL_dconic[b]), _lib.ptr(dL_dop[b]), _lib.ptr(dL_dcol[b]),
+                        _lib.stream(dev)), "alpha_blending_backward")
+        _join(main, streams)
         want_i, want_e = ctx.needs_input_grad[6], ctx.needs_input_grad[7]
         sh = shs is not None
         dL_dxyz = torch.empty((P, 3), dtype=torch.float32, device=dev)

@@ -2,6 +2,7 @@
 (drop-in for msplat/sort_gaussian.py)."""
 from __future__ import annotations
 
+import contextlib
 from typing import Tuple
 
 import torch
@@ -102,10 +103,13 @@ def _sort_reference_layout(u, d, W, H, r, t):
     return idx_sorted, tile_range
 
 
-def sort_gaussian_many(cases):
+def sort_gaussian_many(cases, streams=None):
     """`sort_gaussian` for several cameras with one host read for all of
     them: every camera's prepare is enqueued, the intersection counts of all
-    cameras are read together, then every finish is enqueued.
+    cameras are read together, then every finish is enqueued.  With
+    `streams`, camera b's sort runs on streams[b % len(streams)] (after the
+    work already on the current stream), so small cameras overlap on the
+    device; the results are ready on the current stream on return.
 
     cases: sequence of (uv [P,2], depth [P,1], W, H, radius [P] int32,
     tiles [P] int32) contiguous float32 / int32 CUDA tensors.  Returns a
@@ -114,34 +118,57 @@ def sort_gaussian_many(cases):
     if not cases:
         return []
     dev = cases[0][0].device
-    st = _lib.stream(dev)
+    main = torch.cuda.current_stream(dev)
+    streams = list(streams or [])
+    if streams:
+        ready = torch.cuda.Event()
+        ready.record(main)
+        for s in streams:
+            s.wait_event(ready)
+
+    def on(b):
+        return torch.cuda.stream(streams[b % len(streams)]) if streams else contextlib.nullcontext()
+
     counts = torch.empty((len(cases), 2), dtype=torch.int64, device=dev)
     preps = []
     with _lib.stage("sort_gaussian_prepare"):
         for b, (u, d, W, H, r, t) in enumerate(cases):
             P = u.shape[0]
-            ws_prep = _lib.workspace(lib.msplat_sort_prepare_workspace_size(P, W, H), dev)
-            _lib.check(lib.msplat_sort_gaussian_prepare(
-                P, _lib.ptr(d), _lib.ptr(r), _lib.ptr(t), _lib.ptr(u), W, H, _lib.ptr(counts[b]),
-                _lib.ptr(ws_prep), ws_prep.numel(), st), "sort_gaussian_prepare")
+            with on(b):
+                st = _lib.stream(dev)
+                ws_prep = _lib.workspace(lib.msplat_sort_prepare_workspace_size(P, W, H), dev)
+                _lib.check(lib.msplat_sort_gaussian_prepare(
+                    P, _lib.ptr(d), _lib.ptr(r), _lib.ptr(t), _lib.ptr(u), W, H, _lib.ptr(counts[b]),
+                    _lib.ptr(ws_prep), ws_prep.numel(), st), "sort_gaussian_prepare")
             preps.append(ws_prep)
+    for s in streams:
+        main.wait_stream(s)
     host = counts.tolist()
     out = []
     with _lib.stage("sort_gaussian_finish"):
-        for (u, d, W, H, r, t), ws_prep, (I, n_mismatch) in zip(cases, preps, host):
-            if n_mismatch:
-                out.append(_sort_reference_layout(u, d, W, H, r, t))
-                continue
-            if I > 2**31 - 1:
-                raise RuntimeError(f"sort_gaussian: {I} intersections exceed the int32 range")
-            P = u.shape[0]
-            idx_sorted = torch.empty((I,), dtype=torch.int32, device=dev)
-            tile_range = torch.empty((tt.ntiles(W, H), 2), dtype=torch.int32, device=dev)
-            ws = _lib.workspace(lib.msplat_sort_finish_workspace_size(P, I, W, H), dev)
-            _lib.check(lib.msplat_sort_gaussian_finish(
-                P, _lib.ptr(u), _lib.ptr(d), _lib.ptr(r), W, H, I, _lib.ptr(ws_prep),
-                _lib.ptr(idx_sorted), _lib.ptr(tile_range), _lib.ptr(ws), ws.numel(), st),
-                "sort_gaussian_finish")
-            out.append((idx_sorted, tile_range))
-            del ws
+        for b, ((u, d, W, H, r, t), ws_prep, (I, n_mismatch)) in enumerate(zip(cases, preps, host)):
+            with on(b):
+                if n_mismatch:
+                    res = _sort_reference_layout(u, d, W, H, r, t)
+                else:
+                    if I > 2**31 - 1:
+                        raise RuntimeError(f"sort_gaussian: {I} intersections exceed the int32 range")
+                    P = u.shape[0]
+                    st = _lib.stream(dev)
+                    idx_sorted = torch.empty((I,), dtype=torch.int32, device=dev)
+                    tile_range = torch.empty((tt.ntiles(W, H), 2), dtype=torch.int32, device=dev)
+                    ws = _lib.workspace(lib.msplat_sort_finish_workspace_size(P, I, W, H), dev)
+                    _lib.check(lib.msplat_sort_gaussian_finish(
+                        P, _lib.ptr(u), _lib.ptr(d), _lib.ptr(r), W, H, I, _lib.ptr(ws_prep),
+                        _lib.ptr(idx_sorted), _lib.ptr(tile_range), _lib.ptr(ws), ws.numel(), st),
+                        "sort_gaussian_finish")
+                    res = (idx_sorted, tile_range)
+                    del ws
+                if streams:
+                    # allocated on a side stream, used later on the main one
+                    for x in res:
+                        x.record_stream(main)
+            out.append(res)
+    for s in streams:
+        main.wait_stream(s)
     return out
