@@ -439,6 +439,9 @@ def _finish(args, rank, world, ms, p, stages, clk, ms_step, e2e_ms, h2d, extra):
                                             "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": 4,
                                             "copies": "double-buffered on a second stream, overlapping the "
                                                       "previous step's compute"},
+        "throughput": {"mpix_per_s": round(W_IMG * H_IMG / (ms_step / world) / 1e3, 1),
+                       "gaussians_per_s": round(N_GAUSS / (ms_step / world) * 1e3 / 1e9, 3),
+                       "unit_note": "fwd+bwd frames: pixels and Gaussians processed per second (Gaussians in 1e9/s)"},
         "gpu_launches": int(extra["launches"]),
         "dropin_ms_per_step": None if extra["dropin_ms"] is None else round(extra["dropin_ms"], 4),
         "stage_ms_per_step": stage_ms,
