@@ -363,7 +363,12 @@ def run_ours(args, rank, world, device):
         d1.record(stream)
         barrier()
         dropin_ms = max_over_ranks(d0.elapsed_time(d1) / args.steps, world, device)
-    extra = {"launches": n_launch, "dropin_ms": dropin_ms}
+    # the same step captured once in a CUDA graph (capacity-bounded sort, no
+    # host read) and replayed; valid only if the sort's status stays 0
+    graph_ms = None
+    if not args.no_graph:
+        graph_ms = time_graph(ms, p, weights, args, device, world)
+    extra = {"launches": n_launch, "dropin_ms": dropin_ms, "graph_ms": graph_ms}
 
     # e2e: the same step with host inputs copied in and the loss read back.
     if args.no_e2e:
@@ -407,6 +412,53 @@ def run_ours(args, rank, world, device):
     return _finish(args, rank, world, ms, p, stages, clk, ms_step, e2e_ms, h2d, extra)
 
 
+def time_graph(ms, p, weights, args, device, world):
+    """ms per step of the training step captured in a CUDA graph: the sort
+    takes a capacity of 1.1x this frame's intersection count and keeps the
+    count on the device, so the step has no host read."""
+    with torch.no_grad():
+        uv, depth, conic, radius, tiles, _ = ms.preprocess(p["xyz"], p["scale"], p["rot"], p["intr"], p["extr"],
+                                                           W_IMG, H_IMG)
+        idx, _ = ms.sort_gaussian(uv, depth, W_IMG, H_IMG, radius, tiles)
+    cap = int(idx.numel() * 1.1) + 4096
+    del uv, depth, conic, radius, tiles, idx
+    status = torch.zeros(1, dtype=torch.int32, device=device)
+
+    def step():
+        img = ms.rasterization_sh(p["xyz"], p["scale"], p["rot"], p["opacity"], p["shs"], p["intr"], p["extr"],
+                                  W_IMG, H_IMG, 0.0, capacity=cap, status=status)
+        (img * weights).sum().backward()
+
+    side = torch.cuda.Stream()
+    side.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(side):
+        for _ in range(3):
+            for t in p.values():
+                t.grad = None
+            step()
+    torch.cuda.current_stream().wait_stream(side)
+    for t in p.values():
+        t.grad = None
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph):
+        step()
+    for _ in range(args.warmup):
+        graph.replay()
+    torch.cuda.synchronize()
+    stream = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        graph.replay()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    if int(status.item()) != 0:
+        return None  # capacity exceeded: no valid graph timing
+    ms_step = e0.elapsed_time(e1) / args.steps
+    del graph
+    return max_over_ranks(ms_step, world, device)
+
+
 def _finish(args, rank, world, ms, p, stages, clk, ms_step, e2e_ms, h2d, extra):
     if rank != 0:
         return None
@@ -444,6 +496,7 @@ def _finish(args, rank, world, ms, p, stages, clk, ms_step, e2e_ms, h2d, extra):
                        "unit_note": "fwd+bwd frames: pixels and Gaussians processed per second (Gaussians in 1e9/s)"},
         "gpu_launches": int(extra["launches"]),
         "dropin_ms_per_step": None if extra["dropin_ms"] is None else round(extra["dropin_ms"], 4),
+        "graph_ms_per_step": None if extra["graph_ms"] is None else round(extra["graph_ms"], 4),
         "stage_ms_per_step": stage_ms,
         "roofline": roof,
         "clocks": clk,
@@ -737,6 +790,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer (e2e) loop")
+    ap.add_argument("--no-graph", action="store_true", help="skip timing the CUDA-graph replay of the step")
     ap.add_argument("--no-dropin", action="store_true",
                     help="skip timing the reference call sequence (compute_sh + rasterization)")
     ap.add_argument("--gaussians", type=int, default=N_GAUSS,

@@ -229,6 +229,21 @@ MSPLAT_API int msplat_sort_gaussian_finish(int P, const float *uv, const float *
                                 void *workspace, size_t workspace_bytes,
                                 msplat_stream_t stream);
 
+/* The finish without the host read of counts (for stream capture): the
+ * buffers are sized for `capacity` intersections (idx_sorted [capacity],
+ * workspace msplat_sort_finish_workspace_size(P, capacity, W, H)) and the
+ * kernels take the count from `counts` on the device.  status[0] (int32,
+ * device) is set to 1 when the result is not valid -- more intersections
+ * than the capacity, or counts[1] != 0 (the reference layout is needed) --
+ * and to 0 otherwise; the caller checks it later and redoes the frame with
+ * msplat_sort_gaussian_finish then.  No counterpart in the reference. */
+MSPLAT_API int msplat_sort_gaussian_finish_capacity(int P, const float *uv, const float *depth,
+                                 const int32_t *radius, int W, int H, int64_t capacity,
+                                 const int64_t *counts, const void *prepare_workspace,
+                                 int32_t *idx_sorted, int32_t *tile_range, int32_t *status,
+                                 void *workspace, size_t workspace_bytes,
+                                 msplat_stream_t stream);
+
 /* ------------------------------------------------------------------------ */
 /* Alpha blending: replaces alphaBlendingForward / alphaBlendingBackward
  * (msplat/src/alpha_blending.cu:248-394, :396-573; ext.cpp:24-25).

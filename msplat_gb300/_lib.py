@@ -49,6 +49,8 @@ _SIGNATURES = {
     "msplat_sort_gaussian_prepare": (_I, [_I, _P, _P, _P, _P, _I, _I, _P, _P, _SZ, _P]),
     "msplat_sort_gaussian_finish": (
         _I, [_I, _P, _P, _P, _I, _I, _I64, _P, _P, _P, _P, _SZ, _P]),
+    "msplat_sort_gaussian_finish_capacity": (
+        _I, [_I, _P, _P, _P, _I, _I, _I64, _P, _P, _P, _P, _P, _P, _SZ, _P]),
     "msplat_alpha_blending_forward": (
         _I, [_I, _I, _P, _P, _P, _P, _P, _P, _F, _I, _I, _P, _P, _P, _P]),
     "msplat_alpha_blending_backward": (

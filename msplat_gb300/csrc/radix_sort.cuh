@@ -60,8 +60,9 @@ __device__ __forceinline__ unsigned digit_peers(uint32_t d, unsigned valid) {
 template <typename K, bool FLIP>
 __global__ void __launch_bounds__(kSortThreads)
 radix_upsweep_kernel(const K *__restrict__ keys, int64_t n, int shift, int ntiles,
-                     uint32_t *__restrict__ hist) {
+                     uint32_t *__restrict__ hist, const int64_t *__restrict__ n_dev) {
     __shared__ uint32_t cnt[kSortWarps][kRadix];
+    if (n_dev) n = min(n, *n_dev);  // the length is on the device; n is the capacity
     for (int i = threadIdx.x; i < kSortWarps * kRadix; i += kSortThreads) (&cnt[0][0])[i] = 0;
     __syncthreads();
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -118,7 +119,8 @@ template <typename K, bool FLIP_IN, bool FLIP_OUT>
 __global__ void __launch_bounds__(kSortThreads, sizeof(K) == 4 ? 4 : 3)
 radix_downsweep_kernel(const K *__restrict__ kin, const uint32_t *__restrict__ vin,
                        K *__restrict__ kout, uint32_t *__restrict__ vout, int64_t n, int shift,
-                       int ntiles, const uint32_t *__restrict__ hist, const uint32_t *__restrict__ totals) {
+                       int ntiles, const uint32_t *__restrict__ hist, const uint32_t *__restrict__ totals,
+                       const int64_t *__restrict__ n_dev) {
     extern __shared__ __align__(16) unsigned char sm_raw[];
     K *skeys = reinterpret_cast<K *>(sm_raw);
     uint32_t *svals = reinterpret_cast<uint32_t *>(skeys + kSortTile);
@@ -128,8 +130,9 @@ radix_downsweep_kernel(const K *__restrict__ kin, const uint32_t *__restrict__ v
     __shared__ uint32_t scan_scratch[33];
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    if (n_dev) n = min(n, *n_dev);
     const int64_t base = (int64_t)blockIdx.x * kSortTile;
-    const int tile_n = (int)min((int64_t)kSortTile, n - base);
+    const int tile_n = (int)min((int64_t)kSortTile, n - base);  // <= 0 past a device-side length
     for (int i = tid; i < kSortWarps * kRadix; i += kSortThreads) whist[i] = 0;
     // start of this tile's bucket of digit tid: the digit's start (scan of
     // the totals of the smaller digits) + the tile's offset within the digit
@@ -236,7 +239,7 @@ inline bool radix_take(Workspace &w, int64_t n, int passes, RadixBuffers &b) {
 template <typename K, bool FLIP>
 int radix_sort_pairs(int64_t n, int begin_bit, int passes, const K *kin, const uint32_t *vin,
                      K *kout, uint32_t *vout, K *ktmp, uint32_t *vtmp, const RadixBuffers &b,
-                     cudaStream_t stream) {
+                     cudaStream_t stream, const int64_t *n_dev = nullptr) {
     if (n <= 0 || passes <= 0) return MSPLAT_OK;
     const int nt = sort_tiles(n);
     const size_t smem = radix_downsweep_smem(sizeof(K));
@@ -250,15 +253,15 @@ int radix_sort_pairs(int64_t n, int begin_bit, int passes, const K *kin, const u
         uint32_t *tot = b.totals + p * kRadix;
         const bool first = p == 0, last = p == passes - 1;
         if (FLIP && first)
-            launch(radix_upsweep_kernel<K, true>, nt, kSortThreads, 0, stream, ksrc, n, shift, nt, b.hist);
+            launch(radix_upsweep_kernel<K, true>, nt, kSortThreads, 0, stream, ksrc, n, shift, nt, b.hist, n_dev);
         else
-            launch(radix_upsweep_kernel<K, false>, nt, kSortThreads, 0, stream, ksrc, n, shift, nt, b.hist);
+            launch(radix_upsweep_kernel<K, false>, nt, kSortThreads, 0, stream, ksrc, n, shift, nt, b.hist, n_dev);
         launch(radix_rowscan_kernel, kRadix, 1024, 0, stream, b.hist, tot, nt);
-#define MSPLAT_DOWNSWEEP(FI, FO)                                                                         \
-    do {                                                                                                 \
-        auto kern = radix_downsweep_kernel<K, FI, FO>;                                                   \
-        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);              \
-        launch(kern, nt, kSortThreads, smem, stream, ksrc, vsrc, kdst, vdst, n, shift, nt, b.hist, tot); \
+#define MSPLAT_DOWNSWEEP(FI, FO)                                                                                \
+    do {                                                                                                        \
+        auto kern = radix_downsweep_kernel<K, FI, FO>;                                                          \
+        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);                     \
+        launch(kern, nt, kSortThreads, smem, stream, ksrc, vsrc, kdst, vdst, n, shift, nt, b.hist, tot, n_dev); \
     } while (0)
         if (FLIP && first && last) MSPLAT_DOWNSWEEP(true, true);
         else if (FLIP && first) MSPLAT_DOWNSWEEP(true, false);

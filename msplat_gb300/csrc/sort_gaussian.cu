@@ -154,7 +154,7 @@ __global__ void __launch_bounds__(256)
 emit_kernel(int P, const uint32_t *__restrict__ order, const int64_t *__restrict__ boff,
             const float2 *__restrict__ uv, const float *__restrict__ depth,
             const int32_t *__restrict__ radius, int gx, int gy, uint32_t *__restrict__ tkeys,
-            uint32_t *__restrict__ tvals) {
+            uint32_t *__restrict__ tvals, int64_t cap) {
     __shared__ int scratch[33];
     const int lane = threadIdx.x & 31;
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
@@ -180,7 +180,8 @@ emit_kernel(int P, const uint32_t *__restrict__ order, const int64_t *__restrict
         const int sstart = __shfl_sync(0xffffffffu, start, sl);
         const bool sneg = __shfl_sync(0xffffffffu, (int)neg, sl) != 0;
         const float inv = 1.0f / (float)sw;
-        for (int k = lane; k < sn; k += 32) {
+        const int kmax = (int)min((int64_t)sn, cap - (int64_t)sstart);  // capacity of the output
+        for (int k = lane; k < kmax; k += 32) {
             int ry = (int)(((float)k + 0.5f) * inv);  // k / sw, corrected below
             ry -= (ry * sw > k);
             ry += ((ry + 1) * sw <= k);
@@ -198,7 +199,9 @@ emit_kernel(int P, const uint32_t *__restrict__ order, const int64_t *__restrict
 constexpr int kRangeKeys = 8;
 
 __global__ void __launch_bounds__(256)
-range_from_tilekey_kernel(int64_t I, const uint32_t *__restrict__ keys, int2 *__restrict__ range) {
+range_from_tilekey_kernel(int64_t I, const uint32_t *__restrict__ keys, int2 *__restrict__ range,
+                          const int64_t *__restrict__ I_dev) {
+    if (I_dev) I = min(I, *I_dev);  // the length is on the device; I is the capacity
     const int64_t i0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) * kRangeKeys;
     if (i0 >= I) return;
     constexpr uint32_t kOut = 0xffffffffu;
@@ -488,26 +491,25 @@ extern "C" size_t msplat_sort_finish_workspace_size(int P, int64_t num_intersect
     return finish_bytes(num_intersects, W, H);
 }
 
-extern "C" int msplat_sort_gaussian_finish(int P, const float *uv, const float *depth,
-                                           const int32_t *radius, int W, int H,
-                                           int64_t num_intersects, const void *prepare_workspace,
-                                           int32_t *idx_sorted, int32_t *tile_range, void *workspace,
-                                           size_t workspace_bytes, msplat_stream_t stream) {
-    if (P < 0 || W <= 0 || H <= 0 || num_intersects < 0)
+// Emit, two tile-key passes and ranges.  I is the intersection count, or
+// with I_dev the capacity of the buffers and I_dev the device-side count
+// (entries past the capacity are dropped).
+static int finish_impl(int P, const float *uv, const float *depth, const int32_t *radius, int W, int H, int64_t I,
+                       const int64_t *I_dev, const void *prepare_workspace, int32_t *idx_sorted,
+                       int32_t *tile_range, void *workspace, size_t workspace_bytes, cudaStream_t stream) {
+    if (P < 0 || W <= 0 || H <= 0 || I < 0)
         return set_error(MSPLAT_ERR_INVALID_ARGUMENT, "sort_gaussian_finish: bad sizes");
-    if (num_intersects > INT32_MAX)
-        return set_error(MSPLAT_ERR_CAPACITY, "sort_gaussian_finish: %lld intersections exceed int32",
-                         (long long)num_intersects);
+    if (I > INT32_MAX)
+        return set_error(MSPLAT_ERR_CAPACITY, "sort_gaussian_finish: %lld intersections exceed int32", (long long)I);
     const int gx = ceil_div(W, kTile), gy = ceil_div(H, kTile), nt = gx * gy;
     if (!tile_range) return set_error(MSPLAT_ERR_INVALID_ARGUMENT, "sort_gaussian_finish: null tile_range");
     cudaMemsetAsync(tile_range, 0, sizeof(int32_t) * 2 * nt, stream);
-    if (P == 0 || num_intersects == 0) return check_launch("sort_gaussian_finish");
+    if (P == 0 || I == 0) return check_launch("sort_gaussian_finish");
     if (!uv || !depth || !radius || !prepare_workspace || !idx_sorted)
         return set_error(MSPLAT_ERR_INVALID_ARGUMENT, "sort_gaussian_finish: null pointer");
     Workspace pw(const_cast<void *>(prepare_workspace), prepare_bytes(P));
     PrepareWs prep;
     prepare_carve(pw, P, prep);
-    const int64_t I = num_intersects;
     const int passes = tile_key_passes(W, H);
     Workspace w(workspace, workspace_bytes);
     FinishWs f;
@@ -521,12 +523,42 @@ extern "C" int msplat_sort_gaussian_finish(int P, const float *uv, const float *
     const bool even = passes % 2 == 0;
     uint32_t *vemit = even ? out : f.vt;
     launch(emit_kernel, ceil_div(P, 256), 256, 0, stream, P, prep.order, prep.bsum, (const float2 *)uv, depth,
-                                                      radius, gx, gy, f.ka, vemit);
+           radius, gx, gy, f.ka, vemit, I);
     uint32_t *kout = even ? f.ka : f.kb;
     int st = radix_sort_pairs<uint32_t, false>(I, 0, passes, f.ka, vemit, kout, out, even ? f.kb : f.ka, f.vt,
-                                               f.rb, stream);
+                                               f.rb, stream, I_dev);
     if (st) return st;
     launch(range_from_tilekey_kernel, (unsigned)ceil_div64(ceil_div64(I, kRangeKeys), 256), 256, 0, stream, I, kout,
-           (int2 *)tile_range);
+           (int2 *)tile_range, I_dev);
     return check_launch("sort_gaussian_finish");
+}
+
+// status = 1 when the results of a capacity-bounded finish are not valid:
+// more intersections than the capacity, or tiles[] entries that disagree
+// with the rectangles (those need the reference-layout sort).
+__global__ void capacity_status_kernel(const int64_t *__restrict__ counts, int64_t cap, int32_t *__restrict__ status) {
+    status[0] = (counts[0] > cap || counts[1] != 0) ? 1 : 0;
+}
+
+extern "C" int msplat_sort_gaussian_finish(int P, const float *uv, const float *depth,
+                                           const int32_t *radius, int W, int H,
+                                           int64_t num_intersects, const void *prepare_workspace,
+                                           int32_t *idx_sorted, int32_t *tile_range, void *workspace,
+                                           size_t workspace_bytes, msplat_stream_t stream) {
+    return finish_impl(P, uv, depth, radius, W, H, num_intersects, nullptr, prepare_workspace, idx_sorted,
+                       tile_range, workspace, workspace_bytes, stream);
+}
+
+extern "C" int msplat_sort_gaussian_finish_capacity(int P, const float *uv, const float *depth,
+                                                    const int32_t *radius, int W, int H, int64_t capacity,
+                                                    const int64_t *counts, const void *prepare_workspace,
+                                                    int32_t *idx_sorted, int32_t *tile_range, int32_t *status,
+                                                    void *workspace, size_t workspace_bytes,
+                                                    msplat_stream_t stream) {
+    if (!counts || !status)
+        return set_error(MSPLAT_ERR_INVALID_ARGUMENT, "sort_gaussian_finish_capacity: null counts / status");
+    if (capacity < 0) return set_error(MSPLAT_ERR_INVALID_ARGUMENT, "sort_gaussian_finish_capacity: capacity < 0");
+    launch(capacity_status_kernel, 1, 1, 0, stream, counts, capacity, status);
+    return finish_impl(P, uv, depth, radius, W, H, capacity, counts, prepare_workspace, idx_sorted, tile_range,
+                       workspace, workspace_bytes, stream);
 }

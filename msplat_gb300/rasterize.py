@@ -19,7 +19,7 @@ from torch import Tensor
 from . import _lib
 from . import _tensors as tt
 from .alpha_blending import alpha_blending
-from .sort_gaussian import sort_gaussian
+from .sort_gaussian import sort_gaussian, sort_gaussian_capacity
 
 
 class _Preprocess(torch.autograd.Function):
@@ -104,8 +104,17 @@ def preprocess(xyz: Tensor, scale: Tensor, rotate: Tensor, intr: Tensor, extr: T
     return _Preprocess.apply(xyz, scale, rotate, shs, intr, extr, W, H, nearest, extent)
 
 
+def _sort(uv, depth, W, H, radius, tiles, capacity, status):
+    if capacity is None:
+        return sort_gaussian(uv, depth, W, H, radius, tiles)
+    if status is None:
+        raise RuntimeError("a capacity-bounded sort needs a status tensor to report overflow in")
+    return sort_gaussian_capacity(uv, depth, W, H, radius, tiles, capacity, status)
+
+
 def rasterization(xyz: Tensor, scale: Tensor, rotate: Tensor, opacity: Tensor, feature: Tensor, intr: Tensor,
-                  extr: Tensor, W: int, H: int, bg: float, ndc: Tensor = None, *, return_radius: bool = False):
+                  extr: Tensor, W: int, H: int, bg: float, ndc: Tensor = None, *, return_radius: bool = False,
+                  capacity: int | None = None, status: Tensor | None = None):
     """3-D Gaussian splatting of `feature` (msplat/__init__.py:22-93).
 
     xyz [P,3], scale [P,3], rotate [P,4] unit quaternions (r,x,y,z),
@@ -114,22 +123,30 @@ def rasterization(xyz: Tensor, scale: Tensor, rotate: Tensor, opacity: Tensor, f
     optionally receives dL/duv * (W/2, H/2).  Returns [C, H, W], and with
     return_radius=True also the screen radius [P] int32 (0 = not drawn),
     for density statistics.
+
+    With `capacity` (intersections) and `status` ([1] int32 CUDA tensor) the
+    frame makes no host read, so it can be captured in a CUDA graph; status
+    becomes 1 on the device if the capacity was too small (or the sort
+    needed the reference layout), and the frame must then be redone without
+    a capacity.
     """
     uv, depth, conic, radius, tiles, _ = preprocess(xyz, scale, rotate, intr, extr, W, H)
-    idx_sorted, tile_range = sort_gaussian(uv, depth, W, H, radius, tiles)
+    idx_sorted, tile_range = _sort(uv, depth, W, H, radius, tiles, capacity, status)
     img = alpha_blending(uv, conic, opacity, feature, idx_sorted, tile_range, bg, W, H, ndc)
     return (img, radius) if return_radius else img
 
 
 def rasterization_sh(xyz: Tensor, scale: Tensor, rotate: Tensor, opacity: Tensor, shs: Tensor, intr: Tensor,
-                     extr: Tensor, W: int, H: int, bg: float, ndc: Tensor = None, *, return_radius: bool = False):
+                     extr: Tensor, W: int, H: int, bg: float, ndc: Tensor = None, *, return_radius: bool = False,
+                     capacity: int | None = None, status: Tensor | None = None):
     """`rasterization` of the colour compute_sh(shs, view directions) with
     the view directions d = (xyz - c) / |xyz - c| of the camera centre
     c = -R^T t, evaluated inside the preprocess kernel; gradients flow into
     shs and, through d, into xyz and extr.  shs is [P, C, D] with
     D = (degree + 1)^2, degree <= 10.  Returns [C, H, W] (and the radius
-    [P] with return_radius=True)."""
+    [P] with return_radius=True).  `capacity` / `status` as for
+    `rasterization`."""
     uv, depth, conic, radius, tiles, color = preprocess(xyz, scale, rotate, intr, extr, W, H, shs=shs)
-    idx_sorted, tile_range = sort_gaussian(uv, depth, W, H, radius, tiles)
+    idx_sorted, tile_range = _sort(uv, depth, W, H, radius, tiles, capacity, status)
     img = alpha_blending(uv, conic, opacity, color, idx_sorted, tile_range, bg, W, H, ndc)
     return (img, radius) if return_radius else img

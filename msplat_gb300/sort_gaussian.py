@@ -172,3 +172,40 @@ def sort_gaussian_many(cases, streams=None):
     for s in streams:
         main.wait_stream(s)
     return out
+
+
+def sort_gaussian_capacity(uv: Tensor, depth: Tensor, W: int, H: int, radius: Tensor, tiles: Tensor,
+                           capacity: int, status: Tensor) -> Tuple[Tensor, Tensor]:
+    """`sort_gaussian` without a host read, for stream capture: idx_sorted has
+    `capacity` entries (those past the true count are unused; the tile
+    ranges index the valid ones) and status (a [1] int32 CUDA tensor) is set
+    to 1 on the device when the result is not valid (more intersections than
+    the capacity, or tiles[] disagreeing with the rectangles), else 0."""
+    u = tt.f32(uv, "uv", 2)
+    d = tt.f32(depth, "depth")
+    r = tt.i32(radius, "radius").view(-1)
+    t = tt.cuda(tiles, "tiles")
+    if t.dtype != torch.int32:
+        t = t.to(torch.int32)
+    t = t.contiguous().view(-1)
+    st_t = tt.i32(status, "status")
+    P = u.shape[0]
+    W, H, capacity = int(W), int(H), int(capacity)
+    dev = u.device
+    lib = _lib.load()
+    st = _lib.stream(dev)
+    counts = torch.empty(2, dtype=torch.int64, device=dev)
+    ws_prep = _lib.workspace(lib.msplat_sort_prepare_workspace_size(P, W, H), dev)
+    with _lib.stage("sort_gaussian_prepare"):
+        _lib.check(lib.msplat_sort_gaussian_prepare(
+            P, _lib.ptr(d), _lib.ptr(r), _lib.ptr(t), _lib.ptr(u), W, H, _lib.ptr(counts),
+            _lib.ptr(ws_prep), ws_prep.numel(), st), "sort_gaussian_prepare")
+    idx_sorted = torch.empty((capacity,), dtype=torch.int32, device=dev)
+    tile_range = torch.empty((tt.ntiles(W, H), 2), dtype=torch.int32, device=dev)
+    ws = _lib.workspace(lib.msplat_sort_finish_workspace_size(P, capacity, W, H), dev)
+    with _lib.stage("sort_gaussian_finish"):
+        _lib.check(lib.msplat_sort_gaussian_finish_capacity(
+            P, _lib.ptr(u), _lib.ptr(d), _lib.ptr(r), W, H, capacity, _lib.ptr(counts), _lib.ptr(ws_prep),
+            _lib.ptr(idx_sorted), _lib.ptr(tile_range), _lib.ptr(st_t), _lib.ptr(ws), ws.numel(), st),
+            "sort_gaussian_finish_capacity")
+    return idx_sorted, tile_range

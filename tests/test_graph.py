@@ -1,0 +1,111 @@
+"""The frame without host reads: a capacity-bounded tile sort whose count
+stays on the device, and a forward + backward frame captured in a CUDA
+graph and replayed.
+
+* with enough capacity the sort's valid part and tile ranges equal the
+  exact sort, and status is 0;
+* with too little capacity status is 1 (and nothing is written out of
+  bounds: the ranges stay inside the capacity);
+* the captured frame, replayed on new parameter values copied into its
+  static inputs, gives the eager frame's image bit for bit and its
+  gradients up to the order of float atomics.
+"""
+import numpy as np
+import pytest
+import torch
+
+from _scenes import camera, scene
+
+pytestmark = pytest.mark.gpu
+DEV = "cuda"
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _built():
+    from msplat_gb300 import _build, _lib
+    _build.build()
+    _lib.load()
+    yield
+
+
+def projected(n, W, H, seed):
+    import msplat_gb300 as ms
+    s = scene(n, seed, C=3, sh_deg=2)
+    intr, extr = camera(W, H, seed=seed)
+    p = {k: s[k].to(DEV).contiguous() for k in ("xyz", "scale", "rot", "opacity", "shs")}
+    p["intr"], p["extr"] = torch.as_tensor(intr).to(DEV), torch.as_tensor(extr).to(DEV)
+    uv, depth, conic, radius, tiles, color = ms.preprocess(p["xyz"], p["scale"], p["rot"], p["intr"], p["extr"],
+                                                           W, H, shs=p["shs"])
+    return p, uv, depth, radius, tiles
+
+
+def test_capacity_sort_equals_the_exact_sort_and_reports_overflow():
+    import msplat_gb300 as ms
+    from msplat_gb300.sort_gaussian import sort_gaussian_capacity
+    W, H = 320, 240
+    p, uv, depth, radius, tiles = projected(30000, W, H, 3)
+    idx, tr = ms.sort_gaussian(uv, depth, W, H, radius, tiles)
+    I = idx.numel()
+    assert I > 10000
+    status = torch.full((1,), 7, dtype=torch.int32, device=DEV)
+    cidx, ctr = sort_gaussian_capacity(uv, depth, W, H, radius, tiles, I + 1000, status)
+    assert int(status.item()) == 0
+    assert torch.equal(ctr, tr)
+    assert torch.equal(cidx[:I], idx)
+    small = I // 2
+    cidx, ctr = sort_gaussian_capacity(uv, depth, W, H, radius, tiles, small, status)
+    torch.cuda.synchronize()
+    assert int(status.item()) == 1
+    assert int(ctr.max().item()) <= small
+
+
+def test_captured_frame_replays_the_eager_frame():
+    import msplat_gb300 as ms
+    W, H = 256, 192
+    p, uv, depth, radius, tiles = projected(20000, W, H, 5)
+    idx, _ = ms.sort_gaussian(uv, depth, W, H, radius, tiles)
+    cap = int(idx.numel() * 1.25) + 1024
+    w = torch.randn(3, H, W, generator=torch.Generator().manual_seed(1)).to(DEV)
+    static = {k: v.clone().requires_grad_() for k, v in p.items()}
+    status = torch.zeros(1, dtype=torch.int32, device=DEV)
+
+    def step():
+        img = ms.rasterization_sh(static["xyz"], static["scale"], static["rot"], static["opacity"], static["shs"],
+                                  static["intr"], static["extr"], W, H, 0.0, capacity=cap, status=status)
+        (img * w).sum().backward()
+        return img
+
+    side = torch.cuda.Stream()
+    side.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(side):
+        for _ in range(3):
+            for t in static.values():
+                t.grad = None
+            step()
+    torch.cuda.current_stream().wait_stream(side)
+    for t in static.values():
+        t.grad = None
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph):
+        img_static = step()
+
+    # new parameter values, then replay
+    g = torch.Generator().manual_seed(9)
+    newp = {k: v.detach().clone() for k, v in p.items()}
+    newp["xyz"] += torch.randn(newp["xyz"].shape, generator=g).to(DEV) * 0.01
+    newp["opacity"] = torch.sigmoid(torch.randn(newp["opacity"].shape, generator=g)).to(DEV)
+    with torch.no_grad():
+        for k in static:
+            static[k].copy_(newp[k])
+    graph.replay()
+    torch.cuda.synchronize()
+    assert int(status.item()) == 0
+    eager = {k: v.clone().requires_grad_() for k, v in newp.items()}
+    img = ms.rasterization_sh(eager["xyz"], eager["scale"], eager["rot"], eager["opacity"], eager["shs"],
+                              eager["intr"], eager["extr"], W, H, 0.0)
+    (img * w).sum().backward()
+    assert torch.equal(img_static, img)
+    for k in static:
+        got, ref = static[k].grad, eager[k].grad
+        scale = ref.abs().max().item()
+        assert (got - ref).abs().max().item() <= 1e-5 * max(scale, 1e-30), k
