@@ -59,6 +59,22 @@ def _join(main: torch.cuda.Stream, streams: list) -> None:
         main.wait_stream(s)
 
 
+_DIMS: dict = {}
+
+
+def _dims(sizes, dev: torch.device) -> Tensor:
+    """[B, 2] int32 (W, H) on the device, cached per size list so that a call
+    under stream capture (after a warm-up call) makes no host-to-device
+    copy."""
+    key = (dev.index if dev.index is not None else torch.cuda.current_device(),
+           tuple((int(w), int(h)) for w, h in sizes))
+    if key not in _DIMS:
+        if len(_DIMS) > 64:
+            _DIMS.clear()
+        _DIMS[key] = torch.tensor([list(k) for k in key[1]], dtype=torch.int32, device=dev)
+    return _DIMS[key]
+
+
 def _cameras(intrs: Tensor, extrs: Tensor, B: int):
     intrs = tt.f32(intrs, "intrs")
     extrs = tt.f32(extrs, "extrs")
@@ -72,7 +88,8 @@ def _cameras(intrs: Tensor, extrs: Tensor, B: int):
 
 class _RasterizeBatch(torch.autograd.Function):
     @staticmethod
-    def forward(ctx, xyz, scale, rotate, opacity, shs, feature, intrs, extrs, sizes, bg):
+    def forward(ctx, xyz, scale, rotate, opacity, shs, feature, intrs, extrs, sizes, bg, capacities=None,
+                status=None):
         xyz_c = tt.f32(xyz, "xyz", 3)
         P = xyz_c.shape[0]
         scale_c = tt.f32(scale, "scale", 3)
@@ -83,7 +100,7 @@ class _RasterizeBatch(torch.autograd.Function):
         B = len(sizes)
         dev = xyz.device
         cams = _cameras(intrs, extrs, B)
-        dims = torch.tensor([[int(w), int(h)] for w, h in sizes], dtype=torch.int32, device=dev)
+        dims = _dims(sizes, dev)
         if shs is not None:
             shs_c = tt.f32(shs, "shs")
             if shs_c.dim() != 3 or shs_c.shape[0] != P:
@@ -110,7 +127,7 @@ class _RasterizeBatch(torch.autograd.Function):
                 "batch_preprocess_forward")
         streams = side_streams(dev)
         sorted_ = sort_gaussian_many([(uv[b], depth[b], int(w), int(h), radius[b], tiles[b])
-                                      for b, (w, h) in enumerate(sizes)], streams)
+                                      for b, (w, h) in enumerate(sizes)], streams, capacities, status)
         outs, finals = [], []
         main = _fork(streams, dev)
         with _lib.stage("alpha_blending_forward"):
@@ -192,20 +209,27 @@ class _RasterizeBatch(torch.autograd.Function):
                 g = torch.cat([g, torch.zeros((B, 4), dtype=g.dtype, device=dev)], dim=1)
             dL_dextrs = g.reshape(ctx.extr_shape)
         return (dL_dxyz, dL_dscale, dL_drot, dL_dopacity.view(ctx.op_shape), dL_dshs, dL_dfeature, dL_dintrs,
-                dL_dextrs, None, None)
+                dL_dextrs, None, None, None, None)
 
 
 def rasterization_sh_batch(xyz: Tensor, scale: Tensor, rotate: Tensor, opacity: Tensor, shs: Tensor,
-                           intrs: Tensor, extrs: Tensor, sizes: Sequence[tuple], bg: float = 0.0) -> list:
+                           intrs: Tensor, extrs: Tensor, sizes: Sequence[tuple], bg: float = 0.0, *,
+                           capacities: Sequence[int] | None = None, status: Tensor | None = None) -> list:
     """Renders B cameras of one scene with colour from SH coefficients on
     each camera's view directions (``rasterization_sh`` per camera).
     intrs [B, 4], extrs [B, 3, 4], sizes [(W, H)] * B.  Returns B images
-    [C, H_b, W_b]."""
-    return list(_RasterizeBatch.apply(xyz, scale, rotate, opacity, shs, None, intrs, extrs, tuple(sizes), bg))
+    [C, H_b, W_b].  With per-camera intersection `capacities` and a [B]
+    int32 `status` the call makes no host read (CUDA-graph capturable);
+    status[b] = 1 marks a camera whose capacity was too small."""
+    return list(_RasterizeBatch.apply(xyz, scale, rotate, opacity, shs, None, intrs, extrs, tuple(sizes), bg,
+                                      capacities, status))
 
 
 def rasterization_batch(xyz: Tensor, scale: Tensor, rotate: Tensor, opacity: Tensor, feature: Tensor,
-                        intrs: Tensor, extrs: Tensor, sizes: Sequence[tuple], bg: float = 0.0) -> list:
+                        intrs: Tensor, extrs: Tensor, sizes: Sequence[tuple], bg: float = 0.0, *,
+                        capacities: Sequence[int] | None = None, status: Tensor | None = None) -> list:
     """Renders B cameras of one scene with the same per-Gaussian features
-    (``rasterization`` per camera).  Returns B images [C, H_b, W_b]."""
-    return list(_RasterizeBatch.apply(xyz, scale, rotate, opacity, None, feature, intrs, extrs, tuple(sizes), bg))
+    (``rasterization`` per camera).  Returns B images [C, H_b, W_b];
+    `capacities` / `status` as for ``rasterization_sh_batch``."""
+    return list(_RasterizeBatch.apply(xyz, scale, rotate, opacity, None, feature, intrs, extrs, tuple(sizes), bg,
+                                      capacities, status))

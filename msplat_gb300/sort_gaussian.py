@@ -103,7 +103,7 @@ def _sort_reference_layout(u, d, W, H, r, t):
     return idx_sorted, tile_range
 
 
-def sort_gaussian_many(cases, streams=None):
+def sort_gaussian_many(cases, streams=None, capacities=None, status=None):
     """`sort_gaussian` for several cameras with one host read for all of
     them: every camera's prepare is enqueued, the intersection counts of all
     cameras are read together, then every finish is enqueued.  With
@@ -111,12 +111,19 @@ def sort_gaussian_many(cases, streams=None):
     work already on the current stream), so small cameras overlap on the
     device; the results are ready on the current stream on return.
 
+    With `capacities` (one per camera) and `status` ([B] int32), every
+    camera uses the capacity-bounded finish (sort_gaussian_capacity) and no
+    host read happens at all (stream-capturable); status[b] becomes 1 where
+    camera b's result is not valid.
+
     cases: sequence of (uv [P,2], depth [P,1], W, H, radius [P] int32,
     tiles [P] int32) contiguous float32 / int32 CUDA tensors.  Returns a
     list of (idx_sorted, tile_range)."""
     lib = _lib.load()
     if not cases:
         return []
+    if capacities is not None:
+        return _sort_many_capacity(cases, streams, capacities, status)
     dev = cases[0][0].device
     main = torch.cuda.current_stream(dev)
     streams = list(streams or [])
@@ -209,3 +216,28 @@ def sort_gaussian_capacity(uv: Tensor, depth: Tensor, W: int, H: int, radius: Te
             _lib.ptr(idx_sorted), _lib.ptr(tile_range), _lib.ptr(st_t), _lib.ptr(ws), ws.numel(), st),
             "sort_gaussian_finish_capacity")
     return idx_sorted, tile_range
+
+
+def _sort_many_capacity(cases, streams, capacities, status):
+    if status is None or status.numel() != len(cases):
+        raise RuntimeError("capacity-bounded sorts need a status tensor with one entry per camera")
+    dev = cases[0][0].device
+    main = torch.cuda.current_stream(dev)
+    streams = list(streams or [])
+    if streams:
+        ready = torch.cuda.Event()
+        ready.record(main)
+        for s in streams:
+            s.wait_event(ready)
+    out = []
+    for b, ((u, d, W, H, r, t), cap) in enumerate(zip(cases, capacities)):
+        ctx = torch.cuda.stream(streams[b % len(streams)]) if streams else contextlib.nullcontext()
+        with ctx:
+            res = sort_gaussian_capacity(u, d, W, H, r, t, int(cap), status[b:b + 1])
+            if streams:
+                for x in res:
+                    x.record_stream(main)
+        out.append(res)
+    for s in streams:
+        main.wait_stream(s)
+    return out

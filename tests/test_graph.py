@@ -109,3 +109,52 @@ def test_captured_frame_replays_the_eager_frame():
         got, ref = static[k].grad, eager[k].grad
         scale = ref.abs().max().item()
         assert (got - ref).abs().max().item() <= 1e-5 * max(scale, 1e-30), k
+
+
+def test_captured_batch_replays_the_eager_batch():
+    """Four cameras of one scene, forward + backward, captured in one CUDA
+    graph (the cameras' sorts and blends on side streams inside it)."""
+    import msplat_gb300 as ms
+    from _scenes import sphere_camera
+    sizes = [(128, 96), (160, 120), (96, 96), (200, 104)]
+    s = scene(15000, 8, C=3, sh_deg=1)
+    rng = np.random.default_rng(8)
+    intrs = torch.tensor([[300.0 * w / 256, 300.0 * w / 256, w / 2, h / 2] for w, h in sizes], device=DEV)
+    extrs = torch.tensor(np.stack([sphere_camera(rng) for _ in sizes]), device=DEV)
+    base = {k: s[k].to(DEV).contiguous() for k in ("xyz", "scale", "rot", "opacity", "shs")}
+    static = {k: v.clone().requires_grad_() for k, v in base.items()}
+    ws = [torch.randn(3, h, w, generator=torch.Generator().manual_seed(i)).to(DEV) for i, (w, h) in enumerate(sizes)]
+    status = torch.zeros(len(sizes), dtype=torch.int32, device=DEV)
+    caps = [200_000] * len(sizes)
+
+    def step():
+        imgs = ms.rasterization_sh_batch(static["xyz"], static["scale"], static["rot"], static["opacity"],
+                                         static["shs"], intrs, extrs, sizes, 0.1, capacities=caps, status=status)
+        sum((i * w).sum() for i, w in zip(imgs, ws)).backward()
+        return imgs
+
+    side = torch.cuda.Stream()
+    side.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(side):
+        for _ in range(3):
+            for t in static.values():
+                t.grad = None
+            step()
+    torch.cuda.current_stream().wait_stream(side)
+    for t in static.values():
+        t.grad = None
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph):
+        imgs_static = step()
+    graph.replay()
+    torch.cuda.synchronize()
+    assert int(status.sum().item()) == 0
+    eager = {k: v.clone().requires_grad_() for k, v in base.items()}
+    refs = ms.rasterization_sh_batch(eager["xyz"], eager["scale"], eager["rot"], eager["opacity"], eager["shs"],
+                                     intrs, extrs, sizes, 0.1)
+    sum((i * w).sum() for i, w in zip(refs, ws)).backward()
+    for a, b in zip(imgs_static, refs):
+        assert torch.equal(a, b)
+    for k in static:
+        got, ref = static[k].grad, eager[k].grad
+        assert (got - ref).abs().max().item() <= 1e-5 * max(ref.abs().max().item(), 1e-30), k
