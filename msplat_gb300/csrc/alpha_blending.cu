@@ -35,10 +35,17 @@ struct BlendRec {
 };
 
 // Conservative test: true only if no pixel centre of the tile box
-// [bx0, bx0 + 15] x [by0, by0 + 15] can reach alpha >= 1/255.
+// [bx0, bx0 + 15] x [by0, by0 + 15] can reach alpha >= 1/255.  L receives
+// the threshold it used: a pixel of the box can contribute only where the
+// exact q = a dx^2 + 2 b dx dy + c dy^2 is <= L (INFINITY or NaN when the
+// test gives no such bound).
 __device__ __forceinline__ bool cull_tile(float gx, float gy, float a, float b, float c, float op,
-                                          float bx0, float by0) {
-    if (!(op > 0.0f)) return op <= 0.0f;           // NaN opacity is never culled
+                                          float bx0, float by0, float &L) {
+    L = INFINITY;
+    if (!(op > 0.0f)) {  // NaN opacity is never culled
+        L = op;
+        return op <= 0.0f;
+    }
     const float tau = 2.0f * logf(255.0f * op);    // q <= tau  <=>  op e^{-q/2} >= 1/255
     const float det = a * c - b * b;
     if (!(a > 0.0f) || !(c > 0.0f) || !(det > 0.0f)) return false;  // not an ellipse
@@ -53,6 +60,7 @@ __device__ __forceinline__ bool cull_tile(float gx, float gy, float a, float b, 
     const float err = 1e-5f * (a * DX * DX + c * DY * DY + 2.0f * fabsf(b) * DX * DY) +
                       4.0f * coord_eps * (a * DX + c * DY + 2.0f * fabsf(b) * (DX + DY)) +
                       1e-5f * fabsf(tau) + 1e-4f;
+    L = tau + err;
     if (lx <= 0.0f && hx >= 0.0f && ly <= 0.0f && hy >= 0.0f) return tau + err < 0.0f;
     // Minimum of q(dx, dy) = a dx^2 + 2 b dx dy + c dy^2 over the box edges.
     float qmin = INFINITY;
@@ -73,6 +81,64 @@ __device__ __forceinline__ bool cull_tile(float gx, float gy, float a, float b, 
         }
     }
     return qmin > tau + err;
+}
+
+__device__ __forceinline__ bool cull_tile(float gx, float gy, float a, float b, float c, float op,
+                                          float bx0, float by0) {
+    float L;
+    return cull_tile(gx, gy, a, b, c, op, bx0, by0, L);
+}
+
+// Which warp blocks of a tile a Gaussian kept by cull_tile can reach.  The
+// tile is split into blocks 8 columns wide and RH rows tall, numbered
+// 2 (row band) + (column half); bit w of the result covers block w.  Per
+// column half [x0, x0 + 7] the reachable rows are the y-extent of the
+// ellipse q <= L inside that band: the upper boundary
+// y(x) = (-b x + sqrt(c L - det x^2)) / c is concave with its maximum
+// sqrt(L a / det) at x = -b sqrt(L a / det) / a, so over the band it peaks
+// there or at the nearer band edge (the lower boundary mirrors it); a band
+// beyond the ellipse's x-extent sqrt(L c / det) is not reached at all.
+// Extents are widened by 1 % plus 0.05 px and the coordinates' rounding,
+// which covers their float evaluation (with det >= 0.01 a c the
+// discriminant's rounding moves an extent by < 0.6 %); nearly degenerate
+// conics (det < 0.01 a c), or no usable L, reach every block.  Skipping a
+// block skips only pairs whose alpha is below 1/255: results do not change.
+template <int RH>
+__device__ __forceinline__ unsigned warp_block_mask(float gx, float gy, float a, float b, float c, float L,
+                                                    float bx0, float by0) {
+    constexpr int NBY = kTile / RH;
+    constexpr unsigned FULL = (1u << (2 * NBY)) - 1u;
+    const float det = a * c - b * b;
+    if (!(L >= 0.0f) || !(L < INFINITY) || !(a > 0.0f) || !(c > 0.0f) || !(det >= 0.01f * a * c))
+        return FULL;
+    const float ey = sqrtf(L * a / det), ex = sqrtf(L * c / det);
+    const float xt = -b * ey / a;  // dx of the topmost point; the lowest is at -xt
+    const float my = 0.01f * ey + 0.05f + 4e-6f * (fabsf(gy) + fabsf(by0) + (float)kTile);
+    const float mx = 0.01f * ex + 0.05f + 4e-6f * (fabsf(gx) + fabsf(bx0) + (float)kTile);
+    unsigned mask = 0u;
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        const float lx = bx0 + (float)(8 * h) - gx, hx = lx + 7.0f;
+        if (hx < -ex - mx || lx > ex + mx) continue;  // band beyond the ellipse
+        float top = ey, bot = -ey;
+        if (!(xt >= lx && xt <= hx)) {
+            const float x = fminf(fmaxf(xt, lx), hx);
+            top = (-b * x + sqrtf(fmaxf(c * L - det * x * x, 0.0f))) / c;
+        }
+        if (!(-xt >= lx && -xt <= hx)) {
+            const float x = fminf(fmaxf(-xt, lx), hx);
+            bot = (-b * x - sqrtf(fmaxf(c * L - det * x * x, 0.0f))) / c;
+        }
+        const float lo = gy + bot - my - by0, hi = gy + top + my - by0;  // tile rows, pixel centres at by0 + r
+        if (!(lo <= hi)) return FULL;
+        if (hi < 0.0f || lo > (float)(kTile - 1)) continue;
+        const int glo = (int)floorf(fmaxf(lo, 0.0f)) / RH;
+        const int ghi = (int)ceilf(fminf(hi, (float)(kTile - 1))) / RH;
+#pragma unroll
+        for (int g = 0; g < NBY; ++g)
+            if (g >= glo && g <= ghi) mask |= 1u << (2 * g + h);
+    }
+    return mask;
 }
 
 // power < bound  =>  opacity * exp(power) < 1/255 (with margin for the
@@ -374,17 +440,20 @@ __device__ __forceinline__ PixPow<NPIX> blend_power_n(float a, float b, float c,
 
 // Gathers NPIX entries per thread (thread t owns list positions
 // base + dir * (t * NPIX + r)) and compacts the kept ones into shared
-// memory in list order.  Returns the number kept.
+// memory in list order, with the mask of the warp blocks (8 columns by
+// 4 NPIX rows, one per warp) each one can reach.  Returns the number kept.
 template <int C, int NPIX, bool WITH_ID>
 __device__ __forceinline__ int gather_small(int base, int dir, int lo, int hi,
                                             const int32_t *__restrict__ idx_sorted,
                                             const float2 *__restrict__ uv, const float *__restrict__ conic,
                                             const float *__restrict__ opacity,
                                             const float *__restrict__ feature, float bx0, float by0,
-                                            float4 *sA, float4 *sB, float4 *sF, int *sG, int *scan) {
+                                            float4 *sA, float4 *sB, float4 *sF, int *sG, unsigned char *sM,
+                                            int *scan) {
     constexpr int NT = kTilePixels / NPIX;
     float4 A[NPIX], B[NPIX], F[NPIX];
     int G[NPIX];
+    unsigned M[NPIX];
     bool keep[NPIX];
     int nk = 0;
 #pragma unroll
@@ -396,7 +465,9 @@ __device__ __forceinline__ int gather_small(int base, int dir, int lo, int hi,
             const float2 p = uv[g];
             const float ca = conic[3 * g], cb = conic[3 * g + 1], cc = conic[3 * g + 2];
             const float op = opacity[g];
-            keep[r] = !cull_tile(p.x, p.y, ca, cb, cc, op, bx0, by0);
+            float L;
+            keep[r] = !cull_tile(p.x, p.y, ca, cb, cc, op, bx0, by0, L);
+            M[r] = keep[r] ? warp_block_mask<4 * NPIX>(p.x, p.y, ca, cb, cc, L, bx0, by0) : 0u;
             A[r] = make_float4(p.x, p.y, ca, cb);
             B[r] = make_float4(cc, op, power_bound(op), __int_as_float(j));
             float f[4] = {0.f, 0.f, 0.f, 0.f};
@@ -431,6 +502,7 @@ __device__ __forceinline__ int gather_small(int base, int dir, int lo, int hi,
             sA[pos] = A[r];
             sB[pos] = B[r];
             sF[pos] = F[r];
+            sM[pos] = (unsigned char)M[r];
             if (WITH_ID) sG[pos] = G[r];
             ++pos;
         }
@@ -446,13 +518,19 @@ blend_fwd_small_kernel(int P, const float2 *__restrict__ uv, const float *__rest
                        const int32_t *__restrict__ idx_sorted, const int2 *__restrict__ tile_range, float bg,
                        int W, int H, float *__restrict__ out, float *__restrict__ final_T,
                        int32_t *__restrict__ ncontrib) {
-    constexpr int NT = kTilePixels / NPIX, RS = kTile / NPIX;
+    constexpr int NT = kTilePixels / NPIX;
     __shared__ float4 sA[kBatch], sB[kBatch], sF[kBatch];
+    __shared__ unsigned char sM[kBatch];
     __shared__ int scan[NT / 32];
     const int gxn = (W + kTile - 1) / kTile;
     const int2 range = tile_range[blockIdx.y * gxn + blockIdx.x];
-    const int px = blockIdx.x * kTile + (threadIdx.x & (kTile - 1));
-    const int py0 = blockIdx.y * kTile + (threadIdx.x >> 4);
+    // warp w owns the block of 8 columns (8 (w % 2) ...) by 4 NPIX rows
+    // (4 NPIX (w / 2) ...) that bit w of a gathered entry's mask covers;
+    // lane l takes column l % 8 and rows (l / 8) NPIX + i of it
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int px = blockIdx.x * kTile + 8 * (warp & 1) + (lane & 7);
+    const int py0 = blockIdx.y * kTile + 4 * NPIX * (warp >> 1) + (lane >> 3) * NPIX;
+    const unsigned wbit = 1u << warp;
     const float fx = (float)px;
     const float bx0 = (float)(blockIdx.x * kTile), by0 = (float)(blockIdx.y * kTile);
     float fy[NPIX], T[NPIX], F[NPIX][4];
@@ -460,7 +538,7 @@ blend_fwd_small_kernel(int P, const float2 *__restrict__ uv, const float *__rest
     bool done[NPIX];
 #pragma unroll
     for (int i = 0; i < NPIX; ++i) {
-        const int py = py0 + i * RS;
+        const int py = py0 + i;
         fy[i] = (float)py;
         T[i] = 1.0f;
         last[i] = 0;
@@ -474,12 +552,23 @@ blend_fwd_small_kernel(int P, const float2 *__restrict__ uv, const float *__rest
         for (int i = 0; i < NPIX; ++i) all_done &= done[i];
         if (__syncthreads_count(all_done) == NT) break;
         const int n = gather_small<C, NPIX, false>(start, 1, range.x, range.y, idx_sorted, uv, conic, opacity,
-                                                   feature, bx0, by0, sA, sB, sF, nullptr, scan);
-        for (int k = 0; k < n; ++k) {
+                                                   feature, bx0, by0, sA, sB, sF, nullptr, sM, scan);
+        // Each warp walks, 32 entries at a time, only the entries whose row
+        // mask has its bit (a warp-uniform bit set from one ballot), and
+        // leaves the batch once all of its pixels are done.
+        bool warp_done = false;
+        for (int kw = 0; kw < n && !warp_done; kw += 32) {
+          unsigned bits = __ballot_sync(0xffffffffu, kw + lane < n && (sM[kw + lane] & wbit));
+          while (bits) {
             bool ad = true;
 #pragma unroll
             for (int i = 0; i < NPIX; ++i) ad &= done[i];
-            if (ad) break;
+            if (__all_sync(0xffffffffu, ad)) {
+                warp_done = true;
+                break;
+            }
+            const int k = kw + __ffs(bits) - 1;
+            bits &= bits - 1u;
             const float4 A = sA[k], B = sB[k];
             const float dx = A.x - fx;
             float dy[NPIX];
@@ -504,11 +593,12 @@ blend_fwd_small_kernel(int P, const float2 *__restrict__ uv, const float *__rest
                 T[i] = nT;
                 last[i] = __float_as_int(B.w) - range.x + 1;
             }
+          }
         }
     }
 #pragma unroll
     for (int i = 0; i < NPIX; ++i) {
-        const int py = py0 + i * RS;
+        const int py = py0 + i;
         if (px < W && py < H) {
             const int pix = py * W + px;
             final_T[pix] = T[i];
@@ -565,20 +655,23 @@ blend_bwd_small_kernel(int P, const float2 *__restrict__ uv, const float *__rest
                        const float *__restrict__ dL_dout, float *__restrict__ dL_duv,
                        float *__restrict__ dL_dconic, float *__restrict__ dL_dopacity,
                        float *__restrict__ dL_dfeature) {
-    constexpr int NT = kTilePixels / NPIX, RS = kTile / NPIX;
+    constexpr int NT = kTilePixels / NPIX;
     constexpr int NV = (6 + C) <= 8 ? 8 : 16;
     constexpr int LOG = NV == 16 ? 4 : 3;
     __shared__ float4 sA[kBatch], sB[kBatch], sF[kBatch];
     __shared__ int sG[kBatch];
+    __shared__ unsigned char sM[kBatch];
     __shared__ int scan[NT / 32];
     __shared__ int smax;
     const int gxn = (W + kTile - 1) / kTile;
     const int2 range = tile_range[blockIdx.y * gxn + blockIdx.x];
-    const int px = blockIdx.x * kTile + (threadIdx.x & (kTile - 1));
-    const int py0 = blockIdx.y * kTile + (threadIdx.x >> 4);
+    // pixel layout and warp blocks as in blend_fwd_small_kernel
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int px = blockIdx.x * kTile + 8 * (warp & 1) + (lane & 7);
+    const int py0 = blockIdx.y * kTile + 4 * NPIX * (warp >> 1) + (lane >> 3) * NPIX;
+    const unsigned wbit = 1u << warp;
     const float fx = (float)px;
     const float bx0 = (float)(blockIdx.x * kTile), by0 = (float)(blockIdx.y * kTile);
-    const int lane = threadIdx.x & 31;
 
     // Per pixel: the colour recursion of the reference (accum_rec =
     // last_alpha * last_color + (1 - last_alpha) * accum_rec per channel)
@@ -589,10 +682,9 @@ blend_bwd_small_kernel(int P, const float2 *__restrict__ uv, const float *__rest
     float dp[NPIX][4];
     int last[NPIX];
     int mylast = 0;
-    __shared__ int wmax[NT / 32];
 #pragma unroll
     for (int i = 0; i < NPIX; ++i) {
-        const int py = py0 + i * RS;
+        const int py = py0 + i;
         const bool in = px < W && py < H;
         const int pix = py * W + px;
         fy[i] = (float)py;
@@ -623,11 +715,18 @@ blend_bwd_small_kernel(int P, const float2 *__restrict__ uv, const float *__rest
     for (int bend = end; bend > range.x; bend -= kBatch) {
         const int bstart = max(range.x, bend - kBatch);
         const int n = gather_small<C, NPIX, true>(bend - 1, -1, bstart, bend, idx_sorted, uv, conic, opacity,
-                                                  feature, bx0, by0, sA, sB, sF, sG, scan);
-        for (int k = 0; k < n; ++k) {
+                                                  feature, bx0, by0, sA, sB, sF, sG, sM, scan);
+        // Each warp walks only the entries that reach its rows and precede
+        // its largest ncontrib (a warp-uniform bit set per 32 entries).
+        for (int kw = 0; kw < n; kw += 32) {
+          const int kk = kw + lane;
+          unsigned bits = __ballot_sync(0xffffffffu, kk < n && (sM[kk] & wbit) &&
+                                                         __float_as_int(sB[kk].w) - range.x < warp_last);
+          while (bits) {
+            const int k = kw + __ffs(bits) - 1;
+            bits &= bits - 1u;
             const float4 A = sA[k], B = sB[k];
             const int jl = __float_as_int(B.w) - range.x;
-            if (jl >= warp_last) continue;  // warp-uniform
             const float dx = A.x - fx;
             float dy[NPIX];
 #pragma unroll
@@ -635,7 +734,7 @@ blend_bwd_small_kernel(int P, const float2 *__restrict__ uv, const float *__rest
             const PixPow<NPIX> pw = blend_power_n<NPIX>(A.z, A.w, B.x, dx, dy);
             const float4 f = sF[k];
             const float fv[4] = {f.x, f.y, f.z, f.w};
-            const float ca = A.z, cb = A.w, cc = B.x, op = B.y;
+            const float op = B.y;
             float v[NV];
 #pragma unroll
             for (int q = 0; q < NV; ++q) v[q] = 0.0f;
@@ -704,6 +803,7 @@ blend_bwd_small_kernel(int P, const float2 *__restrict__ uv, const float *__rest
                     }
                 }
             }
+          }
         }
         __syncthreads();
     }

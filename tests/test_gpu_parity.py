@@ -398,14 +398,64 @@ def test_blend_multi_pixel_kernels_match_one_pixel_kernels():
     FMAs) against the one-pixel natural-form kernels that serve C > 4: with
     the same first three channels, transmittance and contributor counts must
     be bit-identical and so must the colours; gradients agree to rounding."""
+    s, it, W, H = blend_inputs(n=8000, W=200, H=120, C=3, seed=31)
+    small_vs_general(it["uv"], it["conic"], s["opacity"].numpy(), s["feat"].numpy(), it["idx_sorted"],
+                     it["tile_range"], W, H)
+
+
+def elongated_2d(n, W, H, seed):
+    """2-D Gaussians built directly on the image: standard deviations 0.5 to
+    60 px with axis ratios down to 1:100, any rotation, opacities from just
+    above 1/255 to 0.9, centres up to 40 px off screen; radius and tile
+    counts as the EWA stage computes them (3 x the largest deviation)."""
+    rng = np.random.default_rng(seed)
+    uv = rng.uniform([-40, -40], [W + 40, H + 40], (n, 2)).astype(np.float32)
+    s1 = np.exp(rng.uniform(np.log(0.5), np.log(60.0), n))
+    s2 = s1 * np.exp(rng.uniform(np.log(0.01), 0.0, n))
+    th = rng.uniform(0.0, np.pi, n)
+    ct, st = np.cos(th), np.sin(th)
+    cxx, cyy, cxy = ct**2 * s1**2 + st**2 * s2**2, st**2 * s1**2 + ct**2 * s2**2, ct * st * (s1**2 - s2**2)
+    det = cxx * cyy - cxy**2
+    conic = np.stack([cyy / det, -cxy / det, cxx / det], 1).astype(np.float32)
+    opacity = np.where(rng.random(n) < 0.25, rng.uniform(1 / 255, 0.02, n), rng.uniform(0.02, 0.9, n))
+    radius = np.ceil(3.0 * s1).astype(np.int32)
+    gx, gy = (W + 15) // 16, (H + 15) // 16
+    x0 = np.clip(np.trunc((uv[:, 0] - radius) / 16.0), 0, gx).astype(np.int64)
+    x1 = np.clip(np.trunc((uv[:, 0] + radius + 15.0) / 16.0), 0, gx).astype(np.int64)
+    y0 = np.clip(np.trunc((uv[:, 1] - radius) / 16.0), 0, gy).astype(np.int64)
+    y1 = np.clip(np.trunc((uv[:, 1] + radius + 15.0) / 16.0), 0, gy).astype(np.int64)
+    tiles = ((x1 - x0) * (y1 - y0)).astype(np.int32)
+    radius[tiles == 0] = 0
+    depth = rng.uniform(1.0, 10.0, n).astype(np.float32)
+    feat = rng.random((n, 3)).astype(np.float32)
+    idx, tr = oracle.sort_gaussian(uv, depth, W, H, radius, tiles)
+    return uv, conic, opacity.astype(np.float32).reshape(n, 1), feat, idx, tr
+
+
+def test_blend_row_cull_keeps_every_contribution():
+    """The C <= 4 kernels skip, per warp, the Gaussians whose alpha >= 1/255
+    ellipse misses that warp's rows; on strongly elongated, rotated and faint
+    Gaussians straddling tile rows their images must still be the oracle's
+    (outside exp-rounding ambiguities) and bit-identical to the kernels that
+    test every pixel."""
+    W, H = 320, 240
+    uv, conic, op, feat, idx, tr = elongated_2d(5000, W, H, seed=5)
+    assert idx.size > 100000
+    out = small_vs_general(uv, conic, op, feat, idx, tr, W, H)
+    oout, oT, onc, amb = oracle.alpha_blending_forward(uv, conic, op, feat, idx, tr, 0.5, W, H)
+    ok = ~amb
+    assert ok.mean() > 0.99
+    np.testing.assert_array_equal(out[2][ok], onc[ok])
+    assert np.abs(out[0] - oout)[:, ok].max() <= 1e-5
+
+
+def small_vs_general(uv, conic, op, f3, idx, tr, W, H):
     from msplat_gb300 import _lib
     lib = _lib.load()
-    s, it, W, H = blend_inputs(n=8000, W=200, H=120, C=3, seed=31)
-    P = s["feat"].shape[0]
-    f3 = s["feat"].numpy()
+    P = f3.shape[0]
     f5 = np.concatenate([f3, np.random.default_rng(0).random((P, 2)).astype(np.float32)], 1)
-    base = [T(it["uv"]), T(it["conic"]), T(s["opacity"])]
-    tail = [T(it["idx_sorted"]), T(it["tile_range"])]
+    base = [T(uv), T(conic), T(op)]
+    tail = [T(idx), T(tr)]
     res = {}
     for C, f in ((3, f3), (5, f5)):
         tf = T(f)
@@ -430,3 +480,4 @@ def test_blend_multi_pixel_kernels_match_one_pixel_kernels():
     for a, b in zip(res[3][3][:3], res[5][3][:3]):
         rel_close(a, b, rtol=1e-5, what="grad")
     rel_close(res[3][3][3], res[5][3][3][:, :3], rtol=1e-5, what="dL/dfeature")
+    return res[3]
