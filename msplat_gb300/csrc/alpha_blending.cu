@@ -609,35 +609,56 @@ blend_fwd_small_kernel(int P, const float2 *__restrict__ uv, const float *__rest
     }
 }
 
-// Reduce-scatter of NV (power of two, 8 or 16) values over a warp: lane l
-// returns the warp total of value (l >> (5 - log2 NV)).
-template <int NV>
-__device__ __forceinline__ float warp_reduce_scatter(float (&v)[NV]) {
-    const int lane = threadIdx.x & 31;
-    constexpr int LOG = NV == 16 ? 4 : 3;
-    constexpr int OMIN = 32 >> LOG;  // smallest halving offset
+// Reduce-scatter of N values over a warp in five halving steps.  At each
+// step (partner lane ^ O) a lane group holding n slots splits them: the
+// group with bit O clear keeps the first ceil(n/2), the other the rest, and
+// each lane sends the half it drops, so a step costs ceil(n/2) shuffles:
+// 9 values take 5 + 3 + 2 + 1 + 1 = 12 shuffles (16 when padded to a
+// power of two).  Afterwards v[0] of the lane that scatter_slot<N> names
+// for a slot holds that slot's warp total.
+template <int N, int O>
+struct ReduceScatter {
+    static __device__ __forceinline__ void run(float *v, int lane) {
+        constexpr int LO = (N + 1) / 2, HI = N - LO;
+        const bool up = (lane & O) != 0;
 #pragma unroll
-    for (int o = 16, n = NV; o >= OMIN; o >>= 1, n >>= 1) {
-        const bool up = (lane & o) != 0;
-        const int h = n >> 1;
-#pragma unroll
-        for (int k = 0; k < h; ++k) {
-            const float send = up ? v[k] : v[k + h];
-            const float keep = up ? v[k + h] : v[k];
-            v[k] = keep + __shfl_xor_sync(0xffffffffu, send, o);
+        for (int k = 0; k < LO; ++k) {
+            const float a = v[k];
+            const float b = k < HI ? v[LO + k] : 0.0f;
+            v[k] = (up ? b : a) + __shfl_xor_sync(0xffffffffu, up ? a : b, O);
         }
+        ReduceScatter<LO, O / 2>::run(v, lane);
     }
-    float r = v[0];
+};
+template <int N>
+struct ReduceScatter<N, 0> {
+    static __device__ __forceinline__ void run(float *, int) {}
+};
+
+// The slot whose total lane `lane` holds after ReduceScatter<N, 16>, or -1.
+template <int N>
+__device__ __forceinline__ int scatter_slot(int lane) {
+    int n = N, real = N, slot = 0;
 #pragma unroll
-    for (int o = OMIN >> 1; o > 0; o >>= 1) r += __shfl_xor_sync(0xffffffffu, r, o);
-    return r;
+    for (int o = 16; o >= 1; o >>= 1) {
+        const int lo = (n + 1) / 2;
+        if (lane & o) {
+            slot += lo;
+            real = max(0, real - lo);
+        } else {
+            real = min(real, lo);
+        }
+        n = lo;
+    }
+    return real >= 1 ? slot : -1;
 }
 
 // A Gaussian's per-warp gradient goes out as direct atomics from each
 // contributing lane when at most this many lanes contribute, else through a
 // warp reduce-scatter first.  Same-address atomics serialise, the reduction
-// costs a fixed ~16 shuffles per value set: the measured optimum of the two at
-// 1M Gaussians / 1080p is 12-16 lanes (blend backward 0.90 ms vs 1.00 ms with
+// costs a fixed 9-12 shuffles per value set (6 + C values): the measured
+// optimum of the two at 1M Gaussians / 1080p is 12-16 lanes (with 16-shuffle
+// reductions, one column per lane: blend backward 0.90 ms vs 1.00 ms with
 // the reduction always and 2.98 ms with atomics always).
 #ifndef MSPLAT_FEW_LANES
 #define MSPLAT_FEW_LANES 12
@@ -656,8 +677,7 @@ blend_bwd_small_kernel(int P, const float2 *__restrict__ uv, const float *__rest
                        float *__restrict__ dL_dconic, float *__restrict__ dL_dopacity,
                        float *__restrict__ dL_dfeature) {
     constexpr int NT = kTilePixels / NPIX;
-    constexpr int NV = (6 + C) <= 8 ? 8 : 16;
-    constexpr int LOG = NV == 16 ? 4 : 3;
+    constexpr int NV = 6 + C;
     __shared__ float4 sA[kBatch], sB[kBatch], sF[kBatch];
     __shared__ int sG[kBatch];
     __shared__ unsigned char sM[kBatch];
@@ -672,6 +692,7 @@ blend_bwd_small_kernel(int P, const float2 *__restrict__ uv, const float *__rest
     const unsigned wbit = 1u << warp;
     const float fx = (float)px;
     const float bx0 = (float)(blockIdx.x * kTile), by0 = (float)(blockIdx.y * kTile);
+    const int vi = scatter_slot<NV>(lane);  // the gradient slot this lane sends after a reduction
 
     // Per pixel: the colour recursion of the reference (accum_rec =
     // last_alpha * last_color + (1 - last_alpha) * accum_rec per channel)
@@ -791,9 +812,9 @@ blend_bwd_small_kernel(int P, const float2 *__restrict__ uv, const float *__rest
                         for (int q = 0; q < C; ++q) atomicAdd(dL_dfeature + (size_t)g * C + q, v[6 + q]);
                     }
                 } else {
-                    const float s = warp_reduce_scatter<NV>(v);
-                    const int vi = lane >> (5 - LOG);
-                    if ((lane & ((1 << (5 - LOG)) - 1)) == 0 && vi < 6 + C) {
+                    ReduceScatter<NV, 16>::run(v, lane);
+                    const float s = v[0];
+                    if (vi >= 0) {
                         float *dst;
                         if (vi == 0) dst = dL_dopacity + g;
                         else if (vi < 3) dst = dL_duv + 2 * g + (vi - 1);
