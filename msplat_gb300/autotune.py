@@ -5,7 +5,8 @@ thread in the blend forward and backward (which also sets the block shape,
 256 / NPIX threads per 16x16 tile), the number of contributing lanes below
 which the backward sends a Gaussian's gradients as direct atomics instead
 of a warp reduction, and the keys per thread of a radix tile (which sets
-the tile size, 256 x items).  The tuner builds a variant of the library for
+the tile size, 256 x items), and optional register caps of the two blend
+kernels (more resident blocks per SM against spills).  The tuner builds a variant of the library for
 each candidate setting (into its own directory), times a forward + backward
 frame of the benchmark's synthetic scene (``synthetic.training_scene``)
 with it in a separate process, searches the settings by coordinate descent
@@ -13,6 +14,10 @@ from the current defaults, and writes the best to
 ``msplat_gb300/tuning.json``, which the build then applies.
 
     python -m msplat_gb300.autotune [--gaussians N --width W --height H]
+                                    [--params MACRO,MACRO...]
+
+(``--params`` searches only the named parameters, the others staying at
+their current tuned values.)
 
 Results are those of any setting (all are parity-tested); only speed
 differs.
@@ -33,9 +38,11 @@ SPACE = {
     "MSPLAT_BLEND_NPIX_BWD": [1, 2, 4],
     "MSPLAT_FEW_LANES": [8, 12, 16],
     "MSPLAT_SORT_ITEMS": [8, 12, 16],
+    "MSPLAT_BLEND_FWD_REGS": [0, 40],
+    "MSPLAT_BLEND_BWD_REGS": [0, 64, 72],
 }
 DEFAULTS = {"MSPLAT_BLEND_NPIX_FWD": 1, "MSPLAT_BLEND_NPIX_BWD": 2, "MSPLAT_FEW_LANES": 12,
-            "MSPLAT_SORT_ITEMS": 12}
+            "MSPLAT_SORT_ITEMS": 12, "MSPLAT_BLEND_FWD_REGS": 0, "MSPLAT_BLEND_BWD_REGS": 0}
 TUNE_DIR = os.path.join(_build.PKG_DIR, "_build", "tune")
 
 
@@ -127,6 +134,7 @@ def main() -> None:
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--rounds", type=int, default=1)
+    ap.add_argument("--params", default="", help="comma-separated subset of the parameters to search")
     ap.add_argument("--time", action="store_true", help="(internal) time the library of this process")
     ap.add_argument("--out", default=_build.TUNING_PATH)
     a = ap.parse_args()
@@ -139,7 +147,15 @@ def main() -> None:
         print(f"{setting} -> {ms:.4f} ms", flush=True)
         return ms
 
-    best, best_ms, seen = coordinate_descent(SPACE, DEFAULTS, objective, rounds=a.rounds)
+    start = dict(DEFAULTS, **{k: v for k, v in _build.tuned_defines().items() if k in SPACE})
+    space = SPACE
+    if a.params:
+        names = [n.strip() for n in a.params.split(",") if n.strip()]
+        unknown = [n for n in names if n not in SPACE]
+        if unknown:
+            raise SystemExit(f"unknown parameters: {unknown}")
+        space = {n: SPACE[n] for n in names}
+    best, best_ms, seen = coordinate_descent(space, start, objective, rounds=a.rounds)
     out = {"defines": best, "ms_per_frame": round(best_ms, 4),
            "workload": {"gaussians": a.gaussians, "width": a.width, "height": a.height},
            "evaluated": [{"defines": dict(k), "ms_per_frame": round(v, 4)} for k, v in seen.items()]}

@@ -29,6 +29,17 @@ namespace msplat {
 constexpr int kBlendThreads = kTilePixels;  // 256: one thread per pixel
 constexpr int kBatch = kBlendThreads;
 
+// Register caps of the C <= 4 blend kernels (compile-time tunables; 0 = the
+// compiler's choice): a cap of R registers asks for 65536 / (R x threads)
+// resident blocks per SM.
+#ifndef MSPLAT_BLEND_FWD_REGS
+#define MSPLAT_BLEND_FWD_REGS 0
+#endif
+#ifndef MSPLAT_BLEND_BWD_REGS
+#define MSPLAT_BLEND_BWD_REGS 0
+#endif
+constexpr int blend_min_blocks(int threads, int regs) { return regs > 0 ? 65536 / (regs * threads) : 1; }
+
 struct BlendRec {
     float4 a;  // uv.x, uv.y, conic.x, conic.y
     float4 b;  // conic.z, opacity, power bound, list index (as int bits)
@@ -512,7 +523,7 @@ __device__ __forceinline__ int gather_small(int base, int dir, int lo, int hi,
 }
 
 template <int C, int NPIX>
-__global__ void __launch_bounds__(kTilePixels / NPIX)
+__global__ void __launch_bounds__(kTilePixels / NPIX, blend_min_blocks(kTilePixels / NPIX, MSPLAT_BLEND_FWD_REGS))
 blend_fwd_small_kernel(int P, const float2 *__restrict__ uv, const float *__restrict__ conic,
                        const float *__restrict__ opacity, const float *__restrict__ feature,
                        const int32_t *__restrict__ idx_sorted, const int2 *__restrict__ tile_range, float bg,
@@ -668,7 +679,7 @@ constexpr int kFewLanes = MSPLAT_FEW_LANES;
 // BG: the background is nonzero, so dL/dalpha has the term
 // -T_final / (1 - alpha) * sum_c bg dL/dpix_c (compiled out for bg == 0).
 template <int C, int NPIX, bool BG>
-__global__ void __launch_bounds__(kTilePixels / NPIX)
+__global__ void __launch_bounds__(kTilePixels / NPIX, blend_min_blocks(kTilePixels / NPIX, MSPLAT_BLEND_BWD_REGS))
 blend_bwd_small_kernel(int P, const float2 *__restrict__ uv, const float *__restrict__ conic,
                        const float *__restrict__ opacity, const float *__restrict__ feature,
                        const int32_t *__restrict__ idx_sorted, const int2 *__restrict__ tile_range, float bg,
