@@ -229,6 +229,25 @@ MSPLAT_API int msplat_sort_gaussian_finish(int P, const float *uv, const float *
                                 void *workspace, size_t workspace_bytes,
                                 msplat_stream_t stream);
 
+/* The prepare of the fused path's culled tile lists: as
+ * msplat_sort_gaussian_prepare, but each Gaussian's tile rectangle is first
+ * shrunk, side by side, while its outer row or column holds no pixel centre
+ * the Gaussian (conic [P,3], opacity [P]) can take to alpha >= 1/255, and
+ * negative-depth Gaussians (in no tile range) emit nothing.  The following
+ * finish (either form) then writes lists without those entries: the blend
+ * of them gives the same images and gradients as the reference's lists, but
+ * idx_sorted, tile_range and the intersection count differ from the
+ * reference's.  counts[1] still compares tiles[] with the unshrunk
+ * rectangles.  Grids up to 32767 tiles a side.  No counterpart in the
+ * reference. */
+MSPLAT_API int msplat_sort_gaussian_prepare_culled(int P, const float *depth,
+                                 const int32_t *radius, const int32_t *tiles,
+                                 const float *uv, const float *conic,
+                                 const float *opacity, int W, int H,
+                                 int64_t *counts, void *workspace,
+                                 size_t workspace_bytes,
+                                 msplat_stream_t stream);
+
 /* The finish without the host read of counts (for stream capture): the
  * buffers are sized for `capacity` intersections (idx_sorted [capacity],
  * workspace msplat_sort_finish_workspace_size(P, capacity, W, H)) and the

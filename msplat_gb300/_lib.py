@@ -47,6 +47,7 @@ _SIGNATURES = {
     "msplat_sort_prepare_workspace_size": (_SZ, [_I, _I, _I]),
     "msplat_sort_finish_workspace_size": (_SZ, [_I, _I64, _I, _I]),
     "msplat_sort_gaussian_prepare": (_I, [_I, _P, _P, _P, _P, _I, _I, _P, _P, _SZ, _P]),
+    "msplat_sort_gaussian_prepare_culled": (_I, [_I, _P, _P, _P, _P, _P, _P, _I, _I, _P, _P, _SZ, _P]),
     "msplat_sort_gaussian_finish": (
         _I, [_I, _P, _P, _P, _I, _I, _I64, _P, _P, _P, _P, _SZ, _P]),
     "msplat_sort_gaussian_finish_capacity": (

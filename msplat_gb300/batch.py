@@ -126,7 +126,8 @@ class _RasterizeBatch(torch.autograd.Function):
                 _lib.ptr(conic), _lib.ptr(radius), _lib.ptr(tiles), _lib.ptr(color), st),
                 "batch_preprocess_forward")
         streams = side_streams(dev)
-        sorted_ = sort_gaussian_many([(uv[b], depth[b], int(w), int(h), radius[b], tiles[b])
+        # culled lists, as the single-camera calls (same images and gradients)
+        sorted_ = sort_gaussian_many([(uv[b], depth[b], int(w), int(h), radius[b], tiles[b], conic[b], op_c)
                                       for b, (w, h) in enumerate(sizes)], streams, capacities, status)
         outs, finals = [], []
         main = _fork(streams, dev)

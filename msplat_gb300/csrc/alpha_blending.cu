@@ -22,7 +22,7 @@
 //    the list, and per-Gaussian gradients are summed over each warp with a
 //    reduce-scatter of shuffles before one atomic per value per warp (the
 //    reference issues C + 6 atomics per pixel-Gaussian pair).
-#include "common.cuh"
+#include "cull.cuh"
 
 namespace msplat {
 
@@ -45,60 +45,6 @@ struct BlendRec {
     float4 b;  // conic.z, opacity, power bound, list index (as int bits)
 };
 
-// Conservative test: true only if no pixel centre of the tile box
-// [bx0, bx0 + 15] x [by0, by0 + 15] can reach alpha >= 1/255.  L receives
-// the threshold it used: a pixel of the box can contribute only where the
-// exact q = a dx^2 + 2 b dx dy + c dy^2 is <= L (INFINITY or NaN when the
-// test gives no such bound).
-__device__ __forceinline__ bool cull_tile(float gx, float gy, float a, float b, float c, float op,
-                                          float bx0, float by0, float &L) {
-    L = INFINITY;
-    if (!(op > 0.0f)) {  // NaN opacity is never culled
-        L = op;
-        return op <= 0.0f;
-    }
-    const float tau = 2.0f * logf(255.0f * op);    // q <= tau  <=>  op e^{-q/2} >= 1/255
-    const float det = a * c - b * b;
-    if (!(a > 0.0f) || !(c > 0.0f) || !(det > 0.0f)) return false;  // not an ellipse
-    const float bx1 = bx0 + (float)(kTile - 1), by1 = by0 + (float)(kTile - 1);
-    const float lx = bx0 - gx, hx = bx1 - gx, ly = by0 - gy, hy = by1 - gy;  // pixel - centre
-    const float DX = fmaxf(fabsf(lx), fabsf(hx)), DY = fmaxf(fabsf(ly), fabsf(hy));
-    // Bound on how far the blend's float evaluation of q at a pixel can sit
-    // below the exact value: product/sum rounding (relative to the term
-    // sizes), rounding of the coordinate differences (relative to the
-    // coordinates), and the approximate logarithm in tau.
-    const float coord_eps = 1e-6f * (fabsf(gx) + fabsf(gy) + fabsf(bx1) + fabsf(by1) + 1.0f);
-    const float err = 1e-5f * (a * DX * DX + c * DY * DY + 2.0f * fabsf(b) * DX * DY) +
-                      4.0f * coord_eps * (a * DX + c * DY + 2.0f * fabsf(b) * (DX + DY)) +
-                      1e-5f * fabsf(tau) + 1e-4f;
-    L = tau + err;
-    if (lx <= 0.0f && hx >= 0.0f && ly <= 0.0f && hy >= 0.0f) return tau + err < 0.0f;
-    // Minimum of q(dx, dy) = a dx^2 + 2 b dx dy + c dy^2 over the box edges.
-    float qmin = INFINITY;
-    {
-        const float xs[2] = {lx, hx};
-#pragma unroll
-        for (int e = 0; e < 2; ++e) {
-            const float dx = xs[e];
-            const float dy = fminf(fmaxf(-b * dx / c, ly), hy);
-            qmin = fminf(qmin, a * dx * dx + 2.0f * b * dx * dy + c * dy * dy);
-        }
-        const float ys[2] = {ly, hy};
-#pragma unroll
-        for (int e = 0; e < 2; ++e) {
-            const float dy = ys[e];
-            const float dx = fminf(fmaxf(-b * dy / a, lx), hx);
-            qmin = fminf(qmin, a * dx * dx + 2.0f * b * dx * dy + c * dy * dy);
-        }
-    }
-    return qmin > tau + err;
-}
-
-__device__ __forceinline__ bool cull_tile(float gx, float gy, float a, float b, float c, float op,
-                                          float bx0, float by0) {
-    float L;
-    return cull_tile(gx, gy, a, b, c, op, bx0, by0, L);
-}
 
 // Which warp blocks of a tile a Gaussian kept by cull_tile can reach.  The
 // tile is split into blocks 8 columns wide and RH rows tall, numbered

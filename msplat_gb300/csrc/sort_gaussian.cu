@@ -24,6 +24,7 @@
 //   (the reference writes their range out of bounds; we skip that write).
 #include <mutex>
 
+#include "cull.cuh"
 #include "radix_sort.cuh"
 
 namespace msplat {
@@ -82,27 +83,44 @@ depth_key_kernel(int P, const float *__restrict__ depth, const int32_t *__restri
 // whose tiles[] entry disagrees with their rectangle (those need the
 // reference layout), the negative-depth emitters (they come first in depth
 // order) and their intersections.
+// With conic and opacity (the culled lists of the fused path) each
+// rectangle is first shrunk by shrink_rect, negative-depth Gaussians (which
+// no tile range includes) emit nothing, and the rectangle used is stored in
+// depth order in rects[j] for emit_kernel.
 __global__ void __launch_bounds__(256)
 depth_order_count_kernel(int P, const uint32_t *__restrict__ order, const float2 *__restrict__ uv,
                          const float *__restrict__ depth, const int32_t *__restrict__ radius,
-                         const int32_t *__restrict__ tiles, int gx, int gy, int64_t *__restrict__ bsum,
-                         int64_t *__restrict__ counts, unsigned long long *__restrict__ neg) {
+                         const int32_t *__restrict__ tiles, const float *__restrict__ conic,
+                         const float *__restrict__ opacity, int gx, int gy, int64_t *__restrict__ bsum,
+                         int64_t *__restrict__ counts, unsigned long long *__restrict__ neg,
+                         short4 *__restrict__ rects) {
     __shared__ int64_t scratch[33];
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     bool bad = false, isneg = false;
     int c = 0;
     if (j < P) {
         const int g = (int)order[j];
+        int x0 = 0, y0 = 0, x1 = 0, y1 = 0, cref = 0;
         if (radius[g] > 0) {
-            int x0, y0, x1, y1;
             const float2 p = uv[g];
             tile_rect(p.x, p.y, radius[g], gx, gy, x0, y0, x1, y1);
-            c = (x1 - x0) * (y1 - y0);
+            cref = (x1 - x0) * (y1 - y0);
             // Sign-bit-set depths sort before all others (signed order).
             isneg = (__float_as_uint(depth[g]) >> 31) != 0;
+            if (conic) {
+                if (isneg) {
+                    x1 = x0;
+                    y1 = y0;
+                } else {
+                    shrink_rect(p.x, p.y, conic[3 * g], conic[3 * g + 1], conic[3 * g + 2], opacity[g], x0, y0, x1,
+                                y1);
+                }
+            }
+            c = (x1 - x0) * (y1 - y0);
             if (isneg && c > 0) atomicAdd(neg + 1, (unsigned long long)c);
         }
-        bad = c != tiles[g];
+        if (conic) rects[j] = make_short4((short)x0, (short)y0, (short)x1, (short)y1);
+        bad = cref != tiles[g];
     }
     const unsigned mb = __ballot_sync(0xffffffffu, bad), mn = __ballot_sync(0xffffffffu, isneg);
     if ((threadIdx.x & 31) == 0) {
@@ -150,11 +168,12 @@ __device__ __forceinline__ void for_rect_tiles(int g, const float2 *__restrict__
 // Tile key 0 marks negative-depth Gaussians, t + 1 tile t.
 // A Gaussian's first slot is its block's base (boff, from the block sums)
 // plus the exclusive scan of the tile counts within the block.
+// With *culled set (by a culled prepare) the rectangles come from rects[j].
 __global__ void __launch_bounds__(256)
 emit_kernel(int P, const uint32_t *__restrict__ order, const int64_t *__restrict__ boff,
             const float2 *__restrict__ uv, const float *__restrict__ depth,
-            const int32_t *__restrict__ radius, int gx, int gy, uint32_t *__restrict__ tkeys,
-            uint32_t *__restrict__ tvals, int64_t cap) {
+            const int32_t *__restrict__ radius, const short4 *__restrict__ rects, const int *__restrict__ culled,
+            int gx, int gy, uint32_t *__restrict__ tkeys, uint32_t *__restrict__ tvals, int64_t cap) {
     __shared__ int scratch[33];
     const int lane = threadIdx.x & 31;
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
@@ -162,7 +181,13 @@ emit_kernel(int P, const uint32_t *__restrict__ order, const int64_t *__restrict
     bool neg = false;
     if (j < P) {
         g = (int)order[j];
-        if (radius[g] > 0) {
+        if (*culled) {
+            const short4 r = rects[j];
+            x0 = r.x;
+            y0 = r.y;
+            x1 = r.z;
+            y1 = r.w;
+        } else if (radius[g] > 0) {
             const float2 p = uv[g];
             tile_rect(p.x, p.y, radius[g], gx, gy, x0, y0, x1, y1);
             neg = (__float_as_uint(depth[g]) >> 31) != 0;
@@ -241,6 +266,8 @@ struct PrepareWs {
     uint32_t *order = nullptr;  // [P] Gaussian ids in depth order
     int64_t *bsum = nullptr;    // [P/256] tile counts per block of 256 in depth order, then their scan
     unsigned long long *neg = nullptr;  // [0] negative emitters, [1] their intersections
+    short4 *rects = nullptr;    // [P] rectangles in depth order (culled prepare)
+    int *culled = nullptr;      // [1] nonzero after a culled prepare
     uint32_t *ka = nullptr, *kb = nullptr, *vt = nullptr;
     RadixBuffers rb{};
 };
@@ -250,6 +277,8 @@ inline void prepare_carve(WS &w, int P, PrepareWs &ws) {
     ws.order = w.template take<uint32_t>(P);
     ws.bsum = w.template take<int64_t>((size_t)ceil_div(P, 256));
     ws.neg = w.template take<unsigned long long>(2);
+    ws.rects = w.template take<short4>(P);
+    ws.culled = w.template take<int>(1);
     ws.ka = w.template take<uint32_t>(P);
     ws.kb = w.template take<uint32_t>(P);
     ws.vt = w.template take<uint32_t>(P);
@@ -454,12 +483,14 @@ extern "C" size_t msplat_sort_prepare_workspace_size(int P, int W, int H) {
     return prepare_bytes(P < 0 ? 0 : P);
 }
 
-extern "C" int msplat_sort_gaussian_prepare(int P, const float *depth, const int32_t *radius,
-                                            const int32_t *tiles, const float *uv, int W, int H,
-                                            int64_t *counts, void *workspace, size_t workspace_bytes,
-                                            msplat_stream_t stream) {
+static int prepare_impl(int P, const float *depth, const int32_t *radius, const int32_t *tiles, const float *uv,
+                        const float *conic, const float *opacity, int W, int H, int64_t *counts, void *workspace,
+                        size_t workspace_bytes, cudaStream_t stream) {
     if (P < 0 || W <= 0 || H <= 0)
         return set_error(MSPLAT_ERR_INVALID_ARGUMENT, "sort_gaussian_prepare: bad sizes");
+    if (conic && (ceil_div(W, kTile) > 32767 || ceil_div(H, kTile) > 32767))  // rects hold int16 tile indices
+        return set_error(MSPLAT_ERR_INVALID_ARGUMENT, "sort_gaussian_prepare_culled: grid of %d x %d tiles too large",
+                         ceil_div(W, kTile), ceil_div(H, kTile));
     if (!counts) return set_error(MSPLAT_ERR_INVALID_ARGUMENT, "sort_gaussian_prepare: null counts");
     Workspace w(workspace, workspace_bytes);
     PrepareWs ws;
@@ -469,6 +500,7 @@ extern "C" int msplat_sort_gaussian_prepare(int P, const float *depth, const int
                          workspace_bytes, prepare_bytes(P));
     cudaMemsetAsync(counts, 0, 2 * sizeof(int64_t), stream);
     cudaMemsetAsync(ws.neg, 0, 2 * sizeof(unsigned long long), stream);
+    cudaMemsetAsync(ws.culled, conic ? 0xff : 0, sizeof(int), stream);
     if (P == 0) return check_launch("sort_gaussian_prepare");
     if (!depth || !radius || !tiles || !uv)
         return set_error(MSPLAT_ERR_INVALID_ARGUMENT, "sort_gaussian_prepare: null pointer");
@@ -480,9 +512,29 @@ extern "C" int msplat_sort_gaussian_prepare(int P, const float *depth, const int
     if (st) return st;
     const int nb = ceil_div(P, 256);
     launch(depth_order_count_kernel, nb, 256, 0, stream,
-        P, ws.order, (const float2 *)uv, depth, radius, tiles, gx, gy, ws.bsum, counts, ws.neg);
+        P, ws.order, (const float2 *)uv, depth, radius, tiles, conic, opacity, gx, gy, ws.bsum, counts, ws.neg,
+        ws.rects);
     launch(block_offsets_kernel, 1, 1024, 0, stream, nb, ws.bsum, counts);
     return check_launch("sort_gaussian_prepare");
+}
+
+extern "C" int msplat_sort_gaussian_prepare(int P, const float *depth, const int32_t *radius,
+                                            const int32_t *tiles, const float *uv, int W, int H,
+                                            int64_t *counts, void *workspace, size_t workspace_bytes,
+                                            msplat_stream_t stream) {
+    return prepare_impl(P, depth, radius, tiles, uv, nullptr, nullptr, W, H, counts, workspace, workspace_bytes,
+                        stream);
+}
+
+extern "C" int msplat_sort_gaussian_prepare_culled(int P, const float *depth, const int32_t *radius,
+                                                   const int32_t *tiles, const float *uv, const float *conic,
+                                                   const float *opacity, int W, int H, int64_t *counts,
+                                                   void *workspace, size_t workspace_bytes,
+                                                   msplat_stream_t stream) {
+    if (P > 0 && (!conic || !opacity))
+        return set_error(MSPLAT_ERR_INVALID_ARGUMENT, "sort_gaussian_prepare_culled: null conic / opacity");
+    return prepare_impl(P, depth, radius, tiles, uv, conic, opacity, W, H, counts, workspace, workspace_bytes,
+                        stream);
 }
 
 extern "C" size_t msplat_sort_finish_workspace_size(int P, int64_t num_intersects, int W, int H) {
@@ -523,7 +575,7 @@ static int finish_impl(int P, const float *uv, const float *depth, const int32_t
     const bool even = passes % 2 == 0;
     uint32_t *vemit = even ? out : f.vt;
     launch(emit_kernel, ceil_div(P, 256), 256, 0, stream, P, prep.order, prep.bsum, (const float2 *)uv, depth,
-           radius, gx, gy, f.ka, vemit, I);
+           radius, (const short4 *)prep.rects, (const int *)prep.culled, gx, gy, f.ka, vemit, I);
     uint32_t *kout = even ? f.ka : f.kb;
     int st = radix_sort_pairs<uint32_t, false>(I, 0, passes, f.ka, vemit, kout, out, even ? f.kb : f.ka, f.vt,
                                                f.rb, stream, I_dev);

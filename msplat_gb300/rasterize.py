@@ -104,12 +104,14 @@ def preprocess(xyz: Tensor, scale: Tensor, rotate: Tensor, intr: Tensor, extr: T
     return _Preprocess.apply(xyz, scale, rotate, shs, intr, extr, W, H, nearest, extent)
 
 
-def _sort(uv, depth, W, H, radius, tiles, capacity, status):
+def _sort(uv, depth, W, H, radius, tiles, capacity, status, cull):
+    # The fused calls sort culled lists: only the image and gradients leave
+    # them, and those equal the reference lists' (see sort_gaussian's cull).
     if capacity is None:
-        return sort_gaussian(uv, depth, W, H, radius, tiles)
+        return sort_gaussian(uv, depth, W, H, radius, tiles, cull=cull)
     if status is None:
         raise RuntimeError("a capacity-bounded sort needs a status tensor to report overflow in")
-    return sort_gaussian_capacity(uv, depth, W, H, radius, tiles, capacity, status)
+    return sort_gaussian_capacity(uv, depth, W, H, radius, tiles, capacity, status, cull=cull)
 
 
 def rasterization(xyz: Tensor, scale: Tensor, rotate: Tensor, opacity: Tensor, feature: Tensor, intr: Tensor,
@@ -131,7 +133,8 @@ def rasterization(xyz: Tensor, scale: Tensor, rotate: Tensor, opacity: Tensor, f
     a capacity.
     """
     uv, depth, conic, radius, tiles, _ = preprocess(xyz, scale, rotate, intr, extr, W, H)
-    idx_sorted, tile_range = _sort(uv, depth, W, H, radius, tiles, capacity, status)
+    cull = (conic.detach(), opacity.detach())
+    idx_sorted, tile_range = _sort(uv, depth, W, H, radius, tiles, capacity, status, cull)
     img = alpha_blending(uv, conic, opacity, feature, idx_sorted, tile_range, bg, W, H, ndc)
     return (img, radius) if return_radius else img
 
@@ -147,6 +150,7 @@ def rasterization_sh(xyz: Tensor, scale: Tensor, rotate: Tensor, opacity: Tensor
     [P] with return_radius=True).  `capacity` / `status` as for
     `rasterization`."""
     uv, depth, conic, radius, tiles, color = preprocess(xyz, scale, rotate, intr, extr, W, H, shs=shs)
-    idx_sorted, tile_range = _sort(uv, depth, W, H, radius, tiles, capacity, status)
+    cull = (conic.detach(), opacity.detach())
+    idx_sorted, tile_range = _sort(uv, depth, W, H, radius, tiles, capacity, status, cull)
     img = alpha_blending(uv, conic, opacity, color, idx_sorted, tile_range, bg, W, H, ndc)
     return (img, radius) if return_radius else img

@@ -12,6 +12,23 @@ from . import _lib
 from . import _tensors as tt
 
 
+def _prepare(lib, P, d, r, t, u, W, H, counts, ws_prep, st, cull):
+    """The sort's prepare step; with cull = (conic [P,3], opacity [P,1]) the
+    culled one (tile rectangles shrunk to what the Gaussians reach)."""
+    if cull is None:
+        _lib.check(lib.msplat_sort_gaussian_prepare(
+            P, _lib.ptr(d), _lib.ptr(r), _lib.ptr(t), _lib.ptr(u), W, H, _lib.ptr(counts),
+            _lib.ptr(ws_prep), ws_prep.numel(), st), "sort_gaussian_prepare")
+        return
+    conic = tt.f32(cull[0], "conic", 3)
+    opacity = tt.f32(cull[1], "opacity")
+    if conic.shape[0] != P or opacity.numel() != P:
+        raise RuntimeError("conic and opacity must describe the same number of points as uv")
+    _lib.check(lib.msplat_sort_gaussian_prepare_culled(
+        P, _lib.ptr(d), _lib.ptr(r), _lib.ptr(t), _lib.ptr(u), _lib.ptr(conic), _lib.ptr(opacity), W, H,
+        _lib.ptr(counts), _lib.ptr(ws_prep), ws_prep.numel(), st), "sort_gaussian_prepare_culled")
+
+
 def sort_gaussian(
     uv: Tensor,
     depth: Tensor,
@@ -19,6 +36,8 @@ def sort_gaussian(
     H: int,
     radius: Tensor,
     tiles: Tensor,
+    *,
+    cull: Tuple[Tensor, Tensor] | None = None,
 ) -> Tuple[Tensor, Tensor]:
     """Sorts the intersections by [tile | depth] (msplat/sort_gaussian.py:8-54).
 
@@ -30,6 +49,12 @@ def sort_gaussian(
 
     One device-to-host read (the intersection count) happens here, as in the
     reference (which reads it twice).
+
+    With cull = (conic [P,3], opacity [P,1]) the lists leave out the tiles a
+    Gaussian cannot reach (alpha < 1/255 at every pixel of them) and the
+    negative-depth Gaussians: alpha_blending over them gives the same images
+    and gradients, with fewer intersections to sort and blend, but the
+    lists are not the reference's.
     """
     u = tt.f32(uv, "uv", 2)
     d = tt.f32(depth, "depth")
@@ -49,9 +74,7 @@ def sort_gaussian(
     counts = torch.empty(2, dtype=torch.int64, device=dev)
     ws_prep = _lib.workspace(lib.msplat_sort_prepare_workspace_size(P, W, H), dev)
     with _lib.stage("sort_gaussian_prepare"):
-        _lib.check(lib.msplat_sort_gaussian_prepare(
-            P, _lib.ptr(d), _lib.ptr(r), _lib.ptr(t), _lib.ptr(u), W, H, _lib.ptr(counts),
-            _lib.ptr(ws_prep), ws_prep.numel(), st), "sort_gaussian_prepare")
+        _prepare(lib, P, d, r, t, u, W, H, counts, ws_prep, st, cull)
     I, n_mismatch = (int(v) for v in counts.tolist())
     if n_mismatch:
         return _sort_reference_layout(u, d, W, H, r, t)
@@ -117,8 +140,9 @@ def sort_gaussian_many(cases, streams=None, capacities=None, status=None):
     camera b's result is not valid.
 
     cases: sequence of (uv [P,2], depth [P,1], W, H, radius [P] int32,
-    tiles [P] int32) contiguous float32 / int32 CUDA tensors.  Returns a
-    list of (idx_sorted, tile_range)."""
+    tiles [P] int32) contiguous float32 / int32 CUDA tensors, optionally
+    followed by (conic [P,3], opacity [P,1]) for culled lists (see
+    `sort_gaussian`'s cull).  Returns a list of (idx_sorted, tile_range)."""
     lib = _lib.load()
     if not cases:
         return []
@@ -139,21 +163,21 @@ def sort_gaussian_many(cases, streams=None, capacities=None, status=None):
     counts = torch.empty((len(cases), 2), dtype=torch.int64, device=dev)
     preps = []
     with _lib.stage("sort_gaussian_prepare"):
-        for b, (u, d, W, H, r, t) in enumerate(cases):
+        for b, case in enumerate(cases):
+            u, d, W, H, r, t = case[:6]
             P = u.shape[0]
             with on(b):
                 st = _lib.stream(dev)
                 ws_prep = _lib.workspace(lib.msplat_sort_prepare_workspace_size(P, W, H), dev)
-                _lib.check(lib.msplat_sort_gaussian_prepare(
-                    P, _lib.ptr(d), _lib.ptr(r), _lib.ptr(t), _lib.ptr(u), W, H, _lib.ptr(counts[b]),
-                    _lib.ptr(ws_prep), ws_prep.numel(), st), "sort_gaussian_prepare")
+                _prepare(lib, P, d, r, t, u, W, H, counts[b], ws_prep, st, _cull_of(case))
             preps.append(ws_prep)
     for s in streams:
         main.wait_stream(s)
     host = counts.tolist()
     out = []
     with _lib.stage("sort_gaussian_finish"):
-        for b, ((u, d, W, H, r, t), ws_prep, (I, n_mismatch)) in enumerate(zip(cases, preps, host)):
+        for b, (case, ws_prep, (I, n_mismatch)) in enumerate(zip(cases, preps, host)):
+            u, d, W, H, r, t = case[:6]
             with on(b):
                 if n_mismatch:
                     res = _sort_reference_layout(u, d, W, H, r, t)
@@ -181,13 +205,19 @@ def sort_gaussian_many(cases, streams=None, capacities=None, status=None):
     return out
 
 
+def _cull_of(case):
+    return (case[6], case[7]) if len(case) > 6 else None
+
+
 def sort_gaussian_capacity(uv: Tensor, depth: Tensor, W: int, H: int, radius: Tensor, tiles: Tensor,
-                           capacity: int, status: Tensor) -> Tuple[Tensor, Tensor]:
+                           capacity: int, status: Tensor, *,
+                           cull: Tuple[Tensor, Tensor] | None = None) -> Tuple[Tensor, Tensor]:
     """`sort_gaussian` without a host read, for stream capture: idx_sorted has
     `capacity` entries (those past the true count are unused; the tile
     ranges index the valid ones) and status (a [1] int32 CUDA tensor) is set
     to 1 on the device when the result is not valid (more intersections than
-    the capacity, or tiles[] disagreeing with the rectangles), else 0."""
+    the capacity, or tiles[] disagreeing with the rectangles), else 0.
+    `cull` as for `sort_gaussian`."""
     u = tt.f32(uv, "uv", 2)
     d = tt.f32(depth, "depth")
     r = tt.i32(radius, "radius").view(-1)
@@ -204,9 +234,7 @@ def sort_gaussian_capacity(uv: Tensor, depth: Tensor, W: int, H: int, radius: Te
     counts = torch.empty(2, dtype=torch.int64, device=dev)
     ws_prep = _lib.workspace(lib.msplat_sort_prepare_workspace_size(P, W, H), dev)
     with _lib.stage("sort_gaussian_prepare"):
-        _lib.check(lib.msplat_sort_gaussian_prepare(
-            P, _lib.ptr(d), _lib.ptr(r), _lib.ptr(t), _lib.ptr(u), W, H, _lib.ptr(counts),
-            _lib.ptr(ws_prep), ws_prep.numel(), st), "sort_gaussian_prepare")
+        _prepare(lib, P, d, r, t, u, W, H, counts, ws_prep, st, cull)
     idx_sorted = torch.empty((capacity,), dtype=torch.int32, device=dev)
     tile_range = torch.empty((tt.ntiles(W, H), 2), dtype=torch.int32, device=dev)
     ws = _lib.workspace(lib.msplat_sort_finish_workspace_size(P, capacity, W, H), dev)
@@ -230,10 +258,11 @@ def _sort_many_capacity(cases, streams, capacities, status):
         for s in streams:
             s.wait_event(ready)
     out = []
-    for b, ((u, d, W, H, r, t), cap) in enumerate(zip(cases, capacities)):
+    for b, (case, cap) in enumerate(zip(cases, capacities)):
+        u, d, W, H, r, t = case[:6]
         ctx = torch.cuda.stream(streams[b % len(streams)]) if streams else contextlib.nullcontext()
         with ctx:
-            res = sort_gaussian_capacity(u, d, W, H, r, t, int(cap), status[b:b + 1])
+            res = sort_gaussian_capacity(u, d, W, H, r, t, int(cap), status[b:b + 1], cull=_cull_of(case))
             if streams:
                 for x in res:
                     x.record_stream(main)

@@ -429,7 +429,7 @@ def elongated_2d(n, W, H, seed):
     depth = rng.uniform(1.0, 10.0, n).astype(np.float32)
     feat = rng.random((n, 3)).astype(np.float32)
     idx, tr = oracle.sort_gaussian(uv, depth, W, H, radius, tiles)
-    return uv, conic, opacity.astype(np.float32).reshape(n, 1), feat, idx, tr
+    return uv, conic, opacity.astype(np.float32).reshape(n, 1), feat, idx, tr, (depth.reshape(n, 1), radius, tiles)
 
 
 def test_blend_row_cull_keeps_every_contribution():
@@ -439,7 +439,7 @@ def test_blend_row_cull_keeps_every_contribution():
     (outside exp-rounding ambiguities) and bit-identical to the kernels that
     test every pixel."""
     W, H = 320, 240
-    uv, conic, op, feat, idx, tr = elongated_2d(5000, W, H, seed=5)
+    uv, conic, op, feat, idx, tr, _ = elongated_2d(5000, W, H, seed=5)
     assert idx.size > 100000
     out = small_vs_general(uv, conic, op, feat, idx, tr, W, H)
     oout, oT, onc, amb = oracle.alpha_blending_forward(uv, conic, op, feat, idx, tr, 0.5, W, H)
@@ -447,6 +447,48 @@ def test_blend_row_cull_keeps_every_contribution():
     assert ok.mean() > 0.99
     np.testing.assert_array_equal(out[2][ok], onc[ok])
     assert np.abs(out[0] - oout)[:, ok].max() <= 1e-5
+
+
+def check_culled_lists(uv, depth, radius, tiles, conic, op, feat, W, H):
+    """sort_gaussian(cull=...) against the exact lists: per tile a
+    subsequence (same order) of the exact list, and the same blended image
+    bit for bit; gradients agree to float-atomic order."""
+    args = [T(uv), T(depth), W, H, T(radius), T(tiles)]
+    idx, tr = ms.sort_gaussian(*args)
+    cidx, ctr = ms.sort_gaussian(*args, cull=(T(conic), T(op)))
+    idx, tr, cidx, ctr = N(idx), N(tr), N(cidx), N(ctr)
+    assert 0 < cidx.size < idx.size
+    for t in range(tr.shape[0]):
+        full = idx[tr[t, 0]:tr[t, 1]]
+        sub = cidx[ctr[t, 0]:ctr[t, 1]]
+        it = iter(full.tolist())
+        assert all(any(g == h for h in it) for g in sub.tolist()), f"tile {t}: not a subsequence"
+    res = []
+    for lists in ((idx, tr), (cidx, ctr)):
+        p = [T(uv).requires_grad_(), T(conic).requires_grad_(), T(op).requires_grad_(), T(feat).requires_grad_()]
+        img = ms.alpha_blending(*p, T(lists[0]), T(lists[1]), 0.5, W, H)
+        (img * T(np.random.default_rng(2).normal(size=img.shape).astype(np.float32))).sum().backward()
+        res.append((N(img), [N(x.grad) for x in p]))
+    np.testing.assert_array_equal(res[0][0], res[1][0])
+    for a, b, what in zip(res[0][1], res[1][1], ("uv", "conic", "opacity", "feature")):
+        rel_close(b, a, rtol=1e-5, what=f"dL/d{what}")
+    return idx.size, cidx.size
+
+
+def test_culled_lists_blend_like_the_exact_lists():
+    """The fused path's culled tile lists (rectangles shrunk to the tiles a
+    Gaussian reaches, negative depths dropped) on projected scenes and on
+    strongly elongated, rotated and faint 2-D Gaussians."""
+    W, H = 320, 240
+    uv, conic, op, feat, _, _, (depth, radius, tiles) = elongated_2d(5000, W, H, seed=7)
+    depth = depth.copy()
+    depth[::20] *= -1.0  # negative-depth emitters: first in the exact list, in no range, dropped when culled
+    n_full, n_cull = check_culled_lists(uv, depth, radius, tiles, conic, op, feat, W, H)
+    assert n_cull < 0.95 * n_full
+    for seed in (1, 2):
+        s, it, _, _ = blend_inputs(n=20000, W=W, H=H, C=3, seed=seed)
+        check_culled_lists(it["uv"], it["depth"], it["radius"], it["tiles"], it["conic"], s["opacity"].numpy(),
+                           s["feat"].numpy(), W, H)
 
 
 def small_vs_general(uv, conic, op, f3, idx, tr, W, H):
