@@ -216,26 +216,33 @@ def fp32_peak_tflops(sm_mhz):
 
 
 def blend_pairs(ms, p, color_dim=3):
-    """Pixel-Gaussian pairs the forward blend evaluates (sum of ncontrib),
-    from one forward on the device outside the timed region."""
+    """Work counts of the frame, from forwards on the device outside the
+    timed region.  For the reference's tile lists and for the culled lists
+    the fused calls sort: intersections, and pixel-entry pairs up to each
+    pixel's last contributor (sum of ncontrib: the pairs the reference's
+    per-pixel loop evaluates over that list)."""
     from msplat_gb300 import _lib
+    out = {}
     with torch.no_grad():
         uv, depth = ms.project_point(p["xyz"], p["intr"], p["extr"], W_IMG, H_IMG)
         vis = depth != 0
         cov = ms.compute_cov3d(p["scale"], p["rot"], vis)
         conic, radius, tiles = ms.ewa_project(p["xyz"], cov, p["intr"], p["extr"], uv, W_IMG, H_IMG, vis)
-        idx, tr = ms.sort_gaussian(uv, depth, W_IMG, H_IMG, radius, tiles)
         col = torch.ones(p["xyz"].shape[0], color_dim, device=uv.device)
         lib = _lib.load()
-        out = torch.empty(color_dim, H_IMG, W_IMG, device=uv.device)
-        T = torch.empty(H_IMG, W_IMG, device=uv.device)
-        nc = torch.empty(H_IMG, W_IMG, dtype=torch.int32, device=uv.device)
-        _lib.check(lib.msplat_alpha_blending_forward(
-            p["xyz"].shape[0], color_dim, uv.data_ptr(), conic.data_ptr(), p["opacity"].data_ptr(),
-            col.data_ptr(), idx.data_ptr(), tr.data_ptr(), 0.0, W_IMG, H_IMG, out.data_ptr(), T.data_ptr(),
-            nc.data_ptr(), _lib.stream()), "blend")
+        for name, cull in (("reference", None), ("culled", (conic, p["opacity"]))):
+            idx, tr = ms.sort_gaussian(uv, depth, W_IMG, H_IMG, radius, tiles, cull=cull)
+            img = torch.empty(color_dim, H_IMG, W_IMG, device=uv.device)
+            T = torch.empty(H_IMG, W_IMG, device=uv.device)
+            nc = torch.empty(H_IMG, W_IMG, dtype=torch.int32, device=uv.device)
+            _lib.check(lib.msplat_alpha_blending_forward(
+                p["xyz"].shape[0], color_dim, uv.data_ptr(), conic.data_ptr(), p["opacity"].data_ptr(),
+                col.data_ptr(), idx.data_ptr(), tr.data_ptr(), 0.0, W_IMG, H_IMG, img.data_ptr(), T.data_ptr(),
+                nc.data_ptr(), _lib.stream()), "blend")
+            out[name] = {"intersections": int(idx.numel()), "blend_pairs": int(nc.sum().item())}
         torch.cuda.synchronize()
-        return int(nc.sum().item()), int(idx.numel()), int((radius > 0).sum().item())
+        out["visible_gaussians"] = int((radius > 0).sum().item())
+    return out
 
 
 # DRAM bytes per launch (read + write) of the blend kernels at the benchmark
@@ -462,7 +469,9 @@ def time_graph(ms, p, weights, args, device, world):
 def _finish(args, rank, world, ms, p, stages, clk, ms_step, e2e_ms, h2d, extra):
     if rank != 0:
         return None
-    pairs, inter, nvis = blend_pairs(ms, p)
+    work = blend_pairs(ms, p)
+    # the fused calls the bench times sort and blend the culled lists
+    pairs, inter, nvis = work["culled"]["blend_pairs"], work["culled"]["intersections"], work["visible_gaussians"]
     peaks, peak_kind = measured_peaks()
     dom, roof = roofline(stages, args.steps, pairs, inter, nvis, clk.get("sm_mhz"), peaks, peak_kind)
     in_mb = (sum(v.numel() * v.element_size() for v in p.values()) + 3 * W_IMG * H_IMG * 4) / 1e6
@@ -483,6 +492,9 @@ def _finish(args, rank, world, ms, p, stages, clk, ms_step, e2e_ms, h2d, extra):
         "config": {"workload": WORKLOAD,
                    "n_gaussians": N_GAUSS, "width": W_IMG, "height": H_IMG, "sh_degree": SH_DEG,
                    "focal": FOCAL, "intersections": inter, "visible_gaussians": nvis, "blend_pairs": pairs,
+                   "lists": "culled tile lists of the fused calls (reference lists: "
+                            f"{work['reference']['intersections']} intersections, "
+                            f"{work['reference']['blend_pairs']} blend pairs)",
                    "parallelism": "replicas" if world > 1 else "single",
                    "l2": f"inputs ({in_mb:.0f} MB) larger than L2 (129 MB); no flush"
                          if in_mb > 129 else f"inputs ({in_mb:.0f} MB) fit in L2; no flush (profiling case)"},
