@@ -38,7 +38,19 @@ constexpr int kBatch = kBlendThreads;
 #ifndef MSPLAT_BLEND_BWD_REGS
 #define MSPLAT_BLEND_BWD_REGS 0
 #endif
-constexpr int blend_min_blocks(int threads, int regs) { return regs > 0 ? 65536 / (regs * threads) : 1; }
+// (Without a cap the kernels name no minimum block count at all: ptxas
+// allocates differently for an explicit minimum of 1 -- 55 instead of 48
+// registers in the forward, one block per SM fewer.)
+#if MSPLAT_BLEND_FWD_REGS > 0
+#define MSPLAT_FWD_BOUNDS(T) __launch_bounds__(T, 65536 / (MSPLAT_BLEND_FWD_REGS * (T)))
+#else
+#define MSPLAT_FWD_BOUNDS(T) __launch_bounds__(T)
+#endif
+#if MSPLAT_BLEND_BWD_REGS > 0
+#define MSPLAT_BWD_BOUNDS(T) __launch_bounds__(T, 65536 / (MSPLAT_BLEND_BWD_REGS * (T)))
+#else
+#define MSPLAT_BWD_BOUNDS(T) __launch_bounds__(T)
+#endif
 
 struct BlendRec {
     float4 a;  // uv.x, uv.y, conic.x, conic.y
@@ -469,7 +481,7 @@ __device__ __forceinline__ int gather_small(int base, int dir, int lo, int hi,
 }
 
 template <int C, int NPIX>
-__global__ void __launch_bounds__(kTilePixels / NPIX, blend_min_blocks(kTilePixels / NPIX, MSPLAT_BLEND_FWD_REGS))
+__global__ void MSPLAT_FWD_BOUNDS(kTilePixels / NPIX)
 blend_fwd_small_kernel(int P, const float2 *__restrict__ uv, const float *__restrict__ conic,
                        const float *__restrict__ opacity, const float *__restrict__ feature,
                        const int32_t *__restrict__ idx_sorted, const int2 *__restrict__ tile_range, float bg,
@@ -625,7 +637,7 @@ constexpr int kFewLanes = MSPLAT_FEW_LANES;
 // BG: the background is nonzero, so dL/dalpha has the term
 // -T_final / (1 - alpha) * sum_c bg dL/dpix_c (compiled out for bg == 0).
 template <int C, int NPIX, bool BG>
-__global__ void __launch_bounds__(kTilePixels / NPIX, blend_min_blocks(kTilePixels / NPIX, MSPLAT_BLEND_BWD_REGS))
+__global__ void MSPLAT_BWD_BOUNDS(kTilePixels / NPIX)
 blend_bwd_small_kernel(int P, const float2 *__restrict__ uv, const float *__restrict__ conic,
                        const float *__restrict__ opacity, const float *__restrict__ feature,
                        const int32_t *__restrict__ idx_sorted, const int2 *__restrict__ tile_range, float bg,
