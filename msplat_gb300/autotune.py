@@ -5,8 +5,9 @@ thread in the blend forward and backward (which also sets the block shape,
 256 / NPIX threads per 16x16 tile), the number of contributing lanes below
 which the backward sends a Gaussian's gradients as direct atomics instead
 of a warp reduction, and the keys per thread of a radix tile (which sets
-the tile size, 256 x items), and optional register caps of the two blend
-kernels (more resident blocks per SM against spills).  The tuner builds a variant of the library for
+the tile size, 256 x items), optional register caps of the two blend
+kernels (more resident blocks per SM against spills) and whether a tile is
+blended by one block or by two of 8 rows each.  The tuner builds a variant of the library for
 each candidate setting (into its own directory), times a forward + backward
 frame of the benchmark's synthetic scene (``synthetic.training_scene``)
 with it in a separate process, searches the settings by coordinate descent
@@ -40,9 +41,12 @@ SPACE = {
     "MSPLAT_SORT_ITEMS": [8, 12, 16],
     "MSPLAT_BLEND_FWD_REGS": [0, 40],
     "MSPLAT_BLEND_BWD_REGS": [0, 64, 72],
+    "MSPLAT_BLEND_SPLIT_FWD": [1, 2],
+    "MSPLAT_BLEND_SPLIT_BWD": [1, 2],
 }
 DEFAULTS = {"MSPLAT_BLEND_NPIX_FWD": 1, "MSPLAT_BLEND_NPIX_BWD": 2, "MSPLAT_FEW_LANES": 12,
-            "MSPLAT_SORT_ITEMS": 12, "MSPLAT_BLEND_FWD_REGS": 0, "MSPLAT_BLEND_BWD_REGS": 0}
+            "MSPLAT_SORT_ITEMS": 12, "MSPLAT_BLEND_FWD_REGS": 0, "MSPLAT_BLEND_BWD_REGS": 0,
+            "MSPLAT_BLEND_SPLIT_FWD": 1, "MSPLAT_BLEND_SPLIT_BWD": 1}
 TUNE_DIR = os.path.join(_build.PKG_DIR, "_build", "tune")
 
 
@@ -143,7 +147,12 @@ def main() -> None:
         return
 
     def objective(setting):
-        ms = time_variant(variant_library(setting), a.gaussians, a.width, a.height, a.steps, a.warmup)
+        try:
+            lib = variant_library(setting)
+        except RuntimeError as e:  # a combination the kernels reject at compile time
+            print(f"{setting} -> does not build ({str(e).splitlines()[0][:120]})", flush=True)
+            return float("inf")
+        ms = time_variant(lib, a.gaussians, a.width, a.height, a.steps, a.warmup)
         print(f"{setting} -> {ms:.4f} ms", flush=True)
         return ms
 

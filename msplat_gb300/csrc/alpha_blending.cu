@@ -58,8 +58,9 @@ struct BlendRec {
 };
 
 
-// Which warp blocks of a tile a Gaussian kept by cull_tile can reach.  The
-// tile is split into blocks 8 columns wide and RH rows tall, numbered
+// Which warp blocks of a tile (or of the ROWS-row part of it a block
+// renders) a Gaussian kept by the tile cull can reach.  The area is split
+// into blocks 8 columns wide and RH rows tall, numbered
 // 2 (row band) + (column half); bit w of the result covers block w.  Per
 // column half [x0, x0 + 7] the reachable rows are the y-extent of the
 // ellipse q <= L inside that band: the upper boundary
@@ -72,10 +73,10 @@ struct BlendRec {
 // discriminant's rounding moves an extent by < 0.6 %); nearly degenerate
 // conics (det < 0.01 a c), or no usable L, reach every block.  Skipping a
 // block skips only pairs whose alpha is below 1/255: results do not change.
-template <int RH>
+template <int RH, int ROWS = kTile>
 __device__ __forceinline__ unsigned warp_block_mask(float gx, float gy, float a, float b, float c, float L,
                                                     float bx0, float by0) {
-    constexpr int NBY = kTile / RH;
+    constexpr int NBY = ROWS / RH;
     constexpr unsigned FULL = (1u << (2 * NBY)) - 1u;
     const float det = a * c - b * b;
     if (!(L >= 0.0f) || !(L < INFINITY) || !(a > 0.0f) || !(c > 0.0f) || !(det >= 0.01f * a * c))
@@ -98,11 +99,11 @@ __device__ __forceinline__ unsigned warp_block_mask(float gx, float gy, float a,
             const float x = fminf(fmaxf(-xt, lx), hx);
             bot = (-b * x - sqrtf(fmaxf(c * L - det * x * x, 0.0f))) / c;
         }
-        const float lo = gy + bot - my - by0, hi = gy + top + my - by0;  // tile rows, pixel centres at by0 + r
+        const float lo = gy + bot - my - by0, hi = gy + top + my - by0;  // rows, pixel centres at by0 + r
         if (!(lo <= hi)) return FULL;
-        if (hi < 0.0f || lo > (float)(kTile - 1)) continue;
+        if (hi < 0.0f || lo > (float)(ROWS - 1)) continue;
         const int glo = (int)floorf(fmaxf(lo, 0.0f)) / RH;
-        const int ghi = (int)ceilf(fminf(hi, (float)(kTile - 1))) / RH;
+        const int ghi = (int)ceilf(fminf(hi, (float)(ROWS - 1))) / RH;
 #pragma unroll
         for (int g = 0; g < NBY; ++g)
             if (g >= glo && g <= ghi) mask |= 1u << (2 * g + h);
@@ -410,8 +411,10 @@ __device__ __forceinline__ PixPow<NPIX> blend_power_n(float a, float b, float c,
 // Gathers NPIX entries per thread (thread t owns list positions
 // base + dir * (t * NPIX + r)) and compacts the kept ones into shared
 // memory in list order, with the mask of the warp blocks (8 columns by
-// 4 NPIX rows, one per warp) each one can reach.  Returns the number kept.
-template <int C, int NPIX, bool WITH_ID>
+// 4 NPIX rows, one per warp) each one can reach.  The block renders the
+// ROWS rows from by0 of the tile, which is also the box of the cull.
+// Returns the number kept.
+template <int C, int NPIX, bool WITH_ID, int ROWS = kTile>
 __device__ __forceinline__ int gather_small(int base, int dir, int lo, int hi,
                                             const int32_t *__restrict__ idx_sorted,
                                             const float2 *__restrict__ uv, const float *__restrict__ conic,
@@ -419,7 +422,7 @@ __device__ __forceinline__ int gather_small(int base, int dir, int lo, int hi,
                                             const float *__restrict__ feature, float bx0, float by0,
                                             float4 *sA, float4 *sB, float4 *sF, int *sG, unsigned char *sM,
                                             int *scan) {
-    constexpr int NT = kTilePixels / NPIX;
+    constexpr int NT = kTile * ROWS / NPIX;
     float4 A[NPIX], B[NPIX], F[NPIX];
     int G[NPIX];
     unsigned M[NPIX];
@@ -435,8 +438,9 @@ __device__ __forceinline__ int gather_small(int base, int dir, int lo, int hi,
             const float ca = conic[3 * g], cb = conic[3 * g + 1], cc = conic[3 * g + 2];
             const float op = opacity[g];
             float L;
-            keep[r] = !cull_tile(p.x, p.y, ca, cb, cc, op, bx0, by0, L);
-            M[r] = keep[r] ? warp_block_mask<4 * NPIX>(p.x, p.y, ca, cb, cc, L, bx0, by0) : 0u;
+            keep[r] = !cull_box(p.x, p.y, ca, cb, cc, op, bx0, by0, bx0 + (float)(kTile - 1),
+                                by0 + (float)(ROWS - 1), L);
+            M[r] = keep[r] ? warp_block_mask<4 * NPIX, ROWS>(p.x, p.y, ca, cb, cc, L, bx0, by0) : 0u;
             A[r] = make_float4(p.x, p.y, ca, cb);
             B[r] = make_float4(cc, op, power_bound(op), __int_as_float(j));
             float f[4] = {0.f, 0.f, 0.f, 0.f};
@@ -480,28 +484,34 @@ __device__ __forceinline__ int gather_small(int base, int dir, int lo, int hi,
     return total;
 }
 
-template <int C, int NPIX>
-__global__ void MSPLAT_FWD_BOUNDS(kTilePixels / NPIX)
+// SPLIT: a tile is rendered by SPLIT blocks of kTile / SPLIT rows each
+// (grid.y = tiles down x SPLIT), each gathering the tile's list against
+// its own part.
+template <int C, int NPIX, int SPLIT>
+__global__ void MSPLAT_FWD_BOUNDS(kTilePixels / NPIX / SPLIT)
 blend_fwd_small_kernel(int P, const float2 *__restrict__ uv, const float *__restrict__ conic,
                        const float *__restrict__ opacity, const float *__restrict__ feature,
                        const int32_t *__restrict__ idx_sorted, const int2 *__restrict__ tile_range, float bg,
                        int W, int H, float *__restrict__ out, float *__restrict__ final_T,
                        int32_t *__restrict__ ncontrib) {
-    constexpr int NT = kTilePixels / NPIX;
-    __shared__ float4 sA[kBatch], sB[kBatch], sF[kBatch];
-    __shared__ unsigned char sM[kBatch];
+    constexpr int ROWS = kTile / SPLIT, NT = kTile * ROWS / NPIX, BATCH = NT * NPIX;
+    static_assert(4 * NPIX <= ROWS, "a warp block of 4 NPIX rows must fit the block's rows");
+    __shared__ float4 sA[BATCH], sB[BATCH], sF[BATCH];
+    __shared__ unsigned char sM[BATCH];
     __shared__ int scan[NT / 32];
     const int gxn = (W + kTile - 1) / kTile;
-    const int2 range = tile_range[blockIdx.y * gxn + blockIdx.x];
+    const int ty = blockIdx.y / SPLIT;
+    const int2 range = tile_range[ty * gxn + blockIdx.x];
     // warp w owns the block of 8 columns (8 (w % 2) ...) by 4 NPIX rows
     // (4 NPIX (w / 2) ...) that bit w of a gathered entry's mask covers;
     // lane l takes column l % 8 and rows (l / 8) NPIX + i of it
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int row0 = ty * kTile + (blockIdx.y % SPLIT) * ROWS;
     const int px = blockIdx.x * kTile + 8 * (warp & 1) + (lane & 7);
-    const int py0 = blockIdx.y * kTile + 4 * NPIX * (warp >> 1) + (lane >> 3) * NPIX;
+    const int py0 = row0 + 4 * NPIX * (warp >> 1) + (lane >> 3) * NPIX;
     const unsigned wbit = 1u << warp;
     const float fx = (float)px;
-    const float bx0 = (float)(blockIdx.x * kTile), by0 = (float)(blockIdx.y * kTile);
+    const float bx0 = (float)(blockIdx.x * kTile), by0 = (float)row0;
     float fy[NPIX], T[NPIX], F[NPIX][4];
     int last[NPIX];
     bool done[NPIX];
@@ -515,13 +525,13 @@ blend_fwd_small_kernel(int P, const float2 *__restrict__ uv, const float *__rest
 #pragma unroll
         for (int q = 0; q < 4; ++q) F[i][q] = 0.0f;
     }
-    for (int start = range.x; start < range.y; start += kBatch) {
+    for (int start = range.x; start < range.y; start += BATCH) {
         bool all_done = true;
 #pragma unroll
         for (int i = 0; i < NPIX; ++i) all_done &= done[i];
         if (__syncthreads_count(all_done) == NT) break;
-        const int n = gather_small<C, NPIX, false>(start, 1, range.x, range.y, idx_sorted, uv, conic, opacity,
-                                                   feature, bx0, by0, sA, sB, sF, nullptr, sM, scan);
+        const int n = gather_small<C, NPIX, false, ROWS>(start, 1, range.x, range.y, idx_sorted, uv, conic,
+                                                         opacity, feature, bx0, by0, sA, sB, sF, nullptr, sM, scan);
         // Each warp walks, 32 entries at a time, only the entries whose row
         // mask has its bit (a warp-uniform bit set from one ballot), and
         // leaves the batch once all of its pixels are done.
@@ -636,8 +646,8 @@ constexpr int kFewLanes = MSPLAT_FEW_LANES;
 
 // BG: the background is nonzero, so dL/dalpha has the term
 // -T_final / (1 - alpha) * sum_c bg dL/dpix_c (compiled out for bg == 0).
-template <int C, int NPIX, bool BG>
-__global__ void MSPLAT_BWD_BOUNDS(kTilePixels / NPIX)
+template <int C, int NPIX, bool BG, int SPLIT>
+__global__ void MSPLAT_BWD_BOUNDS(kTilePixels / NPIX / SPLIT)
 blend_bwd_small_kernel(int P, const float2 *__restrict__ uv, const float *__restrict__ conic,
                        const float *__restrict__ opacity, const float *__restrict__ feature,
                        const int32_t *__restrict__ idx_sorted, const int2 *__restrict__ tile_range, float bg,
@@ -645,22 +655,25 @@ blend_bwd_small_kernel(int P, const float2 *__restrict__ uv, const float *__rest
                        const float *__restrict__ dL_dout, float *__restrict__ dL_duv,
                        float *__restrict__ dL_dconic, float *__restrict__ dL_dopacity,
                        float *__restrict__ dL_dfeature) {
-    constexpr int NT = kTilePixels / NPIX;
+    constexpr int ROWS = kTile / SPLIT, NT = kTile * ROWS / NPIX, BATCH = NT * NPIX;
+    static_assert(4 * NPIX <= ROWS, "a warp block of 4 NPIX rows must fit the block's rows");
     constexpr int NV = 6 + C;
-    __shared__ float4 sA[kBatch], sB[kBatch], sF[kBatch];
-    __shared__ int sG[kBatch];
-    __shared__ unsigned char sM[kBatch];
+    __shared__ float4 sA[BATCH], sB[BATCH], sF[BATCH];
+    __shared__ int sG[BATCH];
+    __shared__ unsigned char sM[BATCH];
     __shared__ int scan[NT / 32];
     __shared__ int smax;
     const int gxn = (W + kTile - 1) / kTile;
-    const int2 range = tile_range[blockIdx.y * gxn + blockIdx.x];
-    // pixel layout and warp blocks as in blend_fwd_small_kernel
+    const int ty = blockIdx.y / SPLIT;
+    const int2 range = tile_range[ty * gxn + blockIdx.x];
+    // pixel layout, warp blocks and SPLIT as in blend_fwd_small_kernel
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int row0 = ty * kTile + (blockIdx.y % SPLIT) * ROWS;
     const int px = blockIdx.x * kTile + 8 * (warp & 1) + (lane & 7);
-    const int py0 = blockIdx.y * kTile + 4 * NPIX * (warp >> 1) + (lane >> 3) * NPIX;
+    const int py0 = row0 + 4 * NPIX * (warp >> 1) + (lane >> 3) * NPIX;
     const unsigned wbit = 1u << warp;
     const float fx = (float)px;
-    const float bx0 = (float)(blockIdx.x * kTile), by0 = (float)(blockIdx.y * kTile);
+    const float bx0 = (float)(blockIdx.x * kTile), by0 = (float)row0;
     const int vi = scatter_slot<NV>(lane);  // the gradient slot this lane sends after a reduction
 
     // Per pixel: the colour recursion of the reference (accum_rec =
@@ -702,10 +715,10 @@ blend_bwd_small_kernel(int P, const float2 *__restrict__ uv, const float *__rest
     // Entries at or past this warp's largest ncontrib touch none of its pixels.
     const int warp_last = mylast;
 
-    for (int bend = end; bend > range.x; bend -= kBatch) {
-        const int bstart = max(range.x, bend - kBatch);
-        const int n = gather_small<C, NPIX, true>(bend - 1, -1, bstart, bend, idx_sorted, uv, conic, opacity,
-                                                  feature, bx0, by0, sA, sB, sF, sG, sM, scan);
+    for (int bend = end; bend > range.x; bend -= BATCH) {
+        const int bstart = max(range.x, bend - BATCH);
+        const int n = gather_small<C, NPIX, true, ROWS>(bend - 1, -1, bstart, bend, idx_sorted, uv, conic,
+                                                        opacity, feature, bx0, by0, sA, sB, sF, sG, sM, scan);
         // Each warp walks only the entries that reach its rows and precede
         // its largest ncontrib (a warp-uniform bit set per 32 entries).
         for (int kw = 0; kw < n; kw += 32) {
@@ -830,20 +843,31 @@ blend_grad_finish_kernel(int P, const float *__restrict__ conic, const float *__
 #endif
 constexpr int kBlendNpixFwd = MSPLAT_BLEND_NPIX_FWD;
 constexpr int kBlendNpixBwd = MSPLAT_BLEND_NPIX_BWD;
+// Blocks per tile of the C <= 4 kernels (1 or 2: whole tiles, or halves of
+// 8 rows with their own gather, cull and end; compile-time tunables).
+#ifndef MSPLAT_BLEND_SPLIT_FWD
+#define MSPLAT_BLEND_SPLIT_FWD 1
+#endif
+#ifndef MSPLAT_BLEND_SPLIT_BWD
+#define MSPLAT_BLEND_SPLIT_BWD 1
+#endif
+constexpr int kSplitFwd = MSPLAT_BLEND_SPLIT_FWD, kSplitBwd = MSPLAT_BLEND_SPLIT_BWD;
 
 template <int C>
 void launch_small(bool bwd, dim3 grid, cudaStream_t stream, int P, const float2 *uv, const float *conic,
                   const float *opacity, const float *feature, const int32_t *idx, const int2 *tr, float bg, int W,
                   int H, float *out, float *final_T, int32_t *nc, const float *fT, const int32_t *nci,
                   const float *dout, float *duv, float *dcon, float *dop, float *dfeat) {
+    const dim3 gf(grid.x, grid.y * kSplitFwd), gb(grid.x, grid.y * kSplitBwd);
+    constexpr int tf = kTilePixels / kBlendNpixFwd / kSplitFwd, tb = kTilePixels / kBlendNpixBwd / kSplitBwd;
     if (!bwd)
-        launch(blend_fwd_small_kernel<C, kBlendNpixFwd>, grid, kTilePixels / kBlendNpixFwd, 0, stream,
+        launch(blend_fwd_small_kernel<C, kBlendNpixFwd, kSplitFwd>, gf, tf, 0, stream,
             P, uv, conic, opacity, feature, idx, tr, bg, W, H, out, final_T, nc);
     else if (bg != 0.0f)
-        launch(blend_bwd_small_kernel<C, kBlendNpixBwd, true>, grid, kTilePixels / kBlendNpixBwd, 0, stream,
+        launch(blend_bwd_small_kernel<C, kBlendNpixBwd, true, kSplitBwd>, gb, tb, 0, stream,
             P, uv, conic, opacity, feature, idx, tr, bg, W, H, fT, nci, dout, duv, dcon, dop, dfeat);
     else
-        launch(blend_bwd_small_kernel<C, kBlendNpixBwd, false>, grid, kTilePixels / kBlendNpixBwd, 0, stream,
+        launch(blend_bwd_small_kernel<C, kBlendNpixBwd, false, kSplitBwd>, gb, tb, 0, stream,
             P, uv, conic, opacity, feature, idx, tr, bg, W, H, fT, nci, dout, duv, dcon, dop, dfeat);
 }
 

@@ -452,7 +452,9 @@ def test_blend_row_cull_keeps_every_contribution():
 def check_culled_lists(uv, depth, radius, tiles, conic, op, feat, W, H):
     """sort_gaussian(cull=...) against the exact lists: per tile a
     subsequence (same order) of the exact list, and the same blended image
-    bit for bit; gradients agree to float-atomic order."""
+    bit for bit; gradients agree to float-atomic order (the gradient bar,
+    1e-4 of the largest: the uv gradients are sums of opposite moments, and
+    with two blocks per tile their atomics arrive in a different order)."""
     args = [T(uv), T(depth), W, H, T(radius), T(tiles)]
     idx, tr = ms.sort_gaussian(*args)
     cidx, ctr = ms.sort_gaussian(*args, cull=(T(conic), T(op)))
@@ -471,7 +473,7 @@ def check_culled_lists(uv, depth, radius, tiles, conic, op, feat, W, H):
         res.append((N(img), [N(x.grad) for x in p]))
     np.testing.assert_array_equal(res[0][0], res[1][0])
     for a, b, what in zip(res[0][1], res[1][1], ("uv", "conic", "opacity", "feature")):
-        rel_close(b, a, rtol=1e-5, what=f"dL/d{what}")
+        rel_close(b, a, rtol=1e-4, what=f"dL/d{what}")
     return idx.size, cidx.size
 
 
