@@ -413,7 +413,12 @@ __device__ __forceinline__ PixPow<NPIX> blend_power_n(float a, float b, float c,
 // memory in list order, with the mask of the warp blocks (8 columns by
 // 4 NPIX rows, one per warp) each one can reach.  The block renders the
 // ROWS rows from by0 of the tile, which is also the box of the cull.
-// Returns the number kept.
+// Returns the number kept, or -1 (nothing written) when every thread's
+// `vote` is set.
+// Its first barrier is the only one between two batches: shared records
+// are written after it, and every warp reaches it only once done with the
+// previous batch, so a warp that finishes a batch early issues the next
+// batch's loads and cull tests while the others still blend.
 template <int C, int NPIX, bool WITH_ID, int ROWS = kTile>
 __device__ __forceinline__ int gather_small(int base, int dir, int lo, int hi,
                                             const int32_t *__restrict__ idx_sorted,
@@ -421,7 +426,7 @@ __device__ __forceinline__ int gather_small(int base, int dir, int lo, int hi,
                                             const float *__restrict__ opacity,
                                             const float *__restrict__ feature, float bx0, float by0,
                                             float4 *sA, float4 *sB, float4 *sF, int *sG, unsigned char *sM,
-                                            int *scan) {
+                                            int *scan, bool vote) {
     constexpr int NT = kTile * ROWS / NPIX;
     float4 A[NPIX], B[NPIX], F[NPIX];
     int G[NPIX];
@@ -460,7 +465,7 @@ __device__ __forceinline__ int gather_small(int base, int dir, int lo, int hi,
         if (lane >= o) inc += n;
     }
     if (lane == 31) scan[warp] = inc;
-    __syncthreads();
+    if (__syncthreads_count(vote) == NT) return -1;
     int wbase = 0, total = 0;
 #pragma unroll
     for (int w = 0; w < NT / 32; ++w) {
@@ -529,9 +534,10 @@ blend_fwd_small_kernel(int P, const float2 *__restrict__ uv, const float *__rest
         bool all_done = true;
 #pragma unroll
         for (int i = 0; i < NPIX; ++i) all_done &= done[i];
-        if (__syncthreads_count(all_done) == NT) break;
         const int n = gather_small<C, NPIX, false, ROWS>(start, 1, range.x, range.y, idx_sorted, uv, conic,
-                                                         opacity, feature, bx0, by0, sA, sB, sF, nullptr, sM, scan);
+                                                         opacity, feature, bx0, by0, sA, sB, sF, nullptr, sM, scan,
+                                                         all_done);
+        if (n < 0) break;  // every pixel of the block is done
         // Each warp walks, 32 entries at a time, only the entries whose row
         // mask has its bit (a warp-uniform bit set from one ballot), and
         // leaves the batch once all of its pixels are done.
@@ -718,7 +724,8 @@ blend_bwd_small_kernel(int P, const float2 *__restrict__ uv, const float *__rest
     for (int bend = end; bend > range.x; bend -= BATCH) {
         const int bstart = max(range.x, bend - BATCH);
         const int n = gather_small<C, NPIX, true, ROWS>(bend - 1, -1, bstart, bend, idx_sorted, uv, conic,
-                                                        opacity, feature, bx0, by0, sA, sB, sF, sG, sM, scan);
+                                                        opacity, feature, bx0, by0, sA, sB, sF, sG, sM, scan,
+                                                        false);
         // Each warp walks only the entries that reach its rows and precede
         // its largest ncontrib (a warp-uniform bit set per 32 entries).
         for (int kw = 0; kw < n; kw += 32) {
@@ -808,7 +815,7 @@ blend_bwd_small_kernel(int P, const float2 *__restrict__ uv, const float *__rest
             }
           }
         }
-        __syncthreads();
+        // no barrier here: the next gather's first barrier orders the batches
     }
 }
 
