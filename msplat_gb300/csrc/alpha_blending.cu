@@ -21,7 +21,10 @@
 //  * backward starts at the tile's largest ncontrib instead of the end of
 //    the list, and per-Gaussian gradients are summed over each warp with a
 //    reduce-scatter of shuffles before one atomic per value per warp (the
-//    reference issues C + 6 atomics per pixel-Gaussian pair).
+//    reference issues C + 6 atomics per pixel-Gaussian pair);
+//  * in the C <= 4 kernels each warp owns an 8-column block of the tile and
+//    walks only the gathered Gaussians whose alpha >= 1/255 ellipse reaches
+//    that block (a conservative per-Gaussian mask built in the gather).
 #include "cull.cuh"
 
 namespace msplat {
