@@ -70,28 +70,72 @@ __device__ __forceinline__ bool cull_tile(float gx, float gy, float a, float b, 
     return cull_tile(gx, gy, a, b, c, op, bx0, by0, L);
 }
 
-// Shrinks a Gaussian's tile rectangle [x0, x1) x [y0, y1) (tile units)
-// from each side while the whole outer row or column is ruled out by
-// cull_box; an empty result has x0 == x1 and y0 == y1.  Every dropped tile
-// is one no pixel of which the Gaussian reaches.  Each loop is bounded by
-// the rectangle's size.
+// Shrinks a Gaussian's tile rectangle [x0, x1) x [y0, y1) (tile units) to
+// the rows and columns its alpha >= 1/255 ellipse reaches; an empty result
+// has x0 == x1 and y0 == y1.  The cut is proposed from the ellipse's
+// bounding box (half-extents sqrt(tau a / det) and sqrt(tau c / det),
+// widened by 0.2 % + 0.05 px) and a side is cut only if cull_box rules out
+// the whole strip cut off, so every dropped tile is one no pixel of which
+// the Gaussian reaches; if it does not, the strip one tile narrower is
+// tried, and failing that the side stays (the rectangle stays
+// conservative, only less tight).  At most eight box tests per Gaussian,
+// usually four; none where the box proposes no cut.
 __device__ __forceinline__ void shrink_rect(float gx, float gy, float a, float b, float c, float op, int &x0,
                                             int &y0, int &x1, int &y1) {
     constexpr float T = (float)kTile;
+    if (x0 >= x1 || y0 >= y1) return;
     float L;
-    while (y0 < y1 && cull_box(gx, gy, a, b, c, op, x0 * T, y0 * T, x1 * T - 1.0f, y0 * T + (T - 1.0f), L)) ++y0;
-    while (y1 > y0 && cull_box(gx, gy, a, b, c, op, x0 * T, (y1 - 1) * T, x1 * T - 1.0f, y1 * T - 1.0f, L)) --y1;
-    if (y0 >= y1) {
-        x1 = x0;
-        y1 = y0;
+    if (!(op > 0.0f)) {  // op <= 0 reaches nothing; NaN keeps everything
+        if (op <= 0.0f) {
+            x1 = x0;
+            y1 = y0;
+        }
         return;
     }
-    while (x0 < x1 && cull_box(gx, gy, a, b, c, op, x0 * T, y0 * T, x0 * T + (T - 1.0f), y1 * T - 1.0f, L)) ++x0;
-    while (x1 > x0 && cull_box(gx, gy, a, b, c, op, (x1 - 1) * T, y0 * T, x1 * T - 1.0f, y1 * T - 1.0f, L)) --x1;
-    if (x0 >= x1) {
-        x1 = x0;
-        y1 = y0;
+    const float tau = 2.0f * logf(255.0f * op);
+    const float det = a * c - b * b;
+    if (!(a > 0.0f) || !(c > 0.0f) || !(det > 0.0f)) return;
+    if (!(tau > 0.0f)) {  // the ellipse is (nearly) empty: try the whole rectangle
+        if (cull_box(gx, gy, a, b, c, op, x0 * T, y0 * T, x1 * T - 1.0f, y1 * T - 1.0f, L)) {
+            x1 = x0;
+            y1 = y0;
+        }
+        return;
     }
+    const float ey = 1.002f * sqrtf(tau * a / det) + 0.05f, ex = 1.002f * sqrtf(tau * c / det) + 0.05f;
+    // proposed tile range: tiles whose pixel rows / columns meet [g - e, g + e]
+    const float fy0 = floorf((gy - ey) / T), fy1 = floorf((gy + ey) / T) + 1.0f;
+    const float fx0 = floorf((gx - ex) / T), fx1 = floorf((gx + ex) / T) + 1.0f;
+    if (!(fy0 == fy0) || !(fx0 == fx0) || !(fy1 == fy1) || !(fx1 == fx1)) return;  // NaN
+    const int py0 = (int)fmaxf(fy0, (float)y0), py1 = (int)fminf(fy1, (float)y1);
+    const int px0 = (int)fmaxf(fx0, (float)x0), px1 = (int)fminf(fx1, (float)x1);
+    if (py0 >= py1 || px0 >= px1) {  // the box misses the rectangle: try all of it
+        if (cull_box(gx, gy, a, b, c, op, x0 * T, y0 * T, x1 * T - 1.0f, y1 * T - 1.0f, L)) {
+            x1 = x0;
+            y1 = y0;
+        }
+        return;
+    }
+    for (int k = py0; k > y0 && k >= py0 - 1; --k)
+        if (cull_box(gx, gy, a, b, c, op, x0 * T, y0 * T, x1 * T - 1.0f, k * T - 1.0f, L)) {
+            y0 = k;
+            break;
+        }
+    for (int k = py1; k < y1 && k <= py1 + 1; ++k)
+        if (cull_box(gx, gy, a, b, c, op, x0 * T, k * T, x1 * T - 1.0f, y1 * T - 1.0f, L)) {
+            y1 = k;
+            break;
+        }
+    for (int k = px0; k > x0 && k >= px0 - 1; --k)
+        if (cull_box(gx, gy, a, b, c, op, x0 * T, y0 * T, k * T - 1.0f, y1 * T - 1.0f, L)) {
+            x0 = k;
+            break;
+        }
+    for (int k = px1; k < x1 && k <= px1 + 1; ++k)
+        if (cull_box(gx, gy, a, b, c, op, k * T, y0 * T, x1 * T - 1.0f, y1 * T - 1.0f, L)) {
+            x1 = k;
+            break;
+        }
 }
 
 }  // namespace msplat
