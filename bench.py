@@ -248,8 +248,8 @@ def blend_pairs(ms, p, color_dim=3):
 # DRAM bytes per launch (read + write) of the blend kernels at the benchmark
 # size over the fused calls' culled lists, from one ncu capture of the timed
 # frame (profiles/dram_traffic_1M_1080p.md).
-NCU_TRAFFIC_1M_1080P = {"alpha_blending_backward": 96.54e6 + 1.49e6,
-                        "alpha_blending_forward": 38.58e6 + 6.17e6}
+NCU_TRAFFIC_1M_1080P = {"alpha_blending_backward": 96.13e6 + 1.27e6,
+                        "alpha_blending_forward": 44.59e6 + 9.15e6}
 
 
 def roofline(stages, steps, pairs, inter, nvis, sm_mhz, peaks, peak_kind):
