@@ -485,6 +485,9 @@ def test_culled_lists_blend_like_the_exact_lists():
     uv, conic, op, feat, _, _, (depth, radius, tiles) = elongated_2d(5000, W, H, seed=7)
     depth = depth.copy()
     depth[::20] *= -1.0  # negative-depth emitters: first in the exact list, in no range, dropped when culled
+    op = op.copy()
+    op[3::50] = 0.002  # below 1/255: reaches no pixel (the whole rectangle is tested)
+    op[7::97] = 0.0
     n_full, n_cull = check_culled_lists(uv, depth, radius, tiles, conic, op, feat, W, H)
     assert n_cull < 0.95 * n_full
     for seed in (1, 2):
