@@ -80,6 +80,24 @@ def coordinate_descent(space: dict, start: dict, objective, rounds: int = 2):
     return best, best_v, {k: v for k, v in seen.items()}
 
 
+def make_objective(build_variant, time_library, log=print):
+    """objective(setting) -> ms for coordinate_descent: builds the variant
+    with build_variant(setting) -> library path and times it with
+    time_library(path) -> ms.  A setting whose build fails (a combination
+    the kernels reject at compile time) scores infinity instead of ending
+    the search."""
+    def objective(setting):
+        try:
+            lib = build_variant(setting)
+        except RuntimeError as e:
+            log(f"{setting} -> does not build ({str(e).splitlines()[0][:120] if str(e) else 'error'})")
+            return float("inf")
+        ms = time_library(lib)
+        log(f"{setting} -> {ms:.4f} ms")
+        return ms
+    return objective
+
+
 def variant_library(defines: dict) -> str:
     """Builds (once) the library with `defines` into its own directory."""
     tag = hashlib.sha1(json.dumps(sorted(defines.items())).encode()).hexdigest()[:12]
@@ -146,15 +164,9 @@ def main() -> None:
         print(_time_here(a.gaussians, a.width, a.height, a.steps, a.warmup))
         return
 
-    def objective(setting):
-        try:
-            lib = variant_library(setting)
-        except RuntimeError as e:  # a combination the kernels reject at compile time
-            print(f"{setting} -> does not build ({str(e).splitlines()[0][:120]})", flush=True)
-            return float("inf")
-        ms = time_variant(lib, a.gaussians, a.width, a.height, a.steps, a.warmup)
-        print(f"{setting} -> {ms:.4f} ms", flush=True)
-        return ms
+    objective = make_objective(
+        variant_library, lambda lib: time_variant(lib, a.gaussians, a.width, a.height, a.steps, a.warmup),
+        log=lambda msg: print(msg, flush=True))
 
     start = dict(DEFAULTS, **{k: v for k, v in _build.tuned_defines().items() if k in SPACE})
     space = SPACE

@@ -31,3 +31,29 @@ def test_build_reads_the_tuning_file(tmp_path):
     assert d == {"MSPLAT_FEW_LANES": 16, "MSPLAT_SORT_ITEMS": 8}
     assert _build.define_flags(d) == ["-DMSPLAT_FEW_LANES=16", "-DMSPLAT_SORT_ITEMS=8"]
     assert _build.tuned_defines(str(tmp_path / "absent.json")) == {}
+
+
+def test_settings_that_do_not_build_score_infinity():
+    logs = []
+
+    def build(setting):
+        if setting["b"] == 16:
+            raise RuntimeError("nvcc failed for alpha_blending.cu:\nstatic assertion failed")
+        return f"lib-{setting['a']}-{setting['b']}"
+
+    def time_lib(lib):
+        a, b = (int(x) for x in lib.split("-")[1:])
+        return abs(a - 2) + abs(b - 16) * 0.1
+
+    objective = autotune.make_objective(build, time_lib, log=logs.append)
+    assert objective({"a": 2, "b": 16}) == float("inf")
+    best, v, seen = autotune.coordinate_descent({"a": [1, 2, 3], "b": [8, 12, 16]}, {"a": 1, "b": 8},
+                                                objective, rounds=2)
+    assert best == {"a": 2, "b": 12} and abs(v - 0.4) < 1e-12
+    assert any("does not build" in m for m in logs)
+
+
+def test_every_space_value_builds_a_distinct_define_set():
+    for name, values in autotune.SPACE.items():
+        flags = {tuple(_build.define_flags(dict(autotune.DEFAULTS, **{name: v}))) for v in values}
+        assert len(flags) == len(values), name
