@@ -57,6 +57,8 @@ def make_scene(seed: int = 0):
 
 
 PARAMS = ["xyz", "scale", "rot", "opacity", "shs", "intr", "extr"]
+DATA_DESC = ("synthetic (seeded: xyz U[-1,1]^3, scales exp U[-5,-3], normalised N(0,1) quaternions, "
+             "sigmoid N(0,1) opacity, N(0,0.3) SH coefficients")
 
 
 def view_dirs(xyz, extr):
@@ -489,7 +491,7 @@ def _finish(args, rank, world, ms, p, stages, clk, ms_step, e2e_ms, h2d, extra):
         "scaling": "weak",
         "vs_baseline": None,
         "dtype": "f32",
-        "data": "synthetic (seeded; config distributions, random look-at camera on a radius-4 sphere)",
+        "data": DATA_DESC + "; random look-at camera on a radius-4 sphere)",
         "config": {"workload": WORKLOAD,
                    "n_gaussians": N_GAUSS, "width": W_IMG, "height": H_IMG, "sh_degree": SH_DEG,
                    "focal": FOCAL, "intersections": inter, "visible_gaussians": nvis, "blend_pairs": pairs,
@@ -595,7 +597,7 @@ def run_reference(args):
         "impl": "reference", "metric": METRIC, "value": ms_frame, "unit": "ms/frame", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_frame, "higher_is_better": False,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-        "data": "synthetic (seeded; config distributions, random look-at camera on a radius-4 sphere)",
+        "data": DATA_DESC + "; random look-at camera on a radius-4 sphere)",
         "config": {"workload": WORKLOAD, "n_gaussians": N_GAUSS, "width": W_IMG, "height": H_IMG,
                    "sh_degree": SH_DEG, "focal": FOCAL},
         "cpu_baseline": base,
@@ -608,7 +610,7 @@ BATCH_SIZES = [(256, 256), (512, 512), (1280, 720), (1920, 1080)]
 
 
 def batch_scene(n, n_cams, seed=0):
-    """One scene with the config-0 distributions (SH degree 3, N(0, 0.3)
+    """One scene with the synthetic distributions of `make_scene` (SH degree 3, N(0, 0.3)
     coefficients) and n_cams sphere cameras, resolutions drawn uniformly
     from BATCH_SIZES, focal length keeping the 1080p field of view."""
     g = torch.Generator().manual_seed(seed)
@@ -639,7 +641,7 @@ def batch_scene(n, n_cams, seed=0):
 
 
 def run_batch(args, device):
-    """Config 3: 64 cameras of one 2M-Gaussian scene, fwd+bwd, through one
+    """Multi-camera batch: 64 cameras of one 2M-Gaussian scene, fwd+bwd, through one
     rasterization_sh_batch call against 64 rasterization_sh calls."""
     import msplat_gb300 as ms
     n, n_cams = args.gaussians if args.gaussians != 1_000_000 else 2_000_000, args.cameras
@@ -694,7 +696,7 @@ def run_batch(args, device):
         "metric": "batched renders/s (fwd+bwd), 64 cameras of one 2M-Gaussian scene",
         "value": round(n_cams / (mb * 1e-3), 2), "unit": "renders/s", "n_gpus": 1, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(mb, 3), "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded; config distributions)",
+        "vs_baseline": None, "dtype": "f32", "data": DATA_DESC + "; sphere cameras)",
         "config": {"workload": f"{n} Gaussians, SH deg 3, {n_cams} sphere cameras at "
                                f"{sorted(set(sizes))}, fwd+bwd, loss sum_b sum(W_b*img_b)",
                    "cameras": n_cams, "n_gaussians": n,
@@ -712,8 +714,8 @@ SERVE_SIZES = [(512, 512), (1280, 720), (1920, 1080)]
 
 
 def serve_workload(rate, duration, seed=0, n_scenes=8):
-    """Config 4: n_scenes resident scenes, N log-uniform in [1e5, 3e6]
-    (config-0 distributions, SH degree 3); Poisson arrivals at `rate`
+    """Serving: n_scenes resident scenes, N log-uniform in [1e5, 3e6]
+    (the distributions of `make_scene`, SH degree 3); Poisson arrivals at `rate`
     requests/s for `duration` s, each a random sphere camera at one of
     SERVE_SIZES, 80 % forward-only, 20 % forward + backward."""
     from msplat_gb300.serve import Request
@@ -778,7 +780,7 @@ def run_serve(args):
         "metric": "served renders/s and p99 latency (continuous batching) vs one request at a time",
         "value": served["renders_per_s"], "unit": "renders/s", "n_gpus": 1, "steps": len(reqs), "warmup": 32,
         "ms_per_step": round(1e3 / served["renders_per_s"], 3), "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded; config distributions, Poisson arrivals)",
+        "vs_baseline": None, "dtype": "f32", "data": DATA_DESC + "; Poisson arrivals)",
         "config": {"workload": f"{len(scenes)} resident scenes (N = {sizes}), SH deg 3, Poisson {args.rate} req/s "
                                f"for {args.duration} s, sizes {SERVE_SIZES}, 80% fwd / 20% fwd+bwd, "
                                f"120 GB budget, {args.streams} streams, batches up to 16",

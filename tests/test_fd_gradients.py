@@ -11,7 +11,7 @@ tests and which alphas sit at the 0.99 clamp.  Those decisions make the
 loss piecewise smooth; the adjoint kernels differentiate the smooth piece
 that the forward selected, and so does the frozen float64 forward.
 
-Cases: the config-1 distributions at 2,000 Gaussians and 64x64 (focal
+Cases: the benchmark scene's distributions at 2,000 Gaussians and 64x64 (focal
 length scaled to keep the 1080p field of view), and a front-facing camera
 with larger Gaussians so that many pairs overlap.
 """
@@ -141,7 +141,7 @@ class Frozen64:
 
 def make_case(kind):
     W = H = 64
-    if kind == "config1":
+    if kind == "bench_scene":
         s = scene(2000, seed=11, C=3, sh_deg=SH_DEG)
         f = 1500.0 * W / 1920.0
         intr, extr = camera(W, H, f=f, seed=4)
@@ -158,7 +158,7 @@ def make_case(kind):
     return p, W, H, weights
 
 
-@pytest.mark.parametrize("kind", ["config1", "front_large"])
+@pytest.mark.parametrize("kind", ["bench_scene", "front_large"])
 def test_gradients_match_fp64_central_differences(kind):
     p, W, H, weights = make_case(kind)
     bg = 0.25

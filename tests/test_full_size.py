@@ -69,7 +69,7 @@ def view_dirs(xyz, extr):
     return d / d.norm(dim=-1, keepdim=True)
 
 
-def test_config1_every_stage_against_the_oracle():
+def test_1m_gaussians_1080p_every_stage_against_the_oracle():
     import msplat_gb300 as ms
     W, H, f = 1920, 1080, 1500.0
     s = big_scene(1_000_000, 0, 3, 0.3)
@@ -128,7 +128,7 @@ def test_config1_every_stage_against_the_oracle():
         rel_close(N(a.grad).reshape(ref.shape), ref, 1e-4, f"dL/d{name}")
 
 
-def test_config2_deg10_sh_and_36_channel_blend_properties():
+def test_2m_gaussians_1024px_deg10_sh_and_36_channel_blend_properties():
     import msplat_gb300 as ms
     W = H = 1024
     f = 800.0
