@@ -211,10 +211,11 @@ def measured_peaks():
 
 
 def fp32_peak_tflops(sm_mhz):
-    # 152 SMs x 128 FP32 lanes x 2 flop/FMA at the sampled SM clock (nominal
-    # rate; no measured FP32 peak exists for this machine).
+    # SMs x 128 FP32 lanes x 2 flop/FMA at the sampled SM clock (nominal
+    # rate; no measured FP32 peak exists for this GPU).
     mhz = sm_mhz or 2070.0
-    return 152 * 128 * 2 * mhz * 1e6 / 1e12
+    sms = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+    return sms * 128 * 2 * mhz * 1e6 / 1e12
 
 
 def blend_pairs(ms, p, color_dim=3):
@@ -248,8 +249,8 @@ def blend_pairs(ms, p, color_dim=3):
 
 
 # DRAM bytes per launch (read + write) of the blend kernels at the benchmark
-# size over the fused calls' culled lists, from one ncu capture of the timed
-# frame (profiles/dram_traffic_1M_1080p.md).
+# size over the fused calls' culled lists: a constant taken from an earlier
+# ncu capture, not measured by this run (reported with that label).
 NCU_TRAFFIC_1M_1080P = {"alpha_blending_backward": 96.13e6 + 1.27e6,
                         "alpha_blending_forward": 44.59e6 + 9.15e6}
 
@@ -275,8 +276,10 @@ def roofline(stages, steps, pairs, inter, nvis, sm_mhz, peaks, peak_kind):
             # the same kernel against the memory roof: DRAM bytes per launch
             # (ncu) over the live launch time
             gbs = traffic / (per_launch_ms * 1e-3) / 1e9
-            out["dram"] = {"achieved_gbs": round(gbs, 1), "peak_gbs": hbm, "frac": round(gbs / hbm, 4),
-                           "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum, one launch"}
+            out["traffic_source"] = ("constant from an earlier ncu capture of this kernel at this size "
+                                     "(dram__bytes_read.sum + dram__bytes_write.sum, one launch); not measured "
+                                     "in this run")
+            out["dram"] = {"achieved_gbs": round(gbs, 1), "peak_gbs": hbm, "frac": round(gbs / hbm, 4)}
         return name, out
     bytes_per = {
         "sort_gaussian_finish": inter * 52.0,
@@ -570,12 +573,17 @@ CPU_SAMPLE = ("one full fwd+bwd frame of the same scene on the CPU oracle (C res
               "blend forward and backward over 1920x1080, and every adjoint")
 
 
-def cpu_baseline(threads):
-    """One warm-up frame, then one timed frame."""
+def cpu_baseline(threads, frames=3):
+    """One warm-up frame, then the mean of `frames` timed frames."""
     scene = make_scene(0)
     cpu_frame(scene, threads)
-    ms_frame, used = cpu_frame(scene, threads)
-    return {"value": round(ms_frame, 1), "unit": "ms/frame", "cores": used, "kind": "port", "sample": CPU_SAMPLE}
+    times, used = [], 1
+    for _ in range(frames):
+        t, used = cpu_frame(scene, threads)
+        times.append(t)
+    return {"value": round(float(np.mean(times)), 1), "unit": "ms/frame", "cores": used, "kind": "port",
+            "sample": CPU_SAMPLE + f"; mean of {frames} frames after one warm-up frame",
+            "frames_ms": [round(t, 1) for t in times]}
 
 
 # ------------------------------------------------------------- reference arm

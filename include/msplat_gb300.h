@@ -178,7 +178,11 @@ MSPLAT_API int msplat_inclusive_scan_i32(int n, const int32_t *in, int32_t *out,
  * that overlap on the GPU (different streams, or different host threads
  * without ordering) race and give wrong sums; serialise them.  The first
  * call on each device looks up the array's device address (with that device
- * current); make that first call before any stream capture.  It never calls
+ * current); make that first call before any stream capture.  The address is
+ * cached for the life of the process: after cudaDeviceReset (or any reset of
+ * the device's primary context) the library's module is loaded anew and the
+ * cached address is stale, so do not call this entry point again in a
+ * process that reset the device it ran on.  It never calls
  * cudaMalloc / cudaFree or any allocating routine.                         */
 #define MSPLAT_SCAN_NOALLOC_MAX_N (64 * 1024 * 1024)
 MSPLAT_API int msplat_inclusive_scan_i32_noalloc(int n, const int32_t *in,

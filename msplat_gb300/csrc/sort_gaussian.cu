@@ -174,7 +174,7 @@ emit_kernel(int P, const uint32_t *__restrict__ order, const int64_t *__restrict
             const float2 *__restrict__ uv, const float *__restrict__ depth,
             const int32_t *__restrict__ radius, const short4 *__restrict__ rects, const int *__restrict__ culled,
             int gx, int gy, uint32_t *__restrict__ tkeys, uint32_t *__restrict__ tvals, int64_t cap) {
-    __shared__ int scratch[33];
+    __shared__ int64_t scratch[33];
     const int lane = threadIdx.x & 31;
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     int g = -1, x0 = 0, y0 = 0, x1 = 0, y1 = 0;
@@ -194,7 +194,9 @@ emit_kernel(int P, const uint32_t *__restrict__ order, const int64_t *__restrict
         }
     }
     const int w = x1 - x0, n = w * (y1 - y0);
-    const int start = (int)boff[blockIdx.x] + block_exclusive_scan<int>(n, scratch, nullptr);
+    // Offsets stay 64-bit: with a capacity-bounded finish the true count (and
+    // so boff) may pass 2^31 while only the first `cap` slots exist.
+    const int64_t start = boff[blockIdx.x] + block_exclusive_scan<int64_t>((int64_t)n, scratch, nullptr);
     unsigned todo = __ballot_sync(0xffffffffu, n > 0);
     while (todo) {
         const int sl = __ffs(todo) - 1;
@@ -202,10 +204,11 @@ emit_kernel(int P, const uint32_t *__restrict__ order, const int64_t *__restrict
         const int sg = __shfl_sync(0xffffffffu, g, sl);
         const int sx0 = __shfl_sync(0xffffffffu, x0, sl), sy0 = __shfl_sync(0xffffffffu, y0, sl);
         const int sw = __shfl_sync(0xffffffffu, w, sl), sn = __shfl_sync(0xffffffffu, n, sl);
-        const int sstart = __shfl_sync(0xffffffffu, start, sl);
+        const int64_t sstart = __shfl_sync(0xffffffffu, (long long)start, sl);
         const bool sneg = __shfl_sync(0xffffffffu, (int)neg, sl) != 0;
         const float inv = 1.0f / (float)sw;
-        const int kmax = (int)min((int64_t)sn, cap - (int64_t)sstart);  // capacity of the output
+        const int64_t room = cap - sstart;  // slots left in the output (may be <= 0)
+        const int kmax = room <= 0 ? 0 : (int)min((int64_t)sn, room);
         for (int k = lane; k < kmax; k += 32) {
             int ry = (int)(((float)k + 0.5f) * inv);  // k / sw, corrected below
             ry -= (ry * sw > k);

@@ -158,3 +158,44 @@ def test_captured_batch_replays_the_eager_batch():
     for k in static:
         got, ref = static[k].grad, eager[k].grad
         assert (got - ref).abs().max().item() <= 1e-5 * max(ref.abs().max().item(), 1e-30), k
+
+
+def test_capacity_finish_past_int32_counts_writes_nothing_out_of_bounds():
+    """600 Gaussians that each cover all 2048 x 2048 tiles of a 32768^2 image
+    give 600 * 2^22 (> 2^31) intersections; the third block of 256 Gaussians
+    starts exactly at 2^31.  With a capacity of 4096 the status is 1, only
+    the first Gaussian in depth order is emitted (its first 4096 tiles), and
+    the guard words around the output and the workspace stay untouched."""
+    from msplat_gb300 import _lib
+    lib = _lib.load()
+    W = H = 32768
+    P, cap, G = 600, 4096, 4096
+    nt = (W // 16) * (H // 16)
+    uv = torch.full((P, 2), 16384.0, device=DEV)
+    depth = torch.linspace(1.0, 2.0, P, device=DEV).reshape(P, 1).flip(0).contiguous()  # last id nearest
+    radius = torch.full((P,), 30000, dtype=torch.int32, device=DEV)
+    tiles = torch.full((P,), nt, dtype=torch.int32, device=DEV)
+    st = _lib.stream()
+    counts = torch.empty(2, dtype=torch.int64, device=DEV)
+    ws_prep = _lib.workspace(lib.msplat_sort_prepare_workspace_size(P, W, H), DEV)
+    _lib.check(lib.msplat_sort_gaussian_prepare(P, _lib.ptr(depth), _lib.ptr(radius), _lib.ptr(tiles), _lib.ptr(uv),
+                                                W, H, _lib.ptr(counts), _lib.ptr(ws_prep), ws_prep.numel(), st),
+               "prepare")
+    sentinel = -123456789
+    idx = torch.full((cap + 2 * G,), sentinel, dtype=torch.int32, device=DEV)
+    wsb = int(lib.msplat_sort_finish_workspace_size(P, cap, W, H))
+    ws = torch.full((wsb + 2 * 4 * G,), 0x5A, dtype=torch.uint8, device=DEV)
+    tr = torch.full((nt, 2), sentinel, dtype=torch.int32, device=DEV)
+    status = torch.zeros(1, dtype=torch.int32, device=DEV)
+    _lib.check(lib.msplat_sort_gaussian_finish_capacity(
+        P, _lib.ptr(uv), _lib.ptr(depth), _lib.ptr(radius), W, H, cap, _lib.ptr(counts), _lib.ptr(ws_prep),
+        idx.data_ptr() + 4 * G, _lib.ptr(tr), _lib.ptr(status), ws.data_ptr() + 4 * G, wsb, st), "finish_capacity")
+    torch.cuda.synchronize()
+    assert int(counts[0].item()) == P * nt > 2**31
+    assert int(status.item()) == 1
+    assert bool((idx[:G] == sentinel).all()) and bool((idx[G + cap:] == sentinel).all())
+    assert bool((ws[:4 * G] == 0x5A).all()) and bool((ws[4 * G + wsb:] == 0x5A).all())
+    assert bool((idx[G:G + cap] == P - 1).all())  # the nearest Gaussian's first 4096 tiles
+    t = torch.arange(cap, dtype=torch.int32, device=DEV)
+    assert torch.equal(tr[:cap], torch.stack([t, t + 1], 1))
+    assert bool((tr[cap:] == 0).all())

@@ -60,3 +60,19 @@ def test_no_alloc_scan_rejects_sizes_beyond_its_scratch(lib):
     st = lib.msplat_inclusive_scan_i32_noalloc(limit + 1, None, None, None, None)
     assert st == 4  # MSPLAT_ERR_CAPACITY, before any device work
     assert "exceeds the maximum" in lib.msplat_last_error().decode()
+
+
+def test_no_alloc_scan_at_tile_edges_and_at_its_maximum_size(lib):
+    """n = 0 (only the total is written), one full 4096-element tile, one
+    element past it, and MSPLAT_SCAN_NOALLOC_MAX_N, which fills every
+    partial-sum slot of the fixed array (a 256 MB input)."""
+    rng = np.random.default_rng(11)
+    limit = 64 * 1024 * 1024
+    for n in (0, 4096, 4097, limit):
+        x = torch.from_numpy(rng.integers(0, 4, size=n, dtype=np.int32)).cuda()
+        ref, ref_total = _scan_with_workspace(lib, x)
+        got, got_total = _scan_no_alloc(lib, x)
+        torch.cuda.synchronize()
+        assert torch.equal(got, ref), n
+        assert int(got_total.item()) == int(ref_total.item()) == int(x.long().sum().item()), n
+        del x, ref, got
