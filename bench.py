@@ -574,16 +574,21 @@ CPU_SAMPLE = ("one full fwd+bwd frame of the same scene on the CPU oracle (C res
 
 
 def cpu_baseline(threads, frames=3):
-    """One warm-up frame, then the mean of `frames` timed frames."""
-    scene = make_scene(0)
-    cpu_frame(scene, threads)
-    times, used = [], 1
-    for _ in range(frames):
-        t, used = cpu_frame(scene, threads)
-        times.append(t)
-    return {"value": round(float(np.mean(times)), 1), "unit": "ms/frame", "cores": used, "kind": "port",
-            "sample": CPU_SAMPLE + f"; mean of {frames} frames after one warm-up frame",
-            "frames_ms": [round(t, 1) for t in times]}
+    """The reference arm's measurement in a fresh process (the same code and
+    process state as `--impl reference`, so the two agree): one warm-up
+    frame, then the mean of `frames` timed frames."""
+    cmd = [sys.executable, os.path.abspath(__file__), "--impl", "reference", "--steps", str(frames), "--warmup", "1",
+           "--gaussians", str(N_GAUSS), "--width", str(W_IMG), "--height", str(H_IMG)]
+    env = dict(os.environ)
+    for k in ("RANK", "WORLD_SIZE", "LOCAL_RANK"):
+        env.pop(k, None)
+    r = subprocess.run(cmd, capture_output=True, text=True, env=env, timeout=1800)
+    if r.returncode != 0:
+        raise RuntimeError(f"cpu baseline failed: {r.stderr[-2000:]}")
+    line = json.loads(r.stdout.strip().splitlines()[-1])
+    base = dict(line["cpu_baseline"])
+    base["sample"] += f"; mean of {frames} frames after one warm-up frame, in a fresh process"
+    return base
 
 
 # ------------------------------------------------------------- reference arm
@@ -600,7 +605,8 @@ def run_reference(args):
         t, used = cpu_frame(scene, threads)
         times.append(t)
     ms_frame = round(float(np.mean(times)), 1)
-    base = {"value": ms_frame, "unit": "ms/frame", "cores": used, "kind": "port", "sample": CPU_SAMPLE}
+    base = {"value": ms_frame, "unit": "ms/frame", "cores": used, "kind": "port", "sample": CPU_SAMPLE,
+            "frames_ms": [round(t, 1) for t in times]}
     return {
         "impl": "reference", "metric": METRIC, "value": ms_frame, "unit": "ms/frame", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_frame, "higher_is_better": False,

@@ -44,6 +44,8 @@ def _load():
             "oracle_compute_cov3d_forward": (None, [i, _P, _P, _P, _P]),
             "oracle_compute_cov3d_backward": (None, [i, _P, _P, _P, _P, _P, _P]),
             "oracle_ewa_project_forward": (None, [i, _P, _P, _P, _P, _P, i, i, _P, _P, _P, _P, _P]),
+            "oracle_ewa_project_forward_alt": (
+                None, [i, _P, _P, _P, _P, _P, i, i, _P, _P, _P, _P, _P, _P, _P, _P]),
             "oracle_ewa_project_backward": (None, [i, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P]),
             "oracle_sh_basis": (None, [i, i, _P, _P, _P]),
             "oracle_compute_sh_forward": (i, [i, i, i, _P, _P, _P, _P]),
@@ -54,6 +56,10 @@ def _load():
                 None, [i, i, _P, _P, _P, _P, _P, _P, f, i, i, _P, _P, _P, _P]),
             "oracle_alpha_blending_backward": (
                 None, [i, i, _P, _P, _P, _P, _P, _P, f, i, i, _P, _P, _P, _P, _P, _P, _P]),
+            "oracle_alpha_blending_forward_guided": (
+                i64, [i, i, _P, _P, _P, _P, _P, _P, f, i, i, _P, _P, _P, _P, _P, _P, _P]),
+            "oracle_alpha_blending_backward_guided": (
+                None, [i, i, _P, _P, _P, _P, _P, _P, f, i, i, _P, _P, _P, _P, _P, _P, _P, _P]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(lib, name)
@@ -165,6 +171,57 @@ def ewa_project_forward(xyz, cov3d, intr, extr, uv, W, H, visible=None):
     return conic, radius, tiles, amb.astype(bool)
 
 
+def ewa_project_alternatives(xyz, cov3d, intr, extr, uv, W, H, visible=None):
+    """Two-branch EWA: the oracle's outcome (conic, radius, tiles) and, where
+    the radius is within rounding reach of another integer (or det of 0),
+    the other outcome a correct implementation can reach: radius_alt /
+    tiles_alt (-1: no alternative; radius_alt 0: invisible) and conic_alt
+    (the conic of a visible alternative)."""
+    xyz, cov = _a(xyz, np.float32), _a(cov3d, np.float32)
+    intr, extr, uv = _a(intr, np.float32), _a(extr, np.float32), _a(uv, np.float32)
+    P = xyz.shape[0]
+    vis = _mask(visible, P)
+    conic = np.zeros((P, 3), np.float32)
+    radius = np.zeros(P, np.int32)
+    tiles = np.zeros(P, np.int32)
+    amb = np.zeros(P, np.uint8)
+    ralt = np.zeros(P, np.int32)
+    talt = np.zeros(P, np.int32)
+    calt = np.zeros((P, 3), np.float32)
+    _load().oracle_ewa_project_forward_alt(P, _p(xyz), _p(cov), _p(intr), _p(extr), _p(uv), int(W), int(H),
+                                           _p(vis), _p(conic), _p(radius), _p(tiles), _p(amb), _p(ralt), _p(talt),
+                                           _p(calt))
+    return conic, radius, tiles, ralt, talt, calt
+
+
+def ewa_check_against(gpu_conic, gpu_radius, gpu_tiles, xyz, cov3d, intr, extr, uv, W, H, visible=None,
+                      conic_rtol=2e-5, conic_atol=1e-7):
+    """Holds a GPU EWA result to the two-branch oracle: every radius equals
+    the oracle's or its alternative rounding, tiles equal the rectangle of
+    the radius taken, and conics agree within the tolerances (exactly 0 for
+    invisible entries).  Returns (n_alternate, max conic error, the
+    oracle's radius / tiles / conic along the GPU's choices); raises
+    AssertionError on any other outcome."""
+    conic, radius, tiles, ralt, talt, calt = ewa_project_alternatives(xyz, cov3d, intr, extr, uv, W, H, visible)
+    gr = np.asarray(gpu_radius).reshape(-1).astype(np.int32)
+    gt = np.asarray(gpu_tiles).reshape(-1).astype(np.int32)
+    gc = np.asarray(gpu_conic, np.float32).reshape(-1, 3)
+    prim = (gr == radius) & (gt == tiles)
+    alt = ~prim & (ralt >= 0) & (gr == ralt) & (gt == talt)
+    bad = ~(prim | alt)
+    assert not bad.any(), (f"{int(bad.sum())} radius/tiles outcomes are neither the oracle's nor its alternative "
+                           f"rounding (first at {np.flatnonzero(bad)[:5].tolist()})")
+    sel_r = np.where(alt, ralt, radius).astype(np.int32)
+    sel_t = np.where(alt, talt, tiles).astype(np.int32)
+    sel_c = np.where(alt[:, None], calt, conic).astype(np.float32)
+    vis_sel = sel_r > 0
+    assert not gc[~vis_sel].any(), "conic of an invisible entry is not 0"
+    err = np.abs(gc[vis_sel].astype(np.float64) - sel_c[vis_sel])
+    lim = conic_rtol * np.abs(sel_c[vis_sel]).astype(np.float64) + conic_atol
+    assert (err <= lim).all(), f"conic beyond {conic_rtol} relative: max err {err.max():.3e}"
+    return int(alt.sum()), float(err.max()) if err.size else 0.0, (sel_r, sel_t, sel_c)
+
+
 def ewa_project_backward(xyz, cov3d, intr, extr, radius, dL_dconic):
     xyz, cov = _a(xyz, np.float32), _a(cov3d, np.float32)
     intr, extr = _a(intr, np.float32), _a(extr, np.float32)
@@ -242,8 +299,34 @@ def alpha_blending_forward(uv, conic, opacity, feature, idx_sorted, tile_range, 
     return out, T, nc, amb.astype(bool)
 
 
+def alpha_blending_forward_guided(uv, conic, opacity, feature, idx_sorted, tile_range, bg, W, H, gpu_T,
+                                  gpu_ncontrib):
+    """Guided (two-branch) replay of the forward blend: per pixel the path
+    whose decisions within rounding reach of a threshold (alpha vs 1/255,
+    T (1 - alpha) vs 1e-4) take the fewest alternate branches and whose
+    outcome matches the given (final T, ncontrib).  Returns the oracle's
+    own out, final_T, ncontrib along those paths, nflips [H, W] (alternate
+    branches taken per pixel; 255 = no such path within 3 flips), forces
+    (the alternate alpha decisions, for alpha_blending_backward) and the
+    number of unresolved pixels."""
+    uv, conic = _a(uv, np.float32), _a(conic, np.float32)
+    op, feat = _a(opacity, np.float32).reshape(-1), _a(feature, np.float32)
+    ids, tr = _a(idx_sorted, np.int32), _a(tile_range, np.int32)
+    gT, gnc = _a(gpu_T, np.float32).reshape(H, W), _a(gpu_ncontrib, np.int32).reshape(H, W)
+    P, C = feat.shape
+    out = np.zeros((C, H, W), np.float32)
+    T = np.zeros((H, W), np.float32)
+    nc = np.zeros((H, W), np.int32)
+    nfl = np.zeros((H, W), np.uint8)
+    forces = np.zeros((H, W, 3), np.int32)
+    unresolved = _load().oracle_alpha_blending_forward_guided(
+        P, C, _p(uv), _p(conic), _p(op), _p(feat), _p(ids), _p(tr), float(bg), int(W), int(H), _p(gT), _p(gnc),
+        _p(out), _p(T), _p(nc), _p(nfl), _p(forces))
+    return out, T, nc, nfl, forces, int(unresolved)
+
+
 def alpha_blending_backward(uv, conic, opacity, feature, idx_sorted, tile_range, bg, W, H, final_T, ncontrib,
-                            dL_dout):
+                            dL_dout, forces=None):
     uv, conic = _a(uv, np.float32), _a(conic, np.float32)
     op, feat = _a(opacity, np.float32).reshape(-1), _a(feature, np.float32)
     ids, tr = _a(idx_sorted, np.int32), _a(tile_range, np.int32)
@@ -253,9 +336,15 @@ def alpha_blending_backward(uv, conic, opacity, feature, idx_sorted, tile_range,
     dcon = np.zeros((P, 3))
     dop = np.zeros(P)
     dfeat = np.zeros((P, C))
-    _load().oracle_alpha_blending_backward(P, C, _p(uv), _p(conic), _p(op), _p(feat), _p(ids), _p(tr), float(bg),
-                                           int(W), int(H), _p(T), _p(nc), _p(g), _p(duv), _p(dcon), _p(dop),
-                                           _p(dfeat))
+    if forces is None:
+        _load().oracle_alpha_blending_backward(P, C, _p(uv), _p(conic), _p(op), _p(feat), _p(ids), _p(tr),
+                                               float(bg), int(W), int(H), _p(T), _p(nc), _p(g), _p(duv), _p(dcon),
+                                               _p(dop), _p(dfeat))
+    else:
+        f = _a(forces, np.int32)
+        _load().oracle_alpha_blending_backward_guided(P, C, _p(uv), _p(conic), _p(op), _p(feat), _p(ids), _p(tr),
+                                                      float(bg), int(W), int(H), _p(T), _p(nc), _p(g), _p(f),
+                                                      _p(duv), _p(dcon), _p(dop), _p(dfeat))
     return duv, dcon, dop, dfeat
 
 

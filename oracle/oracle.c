@@ -313,10 +313,20 @@ static void get_rect(float px, float py, int r, int gx, int gy, int *x0, int *y0
 
 /* msplat/src/ewa_project.cu:16-83.  ambiguous[i] = 1 where the radius (and
  * with it tiles) is within rounding reach of a different integer, given
- * that the GPU divides and takes square roots approximately. */
-void oracle_ewa_project_forward(int P, const float *xyz, const float *cov3d, const float *intr,
-                                const float *extr, const float *uv, int W, int H, const uint8_t *visible,
-                                float *conic, int32_t *radius, int32_t *tiles, uint8_t *ambiguous) {
+ * that the GPU divides and takes square roots approximately.
+ *
+ * Two-branch form: where ambiguous[i] is set, radius_alt[i] / tiles_alt[i]
+ * (when given) hold the other outcome a correct implementation can reach --
+ * ceil(3 sqrt(lambda)) one integer up or down (the side the value lies
+ * nearer to), with its rectangle; radius_alt = 0 means "invisible" (empty
+ * rectangle, or det within rounding reach of 0 and the primary visible).
+ * Elsewhere radius_alt = -1 (no alternative).  conic_alt [P,3] (when
+ * given) holds the conic of a visible alternative (zeros otherwise), which
+ * differs from conic[] only where the primary outcome is invisible. */
+void oracle_ewa_project_forward_alt(int P, const float *xyz, const float *cov3d, const float *intr,
+                                    const float *extr, const float *uv, int W, int H, const uint8_t *visible,
+                                    float *conic, int32_t *radius, int32_t *tiles, uint8_t *ambiguous,
+                                    int32_t *radius_alt, int32_t *tiles_alt, float *conic_alt) {
     const int gx = (W + TILE - 1) / TILE, gy = (H + TILE - 1) / TILE;
     const float fx = intr[0], fy = intr[1];
     PARFOR
@@ -325,6 +335,9 @@ void oracle_ewa_project_forward(int P, const float *xyz, const float *cov3d, con
         radius[i] = 0;
         tiles[i] = 0;
         if (ambiguous) ambiguous[i] = 0;
+        if (radius_alt) radius_alt[i] = -1;
+        if (tiles_alt) tiles_alt[i] = -1;
+        if (conic_alt) conic_alt[3 * i] = conic_alt[3 * i + 1] = conic_alt[3 * i + 2] = 0.f;
         if (visible && !visible[i]) continue;
         float t[3];
         cam_point(extr, xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2], t);
@@ -337,8 +350,11 @@ void oracle_ewa_project_forward(int P, const float *xyz, const float *cov3d, con
         const mat3f c2 = m3_mul(m3_mul(T, V), m3_t(T));
         const float a = c2.m[0][0] + 0.3f, b = c2.m[0][1], c = c2.m[1][1] + 0.3f;
         const float det = msub(a, c, b, b);
-        int amb = fabsf(det) <= 1e-5f * (fabsf(a * c) + b * b);
+        const int det_amb = fabsf(det) <= 1e-5f * (fabsf(a * c) + b * b);
+        int amb = det_amb;
         if (det == 0.0f) {
+            /* the GPU evaluates det with the same operations: an exact 0
+             * there too, so no alternative */
             if (ambiguous) ambiguous[i] = (uint8_t)amb;
             continue;
         }
@@ -347,18 +363,45 @@ void oracle_ewa_project_forward(int P, const float *xyz, const float *cov3d, con
         const float l1 = mid + disc, l2 = mid - disc;
         const float vr = 3.f * sqrtf(fmaxf(l1, l2));
         const float r = ceilf(vr);
-        if (fabsf(vr - rintf(vr)) <= 1e-4f * fmaxf(1.0f, vr)) amb = 1;
+        const int r_amb = fabsf(vr - rintf(vr)) <= 1e-4f * fmaxf(1.0f, vr);
+        if (r_amb) amb = 1;
         int x0, y0, x1, y1;
         get_rect(uv[2 * i], uv[2 * i + 1], (int)r, gx, gy, &x0, &y0, &x1, &y1);
         if (ambiguous) ambiguous[i] = (uint8_t)amb;
-        if ((x1 - x0) * (y1 - y0) == 0) continue;
+        const int n = (x1 - x0) * (y1 - y0);
+        if (r_amb && radius_alt) {
+            /* vr just above an integer k: ceil gives k + 1, the other k;
+             * just below (or at) k: ceil gives k, the other k + 1 */
+            const int ra = vr > rintf(vr) ? (int)r - 1 : (int)r + 1;
+            int ax0, ay0, ax1, ay1;
+            get_rect(uv[2 * i], uv[2 * i + 1], ra, gx, gy, &ax0, &ay0, &ax1, &ay1);
+            const int na = (ax1 - ax0) * (ay1 - ay0);
+            radius_alt[i] = na == 0 ? 0 : ra;
+            if (tiles_alt) tiles_alt[i] = na;
+        } else if (det_amb && radius_alt && n != 0) {
+            radius_alt[i] = 0;
+            if (tiles_alt) tiles_alt[i] = 0;
+        }
         const float inv = 1.f / det;
+        if (conic_alt && radius_alt && radius_alt[i] > 0) {
+            conic_alt[3 * i] = c * inv;
+            conic_alt[3 * i + 1] = -b * inv;
+            conic_alt[3 * i + 2] = a * inv;
+        }
+        if (n == 0) continue;
         conic[3 * i] = c * inv;
         conic[3 * i + 1] = -b * inv;
         conic[3 * i + 2] = a * inv;
         radius[i] = (int)r;
-        tiles[i] = (x1 - x0) * (y1 - y0);
+        tiles[i] = n;
     }
+}
+
+void oracle_ewa_project_forward(int P, const float *xyz, const float *cov3d, const float *intr,
+                                const float *extr, const float *uv, int W, int H, const uint8_t *visible,
+                                float *conic, int32_t *radius, int32_t *tiles, uint8_t *ambiguous) {
+    oracle_ewa_project_forward_alt(P, xyz, cov3d, intr, extr, uv, W, H, visible, conic, radius, tiles, ambiguous,
+                                   NULL, NULL, NULL);
 }
 
 /* msplat/src/ewa_project.cu:85-252, in double. */
@@ -773,13 +816,210 @@ void oracle_alpha_blending_forward(int P, int C, const float *uv, const float *c
     }
 }
 
+/* ------------------------------------------------- guided blend replay */
+/* The blend makes two threshold decisions per pair: skip when alpha < 1/255,
+ * stop when T (1 - alpha) < 1e-4.  The GPU (like the reference's fast-math
+ * build) evaluates exp approximately, within a few 1e-7 relative, so an
+ * alpha within BLEND_ALPHA_WIN (relative) of 1/255 can land on either side;
+ * T is a product of up to hundreds of (1 - alpha) factors, so a T (1 - alpha)
+ * within BLEND_T_WIN of 1e-4 can too.  Every other decision is fixed by the
+ * float operations, which the oracle reproduces.
+ *
+ * The guided replay takes a GPU's per-pixel outcome (final T, ncontrib) and
+ * finds, per pixel, the path through the list whose flagged decisions take
+ * the fewest alternate branches (at most GUIDE_MAX_DEPTH) and whose own
+ * outcome matches: the same ncontrib and a final T within BLEND_MATCH
+ * (relative).  Taking or skipping a pair changes T by a factor of at least
+ * 1 - 1/255 (0.4 %), so the match is unambiguous.  Where no such path
+ * exists the pixel is reported unresolved.  Nothing of the GPU's output is
+ * copied: the colour, T and ncontrib are the oracle's own along that path. */
+#define BLEND_ALPHA_WIN 2e-5f
+#define BLEND_T_WIN 1e-3f
+#define BLEND_MATCH 1e-3f
+#define GUIDE_MAX_DEPTH 3
+#define GUIDE_MAX_CAND 48
+#define GUIDE_MAX_RUNS 8192
+
+typedef struct {
+    int j;    /* list position */
+    int kind; /* 0: the alpha >= 1/255 test (take = blend), 1: the T < 1e-4 test (take = stop) */
+    int take;
+} Decision;
+
+typedef struct {
+    const float *uv, *conic, *opacity, *feature;
+    const int32_t *idx;
+    int s, e, C;
+    float px, py;
+} PixelList;
+
+static int forced(const Decision *f, int nf, int j, int kind, int dflt) {
+    for (int k = 0; k < nf; ++k)
+        if (f[k].j == j && f[k].kind == kind) return f[k].take;
+    return dflt;
+}
+
+/* One front-to-back pass over a pixel's list (msplat/src/alpha_blending.cu:
+ * 74-101) with the decisions in `force` replacing the IEEE ones; records the
+ * decisions within rounding reach (at most maxc) in cand. */
+static void blend_pixel_pass(const PixelList *L, const Decision *force, int nforce, float *F, float *T_out,
+                             int *last_out, Decision *cand, int *ncand, int maxc) {
+    float T = 1.0f;
+    int last = 0, nc = 0;
+    for (int c = 0; c < L->C; ++c) F[c] = 0;
+    for (int j = L->s; j < L->e; ++j) {
+        const int g = L->idx[j];
+        const float dx = L->uv[2 * g] - L->px, dy = L->uv[2 * g + 1] - L->py;
+        const float pw = blend_power(L->conic[3 * g], L->conic[3 * g + 1], L->conic[3 * g + 2], dx, dy);
+        if (pw > 0.0f) continue;
+        const float alpha = fminf(0.99f, L->opacity[g] * (float)exp((double)pw));
+        int take = !(alpha < 1.0f / 255.0f);
+        if (fabsf(alpha - 1.0f / 255.0f) <= BLEND_ALPHA_WIN * (1.0f / 255.0f)) {
+            if (nc < maxc) cand[nc] = (Decision){j, 0, take};
+            ++nc;
+        }
+        take = forced(force, nforce, j, 0, take);
+        if (!take) continue;
+        const float nT = T * (1.0f - alpha);
+        int stop = nT < 0.0001f;
+        if (fabsf(nT - 0.0001f) <= BLEND_T_WIN * 0.0001f) {
+            if (nc < maxc) cand[nc] = (Decision){j, 1, stop};
+            ++nc;
+        }
+        stop = forced(force, nforce, j, 1, stop);
+        if (stop) break;
+        for (int c = 0; c < L->C; ++c) F[c] += L->feature[(size_t)g * L->C + c] * alpha * T;
+        T = nT;
+        last = j - L->s + 1;
+    }
+    *T_out = T;
+    *last_out = last;
+    *ncand = nc < maxc ? nc : maxc;
+}
+
+static int outcome_matches(float T, int last, float gT, int gnc) {
+    return last == gnc && fabsf(T - gT) <= BLEND_MATCH * fmaxf(fabsf(T), fabsf(gT));
+}
+
+typedef struct {
+    const PixelList *L;
+    float gT;
+    int gnc;
+    float *F;
+    int runs;
+    int found;
+    float best_err;
+    int best_n;
+    Decision best[GUIDE_MAX_DEPTH];
+} GuideSearch;
+
+/* Depth-first over flips of flagged decisions after position (j0, kind0),
+ * `left` more flips allowed; keeps the matching path with the smallest
+ * |T - gT| among those with exactly `left` + nf flips. */
+static void guide_dfs(GuideSearch *S, Decision *path, int nf, const Decision *cand, int ncand, int left) {
+    for (int k = 0; k < ncand && S->runs < GUIDE_MAX_RUNS; ++k) {
+        const Decision c = cand[k];
+        if (nf > 0) {
+            const Decision p = path[nf - 1];
+            if (c.j < p.j || (c.j == p.j && c.kind <= p.kind)) continue;
+        }
+        path[nf] = (Decision){c.j, c.kind, !c.take};
+        float T;
+        int last, nc2;
+        Decision cand2[GUIDE_MAX_CAND];
+        blend_pixel_pass(S->L, path, nf + 1, S->F, &T, &last, cand2, &nc2, GUIDE_MAX_CAND);
+        S->runs++;
+        if (left == 1) {
+            if (outcome_matches(T, last, S->gT, S->gnc)) {
+                const float err = fabsf(T - S->gT);
+                if (!S->found || err < S->best_err) {
+                    S->found = 1;
+                    S->best_err = err;
+                    S->best_n = nf + 1;
+                    for (int q = 0; q <= nf; ++q) S->best[q] = path[q];
+                }
+            }
+        } else {
+            guide_dfs(S, path, nf + 1, cand2, nc2, left - 1);
+        }
+    }
+}
+
+/* Guided replay of msplat/src/alpha_blending.cu:16-110 (see above).
+ * gpu_T / gpu_ncontrib: the outcome to follow.  Writes the oracle's own out,
+ * final_T, ncontrib along the chosen path; nflips[pix] = number of alternate
+ * branches taken (0 on the IEEE path), 255 when unresolved; forces[3 pix + k]
+ * (k < 3) = the alternate alpha decisions taken, packed j * 2 + take, -1 for
+ * none (for oracle_alpha_blending_backward_guided).  Returns the number of
+ * unresolved pixels. */
+int64_t oracle_alpha_blending_forward_guided(int P, int C, const float *uv, const float *conic,
+                                             const float *opacity, const float *feature, const int32_t *idx_sorted,
+                                             const int32_t *tile_range, float bg, int W, int H, const float *gpu_T,
+                                             const int32_t *gpu_ncontrib, float *out, float *final_T,
+                                             int32_t *ncontrib, uint8_t *nflips, int32_t *forces) {
+    (void)P;
+    const int gx = (W + TILE - 1) / TILE;
+    int64_t unresolved = 0;
+#ifdef _OPENMP
+#pragma omp parallel num_threads(g_threads) reduction(+ : unresolved)
+#endif
+    {
+    float *F = (float *)malloc(sizeof(float) * (C > 0 ? C : 1));
+#ifdef _OPENMP
+#pragma omp for schedule(dynamic, 4)
+#endif
+    for (int py = 0; py < H; ++py)
+        for (int px = 0; px < W; ++px) {
+            const int tile = (py / TILE) * gx + px / TILE;
+            const int pix = py * W + px;
+            PixelList L = {uv, conic, opacity, feature, idx_sorted, tile_range[2 * tile], tile_range[2 * tile + 1],
+                           C, (float)px, (float)py};
+            Decision cand[GUIDE_MAX_CAND], path[GUIDE_MAX_DEPTH];
+            float T;
+            int last, nc;
+            int nfl = 0;
+            Decision chosen[GUIDE_MAX_DEPTH];
+            blend_pixel_pass(&L, NULL, 0, F, &T, &last, cand, &nc, GUIDE_MAX_CAND);
+            int bad = 0;
+            if (!outcome_matches(T, last, gpu_T[pix], gpu_ncontrib[pix])) {
+                GuideSearch S = {&L, gpu_T[pix], gpu_ncontrib[pix], F, 0, 0, 0.0f, 0, {{0, 0, 0}}};
+                for (int d = 1; d <= GUIDE_MAX_DEPTH && !S.found; ++d) guide_dfs(&S, path, 0, cand, nc, d);
+                if (S.found) {
+                    nfl = S.best_n;
+                    for (int d = 0; d < nfl; ++d) chosen[d] = S.best[d];
+                    Decision none[1];
+                    int n2;
+                    blend_pixel_pass(&L, chosen, nfl, F, &T, &last, none, &n2, 0);
+                } else {
+                    /* unresolved: report the IEEE path */
+                    bad = 1;
+                    ++unresolved;
+                    blend_pixel_pass(&L, NULL, 0, F, &T, &last, cand, &nc, 0);
+                }
+            }
+            final_T[pix] = T;
+            ncontrib[pix] = last;
+            if (nflips) nflips[pix] = (uint8_t)(bad ? 255 : nfl);
+            if (forces) {
+                int k = 0;
+                for (int d = 0; d < nfl; ++d)
+                    if (chosen[d].kind == 0 && k < 3) forces[3 * (size_t)pix + k++] = chosen[d].j * 2 + chosen[d].take;
+                for (; k < 3; ++k) forces[3 * (size_t)pix + k] = -1;
+            }
+            for (int c = 0; c < C; ++c) out[(size_t)c * H * W + pix] = F[c] + T * bg;
+        }
+    free(F);
+    }
+    return unresolved;
+}
+
 /* msplat/src/alpha_blending.cu:112-246, in double given the forward's
  * final_T / ncontrib.  Gradients are written (zero-filled first). */
-void oracle_alpha_blending_backward(int P, int C, const float *uv, const float *conic, const float *opacity,
-                                    const float *feature, const int32_t *idx_sorted, const int32_t *tile_range,
-                                    float bg, int W, int H, const float *final_T, const int32_t *ncontrib,
-                                    const float *dL_dout, double *dL_duv, double *dL_dconic, double *dL_dop,
-                                    double *dL_dfeat) {
+static void blend_backward_impl(int P, int C, const float *uv, const float *conic, const float *opacity,
+                                const float *feature, const int32_t *idx_sorted, const int32_t *tile_range,
+                                float bg, int W, int H, const float *final_T, const int32_t *ncontrib,
+                                const float *dL_dout, const int32_t *forces, double *dL_duv, double *dL_dconic,
+                                double *dL_dop, double *dL_dfeat) {
     const int gx = (W + TILE - 1) / TILE;
     memset(dL_duv, 0, sizeof(double) * 2 * (size_t)P);
     memset(dL_dconic, 0, sizeof(double) * 3 * (size_t)P);
@@ -828,11 +1068,26 @@ void oracle_alpha_blending_backward(int P, int C, const float *uv, const float *
                 const double dx = (double)uv[2 * g] - px, dy = (double)uv[2 * g + 1] - py;
                 const double a = conic[3 * g], b = conic[3 * g + 1], c_ = conic[3 * g + 2];
                 const double pw = -0.5 * (a * dx * dx + c_ * dy * dy) - b * dx * dy;
-                if (pw > 0) continue;
+                if (forces) {
+                    /* the forward's float decisions, with its alternate
+                     * branches (guided replay) */
+                    const float pwf = blend_power(conic[3 * g], conic[3 * g + 1], conic[3 * g + 2],
+                                                  uv[2 * g] - (float)px, uv[2 * g + 1] - (float)py);
+                    if (pwf > 0.0f) continue;
+                    const float af = fminf(0.99f, opacity[g] * (float)exp((double)pwf));
+                    int take = !(af < 1.0f / 255.0f);
+                    for (int k = 0; k < 3; ++k) {
+                        const int32_t f = forces[3 * (size_t)pix + k];
+                        if (f >= 0 && f / 2 == j) take = f & 1;
+                    }
+                    if (!take) continue;
+                } else if (pw > 0) {
+                    continue;
+                }
                 const double G = exp(pw);
                 const double op = opacity[g];
                 const double alpha = fmin(0.99, op * G);
-                if (alpha < 1.0 / 255.0) continue;
+                if (!forces && alpha < 1.0 / 255.0) continue;
                 T = T / (1.0 - alpha);
                 const double dcol = alpha * T;
                 double dL_dalpha = 0;
@@ -870,4 +1125,26 @@ void oracle_alpha_blending_backward(int P, int C, const float *uv, const float *
             }
         free(priv);
     }
+}
+
+void oracle_alpha_blending_backward(int P, int C, const float *uv, const float *conic, const float *opacity,
+                                    const float *feature, const int32_t *idx_sorted, const int32_t *tile_range,
+                                    float bg, int W, int H, const float *final_T, const int32_t *ncontrib,
+                                    const float *dL_dout, double *dL_duv, double *dL_dconic, double *dL_dop,
+                                    double *dL_dfeat) {
+    blend_backward_impl(P, C, uv, conic, opacity, feature, idx_sorted, tile_range, bg, W, H, final_T, ncontrib,
+                        dL_dout, NULL, dL_duv, dL_dconic, dL_dop, dL_dfeat);
+}
+
+/* The backward along the paths of oracle_alpha_blending_forward_guided:
+ * the skip decisions are the forward's float ones with its alternate
+ * branches (`forces`), so the pairs differentiated are those the GPU
+ * blended. */
+void oracle_alpha_blending_backward_guided(int P, int C, const float *uv, const float *conic,
+                                           const float *opacity, const float *feature, const int32_t *idx_sorted,
+                                           const int32_t *tile_range, float bg, int W, int H, const float *final_T,
+                                           const int32_t *ncontrib, const float *dL_dout, const int32_t *forces,
+                                           double *dL_duv, double *dL_dconic, double *dL_dop, double *dL_dfeat) {
+    blend_backward_impl(P, C, uv, conic, opacity, feature, idx_sorted, tile_range, bg, W, H, final_T, ncontrib,
+                        dL_dout, forces, dL_duv, dL_dconic, dL_dop, dL_dfeat);
 }

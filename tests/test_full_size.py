@@ -12,7 +12,9 @@
   properties of a multi-channel blend -- each channel block rendered alone
   is bit-identical to the same channels of the 36-channel render, its
   feature gradients equal up to the order of float atomics, and the uv /
-  conic / opacity gradients are the sums of the blocks' gradients.
+  conic / opacity gradients are the sums of the blocks' gradients; and the
+  36-channel blend, forward and backward, against the oracle on a band of 8
+  tile rows.
 """
 import os
 
@@ -21,6 +23,7 @@ import pytest
 import torch
 
 import oracle
+from _guided import check_blend, gpu_blend_forward
 from _scenes import sphere_camera
 
 pytestmark = pytest.mark.gpu
@@ -88,16 +91,16 @@ def test_1m_gaussians_1080p_every_stage_against_the_oracle():
     ocov = oracle.compute_cov3d_forward(s["scale"].numpy(), s["rot"].numpy(), N(vis))
     assert np.abs(N(cov) - ocov).max() <= 1e-6 * np.abs(ocov).max()
     conic, radius, tiles = ms.ewa_project(t["xyz"], cov, ti, te, uv, W, H, vis)
-    # EWA on the GPU's own covariances so the comparison isolates the stage
-    oconic, orad, otiles, amb = oracle.ewa_project_forward(xyz, N(cov), intr, extr, N(uv), W, H, N(vis))
-    # flagged: 3*sqrt(lambda) within 1e-4 relative of an integer (about 0.7%
-    # of radii near 30 px); the GPU's approximate sqrt may round those the
-    # other way, as the reference's fast-math build does
-    ok = ~amb
-    assert ok.mean() > 0.99
-    print(f"EWA: {int((N(radius) != orad).sum())} of {int(amb.sum())} flagged radii differ")
-    np.testing.assert_array_equal(N(radius)[ok], orad[ok])
-    np.testing.assert_array_equal(N(tiles)[ok], otiles[ok])
+    # EWA on the GPU's own covariances so the comparison isolates the stage.
+    # Where 3 sqrt(lambda) is within rounding reach of an integer (about 0.7 %
+    # of radii near 30 px) the GPU's approximate sqrt may round the other way,
+    # as the reference's fast-math build does: every radius must be the
+    # oracle's or that alternative, with its tiles.
+    n_alt, cerr, _ = oracle.ewa_check_against(N(conic), N(radius), N(tiles), xyz, N(cov), intr, extr, N(uv), W, H,
+                                              N(vis))
+    print(f"EWA: {n_alt} of {int((N(radius) > 0).sum())} radii took the alternative rounding; "
+          f"max conic err {cerr:.2e}")
+    assert n_alt <= 100
 
     idx, tr = ms.sort_gaussian(uv, depth, W, H, radius, tiles)
     oidx, otr = oracle.sort_gaussian(N(uv), N(depth), W, H, N(radius), N(tiles))
@@ -117,13 +120,16 @@ def test_1m_gaussians_1080p_every_stage_against_the_oracle():
     w = np.random.default_rng(1).normal(size=(3, H, W)).astype(np.float32)
     (img * torch.as_tensor(w).to(DEV)).sum().backward()
     a_uv, a_con, a_op, a_col = (N(a) for a in ins)
-    oimg, oT, onc, bamb = oracle.alpha_blending_forward(a_uv, a_con, a_op, a_col, oidx, otr, bg, W, H)
-    # flagged: a skip / stop decision within rounding reach of its threshold
-    # (about 0.8% of pixels at ~180 blended Gaussians per pixel)
-    okp = ~bamb
-    assert okp.mean() > 0.99
-    assert np.abs(N(img) - oimg)[:, okp].max() <= 1e-5
-    grads = oracle.alpha_blending_backward(a_uv, a_con, a_op, a_col, oidx, otr, bg, W, H, oT, onc, w)
+    # every pixel: ncontrib equal, image within 1e-5 of the guided oracle
+    # (which follows the GPU only at skip / stop decisions within rounding
+    # reach of their thresholds)
+    gout, gT, gnc = gpu_blend_forward(a_uv, a_con, a_op, a_col, oidx, otr, bg, W, H)
+    np.testing.assert_array_equal(N(img), gout)
+    st = check_blend(gout, gT, gnc, a_uv, a_con, a_op, a_col, oidx, otr, bg, W, H)
+    print(f"blend: {st['alternate_pixels']} of {st['pixels']} pixels took an alternate branch; "
+          f"max image err {st['max_err']:.2e}, max T err {st['max_T_err']:.2e}")
+    grads = oracle.alpha_blending_backward(a_uv, a_con, a_op, a_col, oidx, otr, bg, W, H, st["final_T"],
+                                           st["ncontrib"], w, forces=st["forces"])
     for a, ref, name in zip(ins, grads, ["uv", "conic", "opacity", "colour"]):
         rel_close(N(a.grad).reshape(ref.shape), ref, 1e-4, f"dL/d{name}")
 
@@ -178,6 +184,61 @@ def test_2m_gaussians_1024px_deg10_sh_and_36_channel_blend_properties():
         rel_close(N(got), N(ref), 1e-4, f"dL/d{name} (36 channels vs sum of blocks)")
 
 
+def test_2m_gaussians_1024px_36_channel_band_against_the_oracle():
+    """The 36-channel blend (SH degree 10 colour, 32 N(0,1) features, depth;
+    bg 0.1) of 2M Gaussians at 1024x1024, forward and backward, against the
+    oracle on a band of 8 tile rows across the middle: the multi-chunk path
+    (32 + 4 channels forward, 4 x 10 backward).  Image within 1e-5 on every
+    band pixel and ncontrib equal (guided oracle); gradients of a loss that
+    weights only the band within 1e-4 of the oracle's adjoint."""
+    import msplat_gb300 as ms
+    W = H = 1024
+    f = 800.0
+    n = 2_000_000
+    s = big_scene(n, 1, 10, 0.1)
+    g = torch.Generator().manual_seed(2)
+    feats = torch.randn(n, 32, generator=g)
+    intr = torch.tensor([f, f, W / 2, H / 2]).to(DEV)
+    extr = torch.as_tensor(sphere_camera(np.random.default_rng(1))).to(DEV)
+    t = {k: v.to(DEV) for k, v in s.items()}
+    with torch.no_grad():
+        color = ms.compute_sh(t["shs"], view_dirs(t["xyz"], extr))
+        uv, depth = ms.project_point(t["xyz"], intr, extr, W, H)
+        vis = depth.reshape(-1) != 0
+        cov = ms.compute_cov3d(t["scale"], t["rot"], vis)
+        conic, radius, tiles = ms.ewa_project(t["xyz"], cov, intr, extr, uv, W, H, vis)
+        idx, tr = ms.sort_gaussian(uv, depth, W, H, radius, tiles)
+    full = torch.cat([color, feats.to(DEV), depth], dim=1).contiguous()
+    C = full.shape[1]
+    assert C == 36
+    gx, gy = W // 16, H // 16
+    r0, rows = gy // 2 - 4, 8
+    y0, y1 = r0 * 16, (r0 + rows) * 16
+    bg = 0.1
+    w = torch.randn(C, H, W, generator=g)
+    w_band = torch.zeros_like(w)
+    w_band[:, y0:y1] = w[:, y0:y1]
+    ins = [uv.clone(), conic.clone(), t["opacity"].clone(), full.clone()]
+    for a in ins:
+        a.requires_grad_()
+    img = ms.alpha_blending(*ins, idx, tr, bg, W, H)
+    (img * w_band.to(DEV)).sum().backward()
+
+    trb = N(tr).reshape(gy, gx, 2)[r0:r0 + rows].reshape(-1, 2)
+    uvb = N(uv).copy()
+    uvb[:, 1] -= y0
+    op, feat = N(t["opacity"]), N(full)
+    gout, gT, gnc = gpu_blend_forward(uvb, N(conic), op, feat, N(idx), trb, bg, W, rows * 16)
+    assert np.abs(N(img)[:, y0:y1] - gout).max() <= 1e-5  # the band rendered alone vs the full frame's band
+    st = check_blend(gout, gT, gnc, uvb, N(conic), op, feat, N(idx), trb, bg, W, rows * 16)
+    print(f"36 channels: {st['alternate_pixels']} of {st['pixels']} band pixels on an alternate branch, "
+          f"max image err {st['max_err']:.2e}")
+    grads = oracle.alpha_blending_backward(uvb, N(conic), op, feat, N(idx), trb, bg, W, rows * 16, st["final_T"],
+                                           st["ncontrib"], w[:, y0:y1].numpy(), forces=st["forces"])
+    for a, ref, name in zip(ins, grads, ["uv", "conic", "opacity", "feature"]):
+        rel_close(N(a.grad).reshape(ref.shape), ref, 1e-4, f"dL/d{name} (36 channels, band)")
+
+
 def test_ndc_receives_the_scaled_uv_gradient():
     import msplat_gb300 as ms
     W, H, f = 320, 240, 300.0
@@ -204,7 +265,7 @@ def test_4k_frame_fits_and_a_band_matches_the_oracle():
     """3840x2160 forward + backward of 1M Gaussians: per pixel only final T
     and the contributor count are kept (8 B), the backward recomputes the
     rest, so the frame fits easily; a band of 8 tile rows across the middle
-    is checked against the oracle (image 1e-5 on non-flagged pixels)."""
+    is checked against the guided oracle (image 1e-5 on every pixel)."""
     import msplat_gb300 as ms
     W, H, f = 3840, 2160, 3000.0
     s = big_scene(1_000_000, 5, 3, 0.3)
@@ -233,8 +294,8 @@ def test_4k_frame_fits_and_a_band_matches_the_oracle():
     trb = N(tr).reshape(gy, gx, 2)[r0:r0 + rows].reshape(-1, 2)
     uvb = N(uv).copy()
     uvb[:, 1] -= r0 * 16
-    oimg, _, _, amb = oracle.alpha_blending_forward(uvb, N(conic), N(t["opacity"]), N(color), N(idx), trb, 0.0, W,
-                                                    rows * 16)
+    op = N(t["opacity"])
+    gout, gT, gnc = gpu_blend_forward(uvb, N(conic), op, N(color), N(idx), trb, 0.0, W, rows * 16)
     got = N(img)[:, r0 * 16:(r0 + rows) * 16]
-    assert (~amb).mean() > 0.99
-    assert np.abs(got - oimg)[:, ~amb].max() <= 1e-5
+    assert np.abs(got - gout).max() <= 1e-5  # the band rendered alone vs the full frame's band
+    check_blend(gout, gT, gnc, uvb, N(conic), op, N(color), N(idx), trb, 0.0, W, rows * 16)

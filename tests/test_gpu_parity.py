@@ -2,12 +2,16 @@
 reference's arithmetic for forward passes, float64 for adjoints).
 
 Bars (from the rasteriser's specification):
-  * radius, tiles_touched, idx_sorted, tile_range: bit-exact (radius may
-    differ only where the oracle flags the value as within rounding reach of
-    an integer boundary -- the GPU divides / square-roots approximately,
-    exactly like the reference's fast-math build);
-  * uv, depth, cov3d: bit-exact (same operations, same FMA contractions);
-  * rendered features: within 1e-5 absolute;
+  * radius, tiles_touched, idx_sorted, tile_range: bit-exact.  The GPU
+    divides and square-roots approximately, exactly like the reference's
+    fast-math build, so where 3 sqrt(lambda) lies within rounding reach of an
+    integer either rounding is correct: every radius must equal the oracle's
+    or that alternative (two-branch oracle), with tiles to match;
+  * uv, depth: bit-exact; cov3d within 1e-6 of the largest term;
+  * rendered features: within 1e-5 absolute on every pixel, ncontrib equal
+    on every pixel -- against the guided oracle, which follows the GPU's
+    branch only at decisions within rounding reach of a threshold (alpha vs
+    1/255, T (1 - alpha) vs 1e-4);
   * gradients: within 1e-4 relative (to the largest magnitude of the output).
 """
 import numpy as np
@@ -16,6 +20,7 @@ import torch
 
 import oracle
 from _golden import load
+from _guided import check_blend, gpu_blend_forward
 from _scenes import camera, scene
 
 pytestmark = pytest.mark.gpu
@@ -164,23 +169,21 @@ def ewa_inputs(n=30000, W=800, H=600, seed=0):
 def test_ewa_project_forward(seed):
     s, intr, extr, uv, vis, cov, W, H = ewa_inputs(seed=seed)
     conic, radius, tiles = ms.ewa_project(T(s["xyz"]), T(cov), T(intr), T(extr), T(uv), W, H, T(vis))
-    oc, orad, otil, amb = oracle.ewa_project_forward(s["xyz"].numpy(), cov, intr, extr, uv, W, H, vis)
-    mism = (N(radius) != orad) | (N(tiles) != otil)
-    assert not (mism & ~amb).any(), f"{(mism & ~amb).sum()} unflagged radius/tiles mismatches"
-    assert mism.sum() <= max(2, int(1e-4 * mism.size))
-    ok = ~mism
-    np.testing.assert_allclose(N(conic)[ok], oc[ok], rtol=2e-5, atol=1e-7)
-    assert (orad > 0).sum() > 1000
+    # every entry: the oracle's radius or its alternative rounding, tiles of
+    # that radius, conic within 2e-5 relative
+    n_alt, err, _ = oracle.ewa_check_against(N(conic), N(radius), N(tiles), s["xyz"].numpy(), cov, intr, extr, uv,
+                                             W, H, vis)
+    print(f"EWA seed {seed}: {n_alt} radii took the alternative rounding, max conic err {err:.2e}")
+    assert n_alt <= max(2, int(1e-4 * radius.numel()))
+    assert int((radius > 0).sum()) > 1000
 
 
 def test_ewa_project_golden():
     g = load("ewa_project")
     conic, radius, tiles = ms.ewa_project(T(g["xyz"]), T(g["cov3d"]), T(g["intr"]), T(g["extr"]), T(g["uv"]),
                                           g["W"], g["H"], T(g["visible"]))
-    oc, orad, otil, amb = oracle.ewa_project_forward(g["xyz"], g["cov3d"], g["intr"], g["extr"], g["uv"],
-                                                     g["W"], g["H"], g["visible"])
-    mism = (N(radius) != orad) | (N(tiles) != otil)
-    assert not (mism & ~amb).any()
+    oracle.ewa_check_against(N(conic), N(radius), N(tiles), g["xyz"], g["cov3d"], g["intr"], g["extr"], g["uv"],
+                             g["W"], g["H"], g["visible"])
     # and against the reference's own PyTorch restatement, as its test does
     mism_ref = (N(radius) != g["radius"]) | (N(tiles) != g["tiles"])
     assert mism_ref.sum() <= 2
@@ -324,30 +327,25 @@ def test_alpha_blending_forward(C):
     s, it, W, H = blend_inputs(C=C, seed=C)
     bg = 0.25
     args = (T(it["uv"]), T(it["conic"]), T(s["opacity"]), T(s["feat"]), T(it["idx_sorted"]), T(it["tile_range"]))
-    out = ms.alpha_blending(*args, bg, W, H)
-    oout, oT, onc, amb = oracle.alpha_blending_forward(it["uv"], it["conic"], s["opacity"].numpy(),
-                                                       s["feat"].numpy(), it["idx_sorted"], it["tile_range"], bg, W, H)
-    ok = ~amb
-    assert ok.mean() > 0.99
-    err = np.abs(N(out) - oout)[:, ok].max()
-    assert err <= 1e-5, err
+    out = N(ms.alpha_blending(*args, bg, W, H))
+    gout, gT, gnc = gpu_blend_forward(it["uv"], it["conic"], s["opacity"].numpy(), s["feat"].numpy(),
+                                      it["idx_sorted"], it["tile_range"], bg, W, H)
+    np.testing.assert_array_equal(out, gout)
+    st = check_blend(gout, gT, gnc, it["uv"], it["conic"], s["opacity"].numpy(), s["feat"].numpy(),
+                     it["idx_sorted"], it["tile_range"], bg, W, H)
+    print(f"C={C}: {st['alternate_pixels']} of {st['pixels']} pixels on an alternate branch, "
+          f"max err {st['max_err']:.2e}")
 
 
 def test_alpha_blending_final_T_and_ncontrib():
     from msplat_gb300 import _lib
     s, it, W, H = blend_inputs(C=3, seed=11)
-    lib = _lib.load()
-    P = s["feat"].shape[0]
-    outs = [torch.empty(3, H, W, device=DEV), torch.empty(H, W, device=DEV),
-            torch.empty(H, W, dtype=torch.int32, device=DEV)]
-    ins = [T(it["uv"]), T(it["conic"]), T(s["opacity"]), T(s["feat"]), T(it["idx_sorted"]), T(it["tile_range"])]
-    _lib.check(lib.msplat_alpha_blending_forward(P, 3, *[x.data_ptr() for x in ins], 0.0, W, H,
-                                                 *[x.data_ptr() for x in outs], _lib.stream()), "blend")
-    oout, oT, onc, amb = oracle.alpha_blending_forward(it["uv"], it["conic"], s["opacity"].numpy(),
-                                                       s["feat"].numpy(), it["idx_sorted"], it["tile_range"], 0.0, W, H)
-    ok = ~amb
-    assert (N(outs[2])[ok] == onc[ok]).mean() > 0.9999
-    np.testing.assert_allclose(N(outs[1])[ok], oT[ok], rtol=1e-5, atol=1e-7)
+    gout, gT, gnc = gpu_blend_forward(it["uv"], it["conic"], s["opacity"].numpy(), s["feat"].numpy(),
+                                      it["idx_sorted"], it["tile_range"], 0.0, W, H)
+    st = check_blend(gout, gT, gnc, it["uv"], it["conic"], s["opacity"].numpy(), s["feat"].numpy(),
+                     it["idx_sorted"], it["tile_range"], 0.0, W, H)
+    # final T relative to itself on every pixel (T spans 1e-4 .. 1)
+    np.testing.assert_allclose(gT, st["final_T"], rtol=1e-4, atol=1e-8)
 
 
 def test_alpha_blending_golden():
@@ -372,25 +370,51 @@ def test_alpha_blending_backward(C, bg):
     out = ms.alpha_blending(*ins, T(it["idx_sorted"]), T(it["tile_range"]), bg, W, H)
     w = np.random.default_rng(C).normal(size=out.shape).astype(np.float32)
     (out * T(w)).sum().backward()
-    oout, oT, onc, amb = oracle.alpha_blending_forward(it["uv"], it["conic"], s["opacity"].numpy(),
-                                                       s["feat"].numpy(), it["idx_sorted"], it["tile_range"], bg, W, H)
+    gout, gT, gnc = gpu_blend_forward(it["uv"], it["conic"], s["opacity"].numpy(), s["feat"].numpy(),
+                                      it["idx_sorted"], it["tile_range"], bg, W, H)
+    st = check_blend(gout, gT, gnc, it["uv"], it["conic"], s["opacity"].numpy(), s["feat"].numpy(),
+                     it["idx_sorted"], it["tile_range"], bg, W, H)
+    # the adjoint along the GPU's paths (the pairs it blended)
     grads = oracle.alpha_blending_backward(it["uv"], it["conic"], s["opacity"].numpy(), s["feat"].numpy(),
-                                           it["idx_sorted"], it["tile_range"], bg, W, H, oT, onc, w)
+                                           it["idx_sorted"], it["tile_range"], bg, W, H, st["final_T"],
+                                           st["ncontrib"], w, forces=st["forces"])
     for a, ref, name in zip(ins, grads, ["uv", "conic", "opacity", "feature"]):
         rel_close(N(a.grad).reshape(ref.shape), ref, rtol=1e-4, what=f"dL/d{name}")
 
 
 # ------------------------------------------------------------- pipeline
 def test_rasterization_matches_oracle_pipeline():
+    """The benchmark's config-0 frame (10k Gaussians, 256x256, intr (300, 300,
+    128, 128), extr [I | (0, 0, 4)], bg 0): the fused rasterization against
+    the oracle's own chain (its projection, covariance and EWA), held on
+    every radius and every pixel through the two-branch oracle."""
     s, it, W, H = blend_inputs(n=10000, seed=3)
     intr, extr = camera(W, H, front=True)
-    img = ms.rasterization(T(s["xyz"]), T(s["scale"]), T(s["rot"]), T(s["opacity"]), T(s["feat"]), T(intr),
-                           T(extr), W, H, 0.0)
-    ref = oracle.rasterization_forward(s["xyz"].numpy(), s["scale"].numpy(), s["rot"].numpy(),
-                                       s["opacity"].numpy(), s["feat"].numpy(), intr, extr, W, H, 0.0)[0]
-    amb = it["blend_ambiguous"]
-    err = np.abs(N(img) - ref)[:, ~amb].max()
-    assert err <= 1e-5, err
+    args = [T(s["xyz"]), T(s["scale"]), T(s["rot"]), T(s["opacity"]), T(s["feat"]), T(intr), T(extr)]
+    img, radius = ms.rasterization(*args, W, H, 0.0, return_radius=True)
+    # the GPU stage chain: same image as the fused call, and the outcome
+    # (final T, ncontrib) the oracle replays
+    uv, depth = ms.project_point(args[0], args[5], args[6], W, H)
+    vis = depth.reshape(-1) != 0
+    cov = ms.compute_cov3d(args[1], args[2], vis)
+    conic, rad, tiles = ms.ewa_project(args[0], cov, args[5], args[6], uv, W, H, vis)
+    assert torch.equal(rad, radius)
+    idx, tr = ms.sort_gaussian(uv, depth, W, H, rad, tiles)
+    gout, gT, gnc = gpu_blend_forward(N(uv), N(conic), s["opacity"].numpy(), s["feat"].numpy(), N(idx), N(tr), 0.0,
+                                      W, H)
+    np.testing.assert_array_equal(N(img), gout)
+    # the oracle chain, following the GPU only at rounding-reach decisions
+    np.testing.assert_array_equal(N(uv), it["uv"])
+    n_alt, _, (orad, otiles, oconic) = oracle.ewa_check_against(
+        N(conic), N(rad), N(tiles), s["xyz"].numpy(), it["cov3d"], intr, extr, it["uv"], W, H, it["visible"],
+        conic_rtol=1e-4)
+    oidx, otr = oracle.sort_gaussian(it["uv"], it["depth"], W, H, orad, otiles)
+    np.testing.assert_array_equal(N(idx), oidx)
+    np.testing.assert_array_equal(N(tr), otr)
+    st = check_blend(gout, gT, gnc, it["uv"], oconic, s["opacity"].numpy(), s["feat"].numpy(), oidx, otr, 0.0, W,
+                     H)
+    print(f"config 0: {n_alt} alternate radii, {st['alternate_pixels']} alternate pixels, "
+          f"max image err {st['max_err']:.2e}")
 
 
 def test_blend_multi_pixel_kernels_match_one_pixel_kernels():
@@ -442,11 +466,7 @@ def test_blend_row_cull_keeps_every_contribution():
     uv, conic, op, feat, idx, tr, _ = elongated_2d(5000, W, H, seed=5)
     assert idx.size > 100000
     out = small_vs_general(uv, conic, op, feat, idx, tr, W, H)
-    oout, oT, onc, amb = oracle.alpha_blending_forward(uv, conic, op, feat, idx, tr, 0.5, W, H)
-    ok = ~amb
-    assert ok.mean() > 0.99
-    np.testing.assert_array_equal(out[2][ok], onc[ok])
-    assert np.abs(out[0] - oout)[:, ok].max() <= 1e-5
+    check_blend(out[0], out[1], out[2], uv, conic, op, feat, idx, tr, 0.5, W, H)
 
 
 def check_culled_lists(uv, depth, radius, tiles, conic, op, feat, W, H):
