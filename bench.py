@@ -255,17 +255,19 @@ NCU_TRAFFIC_1M_1080P = {"alpha_blending_backward": 96.13e6 + 1.27e6,
                         "alpha_blending_forward": 44.59e6 + 9.15e6}
 
 
-def roofline(stages, steps, pairs, inter, nvis, sm_mhz, peaks, peak_kind):
-    """Roofline entry for the stage with the largest share of the step."""
+def roofline(stages, steps, pairs, inter, nvis, sm_mhz, peaks, peak_kind, C=3, n=None, D=16, full=None):
+    """Roofline entry for the stage with the largest share of the step (C
+    blended channels, n Gaussians, D SH coefficients per channel)."""
     name, (calls, total) = max(stages.items(), key=lambda kv: kv[1][1])
     per_launch_ms = total / max(calls, 1)
-    C = 3
+    N_G = N_GAUSS if n is None else n
     if name.startswith("alpha_blending"):
         fl = (12 + 2 * C) if name.endswith("forward") else (30 + 8 * C)
         flops = pairs * (fl + 1)  # + one exponential per pair
         ach = flops / (per_launch_ms * 1e-3) / 1e12
         peak = fp32_peak_tflops(sm_mhz)
-        full = (N_GAUSS, W_IMG, H_IMG) == (1_000_000, 1920, 1080)
+        if full is None:
+            full = (N_GAUSS, W_IMG, H_IMG) == (1_000_000, 1920, 1080)
         traffic = NCU_TRAFFIC_1M_1080P.get(name) if full else None
         hbm = peaks.get("hbm_gbs", 6800.0)
         out = {"bound": "fp32", "achieved": round(ach, 3), "peak": round(peak, 2), "unit": "TFLOP/s",
@@ -281,22 +283,24 @@ def roofline(stages, steps, pairs, inter, nvis, sm_mhz, peaks, peak_kind):
                                      "in this run")
             out["dram"] = {"achieved_gbs": round(gbs, 1), "peak_gbs": hbm, "frac": round(gbs / hbm, 4)}
         return name, out
+    CSH = 3  # SH colour channels
     bytes_per = {
         "sort_gaussian_finish": inter * 52.0,
-        "sort_gaussian_prepare": N_GAUSS * 100.0,
-        "compute_sh_forward": N_GAUSS * (4 * 3 * 16 + 12 + 1 + 12),
-        "compute_sh_backward": N_GAUSS * (2 * 4 * 3 * 16 + 12 + 12 + 12 + 1),
-        "ewa_project_forward": N_GAUSS * 65.0,
-        "ewa_project_backward": N_GAUSS * 88.0,
-        "compute_cov3d_forward": N_GAUSS * 53.0,
-        "compute_cov3d_backward": N_GAUSS * 81.0,
-        "project_point_forward": N_GAUSS * 24.0,
-        "project_point_backward": N_GAUSS * 48.0,
-        # fused: geometry 40 B in + 32 B out; SH 192 B coefficients + 12 B
-        # xyz + 4 B depth in, 12 B colour out
-        "rasterize_preprocess_forward": N_GAUSS * (72.0 + 4 * 3 * 16 + 16 + 12),
-        # SH adjoint 220 B in, 204 B out; geometry adjoint 92 B in, 40 B out
-        "rasterize_preprocess_backward": N_GAUSS * (424.0 + 132.0),
+        "sort_gaussian_prepare": N_G * 100.0,
+        "compute_sh_forward": N_G * (4 * CSH * D + 12 + 1 + 4 * CSH),
+        "compute_sh_backward": N_G * (2 * 4 * CSH * D + 12 + 4 * CSH + 12 + 1),
+        "ewa_project_forward": N_G * 65.0,
+        "ewa_project_backward": N_G * 88.0,
+        "compute_cov3d_forward": N_G * 53.0,
+        "compute_cov3d_backward": N_G * 81.0,
+        "project_point_forward": N_G * 24.0,
+        "project_point_backward": N_G * 48.0,
+        # fused: geometry 40 B in + 32 B out; SH 4 CSH D B coefficients + 12 B
+        # xyz + 4 B depth in, 4 CSH B colour out
+        "rasterize_preprocess_forward": N_G * (72.0 + 4 * CSH * D + 16 + 4 * CSH),
+        # SH adjoint 4 CSH D + 4 CSH + 16 B in, 4 CSH D + 12 B out; geometry
+        # adjoint 92 B in, 40 B out
+        "rasterize_preprocess_backward": N_G * (8.0 * CSH * D + 4 * CSH + 28 + 132.0),
     }.get(name, 0.0)
     ach = bytes_per / (per_launch_ms * 1e-3) / 1e9
     peak = peaks.get("hbm_gbs", 6800.0)
@@ -619,6 +623,95 @@ def run_reference(args):
     }
 
 
+# ------------------------------------------- extensible features (SH degree 10)
+C2_N, C2_W, C2_H, C2_F, C2_SH = 2_000_000, 1024, 1024, 800.0, 10
+
+
+def config2_step(ms, p, weights, W, H):
+    """One fwd+bwd frame of 36 channels: the SH degree-10 colour on the
+    camera's view directions (3), 32 features and the camera-space depth,
+    blended in one pass by the drop-in rasterization."""
+    color = ms.compute_sh(p["shs"], view_dirs(p["xyz"], p["extr"]))
+    zc = p["xyz"] @ p["extr"][2, :3] + p["extr"][2, 3]
+    feat = torch.cat([color, p["feats"], zc[:, None]], 1)
+    img = ms.rasterization(p["xyz"], p["scale"], p["rot"], p["opacity"], feat, p["intr"], p["extr"], W, H, 0.0)
+    loss = (img * weights).sum()
+    loss.backward()
+    return loss
+
+
+def run_config2(args, device):
+    """2M Gaussians, SH degree 10 ([N, 3, 121] coefficients N(0, 0.1)), 32
+    N(0, 1) features and a depth channel (C = 36), 1024x1024 at f = 800 (the
+    1080p field of view), loss sum(W * img) with W ~ N(0, 1) [36, H, W]:
+    device ms per fwd+bwd frame."""
+    import msplat_gb300 as ms
+    from msplat_gb300 import _lib
+    from msplat_gb300.synthetic import feature_scene
+    n = C2_N if args.gaussians == 1_000_000 else args.gaussians
+    W, H = C2_W, C2_H
+    sc = feature_scene(n, W, H, C2_F, seed=1, sh_degree=C2_SH)
+    keys = ["xyz", "scale", "rot", "opacity", "shs", "feats", "intr", "extr"]
+    p = {k: sc[k].to(device).contiguous().requires_grad_() for k in keys}
+    weights = sc["weights"].to(device)
+    C = weights.shape[0]
+    for _ in range(args.warmup):
+        for t in p.values():
+            t.grad = None
+        config2_step(ms, p, weights, W, H)
+    torch.cuda.synchronize()
+    clocks = ClockSampler(torch.cuda.current_device())
+    clocks.start()
+    stream = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    _lib.profile_start()
+    n0 = _lib.kernel_launches()
+    e0.record(stream)
+    for _ in range(args.steps):
+        for t in p.values():
+            t.grad = None
+        config2_step(ms, p, weights, W, H)
+    e1.record(stream)
+    launches = _lib.kernel_launches() - n0
+    torch.cuda.synchronize()
+    stages = _lib.profile_stop()
+    clk = clocks.stop()
+    ms_step = e0.elapsed_time(e1) / args.steps
+    # work counts outside the timed region: intersections and blend pairs of
+    # the culled lists the drop-in call blends
+    with torch.no_grad():
+        uv, depth, conic, radius, tiles, _ = ms.preprocess(p["xyz"], p["scale"], p["rot"], p["intr"], p["extr"], W,
+                                                           H)
+        idx, tr = ms.sort_gaussian(uv, depth, W, H, radius, tiles, cull=(conic, p["opacity"]))
+        ones = torch.ones(n, 1, device=device)
+        img = torch.empty(1, H, W, device=device)
+        T = torch.empty(H, W, device=device)
+        nc = torch.empty(H, W, dtype=torch.int32, device=device)
+        _lib.check(_lib.load().msplat_alpha_blending_forward(
+            n, 1, uv.data_ptr(), conic.data_ptr(), p["opacity"].data_ptr(), ones.data_ptr(), idx.data_ptr(),
+            tr.data_ptr(), 0.0, W, H, img.data_ptr(), T.data_ptr(), nc.data_ptr(), _lib.stream()), "blend")
+        pairs, inter = int(nc.sum().item()), int(idx.numel())
+    peaks, peak_kind = measured_peaks()
+    dom, roof = roofline(stages, args.steps, pairs, inter, n, clk.get("sm_mhz"), peaks, peak_kind, C=C, n=n,
+                         D=(C2_SH + 1) ** 2, full=False)
+    return {
+        "metric": "fwd+bwd ms/frame, 36 channels (SH deg 10 colour + 32 features + depth) @2M Gauss 1024x1024",
+        "value": round(ms_step, 4), "unit": "ms/frame", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(ms_step, 4), "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": DATA_DESC.replace("N(0,0.3) SH", "N(0,0.1) SH degree 10") + "; N(0,1) features; "
+                                "random look-at camera on a radius-4 sphere)",
+        "config": {"workload": f"{n} Gaussians, {W}x{H}, f {C2_F}, SH deg {C2_SH}, C = {C} (3 SH colour + 32 "
+                               f"features + depth), fwd+bwd, loss sum(W*img)",
+                   "n_gaussians": n, "width": W, "height": H, "channels": C, "sh_degree": C2_SH,
+                   "intersections": inter, "blend_pairs": pairs,
+                   "l2": "inputs (2.9 GB of SH coefficients) larger than L2 (129 MB); no flush"},
+        "gpu_launches": int(launches),
+        "stage_ms_per_step": {k: round(v[1] / args.steps, 4) for k, v in sorted(stages.items(),
+                                                                               key=lambda kv: -kv[1][1])},
+        "roofline": roof, "clocks": clk,
+    }
+
+
 # ------------------------------------------------------ multi-camera batch
 BATCH_SIZES = [(256, 256), (512, 512), (1280, 720), (1920, 1080)]
 
@@ -655,17 +748,25 @@ def batch_scene(n, n_cams, seed=0):
 
 
 def run_batch(args, device):
-    """Multi-camera batch: 64 cameras of one 2M-Gaussian scene, fwd+bwd, through one
-    rasterization_sh_batch call against 64 rasterization_sh calls."""
+    """Multi-camera batch: 64 cameras of one 2M-Gaussian scene, fwd+bwd.  The
+    batched arm is one rasterization_sh_batch call (one sort over all
+    cameras, one blend grid over all their tiles) captured in a CUDA graph
+    and replayed; against 64 rasterization_sh calls one after the other, and
+    against 64 calls in the reference's call sequence (compute_sh on view
+    directions computed in PyTorch, then rasterization)."""
     import msplat_gb300 as ms
+    from msplat_gb300 import _lib
+    from msplat_gb300.batch import last_capacity
     n, n_cams = args.gaussians if args.gaussians != 1_000_000 else 2_000_000, args.cameras
     sc, sizes, weights = batch_scene(n, n_cams)
     p = {k: v.to(device).contiguous().requires_grad_() for k, v in sc.items()}
     ws = [w.to(device) for w in weights]
+    status = torch.zeros(1, dtype=torch.int32, device=device)
 
-    def batched():
+    def batched(capacity=None):
         imgs = ms.rasterization_sh_batch(p["xyz"], p["scale"], p["rot"], p["opacity"], p["shs"], p["intrs"],
-                                         p["extrs"], sizes, 0.0)
+                                         p["extrs"], sizes, 0.0, capacity=capacity,
+                                         status=status if capacity else None)
         sum((i * w).sum() for i, w in zip(imgs, ws)).backward()
 
     def sequential():
@@ -674,16 +775,25 @@ def run_batch(args, device):
                                       p["extrs"][b], w, h, 0.0)
             (img * ws[b]).sum().backward()
 
+    def dropin_sequential():
+        for b, (w, h) in enumerate(sizes):
+            color = ms.compute_sh(p["shs"], view_dirs(p["xyz"], p["extrs"][b]))
+            img = ms.rasterization(p["xyz"], p["scale"], p["rot"], p["opacity"], color, p["intrs"][b],
+                                   p["extrs"][b], w, h, 0.0)
+            (img * ws[b]).sum().backward()
+
+    def zero():
+        for t in p.values():
+            t.grad = None
+
     def timed(fn):
         for _ in range(args.warmup):
-            for t in p.values():
-                t.grad = None
+            zero()
             fn()
         torch.cuda.synchronize()
         out = []
         for _ in range(args.steps):
-            for t in p.values():
-                t.grad = None
+            zero()
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             e0.record()
             fn()
@@ -692,32 +802,67 @@ def run_batch(args, device):
             out.append(e0.elapsed_time(e1))
         return out
 
+    # the captured batch: capacity 1.1x this batch's padded intersection count
+    zero()
+    batched()
+    cap = int(last_capacity() * 1.1) + 3072
+    side = torch.cuda.Stream()
+    side.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(side):
+        for _ in range(3):
+            zero()
+            batched(cap)
+    torch.cuda.current_stream().wait_stream(side)
+    zero()
+    graph = torch.cuda.CUDAGraph()
+    n0 = _lib.kernel_launches()
+    with torch.cuda.graph(graph):
+        batched(cap)
+    graph_launches = _lib.kernel_launches() - n0
+
+    def replay():
+        graph.replay()
+
     clocks = ClockSampler(torch.cuda.current_device())
     clocks.start()
+    tg = timed(replay)
     tb = timed(batched)
     ts = timed(sequential)
+    td = timed(dropin_sequential)
     clk = clocks.stop()
-    from msplat_gb300 import _lib
+    torch.cuda.synchronize()
+    graph_ok = int(status.item()) == 0
+    del graph
     stage = {}
     for name, fn in (("batched", batched), ("sequential", sequential)):
-        for t in p.values():
-            t.grad = None
+        zero()
         _lib.profile_start()
+        n1 = _lib.kernel_launches()
         fn()
+        launches = _lib.kernel_launches() - n1
         stage[name] = {k: round(v[1], 3) for k, v in sorted(_lib.profile_stop().items(), key=lambda kv: -kv[1][1])}
-    mb, msq = float(np.median(tb)), float(np.median(ts))
+        stage[name]["library_launches"] = launches
+    mg, mb, msq, mdi = (float(np.median(x)) for x in (tg, tb, ts, td))
+    head = mg if graph_ok else mb
     return {
         "metric": "batched renders/s (fwd+bwd), 64 cameras of one 2M-Gaussian scene",
-        "value": round(n_cams / (mb * 1e-3), 2), "unit": "renders/s", "n_gpus": 1, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": round(mb, 3), "higher_is_better": True, "scaling": "weak",
+        "value": round(n_cams / (head * 1e-3), 2), "unit": "renders/s", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(head, 3), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": DATA_DESC + "; sphere cameras)",
         "config": {"workload": f"{n} Gaussians, SH deg 3, {n_cams} sphere cameras at "
                                f"{sorted(set(sizes))}, fwd+bwd, loss sum_b sum(W_b*img_b)",
                    "cameras": n_cams, "n_gaussians": n,
-                   "pixels": int(sum(w * h for w, h in sizes))},
-        "batched_ms": [round(x, 3) for x in tb], "sequential_ms": [round(x, 3) for x in ts],
+                   "pixels": int(sum(w * h for w, h in sizes)),
+                   "batched_arm": ("one rasterization_sh_batch call (one key space, one blend grid) captured in a "
+                                   "CUDA graph, capacity 1.1x the padded intersection count")
+                   if graph_ok else "eager rasterization_sh_batch (graph capacity exceeded)"},
+        "graph_ms": [round(x, 3) for x in tg], "batched_eager_ms": [round(x, 3) for x in tb],
+        "sequential_ms": [round(x, 3) for x in ts], "dropin_sequential_ms": [round(x, 3) for x in td],
+        "graph_library_launches_per_batch": graph_launches,
         "sequential_renders_per_s": round(n_cams / (msq * 1e-3), 2),
-        "speedup_vs_one_by_one": round(msq / mb, 3),
+        "speedup_vs_one_by_one": round(msq / head, 3),
+        "speedup_vs_one_by_one_reference_sequence": round(mdi / head, 3),
+        "speedup_eager_vs_one_by_one": round(msq / mb, 3),
         "stage_ms_per_batch": stage,
         "clocks": clk,
     }
@@ -826,9 +971,10 @@ def main():
                     help="scene size (a smaller case for profiling; the benchmark is 1M)")
     ap.add_argument("--width", type=int, default=W_IMG)
     ap.add_argument("--height", type=int, default=H_IMG)
-    ap.add_argument("--workload", default="frame", choices=["frame", "batch", "serve"],
+    ap.add_argument("--workload", default="frame", choices=["frame", "batch", "serve", "config2"],
                     help="frame: the 1M / 1080p training frame (default); batch: 64 cameras of a 2M scene; "
-                         "serve: the request server over 8 resident scenes")
+                         "serve: the request server over 8 resident scenes; config2: 36 channels (SH degree 10 "
+                         "+ 32 features + depth) of 2M Gaussians at 1024x1024")
     ap.add_argument("--cameras", type=int, default=64)
     ap.add_argument("--rate", type=float, default=500.0, help="serve: Poisson arrival rate (requests/s)")
     ap.add_argument("--duration", type=float, default=1.0, help="serve: seconds of arrivals")
@@ -848,10 +994,11 @@ def main():
         torch.distributed.init_process_group("nccl", device_id=device)
     from msplat_gb300 import _build
     _build.build()
-    if args.workload in ("batch", "serve"):
+    if args.workload in ("batch", "serve", "config2"):
         if rank == 0:
-            out = run_batch(args, device) if args.workload == "batch" else run_serve(args)
-            print(json.dumps(out), flush=True)
+            run = {"batch": lambda: run_batch(args, device), "serve": lambda: run_serve(args),
+                   "config2": lambda: run_config2(args, device)}[args.workload]
+            print(json.dumps(run()), flush=True)
         return
     out = run_ours(args, rank, world, device)
     if rank == 0:

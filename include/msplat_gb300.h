@@ -360,6 +360,80 @@ MSPLAT_API int msplat_batch_preprocess_backward(int P, int B, const float *xyz, 
                                   msplat_stream_t stream);
 
 /* ------------------------------------------------------------------------ */
+/* Multi-camera batches in one key space.  No counterpart in the reference,
+ * which renders one camera per call (msplat/__init__.py:22-93) and sorts one
+ * camera's intersections per call (msplat/sort_gaussian.py:8-54).  A batch
+ * of B cameras (of one or several scenes) is sorted by (camera, tile,
+ * depth) and blended by one grid over every camera's tiles.
+ *
+ * Layout: per-camera per-Gaussian arrays (uv [.,2], depth, conic [.,3],
+ * radius, tiles, colour [.,C], and the blend's gradients) are stacked
+ * camera after camera -- camera b's rows start at the sum of P over the
+ * cameras before it; opacity (and shared features) are read at
+ * opacity_offset[b] + g; tiles are numbered globally (tile_range has one
+ * row per tile of all cameras); images are stacked: camera b's [C, H_b,
+ * W_b] image starts at C * (pixels of the cameras before it), final_T and
+ * ncontrib at (those pixels).  The order of each camera's list equals the
+ * single-camera culled lists (msplat_sort_gaussian_prepare_culled), so
+ * every camera's image is bit-identical to a single-camera call's. */
+
+/* The plan: a host buffer of msplat_batch_plan_bytes(B) bytes built from the
+ * cameras' dims [B,2] (W, H), npoints [B] (Gaussians of each camera's scene)
+ * and opacity_offset [B] (may be NULL: all 0), all host arrays; the caller
+ * copies it to device memory and passes that copy to the calls below.
+ * sizes (host, 5 entries) receives: total tiles, total stacked rows, total
+ * pixels, depth-key items (padded), tile-key passes. */
+MSPLAT_API size_t msplat_batch_plan_bytes(int B);
+MSPLAT_API int msplat_batch_plan(int B, const int32_t *dims, const int32_t *npoints,
+                                 const int64_t *opacity_offset, void *plan, size_t plan_bytes,
+                                 int64_t *sizes);
+
+/* Depth sort of every camera's Gaussians (one segmented radix sort), the
+ * culled rectangles and intersection counts.  counts (device, int64 [2 + B])
+ * receives the intersections, the padded list length a finish needs (its
+ * capacity) and each camera's intersections. */
+MSPLAT_API size_t msplat_batch_sort_prepare_workspace_size(int B, int64_t depth_items);
+MSPLAT_API int msplat_batch_sort_prepare(const void *plan, int B, int64_t depth_items, const float *uv,
+                                         const float *depth, const int32_t *radius, const float *conic,
+                                         const float *opacity, int64_t *counts, void *workspace,
+                                         size_t workspace_bytes, msplat_stream_t stream);
+
+/* Emission and a segmented stable sort by tile of every camera's list, and
+ * the tile ranges [total_tiles, 2] (positions in idx_sorted [capacity]).
+ * capacity: a multiple of 3072, at least counts[1] of the prepare for a
+ * valid result; no host read happens.  status (device int32, may be NULL)
+ * is set to 1 when the capacity was too small (the result is then not
+ * valid), else 0. */
+MSPLAT_API size_t msplat_batch_sort_finish_workspace_size(int B, int64_t capacity, int passes);
+MSPLAT_API int msplat_batch_sort_finish(const void *plan, int B, int64_t depth_items, int total_tiles, int passes,
+                                        int64_t capacity, const void *prepare_workspace, int32_t *idx_sorted,
+                                        int32_t *tile_range, int32_t *status, void *workspace,
+                                        size_t workspace_bytes, msplat_stream_t stream);
+
+/* One blend grid over every camera's tiles (the semantics of
+ * msplat_alpha_blending_forward per camera).  feature_per_camera: 1 when
+ * feature is stacked per camera (rows like uv), 0 when per scene (rows like
+ * opacity). */
+MSPLAT_API int msplat_batch_alpha_blending_forward(const void *plan, int B, int total_tiles, int C,
+                                                   int feature_per_camera, const float *uv, const float *conic,
+                                                   const float *opacity, const float *feature,
+                                                   const int32_t *idx_sorted, const int32_t *tile_range, float bg,
+                                                   float *out, float *final_T, int32_t *ncontrib,
+                                                   msplat_stream_t stream);
+
+/* Its adjoint: dL_duv [rows,2], dL_dconic [rows,3], dL_dopacity [rows] (the
+ * camera's own opacity gradient) and dL_dfeature [rows,C] per stacked row,
+ * zero on entry (accumulated). */
+MSPLAT_API int msplat_batch_alpha_blending_backward(const void *plan, int B, int total_tiles, int64_t rows, int C,
+                                                    int feature_per_camera, const float *uv, const float *conic,
+                                                    const float *opacity, const float *feature,
+                                                    const int32_t *idx_sorted, const int32_t *tile_range, float bg,
+                                                    const float *final_T, const int32_t *ncontrib,
+                                                    const float *dL_dout, float *dL_duv, float *dL_dconic,
+                                                    float *dL_dopacity, float *dL_dfeature,
+                                                    msplat_stream_t stream);
+
+/* ------------------------------------------------------------------------ */
 /* Density-control statistics after a backward pass.  No kernel counterpart
  * in the reference; accumulates the screen-space gradient that its
  * alpha_blending returns for `ndc` (msplat/alpha_blending.py:107-110).

@@ -11,7 +11,7 @@ from .compute_sh import compute_sh
 from .sort_gaussian import sort_gaussian
 from .alpha_blending import alpha_blending
 from .rasterize import preprocess, rasterization, rasterization_sh
-from .batch import rasterization_batch, rasterization_sh_batch
+from .batch import rasterization_batch, rasterization_sh_batch, rasterization_sh_scenes
 from .density import DensityStats, prune_and_densify
 
 __all__ = [
@@ -26,6 +26,7 @@ __all__ = [
     "preprocess",
     "rasterization_batch",
     "rasterization_sh_batch",
+    "rasterization_sh_scenes",
     "DensityStats",
     "prune_and_densify",
 ]

@@ -65,6 +65,16 @@ _SIGNATURES = {
         _I, [_I, _I, _P, _P, _P, _P, _P, _F, _F, _I, _I, _P, _P, _P, _P, _P, _P, _P, _P]),
     "msplat_batch_preprocess_backward": (
         _I, [_I, _I, _P, _P, _P, _P, _I, _I, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _SZ, _P]),
+    "msplat_batch_plan_bytes": (_SZ, [_I]),
+    "msplat_batch_plan": (_I, [_I, _P, _P, _P, _P, _SZ, _P]),
+    "msplat_batch_sort_prepare_workspace_size": (_SZ, [_I, _I64]),
+    "msplat_batch_sort_prepare": (_I, [_P, _I, _I64, _P, _P, _P, _P, _P, _P, _P, _SZ, _P]),
+    "msplat_batch_sort_finish_workspace_size": (_SZ, [_I, _I64, _I]),
+    "msplat_batch_sort_finish": (_I, [_P, _I, _I64, _I, _I, _I64, _P, _P, _P, _P, _P, _SZ, _P]),
+    "msplat_batch_alpha_blending_forward": (
+        _I, [_P, _I, _I, _I, _I, _P, _P, _P, _P, _P, _P, _F, _P, _P, _P, _P]),
+    "msplat_batch_alpha_blending_backward": (
+        _I, [_P, _I, _I, _I64, _I, _I, _P, _P, _P, _P, _P, _P, _F, _P, _P, _P, _P, _P, _P, _P, _P]),
     "msplat_rasterize_preprocess_backward": (
         _I, [_I, _P, _P, _P, _P, _P, _I, _I, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _SZ, _P]),
 }

@@ -1,71 +1,92 @@
-"""Multi-camera rendering of one scene in one call.
+"""Multi-camera rendering in one key space.
 
 ``rasterization_sh_batch`` / ``rasterization_batch`` render B cameras (any
-mix of image sizes) of the same Gaussians and return B images; their
-backward sums every parameter gradient over the cameras and gives each
-camera its own intrinsic / extrinsic gradient.  Results are those of B
-single-camera calls (``rasterization_sh`` / ``rasterization``).
+mix of image sizes) of one scene, ``rasterization_sh_scenes`` B cameras of
+several scenes; each returns B images.  The backward sums every parameter
+gradient over a scene's cameras and gives each camera its own intrinsic /
+extrinsic gradient.  Results are those of B single-camera calls
+(``rasterization_sh`` / ``rasterization``): images bit for bit, gradients up
+to the order of float atomics.
 
-What is shared across the cameras: one preprocess kernel reads each
-Gaussian (and its SH rows) once and projects it into every camera
-(msplat_batch_preprocess_forward); one adjoint kernel sums the per-camera
-gradients per Gaussian (msplat_batch_preprocess_backward); the B tile
-sorts read their intersection counts with one host synchronisation.  The
-sort and blend of each camera run as in the single-camera path, spread over
-four side streams so that small cameras overlap on the device.
+The whole batch is a handful of launches, whatever B is:
+  * one preprocess kernel per scene reads each Gaussian (and its SH rows)
+    once and projects it into every camera of that scene
+    (msplat_batch_preprocess_forward);
+  * one sort orders every camera's intersections by (camera, tile, depth):
+    a segmented depth sort of all cameras' Gaussians, then a segmented sort
+    by tile of all cameras' lists (msplat_batch_sort_prepare / _finish);
+  * one blend grid covers every camera's tiles, forward and backward
+    (msplat_batch_alpha_blending_forward / _backward);
+  * one adjoint kernel per scene sums the per-camera gradients per Gaussian
+    (msplat_batch_preprocess_backward).
+With a `capacity` (the padded intersection count the sort may use) and a
+`status` tensor the call makes no host read, so a whole batched forward +
+backward can be captured in one CUDA graph.
 """
 from __future__ import annotations
 
 import threading
 from typing import Sequence
 
+import numpy as np
 import torch
 from torch import Tensor
 
 from . import _lib
 from . import _tensors as tt
-from .sort_gaussian import sort_gaussian_many
 
+SORT_TILE = 3072  # items per sort tile: capacities are multiples of it
 
+_PLANS: dict = {}
 _TLS = threading.local()
-N_SIDE_STREAMS = 4
 
 
-def side_streams(dev: torch.device) -> list:
-    """Streams on which the cameras' sorts and blends overlap (camera b on
-    stream b % N_SIDE_STREAMS); one set per device and host thread, so
-    concurrent callers (the server's workers) do not wait on each other."""
-    key = dev.index if dev.index is not None else torch.cuda.current_device()
-    cache = getattr(_TLS, "streams", None)
-    if cache is None:
-        cache = _TLS.streams = {}
-    if key not in cache:
-        cache[key] = [torch.cuda.Stream(device=dev) for _ in range(N_SIDE_STREAMS)]
-    return cache[key]
+def last_capacity() -> int | None:
+    """The padded intersection count the last eager batched call on this
+    thread sorted (a capacity that fits the same batch under capture)."""
+    return getattr(_TLS, "last_capacity", None)
 
 
-def _fork(streams: list, dev) -> torch.cuda.Stream:
-    """Makes every side stream wait for the work so far on the current one."""
-    main = torch.cuda.current_stream(dev)
-    ev = torch.cuda.Event()
-    ev.record(main)
-    for s in streams:
-        s.wait_event(ev)
-    return main
+class _Plan:
+    """A batch's layout (msplat_batch_plan) on the host and on the device.
+    Cached per (device, sizes, scene sizes, opacity offsets), so a call under
+    stream capture (after a warm-up call) makes no host-to-device copy."""
+
+    def __init__(self, dev, dims, npoints, op_off):
+        lib = _lib.load()
+        B = len(dims)
+        nbytes = int(lib.msplat_batch_plan_bytes(B))
+        host = np.zeros(nbytes, np.uint8)
+        sizes = np.zeros(5, np.int64)
+        d = np.ascontiguousarray(np.asarray(dims, np.int32).reshape(B, 2))
+        n = np.ascontiguousarray(np.asarray(npoints, np.int32))
+        o = np.ascontiguousarray(np.asarray(op_off, np.int64))
+        _lib.check(lib.msplat_batch_plan(B, d.ctypes.data, n.ctypes.data, o.ctypes.data, host.ctypes.data, nbytes,
+                                         sizes.ctypes.data), "batch_plan")
+        self.B = B
+        self.dims = [(int(w), int(h)) for w, h in d]
+        self.tiles, self.rows, self.pixels, self.depth_items, self.passes = (int(x) for x in sizes)
+        self.row_off = np.concatenate([[0], np.cumsum(n.astype(np.int64))]).tolist()
+        self.pix_off = np.concatenate([[0], np.cumsum(d[:, 0].astype(np.int64) * d[:, 1])]).tolist()
+        self.device = torch.from_numpy(host).to(dev)
 
 
-def _join(main: torch.cuda.Stream, streams: list) -> None:
-    for s in streams:
-        main.wait_stream(s)
+def _plan(dev, dims, npoints, op_off) -> _Plan:
+    key = (dev.index if dev.index is not None else torch.cuda.current_device(), tuple(dims), tuple(npoints),
+           tuple(op_off))
+    p = _PLANS.get(key)
+    if p is None:
+        if len(_PLANS) > 64:
+            _PLANS.clear()
+        p = _PLANS[key] = _Plan(dev, dims, npoints, op_off)
+    return p
 
 
 _DIMS: dict = {}
 
 
 def _dims(sizes, dev: torch.device) -> Tensor:
-    """[B, 2] int32 (W, H) on the device, cached per size list so that a call
-    under stream capture (after a warm-up call) makes no host-to-device
-    copy."""
+    """[B, 2] int32 (W, H) on the device, cached per size list."""
     key = (dev.index if dev.index is not None else torch.cuda.current_device(),
            tuple((int(w), int(h)) for w, h in sizes))
     if key not in _DIMS:
@@ -86,151 +107,251 @@ def _cameras(intrs: Tensor, extrs: Tensor, B: int):
     return torch.cat([intrs.reshape(B, 4), e[:, :12]], dim=1).contiguous()
 
 
-class _RasterizeBatch(torch.autograd.Function):
+def padded_capacity(n: int) -> int:
+    """A capacity of at least n intersections, as the batched sort needs it
+    (a multiple of its sort tile)."""
+    return -(-int(n) // SORT_TILE) * SORT_TILE
+
+
+def _sort(lib, plan, uv, depth, radius, conic, opacity, capacity, status, dev, st):
+    """The one-key-space sort; returns (idx_sorted, tile_range)."""
+    B = plan.B
+    counts = torch.empty(2 + B, dtype=torch.int64, device=dev)
+    ws_prep = _lib.workspace(lib.msplat_batch_sort_prepare_workspace_size(B, plan.depth_items), dev)
+    with _lib.stage("sort_gaussian_prepare"):
+        _lib.check(lib.msplat_batch_sort_prepare(
+            _lib.ptr(plan.device), B, plan.depth_items, _lib.ptr(uv), _lib.ptr(depth), _lib.ptr(radius),
+            _lib.ptr(conic), _lib.ptr(opacity), _lib.ptr(counts), _lib.ptr(ws_prep), ws_prep.numel(), st),
+            "batch_sort_prepare")
+    if capacity is None:
+        cap = int(counts[1].item())  # the one host read of an eager batch
+        _TLS.last_capacity = cap
+        if cap > 2**31 - 1:
+            raise RuntimeError(f"batched sort: {cap} intersections exceed the int32 range")
+        status = None
+    else:
+        cap = padded_capacity(capacity)
+        if status is None:
+            raise RuntimeError("a capacity-bounded batched sort needs a status tensor to report overflow in")
+        status = tt.i32(status, "status")
+    idx = torch.empty((max(cap, 1),), dtype=torch.int32, device=dev)
+    tr = torch.empty((plan.tiles, 2), dtype=torch.int32, device=dev)
+    ws = _lib.workspace(lib.msplat_batch_sort_finish_workspace_size(B, cap, plan.passes), dev)
+    with _lib.stage("sort_gaussian_finish"):
+        _lib.check(lib.msplat_batch_sort_finish(
+            _lib.ptr(plan.device), B, plan.depth_items, plan.tiles, plan.passes, cap, _lib.ptr(ws_prep),
+            _lib.ptr(idx), _lib.ptr(tr), _lib.ptr(status), _lib.ptr(ws), ws.numel(), st), "batch_sort_finish")
+    return idx, tr
+
+
+class _RasterizeScenes(torch.autograd.Function):
+    """Cameras grouped by scene.  meta = (scene sizes per camera group,
+    image sizes, bg, SH or feature mode, capacity, status); tensors = per
+    scene (xyz, scale, rotate, opacity, shs-or-feature), then intrs, extrs."""
+
     @staticmethod
-    def forward(ctx, xyz, scale, rotate, opacity, shs, feature, intrs, extrs, sizes, bg, capacities=None,
-                status=None):
-        xyz_c = tt.f32(xyz, "xyz", 3)
-        P = xyz_c.shape[0]
-        scale_c = tt.f32(scale, "scale", 3)
-        rot_c = tt.f32_aligned16(rotate, "rotate", 4)
-        op_c = tt.f32(opacity, "opacity")
-        if op_c.numel() != P or scale_c.shape[0] != P or rot_c.shape[0] != P:
-            raise RuntimeError("xyz, scale, rotate and opacity must have the same number of Gaussians")
+    def forward(ctx, meta, *tensors):
+        groups, sizes, bg, use_sh, capacity, status = meta
+        S = len(groups)
+        scene_t = [tensors[5 * s:5 * s + 5] for s in range(S)]
+        intrs, extrs = tensors[5 * S], tensors[5 * S + 1]
         B = len(sizes)
-        dev = xyz.device
+        dev = intrs.device
         cams = _cameras(intrs, extrs, B)
         dims = _dims(sizes, dev)
-        if shs is not None:
-            shs_c = tt.f32(shs, "shs")
-            if shs_c.dim() != 3 or shs_c.shape[0] != P:
-                raise RuntimeError(f"shs must be [P, C, D], got {tuple(shs.shape)}")
-            C, D, feat_c = int(shs_c.shape[1]), int(shs_c.shape[2]), None
-        else:
-            feat_c = tt.f32(feature, "feature")
-            if feat_c.dim() != 2 or feat_c.shape[0] != P:
-                raise RuntimeError(f"feature must be [P, C], got {tuple(feature.shape)}")
-            shs_c, C, D = None, int(feat_c.shape[1]), 0
-        uv = torch.empty((B, P, 2), dtype=torch.float32, device=dev)
-        depth = torch.empty((B, P, 1), dtype=torch.float32, device=dev)
-        conic = torch.empty((B, P, 3), dtype=torch.float32, device=dev)
-        radius = torch.empty((B, P), dtype=torch.int32, device=dev)
-        tiles = torch.empty((B, P), dtype=torch.int32, device=dev)
-        color = torch.empty((B, P, C), dtype=torch.float32, device=dev) if shs_c is not None else None
         lib = _lib.load()
         st = _lib.stream(dev)
+        prep, P_cam, op_off, ops = [], [], [], []
+        off = 0
+        for s, (xyz, scale, rot, op, sf) in enumerate(scene_t):
+            xyz_c = tt.f32(xyz, "xyz", 3)
+            P = xyz_c.shape[0]
+            scale_c = tt.f32(scale, "scale", 3)
+            rot_c = tt.f32_aligned16(rot, "rotate", 4)
+            op_c = tt.f32(op, "opacity").view(-1)
+            if op_c.numel() != P or scale_c.shape[0] != P or rot_c.shape[0] != P:
+                raise RuntimeError("xyz, scale, rotate and opacity must have the same number of Gaussians")
+            sf_c = tt.f32(sf, "shs" if use_sh else "feature")
+            if sf_c.shape[0] != P or sf_c.dim() != (3 if use_sh else 2):
+                raise RuntimeError(f"{'shs must be [P, C, D]' if use_sh else 'feature must be [P, C]'}, got "
+                                   f"{tuple(sf.shape)}")
+            prep.append((xyz_c, scale_c, rot_c, op_c, sf_c))
+            ops.append(op_c)
+            for _ in range(groups[s]):
+                P_cam.append(P)
+                op_off.append(off)
+            off += P
+        C = int(prep[0][4].shape[1])
+        D = int(prep[0][4].shape[2]) if use_sh else 0
+        if any(int(p[4].shape[1]) != C or (use_sh and int(p[4].shape[2]) != D) for p in prep):
+            raise RuntimeError("every scene of a batch must have the same channel count (and SH degree)")
+        plan = _plan(dev, [(int(w), int(h)) for w, h in sizes], P_cam, op_off)
+        op_all = ops[0] if S == 1 else torch.cat(ops)
+        R = plan.rows
+        uv = torch.empty((R, 2), dtype=torch.float32, device=dev)
+        depth = torch.empty((R, 1), dtype=torch.float32, device=dev)
+        conic = torch.empty((R, 3), dtype=torch.float32, device=dev)
+        radius = torch.empty((R,), dtype=torch.int32, device=dev)
+        tiles = torch.empty((R,), dtype=torch.int32, device=dev)
+        color = torch.empty((R, C), dtype=torch.float32, device=dev) if use_sh else None
+        b0 = 0
         with _lib.stage("batch_preprocess_forward"):
-            _lib.check(lib.msplat_batch_preprocess_forward(
-                P, B, _lib.ptr(xyz_c), _lib.ptr(scale_c), _lib.ptr(rot_c), _lib.ptr(cams), _lib.ptr(dims),
-                0.0, 1.3, C if shs_c is not None else 0, D, _lib.ptr(shs_c), _lib.ptr(uv), _lib.ptr(depth),
-                _lib.ptr(conic), _lib.ptr(radius), _lib.ptr(tiles), _lib.ptr(color), st),
-                "batch_preprocess_forward")
-        streams = side_streams(dev)
-        # culled lists, as the single-camera calls (same images and gradients)
-        sorted_ = sort_gaussian_many([(uv[b], depth[b], int(w), int(h), radius[b], tiles[b], conic[b], op_c)
-                                      for b, (w, h) in enumerate(sizes)], streams, capacities, status)
-        outs, finals = [], []
-        main = _fork(streams, dev)
+            for s, (xyz_c, scale_c, rot_c, op_c, sf_c) in enumerate(prep):
+                Bs, P = groups[s], xyz_c.shape[0]
+                if Bs == 0:
+                    continue
+                r0 = plan.row_off[b0]
+                _lib.check(lib.msplat_batch_preprocess_forward(
+                    P, Bs, _lib.ptr(xyz_c), _lib.ptr(scale_c), _lib.ptr(rot_c), _lib.ptr(cams[b0:b0 + Bs]),
+                    _lib.ptr(dims[b0:b0 + Bs]), 0.0, 1.3, C if use_sh else 0, D, _lib.ptr(sf_c) if use_sh else None,
+                    _lib.ptr(uv[r0:]), _lib.ptr(depth[r0:]), _lib.ptr(conic[r0:]), _lib.ptr(radius[r0:]),
+                    _lib.ptr(tiles[r0:]), _lib.ptr(color[r0:]) if use_sh else None, st), "batch_preprocess_forward")
+                b0 += Bs
+        # features: per camera (SH colour, stacked like uv) or per scene
+        feat = color if use_sh else (prep[0][4] if S == 1 else torch.cat([p[4] for p in prep]))
+        idx, tr = _sort(lib, plan, uv, depth, radius, conic, op_all, capacity, status, dev, st)
+        out = torch.empty((C * plan.pixels,), dtype=torch.float32, device=dev)
+        final_T = torch.empty((plan.pixels,), dtype=torch.float32, device=dev)
+        ncontrib = torch.empty((plan.pixels,), dtype=torch.int32, device=dev)
         with _lib.stage("alpha_blending_forward"):
-            for b, (w, h) in enumerate(sizes):
-                w, h = int(w), int(h)
-                feat_b = color[b] if color is not None else feat_c
-                idx, tr = sorted_[b]
-                with torch.cuda.stream(streams[b % len(streams)]):
-                    out = torch.empty((C, h, w), dtype=torch.float32, device=dev)
-                    final_T = torch.empty((h, w), dtype=torch.float32, device=dev)
-                    ncontrib = torch.empty((h, w), dtype=torch.int32, device=dev)
-                    if C > 0:
-                        _lib.check(lib.msplat_alpha_blending_forward(
-                            P, C, _lib.ptr(uv[b]), _lib.ptr(conic[b]), _lib.ptr(op_c), _lib.ptr(feat_b),
-                            _lib.ptr(idx), _lib.ptr(tr), float(bg), w, h, _lib.ptr(out), _lib.ptr(final_T),
-                            _lib.ptr(ncontrib), _lib.stream(dev)), "alpha_blending_forward")
-                    for x in (out, final_T, ncontrib):
-                        x.record_stream(main)
-                outs.append(out)
-                finals.append((final_T, ncontrib))
-        _join(main, streams)
-        ctx.sizes, ctx.bg, ctx.C, ctx.D = [(int(w), int(h)) for w, h in sizes], float(bg), C, D
-        ctx.sorted, ctx.finals = sorted_, finals
-        ctx.intr_shape, ctx.extr_shape, ctx.op_shape = intrs.shape, extrs.shape, opacity.shape
-        ctx.save_for_backward(xyz_c, scale_c, rot_c, op_c, shs_c, feat_c, cams, uv, depth, conic, radius, color)
-        return tuple(outs)
+            _lib.check(lib.msplat_batch_alpha_blending_forward(
+                _lib.ptr(plan.device), B, plan.tiles, C, 1 if use_sh else 0, _lib.ptr(uv), _lib.ptr(conic),
+                _lib.ptr(op_all), _lib.ptr(feat), _lib.ptr(idx), _lib.ptr(tr), float(bg), _lib.ptr(out),
+                _lib.ptr(final_T), _lib.ptr(ncontrib), st), "batch_alpha_blending_forward")
+        imgs = tuple(out[C * plan.pix_off[b]:C * plan.pix_off[b + 1]].view(C, h, w)
+                     for b, (w, h) in enumerate(plan.dims))
+        ctx.meta = (groups, plan, bg, use_sh, C, D)
+        ctx.intr_shape, ctx.extr_shape = intrs.shape, extrs.shape
+        ctx.op_shapes = [t[3].shape for t in scene_t]
+        flat = [x for p in prep for x in p]
+        ctx.save_for_backward(*flat, cams, uv, depth, conic, radius, color, feat, op_all, idx, tr, final_T, ncontrib)
+        return imgs
 
     @staticmethod
     def backward(ctx, *grads):
-        xyz, scale, rot, op, shs, feat, cams, uv, depth, conic, radius, color = ctx.saved_tensors
-        B, P, C, D = len(ctx.sizes), xyz.shape[0], ctx.C, ctx.D
-        dev = xyz.device
+        groups, plan, bg, use_sh, C, D = ctx.meta
+        S = len(groups)
+        saved = ctx.saved_tensors
+        prep = [saved[5 * s:5 * s + 5] for s in range(S)]
+        cams, uv, depth, conic, radius, color, feat, op_all, idx, tr, final_T, ncontrib = saved[5 * S:]
+        B, R = plan.B, plan.rows
+        dev = cams.device
         lib = _lib.load()
         st = _lib.stream(dev)
-        dL_duv = torch.zeros((B, P, 2), dtype=torch.float32, device=dev)
-        dL_dconic = torch.zeros((B, P, 3), dtype=torch.float32, device=dev)
-        dL_dop = torch.zeros((B, P), dtype=torch.float32, device=dev)
-        dL_dcol = torch.zeros((B, P, C), dtype=torch.float32, device=dev)
-        streams = side_streams(dev)
-        main = _fork(streams, dev)
+        gout = torch.empty((C * plan.pixels,), dtype=torch.float32, device=dev)
+        for b, g in enumerate(grads):
+            seg = gout[C * plan.pix_off[b]:C * plan.pix_off[b + 1]]
+            if g is None:
+                seg.zero_()
+            else:
+                seg.copy_(g.reshape(-1))
+        dL_duv = torch.zeros((R, 2), dtype=torch.float32, device=dev)
+        dL_dconic = torch.zeros((R, 3), dtype=torch.float32, device=dev)
+        dL_dop = torch.zeros((R,), dtype=torch.float32, device=dev)
+        dL_dfeat = torch.zeros((R, C), dtype=torch.float32, device=dev)
         with _lib.stage("alpha_blending_backward"):
-            for b, (w, h) in enumerate(ctx.sizes):
-                g = grads[b]
-                if g is None or C == 0:
-                    continue
-                idx, tr = ctx.sorted[b]
-                final_T, ncontrib = ctx.finals[b]
-                feat_b = color[b] if color is not None else feat
-                with torch.cuda.stream(streams[b % len(streams)]):
-                    g = g.float().contiguous()
-                    _lib.check(lib.msplat_alpha_blending_backward(
-                        P, C, _lib.ptr(uv[b]), _lib.ptr(conic[b]), _lib.ptr(op), _lib.ptr(feat_b), _lib.ptr(idx),
-                        _lib.ptr(tr), ctx.bg, w, h, _lib.ptr(final_T), _lib.ptr(ncontrib), _lib.ptr(g),
-                        _lib.ptr(dL_duv[b]), _lib.ptr(dL_dconic[b]), _lib.ptr(dL_dop[b]), _lib.ptr(dL_dcol[b]),
-                        _lib.stream(dev)), "alpha_blending_backward")
-        _join(main, streams)
-        want_i, want_e = ctx.needs_input_grad[6], ctx.needs_input_grad[7]
-        sh = shs is not None
-        dL_dxyz = torch.empty((P, 3), dtype=torch.float32, device=dev)
-        dL_dscale = torch.empty((P, 3), dtype=torch.float32, device=dev)
-        dL_drot = torch.empty((P, 4), dtype=torch.float32, device=dev)
-        dL_dopacity = torch.empty((P,), dtype=torch.float32, device=dev)
-        dL_dshs = torch.empty((P, C, D), dtype=torch.float32, device=dev) if sh else None
+            _lib.check(lib.msplat_batch_alpha_blending_backward(
+                _lib.ptr(plan.device), B, plan.tiles, R, C, 1 if use_sh else 0, _lib.ptr(uv), _lib.ptr(conic),
+                _lib.ptr(op_all), _lib.ptr(feat), _lib.ptr(idx), _lib.ptr(tr), float(bg), _lib.ptr(final_T),
+                _lib.ptr(ncontrib), _lib.ptr(gout), _lib.ptr(dL_duv), _lib.ptr(dL_dconic), _lib.ptr(dL_dop),
+                _lib.ptr(dL_dfeat), st), "batch_alpha_blending_backward")
+        n_in = 5 * S + 2
+        want_i, want_e = ctx.needs_input_grad[1 + 5 * S], ctx.needs_input_grad[2 + 5 * S]
         dL_dcams = torch.empty((B, 16), dtype=torch.float32, device=dev) if (want_i or want_e) else None
-        ws = _lib.workspace(lib.msplat_batch_preprocess_workspace_size(P, B, C if sh else 0, D), dev)
+        out = [None] * n_in
+        b0 = 0
         with _lib.stage("batch_preprocess_backward"):
-            _lib.check(lib.msplat_batch_preprocess_backward(
-                P, B, _lib.ptr(xyz), _lib.ptr(scale), _lib.ptr(rot), _lib.ptr(cams), C if sh else 0, D,
-                _lib.ptr(shs), _lib.ptr(depth), _lib.ptr(radius), _lib.ptr(dL_duv), _lib.ptr(dL_dconic),
-                _lib.ptr(dL_dcol) if sh else None, _lib.ptr(dL_dop), _lib.ptr(dL_dxyz), _lib.ptr(dL_dscale),
-                _lib.ptr(dL_drot), _lib.ptr(dL_dshs), _lib.ptr(dL_dopacity), _lib.ptr(dL_dcams), _lib.ptr(ws),
-                ws.numel(), st), "batch_preprocess_backward")
-        dL_dfeature = dL_dcol.sum(0) if (not sh and ctx.needs_input_grad[5]) else None
-        dL_dintrs = dL_dcams[:, :4].reshape(ctx.intr_shape) if want_i else None
-        dL_dextrs = None
+            for s, (xyz, scale, rot, op, sf) in enumerate(prep):
+                Bs, P = groups[s], xyz.shape[0]
+                gx = torch.zeros((P, 3), dtype=torch.float32, device=dev)
+                gs = torch.zeros((P, 3), dtype=torch.float32, device=dev)
+                gr = torch.zeros((P, 4), dtype=torch.float32, device=dev)
+                go = torch.zeros((P,), dtype=torch.float32, device=dev)
+                gsh = torch.zeros((P, C, D), dtype=torch.float32, device=dev) if use_sh else None
+                gf = None
+                if Bs > 0:
+                    r0, r1 = plan.row_off[b0], plan.row_off[b0 + Bs]
+                    ws = _lib.workspace(lib.msplat_batch_preprocess_workspace_size(P, Bs, C if use_sh else 0, D), dev)
+                    _lib.check(lib.msplat_batch_preprocess_backward(
+                        P, Bs, _lib.ptr(xyz), _lib.ptr(scale), _lib.ptr(rot), _lib.ptr(cams[b0:b0 + Bs]),
+                        C if use_sh else 0, D, _lib.ptr(sf) if use_sh else None, _lib.ptr(depth[r0:r1]),
+                        _lib.ptr(radius[r0:r1]), _lib.ptr(dL_duv[r0:r1]), _lib.ptr(dL_dconic[r0:r1]),
+                        _lib.ptr(dL_dfeat[r0:r1]) if use_sh else None, _lib.ptr(dL_dop[r0:r1]), _lib.ptr(gx),
+                        _lib.ptr(gs), _lib.ptr(gr), _lib.ptr(gsh), _lib.ptr(go),
+                        _lib.ptr(dL_dcams[b0:b0 + Bs]) if dL_dcams is not None else None, _lib.ptr(ws), ws.numel(),
+                        st), "batch_preprocess_backward")
+                    if not use_sh and ctx.needs_input_grad[1 + 5 * s + 4]:
+                        gf = dL_dfeat[r0:r1].view(Bs, P, C).sum(0)
+                elif not use_sh:
+                    gf = torch.zeros_like(sf)
+                out[5 * s:5 * s + 5] = [gx, gs, gr, go.view(ctx.op_shapes[s]), gsh if use_sh else gf]
+                b0 += Bs
+        if want_i:
+            out[5 * S] = dL_dcams[:, :4].reshape(ctx.intr_shape)
         if want_e:
             g = dL_dcams[:, 4:]
-            if ctx.extr_shape[-2:] == (4, 4):
+            if tuple(ctx.extr_shape[-2:]) == (4, 4):
                 g = torch.cat([g, torch.zeros((B, 4), dtype=g.dtype, device=dev)], dim=1)
-            dL_dextrs = g.reshape(ctx.extr_shape)
-        return (dL_dxyz, dL_dscale, dL_drot, dL_dopacity.view(ctx.op_shape), dL_dshs, dL_dfeature, dL_dintrs,
-                dL_dextrs, None, None, None, None)
+            out[5 * S + 1] = g.reshape(ctx.extr_shape)
+        return (None, *out)
+
+
+def _apply(scenes, scene_of, intrs, extrs, sizes, bg, use_sh, capacity, status):
+    B = len(sizes)
+    if len(scene_of) != B:
+        raise RuntimeError("scene_of must name a scene for every camera")
+    if B == 0:
+        return []
+    order = sorted(range(B), key=lambda b: int(scene_of[b]))  # cameras grouped by scene (stable)
+    groups = [0] * len(scenes)
+    for b in order:
+        groups[int(scene_of[b])] += 1
+    inv = list(order) != list(range(B))
+    if inv:
+        perm = torch.as_tensor(order, device=intrs.device)
+        intrs, extrs = intrs.reshape(B, -1)[perm], extrs.reshape(B, *extrs.shape[-2:])[perm]
+        sizes = [sizes[b] for b in order]
+    flat = [t for sc in scenes for t in sc]
+    meta = (groups, tuple((int(w), int(h)) for w, h in sizes), float(bg), use_sh, capacity, status)
+    imgs = _RasterizeScenes.apply(meta, *flat, intrs, extrs)
+    if not inv:
+        return list(imgs)
+    out = [None] * B
+    for k, b in enumerate(order):
+        out[b] = imgs[k]
+    return out
 
 
 def rasterization_sh_batch(xyz: Tensor, scale: Tensor, rotate: Tensor, opacity: Tensor, shs: Tensor,
                            intrs: Tensor, extrs: Tensor, sizes: Sequence[tuple], bg: float = 0.0, *,
-                           capacities: Sequence[int] | None = None, status: Tensor | None = None) -> list:
+                           capacity: int | None = None, status: Tensor | None = None) -> list:
     """Renders B cameras of one scene with colour from SH coefficients on
     each camera's view directions (``rasterization_sh`` per camera).
     intrs [B, 4], extrs [B, 3, 4], sizes [(W, H)] * B.  Returns B images
-    [C, H_b, W_b].  With per-camera intersection `capacities` and a [B]
-    int32 `status` the call makes no host read (CUDA-graph capturable);
-    status[b] = 1 marks a camera whose capacity was too small."""
-    return list(_RasterizeBatch.apply(xyz, scale, rotate, opacity, shs, None, intrs, extrs, tuple(sizes), bg,
-                                      capacities, status))
+    [C, H_b, W_b].  With a `capacity` (intersections the sort may hold over
+    all cameras, padded) and a [1] int32 `status` the call makes no host
+    read (CUDA-graph capturable); status = 1 marks a capacity that was too
+    small (the images are then not valid)."""
+    return _apply([(xyz, scale, rotate, opacity, shs)], [0] * len(sizes), intrs, extrs, sizes, bg, True, capacity,
+                  status)
 
 
 def rasterization_batch(xyz: Tensor, scale: Tensor, rotate: Tensor, opacity: Tensor, feature: Tensor,
                         intrs: Tensor, extrs: Tensor, sizes: Sequence[tuple], bg: float = 0.0, *,
-                        capacities: Sequence[int] | None = None, status: Tensor | None = None) -> list:
+                        capacity: int | None = None, status: Tensor | None = None) -> list:
     """Renders B cameras of one scene with the same per-Gaussian features
     (``rasterization`` per camera).  Returns B images [C, H_b, W_b];
-    `capacities` / `status` as for ``rasterization_sh_batch``."""
-    return list(_RasterizeBatch.apply(xyz, scale, rotate, opacity, None, feature, intrs, extrs, tuple(sizes), bg,
-                                      capacities, status))
+    `capacity` / `status` as for ``rasterization_sh_batch``."""
+    return _apply([(xyz, scale, rotate, opacity, feature)], [0] * len(sizes), intrs, extrs, sizes, bg, False,
+                  capacity, status)
+
+
+def rasterization_sh_scenes(scenes: Sequence[tuple], scene_of: Sequence[int], intrs: Tensor, extrs: Tensor,
+                            sizes: Sequence[tuple], bg: float = 0.0, *, capacity: int | None = None,
+                            status: Tensor | None = None) -> list:
+    """Renders B cameras of several scenes in one batch: scenes is a list of
+    (xyz, scale, rotate, opacity, shs), scene_of[b] the scene of camera b
+    (any order).  Returns B images; each scene's parameters get the
+    gradients summed over its cameras.  `capacity` / `status` as for
+    ``rasterization_sh_batch``."""
+    return _apply(list(scenes), list(scene_of), intrs, extrs, sizes, bg, True, capacity, status)

@@ -25,9 +25,58 @@
 //  * in the C <= 4 kernels each warp owns an 8-column block of the tile and
 //    walks only the gathered Gaussians whose alpha >= 1/255 ellipse reaches
 //    that block (a conservative per-Gaussian mask built in the gather).
+#include "batch_plan.cuh"
 #include "cull.cuh"
 
 namespace msplat {
+
+// A multi-camera batch (batch_plan.cuh): one grid over every camera's
+// tiles.  Per block, the camera of its tile gives the image size and the
+// offsets into the stacked per-camera arrays; features are stacked per
+// camera (feat_per_cam, rows like uv) or per scene (rows like opacity).
+struct BlendBatch {
+    BatchPlanView pv;
+    int feat_per_cam;
+};
+
+// Where a block renders: its tile (coordinates, row of tile_range, split
+// part), the image size, and in a multi-camera batch (BATCH) the offsets of
+// the tile's camera into the stacked arrays (zero for a single camera).
+struct BlendSite {
+    int tx, ty, tidx, part, W, H;
+    int64_t row_off, op_off, feat_off, pix_off;
+};
+
+template <bool BATCH, int SPLIT>
+__device__ __forceinline__ BlendSite blend_site(const BlendBatch &bb, int W, int H) {
+    BlendSite s;
+    if (BATCH) {
+        const int t = blockIdx.x;
+        const int b = batch_camera_of_tile(bb.pv, t);
+        const BatchCam &c = bb.pv.cams[b];
+        s.W = c.W;
+        s.H = c.H;
+        const int lt = t - c.tile_off;
+        s.ty = lt / c.gx;
+        s.tx = lt - s.ty * c.gx;
+        s.tidx = t;
+        s.part = 0;
+        s.row_off = c.row_off;
+        s.op_off = c.op_off;
+        s.feat_off = bb.feat_per_cam ? c.row_off : c.op_off;
+        s.pix_off = c.pix_off;
+    } else {
+        const int gxn = (W + kTile - 1) / kTile;
+        s.W = W;
+        s.H = H;
+        s.tx = blockIdx.x;
+        s.ty = blockIdx.y / SPLIT;
+        s.part = blockIdx.y % SPLIT;
+        s.tidx = s.ty * gxn + s.tx;
+        s.row_off = s.op_off = s.feat_off = s.pix_off = 0;
+    }
+    return s;
+}
 
 constexpr int kBlendThreads = kTilePixels;  // 256: one thread per pixel
 constexpr int kBatch = kBlendThreads;
@@ -167,26 +216,36 @@ __device__ __forceinline__ int gather_batch(bool valid, int j, const int32_t *__
     return total;
 }
 
-template <int CMAX>
+template <int CMAX, bool BATCH = false>
 __global__ void __launch_bounds__(kBlendThreads)
 blend_fwd_kernel(int P, int C, int c0, const float2 *__restrict__ uv, const float *__restrict__ conic,
                  const float *__restrict__ opacity, const float *__restrict__ feature,
                  const int32_t *__restrict__ idx_sorted, const int2 *__restrict__ tile_range, float bg,
                  int W, int H, float *__restrict__ out, float *__restrict__ final_T,
-                 int32_t *__restrict__ ncontrib) {
+                 int32_t *__restrict__ ncontrib, BlendBatch bb = {}) {
     __shared__ BlendRec srec[kBatch];
     __shared__ float sfeat[CMAX * kBatch];
     __shared__ int sgid[kBatch];
     __shared__ int swarp[kBlendThreads / 32];
     const int nc = min(CMAX, C - c0);
-    const int gxn = (W + kTile - 1) / kTile;
-    const int tile = blockIdx.y * gxn + blockIdx.x;
-    const int px = blockIdx.x * kTile + (threadIdx.x & (kTile - 1));
-    const int py = blockIdx.y * kTile + (threadIdx.x >> 4);
+    const BlendSite site = blend_site<BATCH, 1>(bb, W, H);
+    if (BATCH) {
+        W = site.W;
+        H = site.H;
+        uv += site.row_off;
+        conic += 3 * site.row_off;
+        opacity += site.op_off;
+        feature += (size_t)C * site.feat_off;
+        out += (size_t)C * site.pix_off;
+        final_T += site.pix_off;
+        ncontrib += site.pix_off;
+    }
+    const int px = site.tx * kTile + (threadIdx.x & (kTile - 1));
+    const int py = site.ty * kTile + (threadIdx.x >> 4);
     const bool inside = px < W && py < H;
     const float fx = (float)px, fy = (float)py;
-    const float bx0 = (float)(blockIdx.x * kTile), by0 = (float)(blockIdx.y * kTile);
-    const int2 range = tile_range[tile];
+    const float bx0 = (float)(site.tx * kTile), by0 = (float)(site.ty * kTile);
+    const int2 range = tile_range[site.tidx];
 
     bool done = !inside;
     float T = 1.0f;
@@ -251,6 +310,7 @@ __device__ __forceinline__ float warp_reduce_scatter16(float (&v)[16]) {
 
 constexpr int kBwdC = 10;  // channels per backward pass (6 + 10 = 16 values)
 
+template <bool BATCH = false>
 __global__ void __launch_bounds__(kBlendThreads)
 blend_bwd_kernel(int P, int C, int c0, const float2 *__restrict__ uv, const float *__restrict__ conic,
                  const float *__restrict__ opacity, const float *__restrict__ feature,
@@ -258,21 +318,35 @@ blend_bwd_kernel(int P, int C, int c0, const float2 *__restrict__ uv, const floa
                  int W, int H, const float *__restrict__ final_T, const int32_t *__restrict__ ncontrib,
                  const float *__restrict__ dL_dout, float *__restrict__ dL_duv,
                  float *__restrict__ dL_dconic, float *__restrict__ dL_dopacity,
-                 float *__restrict__ dL_dfeature) {
+                 float *__restrict__ dL_dfeature, BlendBatch bb = {}) {
     __shared__ BlendRec srec[kBatch];
     __shared__ float sfeat[kBwdC * kBatch];
     __shared__ int sgid[kBatch];
     __shared__ int swarp[kBlendThreads / 32];
     __shared__ int smax;
     const int nc = min(kBwdC, C - c0);
-    const int gxn = (W + kTile - 1) / kTile;
-    const int tile = blockIdx.y * gxn + blockIdx.x;
-    const int px = blockIdx.x * kTile + (threadIdx.x & (kTile - 1));
-    const int py = blockIdx.y * kTile + (threadIdx.x >> 4);
+    const BlendSite site = blend_site<BATCH, 1>(bb, W, H);
+    if (BATCH) {
+        W = site.W;
+        H = site.H;
+        uv += site.row_off;
+        conic += 3 * site.row_off;
+        opacity += site.op_off;
+        feature += (size_t)C * site.feat_off;
+        final_T += site.pix_off;
+        ncontrib += site.pix_off;
+        dL_dout += (size_t)C * site.pix_off;
+        dL_duv += 2 * site.row_off;
+        dL_dconic += 3 * site.row_off;
+        dL_dopacity += site.row_off;
+        dL_dfeature += (size_t)C * site.row_off;
+    }
+    const int px = site.tx * kTile + (threadIdx.x & (kTile - 1));
+    const int py = site.ty * kTile + (threadIdx.x >> 4);
     const bool inside = px < W && py < H;
     const float fx = (float)px, fy = (float)py;
-    const float bx0 = (float)(blockIdx.x * kTile), by0 = (float)(blockIdx.y * kTile);
-    const int2 range = tile_range[tile];
+    const float bx0 = (float)(site.tx * kTile), by0 = (float)(site.ty * kTile);
+    const int2 range = tile_range[site.tidx];
     const int pix = py * W + px;
     const int lane = threadIdx.x & 31;
 
@@ -495,31 +569,42 @@ __device__ __forceinline__ int gather_small(int base, int dir, int lo, int hi,
 // SPLIT: a tile is rendered by SPLIT blocks of kTile / SPLIT rows each
 // (grid.y = tiles down x SPLIT), each gathering the tile's list against
 // its own part.
-template <int C, int NPIX, int SPLIT>
+template <int C, int NPIX, int SPLIT, bool BATCH = false>
 __global__ void MSPLAT_FWD_BOUNDS(kTilePixels / NPIX / SPLIT)
 blend_fwd_small_kernel(int P, const float2 *__restrict__ uv, const float *__restrict__ conic,
                        const float *__restrict__ opacity, const float *__restrict__ feature,
                        const int32_t *__restrict__ idx_sorted, const int2 *__restrict__ tile_range, float bg,
                        int W, int H, float *__restrict__ out, float *__restrict__ final_T,
-                       int32_t *__restrict__ ncontrib) {
-    constexpr int ROWS = kTile / SPLIT, NT = kTile * ROWS / NPIX, BATCH = NT * NPIX;
+                       int32_t *__restrict__ ncontrib, BlendBatch bb = {}) {
+    static_assert(!BATCH || SPLIT == 1, "batched blends render whole tiles");
+    constexpr int ROWS = kTile / SPLIT, NT = kTile * ROWS / NPIX, BATCH_N = NT * NPIX;
     static_assert(4 * NPIX <= ROWS, "a warp block of 4 NPIX rows must fit the block's rows");
-    __shared__ float4 sA[BATCH], sB[BATCH], sF[BATCH];
-    __shared__ unsigned char sM[BATCH];
+    __shared__ float4 sA[BATCH_N], sB[BATCH_N], sF[BATCH_N];
+    __shared__ unsigned char sM[BATCH_N];
     __shared__ int scan[NT / 32];
-    const int gxn = (W + kTile - 1) / kTile;
-    const int ty = blockIdx.y / SPLIT;
-    const int2 range = tile_range[ty * gxn + blockIdx.x];
+    const BlendSite site = blend_site<BATCH, SPLIT>(bb, W, H);
+    if (BATCH) {
+        W = site.W;
+        H = site.H;
+        uv += site.row_off;
+        conic += 3 * site.row_off;
+        opacity += site.op_off;
+        feature += (size_t)C * site.feat_off;
+        out += (size_t)C * site.pix_off;
+        final_T += site.pix_off;
+        ncontrib += site.pix_off;
+    }
+    const int2 range = tile_range[site.tidx];
     // warp w owns the block of 8 columns (8 (w % 2) ...) by 4 NPIX rows
     // (4 NPIX (w / 2) ...) that bit w of a gathered entry's mask covers;
     // lane l takes column l % 8 and rows (l / 8) NPIX + i of it
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int row0 = ty * kTile + (blockIdx.y % SPLIT) * ROWS;
-    const int px = blockIdx.x * kTile + 8 * (warp & 1) + (lane & 7);
+    const int row0 = site.ty * kTile + site.part * ROWS;
+    const int px = site.tx * kTile + 8 * (warp & 1) + (lane & 7);
     const int py0 = row0 + 4 * NPIX * (warp >> 1) + (lane >> 3) * NPIX;
     const unsigned wbit = 1u << warp;
     const float fx = (float)px;
-    const float bx0 = (float)(blockIdx.x * kTile), by0 = (float)row0;
+    const float bx0 = (float)(site.tx * kTile), by0 = (float)row0;
     float fy[NPIX], T[NPIX], F[NPIX][4];
     int last[NPIX];
     bool done[NPIX];
@@ -533,7 +618,7 @@ blend_fwd_small_kernel(int P, const float2 *__restrict__ uv, const float *__rest
 #pragma unroll
         for (int q = 0; q < 4; ++q) F[i][q] = 0.0f;
     }
-    for (int start = range.x; start < range.y; start += BATCH) {
+    for (int start = range.x; start < range.y; start += BATCH_N) {
         bool all_done = true;
 #pragma unroll
         for (int i = 0; i < NPIX; ++i) all_done &= done[i];
@@ -655,7 +740,7 @@ constexpr int kFewLanes = MSPLAT_FEW_LANES;
 
 // BG: the background is nonzero, so dL/dalpha has the term
 // -T_final / (1 - alpha) * sum_c bg dL/dpix_c (compiled out for bg == 0).
-template <int C, int NPIX, bool BG, int SPLIT>
+template <int C, int NPIX, bool BG, int SPLIT, bool BATCH = false>
 __global__ void MSPLAT_BWD_BOUNDS(kTilePixels / NPIX / SPLIT)
 blend_bwd_small_kernel(int P, const float2 *__restrict__ uv, const float *__restrict__ conic,
                        const float *__restrict__ opacity, const float *__restrict__ feature,
@@ -663,26 +748,42 @@ blend_bwd_small_kernel(int P, const float2 *__restrict__ uv, const float *__rest
                        int W, int H, const float *__restrict__ final_T, const int32_t *__restrict__ ncontrib,
                        const float *__restrict__ dL_dout, float *__restrict__ dL_duv,
                        float *__restrict__ dL_dconic, float *__restrict__ dL_dopacity,
-                       float *__restrict__ dL_dfeature) {
-    constexpr int ROWS = kTile / SPLIT, NT = kTile * ROWS / NPIX, BATCH = NT * NPIX;
+                       float *__restrict__ dL_dfeature, BlendBatch bb = {}) {
+    static_assert(!BATCH || SPLIT == 1, "batched blends render whole tiles");
+    constexpr int ROWS = kTile / SPLIT, NT = kTile * ROWS / NPIX, BATCH_N = NT * NPIX;
     static_assert(4 * NPIX <= ROWS, "a warp block of 4 NPIX rows must fit the block's rows");
     constexpr int NV = 6 + C;
-    __shared__ float4 sA[BATCH], sB[BATCH], sF[BATCH];
-    __shared__ int sG[BATCH];
-    __shared__ unsigned char sM[BATCH];
+    __shared__ float4 sA[BATCH_N], sB[BATCH_N], sF[BATCH_N];
+    __shared__ int sG[BATCH_N];
+    __shared__ unsigned char sM[BATCH_N];
     __shared__ int scan[NT / 32];
     __shared__ int smax;
-    const int gxn = (W + kTile - 1) / kTile;
-    const int ty = blockIdx.y / SPLIT;
-    const int2 range = tile_range[ty * gxn + blockIdx.x];
+    const BlendSite site = blend_site<BATCH, SPLIT>(bb, W, H);
+    if (BATCH) {
+        W = site.W;
+        H = site.H;
+        uv += site.row_off;
+        conic += 3 * site.row_off;
+        opacity += site.op_off;
+        feature += (size_t)C * site.feat_off;
+        // per-camera gradient rows (opacity too: the camera's own row)
+        final_T += site.pix_off;
+        ncontrib += site.pix_off;
+        dL_dout += (size_t)C * site.pix_off;
+        dL_duv += 2 * site.row_off;
+        dL_dconic += 3 * site.row_off;
+        dL_dopacity += site.row_off;
+        dL_dfeature += (size_t)C * site.row_off;
+    }
+    const int2 range = tile_range[site.tidx];
     // pixel layout, warp blocks and SPLIT as in blend_fwd_small_kernel
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int row0 = ty * kTile + (blockIdx.y % SPLIT) * ROWS;
-    const int px = blockIdx.x * kTile + 8 * (warp & 1) + (lane & 7);
+    const int row0 = site.ty * kTile + site.part * ROWS;
+    const int px = site.tx * kTile + 8 * (warp & 1) + (lane & 7);
     const int py0 = row0 + 4 * NPIX * (warp >> 1) + (lane >> 3) * NPIX;
     const unsigned wbit = 1u << warp;
     const float fx = (float)px;
-    const float bx0 = (float)(blockIdx.x * kTile), by0 = (float)row0;
+    const float bx0 = (float)(site.tx * kTile), by0 = (float)row0;
     const int vi = scatter_slot<NV>(lane);  // the gradient slot this lane sends after a reduction
 
     // Per pixel: the colour recursion of the reference (accum_rec =
@@ -724,8 +825,8 @@ blend_bwd_small_kernel(int P, const float2 *__restrict__ uv, const float *__rest
     // Entries at or past this warp's largest ncontrib touch none of its pixels.
     const int warp_last = mylast;
 
-    for (int bend = end; bend > range.x; bend -= BATCH) {
-        const int bstart = max(range.x, bend - BATCH);
+    for (int bend = end; bend > range.x; bend -= BATCH_N) {
+        const int bstart = max(range.x, bend - BATCH_N);
         const int n = gather_small<C, NPIX, true, ROWS>(bend - 1, -1, bstart, bend, idx_sorted, uv, conic,
                                                         opacity, feature, bx0, by0, sA, sB, sF, sG, sM, scan,
                                                         false);
@@ -844,6 +945,32 @@ blend_grad_finish_kernel(int P, const float *__restrict__ conic, const float *__
     dL_dconic[3 * g + 2] = -0.5f * o * syy;
 }
 
+// blend_grad_finish_kernel over the stacked rows of a batch: row r is
+// Gaussian r - row_off of its camera, whose opacity is opacity[op_off + g].
+__global__ void __launch_bounds__(256)
+batch_blend_grad_finish_kernel(BatchPlanView pv, int64_t rows, const float *__restrict__ conic,
+                               const float *__restrict__ opacity, float *__restrict__ dL_duv,
+                               float *__restrict__ dL_dconic) {
+    const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= rows) return;
+    int lo = 0, hi = pv.B - 1;  // the camera of row r: last b with row_off <= r
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (pv.cams[mid].row_off <= r) lo = mid;
+        else hi = mid - 1;
+    }
+    const BatchCam &c = pv.cams[lo];
+    const float o = opacity[c.op_off + (r - c.row_off)];
+    const float a = conic[3 * r], b = conic[3 * r + 1], cc = conic[3 * r + 2];
+    const float sx = dL_duv[2 * r], sy = dL_duv[2 * r + 1];
+    const float sxx = dL_dconic[3 * r], sxy = dL_dconic[3 * r + 1], syy = dL_dconic[3 * r + 2];
+    dL_duv[2 * r] = -o * (a * sx + b * sy);
+    dL_duv[2 * r + 1] = -o * (cc * sy + b * sx);
+    dL_dconic[3 * r] = -0.5f * o * sxx;
+    dL_dconic[3 * r + 1] = -o * sxy;
+    dL_dconic[3 * r + 2] = -0.5f * o * syy;
+}
+
 // Pixels per thread of the C <= 4 kernels (compile-time tunables).
 #ifndef MSPLAT_BLEND_NPIX_FWD
 #define MSPLAT_BLEND_NPIX_FWD 1
@@ -872,13 +999,13 @@ void launch_small(bool bwd, dim3 grid, cudaStream_t stream, int P, const float2 
     constexpr int tf = kTilePixels / kBlendNpixFwd / kSplitFwd, tb = kTilePixels / kBlendNpixBwd / kSplitBwd;
     if (!bwd)
         launch(blend_fwd_small_kernel<C, kBlendNpixFwd, kSplitFwd>, gf, tf, 0, stream,
-            P, uv, conic, opacity, feature, idx, tr, bg, W, H, out, final_T, nc);
+            P, uv, conic, opacity, feature, idx, tr, bg, W, H, out, final_T, nc, BlendBatch{});
     else if (bg != 0.0f)
         launch(blend_bwd_small_kernel<C, kBlendNpixBwd, true, kSplitBwd>, gb, tb, 0, stream,
-            P, uv, conic, opacity, feature, idx, tr, bg, W, H, fT, nci, dout, duv, dcon, dop, dfeat);
+            P, uv, conic, opacity, feature, idx, tr, bg, W, H, fT, nci, dout, duv, dcon, dop, dfeat, BlendBatch{});
     else
         launch(blend_bwd_small_kernel<C, kBlendNpixBwd, false, kSplitBwd>, gb, tb, 0, stream,
-            P, uv, conic, opacity, feature, idx, tr, bg, W, H, fT, nci, dout, duv, dcon, dop, dfeat);
+            P, uv, conic, opacity, feature, idx, tr, bg, W, H, fT, nci, dout, duv, dcon, dop, dfeat, BlendBatch{});
 }
 
 inline void dispatch_small(bool bwd, int C, dim3 grid, cudaStream_t stream, int P, const float2 *uv,
@@ -924,15 +1051,15 @@ extern "C" int msplat_alpha_blending_forward(int P, int C, const float *uv, cons
         if (nc <= 4)
             launch(blend_fwd_kernel<4>, grid, kBlendThreads, 0, stream, P, C, c0, (const float2 *)uv, conic, opacity,
                                                                     feature, idx_sorted, (const int2 *)tile_range,
-                                                                    bg, W, H, out, final_T, ncontrib);
+                                                                    bg, W, H, out, final_T, ncontrib, BlendBatch{});
         else if (nc <= 16)
             launch(blend_fwd_kernel<16>, grid, kBlendThreads, 0, stream, P, C, c0, (const float2 *)uv, conic, opacity,
                                                                      feature, idx_sorted, (const int2 *)tile_range,
-                                                                     bg, W, H, out, final_T, ncontrib);
+                                                                     bg, W, H, out, final_T, ncontrib, BlendBatch{});
         else
             launch(blend_fwd_kernel<32>, grid, kBlendThreads, 0, stream, P, C, c0, (const float2 *)uv, conic, opacity,
                                                                      feature, idx_sorted, (const int2 *)tile_range,
-                                                                     bg, W, H, out, final_T, ncontrib);
+                                                                     bg, W, H, out, final_T, ncontrib, BlendBatch{});
     }
     return check_launch("alpha_blending_forward");
 }
@@ -959,9 +1086,113 @@ extern "C" int msplat_alpha_blending_backward(int P, int C, const float *uv, con
         return check_launch("alpha_blending_backward");
     }
     for (int c0 = 0; c0 < C; c0 += kBwdC)
-        launch(blend_bwd_kernel, grid, kBlendThreads, 0, stream, P, C, c0, (const float2 *)uv, conic, opacity, feature,
+        launch(blend_bwd_kernel<false>, grid, kBlendThreads, 0, stream, P, C, c0, (const float2 *)uv, conic, opacity, feature,
                                                              idx_sorted, (const int2 *)tile_range, bg, W, H, final_T,
                                                              ncontrib, dL_dout, dL_duv, dL_dconic, dL_dopacity,
-                                                             dL_dfeature);
+                                                             dL_dfeature, BlendBatch{});
     return check_launch("alpha_blending_backward");
+}
+
+// ------------------------------------------------------------ batches
+namespace {
+
+template <int C>
+void launch_small_batch(bool bwd, int tiles, cudaStream_t stream, const BlendBatch &bb, const float2 *uv,
+                        const float *conic, const float *opacity, const float *feature, const int32_t *idx,
+                        const int2 *tr, float bg, float *out, float *final_T, int32_t *nc, const float *fT,
+                        const int32_t *nci, const float *dout, float *duv, float *dcon, float *dop, float *dfeat) {
+    constexpr int tf = kTilePixels / kBlendNpixFwd, tb = kTilePixels / kBlendNpixBwd;
+    if (!bwd)
+        launch(blend_fwd_small_kernel<C, kBlendNpixFwd, 1, true>, tiles, tf, 0, stream, 0, uv, conic, opacity,
+               feature, idx, tr, bg, 1, 1, out, final_T, nc, bb);
+    else if (bg != 0.0f)
+        launch(blend_bwd_small_kernel<C, kBlendNpixBwd, true, 1, true>, tiles, tb, 0, stream, 0, uv, conic, opacity,
+               feature, idx, tr, bg, 1, 1, fT, nci, dout, duv, dcon, dop, dfeat, bb);
+    else
+        launch(blend_bwd_small_kernel<C, kBlendNpixBwd, false, 1, true>, tiles, tb, 0, stream, 0, uv, conic,
+               opacity, feature, idx, tr, bg, 1, 1, fT, nci, dout, duv, dcon, dop, dfeat, bb);
+}
+
+void dispatch_small_batch(bool bwd, int C, int tiles, cudaStream_t stream, const BlendBatch &bb, const float2 *uv,
+                          const float *conic, const float *opacity, const float *feature, const int32_t *idx,
+                          const int2 *tr, float bg, float *out, float *final_T, int32_t *nc, const float *fT,
+                          const int32_t *nci, const float *dout, float *duv, float *dcon, float *dop, float *dfeat) {
+    switch (C) {
+#define MSPLAT_SMALL_B(CC)                                                                                   \
+    case CC:                                                                                                 \
+        launch_small_batch<CC>(bwd, tiles, stream, bb, uv, conic, opacity, feature, idx, tr, bg, out, final_T, \
+                               nc, fT, nci, dout, duv, dcon, dop, dfeat);                                    \
+        break;
+        MSPLAT_SMALL_B(1) MSPLAT_SMALL_B(2) MSPLAT_SMALL_B(3) MSPLAT_SMALL_B(4)
+#undef MSPLAT_SMALL_B
+        default: break;
+    }
+}
+
+}  // namespace
+
+extern "C" int msplat_batch_alpha_blending_forward(const void *plan, int B, int total_tiles, int C,
+                                                   int feature_per_camera, const float *uv, const float *conic,
+                                                   const float *opacity, const float *feature,
+                                                   const int32_t *idx_sorted, const int32_t *tile_range, float bg,
+                                                   float *out, float *final_T, int32_t *ncontrib,
+                                                   msplat_stream_t stream) {
+    if (B <= 0 || total_tiles < 0 || C <= 0)
+        return set_error(MSPLAT_ERR_INVALID_ARGUMENT, "batch_alpha_blending_forward: bad sizes B=%d C=%d", B, C);
+    if (!plan || !uv || !conic || !opacity || !feature || !tile_range || !out || !final_T || !ncontrib)
+        return set_error(MSPLAT_ERR_INVALID_ARGUMENT, "batch_alpha_blending_forward: null pointer");
+    if (total_tiles == 0) return MSPLAT_OK;
+    const BlendBatch bb{batch_plan_view(plan, B), feature_per_camera};
+    if (C <= 4) {
+        dispatch_small_batch(false, C, total_tiles, stream, bb, (const float2 *)uv, conic, opacity, feature, idx_sorted,
+                             (const int2 *)tile_range, bg, out, final_T, ncontrib, nullptr, nullptr, nullptr, nullptr,
+                             nullptr, nullptr, nullptr);
+        return check_launch("batch_alpha_blending_forward");
+    }
+    for (int c0 = 0; c0 < C; c0 += 32) {
+        const int nc = min(32, C - c0);
+        if (nc <= 4)
+            launch(blend_fwd_kernel<4, true>, total_tiles, kBlendThreads, 0, stream, 0, C, c0, (const float2 *)uv,
+                   conic, opacity, feature, idx_sorted, (const int2 *)tile_range, bg, 1, 1, out, final_T, ncontrib,
+                   bb);
+        else if (nc <= 16)
+            launch(blend_fwd_kernel<16, true>, total_tiles, kBlendThreads, 0, stream, 0, C, c0, (const float2 *)uv,
+                   conic, opacity, feature, idx_sorted, (const int2 *)tile_range, bg, 1, 1, out, final_T, ncontrib,
+                   bb);
+        else
+            launch(blend_fwd_kernel<32, true>, total_tiles, kBlendThreads, 0, stream, 0, C, c0, (const float2 *)uv,
+                   conic, opacity, feature, idx_sorted, (const int2 *)tile_range, bg, 1, 1, out, final_T, ncontrib,
+                   bb);
+    }
+    return check_launch("batch_alpha_blending_forward");
+}
+
+extern "C" int msplat_batch_alpha_blending_backward(const void *plan, int B, int total_tiles, int64_t rows, int C,
+                                                    int feature_per_camera, const float *uv, const float *conic,
+                                                    const float *opacity, const float *feature,
+                                                    const int32_t *idx_sorted, const int32_t *tile_range, float bg,
+                                                    const float *final_T, const int32_t *ncontrib,
+                                                    const float *dL_dout, float *dL_duv, float *dL_dconic,
+                                                    float *dL_dopacity, float *dL_dfeature,
+                                                    msplat_stream_t stream) {
+    if (B <= 0 || total_tiles < 0 || C <= 0 || rows < 0)
+        return set_error(MSPLAT_ERR_INVALID_ARGUMENT, "batch_alpha_blending_backward: bad sizes");
+    if (!plan || !uv || !conic || !opacity || !feature || !tile_range || !final_T || !ncontrib || !dL_dout ||
+        !dL_duv || !dL_dconic || !dL_dopacity || !dL_dfeature)
+        return set_error(MSPLAT_ERR_INVALID_ARGUMENT, "batch_alpha_blending_backward: null pointer");
+    if (total_tiles == 0 || rows == 0) return MSPLAT_OK;
+    const BlendBatch bb{batch_plan_view(plan, B), feature_per_camera};
+    if (C <= 4) {
+        dispatch_small_batch(true, C, total_tiles, stream, bb, (const float2 *)uv, conic, opacity, feature, idx_sorted,
+                             (const int2 *)tile_range, bg, nullptr, nullptr, nullptr, final_T, ncontrib, dL_dout,
+                             dL_duv, dL_dconic, dL_dopacity, dL_dfeature);
+        launch(batch_blend_grad_finish_kernel, (unsigned)ceil_div64(rows, 256), 256, 0, stream, bb.pv, rows, conic,
+               opacity, dL_duv, dL_dconic);
+        return check_launch("batch_alpha_blending_backward");
+    }
+    for (int c0 = 0; c0 < C; c0 += kBwdC)
+        launch(blend_bwd_kernel<true>, total_tiles, kBlendThreads, 0, stream, 0, C, c0, (const float2 *)uv, conic,
+               opacity, feature, idx_sorted, (const int2 *)tile_range, bg, 1, 1, final_T, ncontrib, dL_dout, dL_duv,
+               dL_dconic, dL_dopacity, dL_dfeature, bb);
+    return check_launch("batch_alpha_blending_backward");
 }

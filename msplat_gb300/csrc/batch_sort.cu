@@ -1,0 +1,424 @@
+// Multi-camera tile sort in one key space: the intersections of every
+// camera of a batch ordered by (camera, tile, depth) with one set of
+// launches.  No counterpart in the reference, which sorts one camera per
+// call (msplat/sort_gaussian.py:8-54, called from msplat/__init__.py:70-93).
+//
+// Per camera the order is the single-camera fast path's (and so the
+// reference's order restricted to the culled lists): Gaussians sorted by
+// depth (stable, ties by id), intersections emitted in that order, then
+// stably sorted by tile.  Batched:
+//   prepare  depth keys of every camera's Gaussians in one array of padded
+//            segments (one per camera), one segmented 4-pass radix sort,
+//            the culled rectangles and tile counts in depth order, block
+//            offsets scanned per camera (one block per camera), and the
+//            camera segments of the intersection list (each padded to a
+//            sort tile) -- all on the device;
+//   finish   emit every camera's (local tile + 1, Gaussian) pairs into its
+//            segment, one segmented radix sort by local tile (2 passes at
+//            1080p), and the tile ranges in the global tile numbering.
+// The finish takes a capacity (the padded list length it may use) and the
+// counts from device memory, so a batch needs at most one host read (the
+// padded length) and none with a caller-given capacity.
+#include <cstring>
+
+#include "batch_plan.cuh"
+#include "cull.cuh"
+#include "radix_sort.cuh"
+
+namespace msplat {
+
+constexpr int kBatchDepthPasses = 4;
+constexpr int kBlocksPerSortTile = kSortTile / 256;
+
+// Depth keys of every camera's Gaussians in its padded segment (sign-flipped
+// float bits; Gaussians that emit nothing sort last).
+__global__ void __launch_bounds__(256)
+batch_depth_key_kernel(BatchPlanView pv, int64_t n, const float *__restrict__ depth,
+                       const int32_t *__restrict__ radius, uint32_t *__restrict__ keys) {
+    const int64_t pos = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (pos >= n) return;
+    const int b = upper_index(pv.dtile_start, pv.B, pos / kSortTile);
+    const BatchCam &c = pv.cams[b];
+    const int64_t j = pos - (int64_t)pv.dtile_start[b] * kSortTile;
+    if (j >= c.P) return;  // padding: never read by the segmented sort
+    const int64_t q = c.row_off + j;
+    keys[pos] = radius[q] > 0 ? (__float_as_uint(depth[q]) ^ 0x80000000u) : 0xffffffffu;
+}
+
+// Culled rectangles (as the single-camera culled prepare: negative depths
+// emit nothing, rectangles shrunk by shrink_rect) and tile counts of every
+// camera's Gaussians in depth order; the sum per block of 256 (blocks never
+// straddle cameras: segments are padded to sort tiles of 12 blocks).
+__global__ void __launch_bounds__(256)
+batch_count_kernel(BatchPlanView pv, const uint32_t *__restrict__ order, const float2 *__restrict__ uv,
+                   const float *__restrict__ depth, const int32_t *__restrict__ radius,
+                   const float *__restrict__ conic, const float *__restrict__ opacity, short4 *__restrict__ rects,
+                   int64_t *__restrict__ bsum) {
+    __shared__ int64_t scratch[33];
+    const int64_t pos = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int b = upper_index(pv.dtile_start, pv.B, (int64_t)blockIdx.x / kBlocksPerSortTile);
+    const BatchCam &c = pv.cams[b];
+    const int64_t j = pos - (int64_t)pv.dtile_start[b] * kSortTile;
+    int x0 = 0, y0 = 0, x1 = 0, y1 = 0;
+    if (j < c.P) {
+        const int g = (int)order[pos];
+        const int64_t q = c.row_off + g;
+        if (radius[q] > 0 && (__float_as_uint(depth[q]) >> 31) == 0) {
+            const float2 p = uv[q];
+            tile_rect(p.x, p.y, radius[q], c.gx, c.gy, x0, y0, x1, y1);
+            shrink_rect(p.x, p.y, conic[3 * q], conic[3 * q + 1], conic[3 * q + 2], opacity[c.op_off + g], x0, y0,
+                        x1, y1);
+        }
+    }
+    rects[pos] = make_short4((short)x0, (short)y0, (short)x1, (short)y1);
+    int64_t total;
+    block_exclusive_scan<int64_t>((int64_t)((x1 - x0) * (y1 - y0)), scratch, &total);
+    if (threadIdx.x == 0) bsum[blockIdx.x] = total;
+}
+
+// One block per camera: exclusive scan of its block sums in place and its
+// intersection count.
+__global__ void __launch_bounds__(1024)
+batch_block_offsets_kernel(BatchPlanView pv, int64_t *__restrict__ bsum, int64_t *__restrict__ cam_count) {
+    __shared__ int64_t scratch[33];
+    const int b = blockIdx.x;
+    const int64_t k0 = (int64_t)pv.dtile_start[b] * kBlocksPerSortTile;
+    const int64_t k1 = (int64_t)pv.dtile_start[b + 1] * kBlocksPerSortTile;
+    int64_t carry = 0;
+    for (int64_t c0 = k0; c0 < k1; c0 += blockDim.x) {
+        const int64_t i = c0 + threadIdx.x;
+        const int64_t v = i < k1 ? bsum[i] : 0;
+        int64_t tot;
+        const int64_t ex = block_exclusive_scan<int64_t>(v, scratch, &tot);
+        if (i < k1) bsum[i] = carry + ex;
+        carry += tot;
+    }
+    if (threadIdx.x == 0) cam_count[b] = carry;
+}
+
+// The camera segments of the intersection list (sort tiles, padded) and the
+// counts the caller reads: counts[0] = intersections, counts[1] = padded
+// length (the capacity a finish needs), counts[2 + b] = camera b's.
+__global__ void __launch_bounds__(256)
+batch_layout_kernel(int B, const int64_t *__restrict__ cam_count, int32_t *__restrict__ fin_start,
+                    int64_t *__restrict__ counts) {
+    if (threadIdx.x != 0) return;
+    int64_t tiles = 0, total = 0;
+    for (int b = 0; b < B; ++b) {
+        fin_start[b] = (int32_t)min(tiles, (int64_t)INT32_MAX);
+        tiles += ceil_div64(cam_count[b], kSortTile);
+        total += cam_count[b];
+        counts[2 + b] = cam_count[b];
+    }
+    fin_start[B] = (int32_t)min(tiles, (int64_t)INT32_MAX);
+    counts[0] = total;
+    counts[1] = tiles * kSortTile;
+}
+
+// The finish's segments clipped to a capacity of ntiles sort tiles (only
+// ever smaller when the capacity is exceeded, and then status = 1).
+__global__ void __launch_bounds__(256)
+batch_finish_segs_kernel(int B, int ntiles, const int32_t *__restrict__ fin_start,
+                         const int64_t *__restrict__ cam_count, int32_t *__restrict__ seg_start,
+                         int64_t *__restrict__ seg_count, int32_t *__restrict__ status) {
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b <= B) seg_start[b] = min(fin_start[b], ntiles);
+    if (b < B) {
+        const int64_t room = (int64_t)(ntiles - min(fin_start[b], ntiles)) * kSortTile;
+        seg_count[b] = max((int64_t)0, min(cam_count[b], room));
+    }
+    if (b == 0 && status) status[0] = fin_start[B] > ntiles ? 1 : 0;
+}
+
+// Emits each camera's (local tile + 1, Gaussian id) pairs into its segment,
+// in depth order (as emit_kernel: a warp writes each Gaussian's run with
+// its lanes spread over the run); nothing at or past the capacity `cap`.
+__global__ void __launch_bounds__(256)
+batch_emit_kernel(BatchPlanView pv, const uint32_t *__restrict__ order, const short4 *__restrict__ rects,
+                  const int64_t *__restrict__ boff, const int32_t *__restrict__ seg_start,
+                  uint32_t *__restrict__ tkeys, uint32_t *__restrict__ tvals, int64_t cap) {
+    __shared__ int64_t scratch[33];
+    const int lane = threadIdx.x & 31;
+    const int64_t pos = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int b = upper_index(pv.dtile_start, pv.B, (int64_t)blockIdx.x / kBlocksPerSortTile);
+    const BatchCam &c = pv.cams[b];
+    const int64_t j = pos - (int64_t)pv.dtile_start[b] * kSortTile;
+    int g = 0;
+    short4 r = make_short4(0, 0, 0, 0);
+    if (j < c.P) {
+        g = (int)order[pos];
+        r = rects[pos];
+    }
+    const int w = r.z - r.x, n = w * (r.w - r.y);
+    const int64_t start = (int64_t)seg_start[b] * kSortTile + boff[blockIdx.x] +
+                          block_exclusive_scan<int64_t>((int64_t)n, scratch, nullptr);
+    unsigned todo = __ballot_sync(0xffffffffu, n > 0);
+    while (todo) {
+        const int sl = __ffs(todo) - 1;
+        todo &= todo - 1;
+        const int sg = __shfl_sync(0xffffffffu, g, sl);
+        const int sx0 = __shfl_sync(0xffffffffu, (int)r.x, sl), sy0 = __shfl_sync(0xffffffffu, (int)r.y, sl);
+        const int sw = __shfl_sync(0xffffffffu, w, sl), sn = __shfl_sync(0xffffffffu, n, sl);
+        const int64_t sstart = __shfl_sync(0xffffffffu, (long long)start, sl);
+        const float inv = 1.0f / (float)sw;
+        const int64_t room = cap - sstart;
+        const int kmax = room <= 0 ? 0 : (int)min((int64_t)sn, room);
+        for (int k = lane; k < kmax; k += 32) {
+            int ry = (int)(((float)k + 0.5f) * inv);  // k / sw, corrected below
+            ry -= (ry * sw > k);
+            ry += ((ry + 1) * sw <= k);
+            tkeys[sstart + k] = (uint32_t)((sy0 + ry) * c.gx + sx0 + (k - ry * sw) + 1);
+            tvals[sstart + k] = (uint32_t)sg;
+        }
+    }
+}
+
+// Tile ranges in the global tile numbering from the sorted segments: each
+// thread reads 8 keys of one camera's segment (segments start on sort
+// tiles, so the 8 never straddle two) with a neighbour on each side; a
+// neighbour outside the segment's items counts as "outside".
+__global__ void __launch_bounds__(256)
+batch_range_kernel(BatchPlanView pv, int ntiles, const int32_t *__restrict__ seg_start,
+                   const int64_t *__restrict__ seg_count, const uint32_t *__restrict__ keys,
+                   int2 *__restrict__ range) {
+    constexpr int K = 8;
+    const int64_t i0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) * K;
+    if (i0 >= (int64_t)ntiles * kSortTile) return;
+    const int st = (int)(i0 / kSortTile);
+    if (st >= seg_start[pv.B]) return;
+    const int b = upper_index(seg_start, pv.B, st);
+    const int64_t s0 = (int64_t)seg_start[b] * kSortTile, s1 = s0 + seg_count[b];
+    if (i0 >= s1) return;
+    constexpr uint32_t kOut = 0xffffffffu;
+    uint32_t k[K + 2];
+#pragma unroll
+    for (int u = -1; u <= K; ++u) {
+        const int64_t i = i0 + u;
+        k[u + 1] = (i >= s0 && i < s1) ? keys[i] : kOut;
+    }
+    const int toff = pv.cams[b].tile_off;
+#pragma unroll
+    for (int u = 1; u <= K; ++u) {
+        const uint32_t key = k[u];
+        if (key == 0 || key == kOut) continue;
+        const int64_t i = i0 + u - 1;
+        if (k[u - 1] != key) range[toff + key - 1].x = (int)i;
+        if (k[u + 1] != key) range[toff + key - 1].y = (int)(i + 1);
+    }
+}
+
+struct BatchPrepareWs {
+    uint32_t *ka, *kb, *vt, *order;
+    short4 *rects;
+    int64_t *bsum, *cam_count;
+    int32_t *fin_start;
+    uint32_t *hist, *totals;
+};
+
+template <typename WS>
+inline void batch_prepare_carve(WS &w, int B, int64_t dn, BatchPrepareWs &ws) {
+    ws.ka = w.template take<uint32_t>(dn);
+    ws.kb = w.template take<uint32_t>(dn);
+    ws.vt = w.template take<uint32_t>(dn);
+    ws.order = w.template take<uint32_t>(dn);
+    ws.rects = w.template take<short4>(dn);
+    ws.bsum = w.template take<int64_t>((size_t)(dn / 256));
+    ws.cam_count = w.template take<int64_t>(B);
+    ws.fin_start = w.template take<int32_t>(B + 1);
+    ws.hist = w.template take<uint32_t>((size_t)kRadix * (dn / kSortTile));
+    ws.totals = w.template take<uint32_t>((size_t)kRadix * kBatchDepthPasses * B);
+}
+
+struct BatchFinishWs {
+    uint32_t *ka, *kb, *vt, *hist, *totals;
+    int32_t *seg_start;
+    int64_t *seg_count;
+};
+
+template <typename WS>
+inline void batch_finish_carve(WS &w, int B, int64_t cap, int passes, BatchFinishWs &f) {
+    f.ka = w.template take<uint32_t>(cap);
+    f.kb = w.template take<uint32_t>(cap);
+    f.vt = w.template take<uint32_t>(cap);
+    f.hist = w.template take<uint32_t>((size_t)kRadix * (cap / kSortTile));
+    f.totals = w.template take<uint32_t>((size_t)kRadix * passes * B);
+    f.seg_start = w.template take<int32_t>(B + 1);
+    f.seg_count = w.template take<int64_t>(B);
+}
+
+struct SizeOnlyB {
+    WorkspaceSizer s;
+    template <typename T> T *take(size_t n) { s.take<T>(n); return nullptr; }
+};
+
+inline int batch_tile_passes(int max_tiles) {
+    int bits = 0;
+    while (bits < 32 && ((uint32_t)max_tiles >> bits) != 0) ++bits;  // keys span [1, max_tiles]
+    return ceil_div(bits > 0 ? bits : 1, kRadixBits);
+}
+
+}  // namespace msplat
+
+using namespace msplat;
+
+extern "C" size_t msplat_batch_plan_bytes(int B) { return B > 0 ? batch_plan_bytes(B) : 0; }
+
+extern "C" int msplat_batch_plan(int B, const int32_t *dims, const int32_t *npoints, const int64_t *opacity_offset,
+                                 void *plan, size_t plan_bytes, int64_t *sizes) {
+    if (B <= 0 || !dims || !npoints || !plan || !sizes)
+        return set_error(MSPLAT_ERR_INVALID_ARGUMENT, "batch_plan: B = %d or a null pointer", B);
+    if (plan_bytes < batch_plan_bytes(B))
+        return set_error(MSPLAT_ERR_WORKSPACE, "batch_plan: %zu bytes < %zu", plan_bytes, batch_plan_bytes(B));
+    char *p = static_cast<char *>(plan);
+    memset(p, 0, batch_plan_bytes(B));
+    BatchCam *cams = reinterpret_cast<BatchCam *>(p);
+    int32_t *dstart = reinterpret_cast<int32_t *>(p + batch_plan_off_dtile(B));
+    int64_t *dcount = reinterpret_cast<int64_t *>(p + batch_plan_off_dcount(B));
+    int32_t *tstart = reinterpret_cast<int32_t *>(p + batch_plan_off_tiles(B));
+    int64_t rows = 0, pix = 0, dt = 0, tiles = 0;
+    int max_tiles = 1;
+    for (int b = 0; b < B; ++b) {
+        const int W = dims[2 * b], H = dims[2 * b + 1], P = npoints[b];
+        if (W <= 0 || H <= 0 || P < 0)
+            return set_error(MSPLAT_ERR_INVALID_ARGUMENT, "batch_plan: camera %d has W=%d H=%d P=%d", b, W, H, P);
+        BatchCam &c = cams[b];
+        c.W = W;
+        c.H = H;
+        c.gx = ceil_div(W, kTile);
+        c.gy = ceil_div(H, kTile);
+        if (c.gx > 32767 || c.gy > 32767)
+            return set_error(MSPLAT_ERR_INVALID_ARGUMENT, "batch_plan: camera %d grid too large", b);
+        c.P = P;
+        c.tile_off = (int32_t)tiles;
+        c.dtile = (int32_t)dt;
+        c.row_off = rows;
+        c.op_off = opacity_offset ? opacity_offset[b] : 0;
+        c.pix_off = pix;
+        dstart[b] = (int32_t)dt;
+        dcount[b] = P;
+        tstart[b] = (int32_t)tiles;
+        const int nt = c.gx * c.gy;
+        max_tiles = max(max_tiles, nt);
+        tiles += nt;
+        rows += P;
+        pix += (int64_t)W * H;
+        dt += ceil_div64(P, kSortTile);
+        if (tiles > INT32_MAX || dt > INT32_MAX / kSortTile)
+            return set_error(MSPLAT_ERR_CAPACITY, "batch_plan: batch too large");
+    }
+    dstart[B] = (int32_t)dt;
+    tstart[B] = (int32_t)tiles;
+    sizes[0] = tiles;                       // total tiles (tile_range rows)
+    sizes[1] = rows;                        // total per-camera Gaussian rows
+    sizes[2] = pix;                         // total pixels
+    sizes[3] = dt * kSortTile;              // padded depth-key items
+    sizes[4] = batch_tile_passes(max_tiles);  // tile-key passes of the finish
+    return MSPLAT_OK;
+}
+
+extern "C" size_t msplat_batch_sort_prepare_workspace_size(int B, int64_t depth_items) {
+    if (B <= 0 || depth_items < 0) return 0;
+    SizeOnlyB z;
+    BatchPrepareWs ws;
+    batch_prepare_carve(z, B, depth_items, ws);
+    return z.s.used;
+}
+
+extern "C" int msplat_batch_sort_prepare(const void *plan, int B, int64_t depth_items, const float *uv,
+                                         const float *depth, const int32_t *radius, const float *conic,
+                                         const float *opacity, int64_t *counts, void *workspace,
+                                         size_t workspace_bytes, msplat_stream_t stream) {
+    if (B <= 0 || depth_items < 0 || depth_items % kSortTile != 0)
+        return set_error(MSPLAT_ERR_INVALID_ARGUMENT, "batch_sort_prepare: B = %d, depth items %lld", B,
+                         (long long)depth_items);
+    if (!plan || !counts) return set_error(MSPLAT_ERR_INVALID_ARGUMENT, "batch_sort_prepare: null plan / counts");
+    Workspace w(workspace, workspace_bytes);
+    BatchPrepareWs ws;
+    batch_prepare_carve(w, B, depth_items, ws);
+    if (w.overflow)
+        return set_error(MSPLAT_ERR_WORKSPACE, "batch_sort_prepare: workspace of %zu bytes < %zu", workspace_bytes,
+                         msplat_batch_sort_prepare_workspace_size(B, depth_items));
+    const BatchPlanView pv = batch_plan_view(plan, B);
+    if (depth_items == 0) {
+        cudaMemsetAsync(ws.cam_count, 0, sizeof(int64_t) * B, stream);
+        launch(batch_layout_kernel, 1, 32, 0, stream, B, (const int64_t *)ws.cam_count, ws.fin_start, counts);
+        return check_launch("batch_sort_prepare");
+    }
+    if (!uv || !depth || !radius || !conic || !opacity)
+        return set_error(MSPLAT_ERR_INVALID_ARGUMENT, "batch_sort_prepare: null pointer");
+    const int dtiles = (int)(depth_items / kSortTile);
+    launch(batch_depth_key_kernel, (unsigned)ceil_div64(depth_items, 256), 256, 0, stream, pv, depth_items, depth,
+           radius, ws.ka);
+    SortSegs segs;
+    segs.tile_start = pv.dtile_start;
+    segs.count = pv.dcount;
+    segs.nseg = B;
+    // 4 passes (even): ka -> kb -> ka ... the values land in order
+    int st = radix_sort_segmented<uint32_t>(dtiles, segs, 0, kBatchDepthPasses, ws.ka, nullptr, ws.ka, ws.order,
+                                            ws.kb, ws.vt, ws.hist, ws.totals, stream);
+    if (st) return st;
+    launch(batch_count_kernel, (unsigned)(depth_items / 256), 256, 0, stream, pv, (const uint32_t *)ws.order,
+           (const float2 *)uv, depth, radius, conic, opacity, ws.rects, ws.bsum);
+    launch(batch_block_offsets_kernel, B, 1024, 0, stream, pv, ws.bsum, ws.cam_count);
+    launch(batch_layout_kernel, 1, 32, 0, stream, B, (const int64_t *)ws.cam_count, ws.fin_start, counts);
+    return check_launch("batch_sort_prepare");
+}
+
+extern "C" size_t msplat_batch_sort_finish_workspace_size(int B, int64_t capacity, int passes) {
+    if (B <= 0 || capacity < 0 || passes <= 0) return 0;
+    SizeOnlyB z;
+    BatchFinishWs f;
+    batch_finish_carve(z, B, ceil_div64(capacity, kSortTile) * kSortTile, passes, f);
+    return z.s.used;
+}
+
+extern "C" int msplat_batch_sort_finish(const void *plan, int B, int64_t depth_items, int total_tiles, int passes,
+                                        int64_t capacity, const void *prepare_workspace, int32_t *idx_sorted,
+                                        int32_t *tile_range, int32_t *status, void *workspace,
+                                        size_t workspace_bytes, msplat_stream_t stream) {
+    if (B <= 0 || depth_items < 0 || depth_items % kSortTile != 0 || total_tiles < 0 || passes <= 0 ||
+        passes > 4 || capacity < 0)
+        return set_error(MSPLAT_ERR_INVALID_ARGUMENT, "batch_sort_finish: bad sizes");
+    if (capacity % kSortTile != 0)
+        return set_error(MSPLAT_ERR_INVALID_ARGUMENT, "batch_sort_finish: capacity %lld is not a multiple of %d",
+                         (long long)capacity, kSortTile);
+    if (capacity > INT32_MAX)
+        return set_error(MSPLAT_ERR_CAPACITY, "batch_sort_finish: capacity %lld exceeds int32",
+                         (long long)capacity);
+    if (!plan || !prepare_workspace || !tile_range || (capacity > 0 && !idx_sorted))
+        return set_error(MSPLAT_ERR_INVALID_ARGUMENT, "batch_sort_finish: null pointer");
+    Workspace pw(const_cast<void *>(prepare_workspace), msplat_batch_sort_prepare_workspace_size(B, depth_items));
+    BatchPrepareWs prep;
+    batch_prepare_carve(pw, B, depth_items, prep);
+    Workspace w(workspace, workspace_bytes);
+    BatchFinishWs f;
+    batch_finish_carve(w, B, capacity, passes, f);
+    if (w.overflow)
+        return set_error(MSPLAT_ERR_WORKSPACE, "batch_sort_finish: workspace of %zu bytes < %zu", workspace_bytes,
+                         msplat_batch_sort_finish_workspace_size(B, capacity, passes));
+    const BatchPlanView pv = batch_plan_view(plan, B);
+    const int ntiles = (int)(capacity / kSortTile);
+    cudaMemsetAsync(tile_range, 0, sizeof(int32_t) * 2 * (size_t)total_tiles, stream);
+    launch(batch_finish_segs_kernel, ceil_div(B + 1, 256), 256, 0, stream, B, ntiles,
+           (const int32_t *)prep.fin_start, (const int64_t *)prep.cam_count, f.seg_start, f.seg_count, status);
+    if (capacity == 0 || depth_items == 0) return check_launch("batch_sort_finish");
+    // Even pass count: emit the ids straight into idx_sorted; odd: into the
+    // temporary (as the single-camera finish).
+    uint32_t *out = (uint32_t *)idx_sorted;
+    const bool even = passes % 2 == 0;
+    uint32_t *vemit = even ? out : f.vt;
+    launch(batch_emit_kernel, (unsigned)(depth_items / 256), 256, 0, stream, pv, (const uint32_t *)prep.order,
+           (const short4 *)prep.rects, (const int64_t *)prep.bsum, (const int32_t *)f.seg_start, f.ka, vemit,
+           capacity);
+    SortSegs segs;
+    segs.tile_start = f.seg_start;
+    segs.count = f.seg_count;
+    segs.nseg = B;
+    uint32_t *kout = even ? f.ka : f.kb;
+    int st = radix_sort_segmented<uint32_t>(ntiles, segs, 0, passes, f.ka, vemit, kout, out, even ? f.kb : f.ka,
+                                            f.vt, f.hist, f.totals, stream);
+    if (st) return st;
+    launch(batch_range_kernel, (unsigned)ceil_div64(capacity / 8, 256), 256, 0, stream, pv, ntiles,
+           (const int32_t *)f.seg_start, (const int64_t *)f.seg_count, (const uint32_t *)kout, (int2 *)tile_range);
+    return check_launch("batch_sort_finish");
+}

@@ -39,6 +39,39 @@ __device__ __forceinline__ uint32_t digit_of(K k, int shift) {
 
 inline int sort_tiles(int64_t n) { return (int)ceil_div64(n, kSortTile); }
 
+// Segments of a segmented sort: segment s holds count[s] items starting at
+// item tile_start[s] * kSortTile (segments start on sort-tile boundaries,
+// the gap after a segment's last item is padding that is neither read nor
+// written).  Each segment is sorted on its own, in place of the same
+// layout: the sorted items of segment s land in the same positions.  Both
+// arrays live in device memory (the counts may come from a kernel), so a
+// segmented sort needs no host read.
+struct SortSegs {
+    const int32_t *tile_start = nullptr;  // [nseg + 1]
+    const int64_t *count = nullptr;       // [nseg]
+    int nseg = 0;
+};
+
+// The segment holding sort tile t, or -1 past the last segment.
+__device__ __forceinline__ int seg_of_tile(const SortSegs &sg, int t) {
+    if (t >= sg.tile_start[sg.nseg]) return -1;
+    int lo = 0, hi = sg.nseg - 1;  // last s with tile_start[s] <= t
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (sg.tile_start[mid] <= t) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+// Items of sort tile t inside its segment (0 past the last segment).
+__device__ __forceinline__ int seg_tile_items(const SortSegs &sg, int t, int &seg) {
+    seg = seg_of_tile(sg, t);
+    if (seg < 0) return 0;
+    const int64_t left = sg.count[seg] - (int64_t)(t - sg.tile_start[seg]) * kSortTile;
+    return (int)max((int64_t)0, min((int64_t)kSortTile, left));
+}
+
 // Lanes of `valid` holding the same 8-bit digit as this lane, from eight
 // ballots (much cheaper than __match_any_sync, whose throughput limits a
 // ranking loop).  Every lane of the warp must call it.
@@ -57,12 +90,19 @@ __device__ __forceinline__ unsigned digit_peers(uint32_t d, unsigned valid) {
 // All of a thread's keys are loaded before any counting so that the loads
 // are in flight together; counts go to per-warp shared histograms with plain
 // shared atomics (cheaper than aggregating equal digits first).
-template <typename K, bool FLIP>
+template <typename K, bool FLIP, bool SEG = false>
 __global__ void __launch_bounds__(kSortThreads)
 radix_upsweep_kernel(const K *__restrict__ keys, int64_t n, int shift, int ntiles,
-                     uint32_t *__restrict__ hist, const int64_t *__restrict__ n_dev) {
+                     uint32_t *__restrict__ hist, const int64_t *__restrict__ n_dev, SortSegs segs = {}) {
     __shared__ uint32_t cnt[kSortWarps][kRadix];
-    if (n_dev) n = min(n, *n_dev);  // the length is on the device; n is the capacity
+    if (SEG) {
+        // items of this tile within its segment, as a length relative to
+        // the tile's first item
+        int sg;
+        n = (int64_t)blockIdx.x * kSortTile + seg_tile_items(segs, blockIdx.x, sg);
+    } else if (n_dev) {
+        n = min(n, *n_dev);  // the length is on the device; n is the capacity
+    }
     for (int i = threadIdx.x; i < kSortWarps * kRadix; i += kSortThreads) (&cnt[0][0])[i] = 0;
     __syncthreads();
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -89,18 +129,27 @@ radix_upsweep_kernel(const K *__restrict__ keys, int64_t n, int shift, int ntile
 // Block d: exclusive scan of row d of hist in place, and the row's total.
 // (A total per digit written once replaces atomics from every upsweep tile
 // onto 256 addresses, which serialised when the digits were diverse.)
-__global__ void __launch_bounds__(1024)
-radix_rowscan_kernel(uint32_t *__restrict__ hist, uint32_t *__restrict__ totals, int ntiles) {
+// Segmented (grid.y = segment s): the row's part [tile_start[s],
+// tile_start[s + 1]) is scanned, and the total goes to totals[s][d].
+static __global__ void __launch_bounds__(1024)
+radix_rowscan_kernel(uint32_t *__restrict__ hist, uint32_t *__restrict__ totals, int ntiles,
+                     SortSegs segs = {}) {
     __shared__ uint32_t scratch[33];
     const int d = blockIdx.x;
     uint32_t carry = 0;
+    int t0 = 0, t1 = ntiles;
+    if (segs.nseg) {
+        t0 = segs.tile_start[blockIdx.y];
+        t1 = segs.tile_start[blockIdx.y + 1];
+        totals += (size_t)blockIdx.y * kRadix;
+    }
     uint32_t *row = hist + (size_t)d * ntiles;
-    for (int c0 = 0; c0 < ntiles; c0 += blockDim.x) {
+    for (int c0 = t0; c0 < t1; c0 += blockDim.x) {
         const int i = c0 + threadIdx.x;
-        const uint32_t v = i < ntiles ? row[i] : 0u;
+        const uint32_t v = i < t1 ? row[i] : 0u;
         uint32_t tot;
         const uint32_t ex = block_exclusive_scan<uint32_t>(v, scratch, &tot);
-        if (i < ntiles) row[i] = carry + ex;
+        if (i < t1) row[i] = carry + ex;
         carry += tot;
     }
     if (threadIdx.x == 0) totals[d] = carry;
@@ -115,12 +164,12 @@ inline size_t radix_downsweep_smem(size_t key_bytes) {
 // the key's sign bit on load / store (signed-integer order).
 // 32-bit keys: capped at 64 registers for 4 blocks per SM (no spill); the
 // 64-bit keys of the reference-layout sort would spill there and keep 3.
-template <typename K, bool FLIP_IN, bool FLIP_OUT>
+template <typename K, bool FLIP_IN, bool FLIP_OUT, bool SEG = false>
 __global__ void __launch_bounds__(kSortThreads, sizeof(K) == 4 ? 4 : 3)
 radix_downsweep_kernel(const K *__restrict__ kin, const uint32_t *__restrict__ vin,
                        K *__restrict__ kout, uint32_t *__restrict__ vout, int64_t n, int shift,
                        int ntiles, const uint32_t *__restrict__ hist, const uint32_t *__restrict__ totals,
-                       const int64_t *__restrict__ n_dev) {
+                       const int64_t *__restrict__ n_dev, SortSegs segs = {}) {
     extern __shared__ __align__(16) unsigned char sm_raw[];
     K *skeys = reinterpret_cast<K *>(sm_raw);
     uint32_t *svals = reinterpret_cast<uint32_t *>(skeys + kSortTile);
@@ -130,9 +179,19 @@ radix_downsweep_kernel(const K *__restrict__ kin, const uint32_t *__restrict__ v
     __shared__ uint32_t scan_scratch[33];
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    if (n_dev) n = min(n, *n_dev);
     const int64_t base = (int64_t)blockIdx.x * kSortTile;
-    const int tile_n = (int)min((int64_t)kSortTile, n - base);  // <= 0 past a device-side length
+    int tile_n;
+    int64_t out_base = 0;  // first item of the segment in the arrays
+    if (SEG) {
+        int sg;
+        tile_n = seg_tile_items(segs, blockIdx.x, sg);
+        if (sg < 0) return;  // past the last segment: nothing to move (uniform over the block)
+        totals += (size_t)sg * kRadix;
+        out_base = (int64_t)segs.tile_start[sg] * kSortTile;
+    } else {
+        if (n_dev) n = min(n, *n_dev);
+        tile_n = (int)min((int64_t)kSortTile, n - base);  // <= 0 past a device-side length
+    }
     for (int i = tid; i < kSortWarps * kRadix; i += kSortThreads) whist[i] = 0;
     // start of this tile's bucket of digit tid: the digit's start (scan of
     // the totals of the smaller digits) + the tile's offset within the digit
@@ -155,7 +214,7 @@ radix_downsweep_kernel(const K *__restrict__ kin, const uint32_t *__restrict__ v
         if (valid) {
             k = __ldcs(kin + base + li);
             if (FLIP_IN) k ^= sign_bit<K>();
-            v = vin ? __ldcs(vin + base + li) : (uint32_t)(base + li);
+            v = vin ? __ldcs(vin + base + li) : (uint32_t)(base + li - out_base);  // index within the segment
         }
         key[r] = k;
         val[r] = v;
@@ -203,7 +262,7 @@ radix_downsweep_kernel(const K *__restrict__ kin, const uint32_t *__restrict__ v
     for (int i = tid; i < tile_n; i += kSortThreads) {
         K k = skeys[i];
         const uint32_t d = digit_of(k, shift);
-        const size_t o = (size_t)gstart[d] + (size_t)(i - (int)lstart[d]);
+        const size_t o = (size_t)out_base + (size_t)gstart[d] + (size_t)(i - (int)lstart[d]);
         if (FLIP_OUT) k ^= sign_bit<K>();
         if (kout) kout[o] = k;
         vout[o] = svals[i];
@@ -253,15 +312,18 @@ int radix_sort_pairs(int64_t n, int begin_bit, int passes, const K *kin, const u
         uint32_t *tot = b.totals + p * kRadix;
         const bool first = p == 0, last = p == passes - 1;
         if (FLIP && first)
-            launch(radix_upsweep_kernel<K, true>, nt, kSortThreads, 0, stream, ksrc, n, shift, nt, b.hist, n_dev);
+            launch(radix_upsweep_kernel<K, true>, nt, kSortThreads, 0, stream, ksrc, n, shift, nt, b.hist, n_dev,
+                   SortSegs{});
         else
-            launch(radix_upsweep_kernel<K, false>, nt, kSortThreads, 0, stream, ksrc, n, shift, nt, b.hist, n_dev);
-        launch(radix_rowscan_kernel, kRadix, 1024, 0, stream, b.hist, tot, nt);
+            launch(radix_upsweep_kernel<K, false>, nt, kSortThreads, 0, stream, ksrc, n, shift, nt, b.hist, n_dev,
+                   SortSegs{});
+        launch(radix_rowscan_kernel, kRadix, 1024, 0, stream, b.hist, tot, nt, SortSegs{});
 #define MSPLAT_DOWNSWEEP(FI, FO)                                                                                \
     do {                                                                                                        \
         auto kern = radix_downsweep_kernel<K, FI, FO>;                                                          \
         cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);                     \
-        launch(kern, nt, kSortThreads, smem, stream, ksrc, vsrc, kdst, vdst, n, shift, nt, b.hist, tot, n_dev); \
+        launch(kern, nt, kSortThreads, smem, stream, ksrc, vsrc, kdst, vdst, n, shift, nt, b.hist, tot, n_dev,    \
+               SortSegs{});                                                                             \
     } while (0)
         if (FLIP && first && last) MSPLAT_DOWNSWEEP(true, true);
         else if (FLIP && first) MSPLAT_DOWNSWEEP(true, false);
@@ -274,12 +336,45 @@ int radix_sort_pairs(int64_t n, int begin_bit, int passes, const K *kin, const u
     return check_launch("radix_sort_pairs");
 }
 
+// Segmented stable sort of unsigned keys (see SortSegs): every segment's
+// items sorted by key bits [begin_bit, begin_bit + 8 * passes) in place of
+// the same layout, with the pass chain of radix_sort_pairs.  ntiles = the
+// sort tiles the launches cover (at least segs.tile_start[nseg]); hist
+// [radix][ntiles], totals [passes][nseg][radix].  vin == nullptr means value
+// = index within the segment.
+template <typename K>
+int radix_sort_segmented(int ntiles, const SortSegs &segs, int begin_bit, int passes, const K *kin,
+                         const uint32_t *vin, K *kout, uint32_t *vout, K *ktmp, uint32_t *vtmp, uint32_t *hist,
+                         uint32_t *totals, cudaStream_t stream) {
+    if (ntiles <= 0 || passes <= 0 || segs.nseg <= 0) return MSPLAT_OK;
+    const size_t smem = radix_downsweep_smem(sizeof(K));
+    const K *ksrc = kin;
+    const uint32_t *vsrc = vin;
+    auto down = radix_downsweep_kernel<K, false, false, true>;
+    cudaFuncSetAttribute(down, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    for (int p = 0; p < passes; ++p) {
+        const int shift = begin_bit + p * kRadixBits;
+        const bool to_out = ((passes - 1 - p) & 1) == 0;
+        K *kdst = to_out ? kout : ktmp;
+        uint32_t *vdst = to_out ? vout : vtmp;
+        uint32_t *tot = totals + (size_t)p * segs.nseg * kRadix;
+        launch(radix_upsweep_kernel<K, false, true>, ntiles, kSortThreads, 0, stream, ksrc, (int64_t)0, shift,
+               ntiles, hist, (const int64_t *)nullptr, segs);
+        launch(radix_rowscan_kernel, dim3(kRadix, segs.nseg), 1024, 0, stream, hist, tot, ntiles, segs);
+        launch(down, ntiles, kSortThreads, smem, stream, ksrc, vsrc, kdst, vdst, (int64_t)0, shift, ntiles, hist,
+               (const uint32_t *)tot, (const int64_t *)nullptr, segs);
+        ksrc = kdst;
+        vsrc = vdst;
+    }
+    return check_launch("radix_sort_segmented");
+}
+
 // ------------------------------------------------------------------- scan
 constexpr int kScanThreads = 256;
 constexpr int kScanItems = 16;
 constexpr int kScanTile = kScanThreads * kScanItems;
 
-__global__ void __launch_bounds__(kScanThreads)
+static __global__ void __launch_bounds__(kScanThreads)
 scan_reduce_kernel(const int32_t *__restrict__ in, int n, int64_t *__restrict__ partials) {
     const int64_t base = (int64_t)blockIdx.x * kScanTile;
     int64_t s = 0;
@@ -300,7 +395,7 @@ scan_reduce_kernel(const int32_t *__restrict__ in, int n, int64_t *__restrict__ 
 }
 
 // One block: exclusive scan of the tile sums (in place), total -> *total.
-__global__ void __launch_bounds__(1024)
+static __global__ void __launch_bounds__(1024)
 scan_partials_kernel(int64_t *__restrict__ partials, int nparts, int64_t *__restrict__ total) {
     __shared__ int64_t scratch[33];
     int64_t carry = 0;
@@ -317,7 +412,7 @@ scan_partials_kernel(int64_t *__restrict__ partials, int nparts, int64_t *__rest
 
 // Rescans each tile with its carry-in; writes inclusive or exclusive sums.
 // Items are blocked per thread (16 consecutive) for a thread-local prefix.
-__global__ void __launch_bounds__(kScanThreads)
+static __global__ void __launch_bounds__(kScanThreads)
 scan_apply_kernel(const int32_t *__restrict__ in, int n, const int64_t *__restrict__ partials,
                   int32_t *__restrict__ out, bool inclusive) {
     __shared__ int64_t scratch[33];

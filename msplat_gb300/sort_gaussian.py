@@ -2,7 +2,6 @@
 (drop-in for msplat/sort_gaussian.py)."""
 from __future__ import annotations
 
-import contextlib
 from typing import Tuple
 
 import torch
@@ -126,89 +125,6 @@ def _sort_reference_layout(u, d, W, H, r, t):
     return idx_sorted, tile_range
 
 
-def sort_gaussian_many(cases, streams=None, capacities=None, status=None):
-    """`sort_gaussian` for several cameras with one host read for all of
-    them: every camera's prepare is enqueued, the intersection counts of all
-    cameras are read together, then every finish is enqueued.  With
-    `streams`, camera b's sort runs on streams[b % len(streams)] (after the
-    work already on the current stream), so small cameras overlap on the
-    device; the results are ready on the current stream on return.
-
-    With `capacities` (one per camera) and `status` ([B] int32), every
-    camera uses the capacity-bounded finish (sort_gaussian_capacity) and no
-    host read happens at all (stream-capturable); status[b] becomes 1 where
-    camera b's result is not valid.
-
-    cases: sequence of (uv [P,2], depth [P,1], W, H, radius [P] int32,
-    tiles [P] int32) contiguous float32 / int32 CUDA tensors, optionally
-    followed by (conic [P,3], opacity [P,1]) for culled lists (see
-    `sort_gaussian`'s cull).  Returns a list of (idx_sorted, tile_range)."""
-    lib = _lib.load()
-    if not cases:
-        return []
-    if capacities is not None:
-        return _sort_many_capacity(cases, streams, capacities, status)
-    dev = cases[0][0].device
-    main = torch.cuda.current_stream(dev)
-    streams = list(streams or [])
-    if streams:
-        ready = torch.cuda.Event()
-        ready.record(main)
-        for s in streams:
-            s.wait_event(ready)
-
-    def on(b):
-        return torch.cuda.stream(streams[b % len(streams)]) if streams else contextlib.nullcontext()
-
-    counts = torch.empty((len(cases), 2), dtype=torch.int64, device=dev)
-    preps = []
-    with _lib.stage("sort_gaussian_prepare"):
-        for b, case in enumerate(cases):
-            u, d, W, H, r, t = case[:6]
-            P = u.shape[0]
-            with on(b):
-                st = _lib.stream(dev)
-                ws_prep = _lib.workspace(lib.msplat_sort_prepare_workspace_size(P, W, H), dev)
-                _prepare(lib, P, d, r, t, u, W, H, counts[b], ws_prep, st, _cull_of(case))
-            preps.append(ws_prep)
-    for s in streams:
-        main.wait_stream(s)
-    host = counts.tolist()
-    out = []
-    with _lib.stage("sort_gaussian_finish"):
-        for b, (case, ws_prep, (I, n_mismatch)) in enumerate(zip(cases, preps, host)):
-            u, d, W, H, r, t = case[:6]
-            with on(b):
-                if n_mismatch:
-                    res = _sort_reference_layout(u, d, W, H, r, t)
-                else:
-                    if I > 2**31 - 1:
-                        raise RuntimeError(f"sort_gaussian: {I} intersections exceed the int32 range")
-                    P = u.shape[0]
-                    st = _lib.stream(dev)
-                    idx_sorted = torch.empty((I,), dtype=torch.int32, device=dev)
-                    tile_range = torch.empty((tt.ntiles(W, H), 2), dtype=torch.int32, device=dev)
-                    ws = _lib.workspace(lib.msplat_sort_finish_workspace_size(P, I, W, H), dev)
-                    _lib.check(lib.msplat_sort_gaussian_finish(
-                        P, _lib.ptr(u), _lib.ptr(d), _lib.ptr(r), W, H, I, _lib.ptr(ws_prep),
-                        _lib.ptr(idx_sorted), _lib.ptr(tile_range), _lib.ptr(ws), ws.numel(), st),
-                        "sort_gaussian_finish")
-                    res = (idx_sorted, tile_range)
-                    del ws
-                if streams:
-                    # allocated on a side stream, used later on the main one
-                    for x in res:
-                        x.record_stream(main)
-            out.append(res)
-    for s in streams:
-        main.wait_stream(s)
-    return out
-
-
-def _cull_of(case):
-    return (case[6], case[7]) if len(case) > 6 else None
-
-
 def sort_gaussian_capacity(uv: Tensor, depth: Tensor, W: int, H: int, radius: Tensor, tiles: Tensor,
                            capacity: int, status: Tensor, *,
                            cull: Tuple[Tensor, Tensor] | None = None) -> Tuple[Tensor, Tensor]:
@@ -244,29 +160,3 @@ def sort_gaussian_capacity(uv: Tensor, depth: Tensor, W: int, H: int, radius: Te
             _lib.ptr(idx_sorted), _lib.ptr(tile_range), _lib.ptr(st_t), _lib.ptr(ws), ws.numel(), st),
             "sort_gaussian_finish_capacity")
     return idx_sorted, tile_range
-
-
-def _sort_many_capacity(cases, streams, capacities, status):
-    if status is None or status.numel() != len(cases):
-        raise RuntimeError("capacity-bounded sorts need a status tensor with one entry per camera")
-    dev = cases[0][0].device
-    main = torch.cuda.current_stream(dev)
-    streams = list(streams or [])
-    if streams:
-        ready = torch.cuda.Event()
-        ready.record(main)
-        for s in streams:
-            s.wait_event(ready)
-    out = []
-    for b, (case, cap) in enumerate(zip(cases, capacities)):
-        u, d, W, H, r, t = case[:6]
-        ctx = torch.cuda.stream(streams[b % len(streams)]) if streams else contextlib.nullcontext()
-        with ctx:
-            res = sort_gaussian_capacity(u, d, W, H, r, t, int(cap), status[b:b + 1], cull=_cull_of(case))
-            if streams:
-                for x in res:
-                    x.record_stream(main)
-        out.append(res)
-    for s in streams:
-        main.wait_stream(s)
-    return out

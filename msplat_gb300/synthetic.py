@@ -32,3 +32,18 @@ def training_scene(n: int, width: int, height: int, focal: float, seed: int = 0,
     intr = torch.tensor([focal, focal, width / 2, height / 2], dtype=torch.float32)
     weights = torch.randn(3, height, width, generator=g)
     return dict(xyz=xyz, scale=scale, rot=rot, opacity=opacity, shs=shs, intr=intr, extr=extr, weights=weights)
+
+
+def feature_scene(n: int, width: int, height: int, focal: float, seed: int = 1, sh_degree: int = 10,
+                  n_features: int = 32) -> dict:
+    """The extensible-features scene: `training_scene`'s distributions with SH
+    coefficients N(0, 0.1) of degree `sh_degree`, plus `n_features` N(0, 1)
+    features per Gaussian; the rendered channels are the SH colour (3), the
+    features and the camera-space depth, so the loss weights are
+    [3 + n_features + 1, H, W]."""
+    s = training_scene(n, width, height, focal, seed=seed, sh_degree=sh_degree)
+    g = torch.Generator().manual_seed(seed + 1000)
+    s["shs"] = s["shs"] * (0.1 / 0.3)
+    s["feats"] = torch.randn(n, n_features, generator=g)
+    s["weights"] = torch.randn(3 + n_features + 1, height, width, generator=g)
+    return s

@@ -1,9 +1,13 @@
-"""Multi-camera rendering against one single-camera call per camera.
+"""Multi-camera rendering in one key space against one single-camera call
+per camera.
 
 Images must be bit-identical (the batched preprocess evaluates the same
-device code per camera, the sort and blend are the single-camera ones);
-gradients summed over the cameras agree up to float summation order, and
-every camera gets its own intrinsic / extrinsic gradient.
+device code per camera; the batched sort orders each camera's list exactly
+as the single-camera culled sort; the blend grid over all cameras runs the
+single-camera per-pixel arithmetic); gradients summed over the cameras
+agree up to float summation order, and every camera gets its own intrinsic
+/ extrinsic gradient.  Also: several scenes in one batch (cameras in any
+order), more than four channels, and a capacity too small for the sort.
 """
 import numpy as np
 import pytest
@@ -83,3 +87,74 @@ def test_batch_with_one_camera_and_no_grad_cameras():
     assert torch.equal(imgs[0], ref)
     imgs[0].sum().backward()
     assert torch.isfinite(p["shs"].grad).all() and p["xyz"].grad.abs().sum() > 0
+
+
+def test_batch_over_several_scenes_in_any_camera_order():
+    import msplat_gb300 as ms
+    s1 = scene(15000, 5, C=3, sh_deg=2)
+    s2 = scene(7000, 6, C=3, sh_deg=2)
+    sizes = [(160, 120), (128, 128), (96, 144), (200, 104), (64, 64)]
+    scene_of = [1, 0, 1, 0, 0]
+    intrs, extrs = cameras(sizes, 12)
+    keys = ("xyz", "scale", "rot", "opacity", "shs")
+    a = [leaves({k: sc[k] for k in keys}) for sc in (s1, s2)]
+    r = [leaves({k: sc[k] for k in keys}) for sc in (s1, s2)]
+    ci, ce = intrs.to(DEV).requires_grad_(), extrs.to(DEV).requires_grad_()
+    ri, re = intrs.to(DEV).requires_grad_(), extrs.to(DEV).requires_grad_()
+    imgs = ms.rasterization_sh_scenes([tuple(p[k] for k in keys) for p in a], scene_of, ci, ce, sizes, 0.1)
+    refs = [ms.rasterization_sh(*(r[scene_of[b]][k] for k in keys), ri[b], re[b], w, h, 0.1)
+            for b, (w, h) in enumerate(sizes)]
+    gen = torch.Generator().manual_seed(5)
+    ws = [torch.randn(img.shape, generator=gen).to(DEV) for img in refs]
+    for b, (img, ref) in enumerate(zip(imgs, refs)):
+        assert torch.equal(img, ref), f"camera {b}"
+    sum((i * w).sum() for i, w in zip(imgs, ws)).backward()
+    sum((i * w).sum() for i, w in zip(refs, ws)).backward()
+    for sa, sr in zip(a, r):
+        for k in keys:
+            rel_close(sa[k].grad, sr[k].grad, 1e-4, f"dL/d{k}")
+    rel_close(ci.grad, ri.grad, 1e-4, "dL/dintrs")
+    rel_close(ce.grad, re.grad, 1e-4, "dL/dextrs")
+
+
+def test_batch_with_more_than_four_channels():
+    import msplat_gb300 as ms
+    s = scene(12000, 7, C=6)
+    sizes = [(128, 96), (80, 80), (144, 112)]
+    intrs, extrs = cameras(sizes, 3)
+    base = {"xyz": s["xyz"], "scale": s["scale"], "rot": s["rot"], "opacity": s["opacity"], "feat": s["feat"]}
+    a, r = leaves(base), leaves(base)
+    imgs = ms.rasterization_batch(a["xyz"], a["scale"], a["rot"], a["opacity"], a["feat"], intrs.to(DEV),
+                                  extrs.to(DEV), sizes, 0.3)
+    refs = [ms.rasterization(r["xyz"], r["scale"], r["rot"], r["opacity"], r["feat"], intrs[b].to(DEV),
+                             extrs[b].to(DEV), w, h, 0.3) for b, (w, h) in enumerate(sizes)]
+    for b, (img, ref) in enumerate(zip(imgs, refs)):
+        assert torch.equal(img, ref), f"camera {b}"
+    gen = torch.Generator().manual_seed(2)
+    ws = [torch.randn(img.shape, generator=gen).to(DEV) for img in refs]
+    sum((i * w).sum() for i, w in zip(imgs, ws)).backward()
+    sum((i * w).sum() for i, w in zip(refs, ws)).backward()
+    for k in base:
+        rel_close(a[k].grad, r[k].grad, 1e-4, f"dL/d{k}")
+
+
+def test_batch_capacity_too_small_reports_status():
+    import msplat_gb300 as ms
+    s = scene(20000, 8, C=3, sh_deg=1)
+    sizes = [(160, 160), (128, 96)]
+    intrs, extrs = cameras(sizes, 4)
+    p = leaves({"xyz": s["xyz"], "scale": s["scale"], "rot": s["rot"], "opacity": s["opacity"], "shs": s["shs"]})
+    status = torch.full((1,), 7, dtype=torch.int32, device=DEV)
+    with torch.no_grad():
+        ms.rasterization_sh_batch(p["xyz"], p["scale"], p["rot"], p["opacity"], p["shs"], intrs.to(DEV),
+                                  extrs.to(DEV), sizes, capacity=3072, status=status)
+    torch.cuda.synchronize()
+    assert int(status.item()) == 1
+    with torch.no_grad():
+        imgs = ms.rasterization_sh_batch(p["xyz"], p["scale"], p["rot"], p["opacity"], p["shs"], intrs.to(DEV),
+                                         extrs.to(DEV), sizes, capacity=4_000_000, status=status)
+        ref = ms.rasterization_sh(p["xyz"], p["scale"], p["rot"], p["opacity"], p["shs"], intrs[1].to(DEV),
+                                  extrs[1].to(DEV), 128, 96, 0.0)
+    torch.cuda.synchronize()
+    assert int(status.item()) == 0
+    assert torch.equal(imgs[1], ref)

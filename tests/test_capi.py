@@ -87,3 +87,40 @@ def test_ops_require_cuda_tensors():
 
 def test_launch_counter_starts_at_zero_without_gpu_work(lib):
     assert lib.msplat_kernel_launches() == 0
+
+
+def test_batch_plan_layout_on_the_host(lib):
+    """msplat_batch_plan is host-only: tile, row, pixel and padded depth-key
+    offsets of a three-camera batch over two scenes."""
+    import numpy as np
+    B = 3
+    dims = np.array([[100, 50], [1920, 1080], [16, 16]], np.int32)
+    npts = np.array([5000, 7000, 5000], np.int32)
+    opoff = np.array([0, 5000, 0], np.int64)
+    nbytes = int(lib.msplat_batch_plan_bytes(B))
+    blob = np.zeros(nbytes, np.uint8)
+    sizes = np.zeros(5, np.int64)
+    st = lib.msplat_batch_plan(B, dims.ctypes.data, npts.ctypes.data, opoff.ctypes.data, blob.ctypes.data, nbytes,
+                               sizes.ctypes.data)
+    assert st == 0
+    tiles = [7 * 4, 120 * 68, 1]
+    assert sizes[0] == sum(tiles)
+    assert sizes[1] == npts.sum()
+    assert sizes[2] == (dims[:, 0].astype(np.int64) * dims[:, 1]).sum()
+    assert sizes[3] == 3072 * (2 + 3 + 2)  # each camera's depth keys padded to 3072
+    assert sizes[4] == 2  # 8160 tiles: two 8-bit passes
+    cams = np.frombuffer(blob[:64 * B].tobytes(), dtype=np.dtype([("W", "i4"), ("H", "i4"), ("gx", "i4"),
+                                                                     ("gy", "i4"), ("P", "i4"), ("tile_off", "i4"),
+                                                                     ("dtile", "i4"), ("pad0", "i4"),
+                                                                     ("row_off", "i8"), ("op_off", "i8"),
+                                                                     ("pix_off", "i8"), ("pad1", "i8")]))
+    assert list(cams["tile_off"]) == [0, 28, 28 + 8160]
+    assert list(cams["row_off"]) == [0, 5000, 12000]
+    assert list(cams["op_off"]) == [0, 5000, 0]
+    assert list(cams["dtile"]) == [0, 2, 5]
+    assert lib.msplat_batch_plan(B, dims.ctypes.data, npts.ctypes.data, None, blob.ctypes.data, nbytes - 1,
+                                 sizes.ctypes.data) == 2  # buffer too small
+    bad = dims.copy()
+    bad[1, 0] = 0
+    assert lib.msplat_batch_plan(B, bad.ctypes.data, npts.ctypes.data, None, blob.ctypes.data, nbytes,
+                                 sizes.ctypes.data) == 1
