@@ -55,11 +55,16 @@ def sources() -> list[str]:
 
 
 def tuned_defines(path: str = TUNING_PATH) -> dict:
-    """The autotuner's choices {macro: value}, or {} without a tuning file."""
+    """The autotuner's choices {macro: value} -- the frame's and every other
+    workload's (their macros are disjoint) -- or {} without a tuning file."""
     if not os.path.exists(path):
         return {}
     with open(path) as f:
-        return {str(k): int(v) for k, v in json.load(f).get("defines", {}).items()}
+        data = json.load(f)
+    out = {str(k): int(v) for k, v in data.get("defines", {}).items()}
+    for w in data.get("workloads", {}).values():
+        out.update({str(k): int(v) for k, v in w.get("defines", {}).items()})
+    return out
 
 
 def define_flags(defines: dict) -> list[str]:

@@ -485,8 +485,8 @@ __device__ __forceinline__ PixPow<NPIX> blend_power_n(float a, float b, float c,
     return out;
 }
 
-// Gathers NPIX entries per thread (thread t owns list positions
-// base + dir * (t * NPIX + r)) and compacts the kept ones into shared
+// Gathers GE entries per thread (thread t owns list positions
+// base + dir * (t * GE + r)) and compacts the kept ones into shared
 // memory in list order, with the mask of the warp blocks (8 columns by
 // 4 NPIX rows, one per warp) each one can reach.  The block renders the
 // ROWS rows from by0 of the tile, which is also the box of the cull.
@@ -496,7 +496,7 @@ __device__ __forceinline__ PixPow<NPIX> blend_power_n(float a, float b, float c,
 // are written after it, and every warp reaches it only once done with the
 // previous batch, so a warp that finishes a batch early issues the next
 // batch's loads and cull tests while the others still blend.
-template <int C, int NPIX, bool WITH_ID, int ROWS = kTile>
+template <int C, int NPIX, bool WITH_ID, int ROWS = kTile, int GE = NPIX>
 __device__ __forceinline__ int gather_small(int base, int dir, int lo, int hi,
                                             const int32_t *__restrict__ idx_sorted,
                                             const float2 *__restrict__ uv, const float *__restrict__ conic,
@@ -505,14 +505,14 @@ __device__ __forceinline__ int gather_small(int base, int dir, int lo, int hi,
                                             float4 *sA, float4 *sB, float4 *sF, int *sG, unsigned char *sM,
                                             int *scan, bool vote) {
     constexpr int NT = kTile * ROWS / NPIX;
-    float4 A[NPIX], B[NPIX], F[NPIX];
-    int G[NPIX];
-    unsigned M[NPIX];
-    bool keep[NPIX];
+    float4 A[GE], B[GE], F[GE];
+    int G[GE];
+    unsigned M[GE];
+    bool keep[GE];
     int nk = 0;
 #pragma unroll
-    for (int r = 0; r < NPIX; ++r) {
-        const int j = base + dir * ((int)threadIdx.x * NPIX + r);
+    for (int r = 0; r < GE; ++r) {
+        const int j = base + dir * ((int)threadIdx.x * GE + r);
         keep[r] = false;
         if (j >= lo && j < hi) {
             const int g = idx_sorted[j];
@@ -552,7 +552,7 @@ __device__ __forceinline__ int gather_small(int base, int dir, int lo, int hi,
     }
     int pos = wbase + inc - nk;
 #pragma unroll
-    for (int r = 0; r < NPIX; ++r) {
+    for (int r = 0; r < GE; ++r) {
         if (keep[r]) {
             sA[pos] = A[r];
             sB[pos] = B[r];
@@ -569,7 +569,7 @@ __device__ __forceinline__ int gather_small(int base, int dir, int lo, int hi,
 // SPLIT: a tile is rendered by SPLIT blocks of kTile / SPLIT rows each
 // (grid.y = tiles down x SPLIT), each gathering the tile's list against
 // its own part.
-template <int C, int NPIX, int SPLIT, bool BATCH = false>
+template <int C, int NPIX, int SPLIT, bool BATCH = false, int GE = NPIX>
 __global__ void MSPLAT_FWD_BOUNDS(kTilePixels / NPIX / SPLIT)
 blend_fwd_small_kernel(int P, const float2 *__restrict__ uv, const float *__restrict__ conic,
                        const float *__restrict__ opacity, const float *__restrict__ feature,
@@ -577,7 +577,8 @@ blend_fwd_small_kernel(int P, const float2 *__restrict__ uv, const float *__rest
                        int W, int H, float *__restrict__ out, float *__restrict__ final_T,
                        int32_t *__restrict__ ncontrib, BlendBatch bb = {}) {
     static_assert(!BATCH || SPLIT == 1, "batched blends render whole tiles");
-    constexpr int ROWS = kTile / SPLIT, NT = kTile * ROWS / NPIX, BATCH_N = NT * NPIX;
+    // GE entries gathered per thread: BATCH_N Gaussians per shared-memory batch
+    constexpr int ROWS = kTile / SPLIT, NT = kTile * ROWS / NPIX, BATCH_N = NT * GE;
     static_assert(4 * NPIX <= ROWS, "a warp block of 4 NPIX rows must fit the block's rows");
     __shared__ float4 sA[BATCH_N], sB[BATCH_N], sF[BATCH_N];
     __shared__ unsigned char sM[BATCH_N];
@@ -622,7 +623,7 @@ blend_fwd_small_kernel(int P, const float2 *__restrict__ uv, const float *__rest
         bool all_done = true;
 #pragma unroll
         for (int i = 0; i < NPIX; ++i) all_done &= done[i];
-        const int n = gather_small<C, NPIX, false, ROWS>(start, 1, range.x, range.y, idx_sorted, uv, conic,
+        const int n = gather_small<C, NPIX, false, ROWS, GE>(start, 1, range.x, range.y, idx_sorted, uv, conic,
                                                          opacity, feature, bx0, by0, sA, sB, sF, nullptr, sM, scan,
                                                          all_done);
         if (n < 0) break;  // every pixel of the block is done
@@ -740,7 +741,7 @@ constexpr int kFewLanes = MSPLAT_FEW_LANES;
 
 // BG: the background is nonzero, so dL/dalpha has the term
 // -T_final / (1 - alpha) * sum_c bg dL/dpix_c (compiled out for bg == 0).
-template <int C, int NPIX, bool BG, int SPLIT, bool BATCH = false>
+template <int C, int NPIX, bool BG, int SPLIT, bool BATCH = false, int GE = NPIX>
 __global__ void MSPLAT_BWD_BOUNDS(kTilePixels / NPIX / SPLIT)
 blend_bwd_small_kernel(int P, const float2 *__restrict__ uv, const float *__restrict__ conic,
                        const float *__restrict__ opacity, const float *__restrict__ feature,
@@ -750,7 +751,7 @@ blend_bwd_small_kernel(int P, const float2 *__restrict__ uv, const float *__rest
                        float *__restrict__ dL_dconic, float *__restrict__ dL_dopacity,
                        float *__restrict__ dL_dfeature, BlendBatch bb = {}) {
     static_assert(!BATCH || SPLIT == 1, "batched blends render whole tiles");
-    constexpr int ROWS = kTile / SPLIT, NT = kTile * ROWS / NPIX, BATCH_N = NT * NPIX;
+    constexpr int ROWS = kTile / SPLIT, NT = kTile * ROWS / NPIX, BATCH_N = NT * GE;
     static_assert(4 * NPIX <= ROWS, "a warp block of 4 NPIX rows must fit the block's rows");
     constexpr int NV = 6 + C;
     __shared__ float4 sA[BATCH_N], sB[BATCH_N], sF[BATCH_N];
@@ -827,7 +828,7 @@ blend_bwd_small_kernel(int P, const float2 *__restrict__ uv, const float *__rest
 
     for (int bend = end; bend > range.x; bend -= BATCH_N) {
         const int bstart = max(range.x, bend - BATCH_N);
-        const int n = gather_small<C, NPIX, true, ROWS>(bend - 1, -1, bstart, bend, idx_sorted, uv, conic,
+        const int n = gather_small<C, NPIX, true, ROWS, GE>(bend - 1, -1, bstart, bend, idx_sorted, uv, conic,
                                                         opacity, feature, bx0, by0, sA, sB, sF, sG, sM, scan,
                                                         false);
         // Each warp walks only the entries that reach its rows and precede
@@ -980,6 +981,31 @@ batch_blend_grad_finish_kernel(BatchPlanView pv, int64_t rows, const float *__re
 #endif
 constexpr int kBlendNpixFwd = MSPLAT_BLEND_NPIX_FWD;
 constexpr int kBlendNpixBwd = MSPLAT_BLEND_NPIX_BWD;
+// Entries gathered per thread per shared-memory batch (so Gaussians per
+// batch = threads x this; compile-time tunables, default one per pixel).
+#ifndef MSPLAT_BLEND_GATHER_FWD
+#define MSPLAT_BLEND_GATHER_FWD MSPLAT_BLEND_NPIX_FWD
+#endif
+#ifndef MSPLAT_BLEND_GATHER_BWD
+#define MSPLAT_BLEND_GATHER_BWD MSPLAT_BLEND_NPIX_BWD
+#endif
+constexpr int kGatherFwd = MSPLAT_BLEND_GATHER_FWD, kGatherBwd = MSPLAT_BLEND_GATHER_BWD;
+// The same shape parameters for the multi-camera blend grid, tuned on the
+// multi-camera workload (default: the single-camera values).
+#ifndef MSPLAT_BATCH_BLEND_NPIX_FWD
+#define MSPLAT_BATCH_BLEND_NPIX_FWD MSPLAT_BLEND_NPIX_FWD
+#endif
+#ifndef MSPLAT_BATCH_BLEND_NPIX_BWD
+#define MSPLAT_BATCH_BLEND_NPIX_BWD MSPLAT_BLEND_NPIX_BWD
+#endif
+#ifndef MSPLAT_BATCH_BLEND_GATHER_FWD
+#define MSPLAT_BATCH_BLEND_GATHER_FWD MSPLAT_BATCH_BLEND_NPIX_FWD
+#endif
+#ifndef MSPLAT_BATCH_BLEND_GATHER_BWD
+#define MSPLAT_BATCH_BLEND_GATHER_BWD MSPLAT_BATCH_BLEND_NPIX_BWD
+#endif
+constexpr int kBatchNpixFwd = MSPLAT_BATCH_BLEND_NPIX_FWD, kBatchNpixBwd = MSPLAT_BATCH_BLEND_NPIX_BWD;
+constexpr int kBatchGatherFwd = MSPLAT_BATCH_BLEND_GATHER_FWD, kBatchGatherBwd = MSPLAT_BATCH_BLEND_GATHER_BWD;
 // Blocks per tile of the C <= 4 kernels (1 or 2: whole tiles, or halves of
 // 8 rows with their own gather, cull and end; compile-time tunables).
 #ifndef MSPLAT_BLEND_SPLIT_FWD
@@ -998,13 +1024,13 @@ void launch_small(bool bwd, dim3 grid, cudaStream_t stream, int P, const float2 
     const dim3 gf(grid.x, grid.y * kSplitFwd), gb(grid.x, grid.y * kSplitBwd);
     constexpr int tf = kTilePixels / kBlendNpixFwd / kSplitFwd, tb = kTilePixels / kBlendNpixBwd / kSplitBwd;
     if (!bwd)
-        launch(blend_fwd_small_kernel<C, kBlendNpixFwd, kSplitFwd>, gf, tf, 0, stream,
+        launch(blend_fwd_small_kernel<C, kBlendNpixFwd, kSplitFwd, false, kGatherFwd>, gf, tf, 0, stream,
             P, uv, conic, opacity, feature, idx, tr, bg, W, H, out, final_T, nc, BlendBatch{});
     else if (bg != 0.0f)
-        launch(blend_bwd_small_kernel<C, kBlendNpixBwd, true, kSplitBwd>, gb, tb, 0, stream,
+        launch(blend_bwd_small_kernel<C, kBlendNpixBwd, true, kSplitBwd, false, kGatherBwd>, gb, tb, 0, stream,
             P, uv, conic, opacity, feature, idx, tr, bg, W, H, fT, nci, dout, duv, dcon, dop, dfeat, BlendBatch{});
     else
-        launch(blend_bwd_small_kernel<C, kBlendNpixBwd, false, kSplitBwd>, gb, tb, 0, stream,
+        launch(blend_bwd_small_kernel<C, kBlendNpixBwd, false, kSplitBwd, false, kGatherBwd>, gb, tb, 0, stream,
             P, uv, conic, opacity, feature, idx, tr, bg, W, H, fT, nci, dout, duv, dcon, dop, dfeat, BlendBatch{});
 }
 
@@ -1101,16 +1127,16 @@ void launch_small_batch(bool bwd, int tiles, cudaStream_t stream, const BlendBat
                         const float *conic, const float *opacity, const float *feature, const int32_t *idx,
                         const int2 *tr, float bg, float *out, float *final_T, int32_t *nc, const float *fT,
                         const int32_t *nci, const float *dout, float *duv, float *dcon, float *dop, float *dfeat) {
-    constexpr int tf = kTilePixels / kBlendNpixFwd, tb = kTilePixels / kBlendNpixBwd;
+    constexpr int tf = kTilePixels / kBatchNpixFwd, tb = kTilePixels / kBatchNpixBwd;
     if (!bwd)
-        launch(blend_fwd_small_kernel<C, kBlendNpixFwd, 1, true>, tiles, tf, 0, stream, 0, uv, conic, opacity,
-               feature, idx, tr, bg, 1, 1, out, final_T, nc, bb);
+        launch(blend_fwd_small_kernel<C, kBatchNpixFwd, 1, true, kBatchGatherFwd>, tiles, tf, 0, stream, 0, uv,
+               conic, opacity, feature, idx, tr, bg, 1, 1, out, final_T, nc, bb);
     else if (bg != 0.0f)
-        launch(blend_bwd_small_kernel<C, kBlendNpixBwd, true, 1, true>, tiles, tb, 0, stream, 0, uv, conic, opacity,
-               feature, idx, tr, bg, 1, 1, fT, nci, dout, duv, dcon, dop, dfeat, bb);
+        launch(blend_bwd_small_kernel<C, kBatchNpixBwd, true, 1, true, kBatchGatherBwd>, tiles, tb, 0, stream, 0, uv,
+               conic, opacity, feature, idx, tr, bg, 1, 1, fT, nci, dout, duv, dcon, dop, dfeat, bb);
     else
-        launch(blend_bwd_small_kernel<C, kBlendNpixBwd, false, 1, true>, tiles, tb, 0, stream, 0, uv, conic,
-               opacity, feature, idx, tr, bg, 1, 1, fT, nci, dout, duv, dcon, dop, dfeat, bb);
+        launch(blend_bwd_small_kernel<C, kBatchNpixBwd, false, 1, true, kBatchGatherBwd>, tiles, tb, 0, stream, 0,
+               uv, conic, opacity, feature, idx, tr, bg, 1, 1, fT, nci, dout, duv, dcon, dop, dfeat, bb);
 }
 
 void dispatch_small_batch(bool bwd, int C, int tiles, cudaStream_t stream, const BlendBatch &bb, const float2 *uv,

@@ -57,3 +57,20 @@ def test_every_space_value_builds_a_distinct_define_set():
     for name, values in autotune.SPACE.items():
         flags = {tuple(_build.define_flags(dict(autotune.DEFAULTS, **{name: v}))) for v in values}
         assert len(flags) == len(values), name
+
+
+def test_each_workload_keeps_its_own_section(tmp_path):
+    """Tuning the batch workload stores its choice beside the frame's, and the
+    build applies both (the multi-camera grid's macros are its own)."""
+    p = str(tmp_path / "tuning.json")
+    autotune.write_tuning(p, "frame", {"MSPLAT_FEW_LANES": 16}, 1.9, {"gaussians": 1, "width": 2, "height": 3}, [])
+    autotune.write_tuning(p, "batch", {"MSPLAT_BATCH_BLEND_GATHER_FWD": 2}, 80.0,
+                          {"gaussians": 1, "width": 2, "height": 3, "cameras": 16}, [])
+    autotune.write_tuning(p, "frame", {"MSPLAT_FEW_LANES": 12}, 1.8, {"gaussians": 1, "width": 2, "height": 3}, [])
+    data = json.load(open(p))
+    assert data["defines"] == {"MSPLAT_FEW_LANES": 12}
+    assert data["workloads"]["batch"]["defines"] == {"MSPLAT_BATCH_BLEND_GATHER_FWD": 2}
+    assert _build.tuned_defines(p) == {"MSPLAT_FEW_LANES": 12, "MSPLAT_BATCH_BLEND_GATHER_FWD": 2}
+    assert not set(autotune.SPACE) & set(autotune.BATCH_SPACE)
+    for k, v in autotune.BATCH_DEFAULTS.items():
+        assert v in autotune.BATCH_SPACE[k]

@@ -73,9 +73,12 @@ def test_served_results_equal_requests_alone():
     from msplat_gb300.serve import Server
     scs = scenes()
     reqs = requests(32, 0, 0.05)
-    served = Server(scs, hbm_budget=8 << 30, streams=3, max_batch=8).serve(reqs, timeout=120)
+    srv = Server(scs, hbm_budget=8 << 30, streams=3, max_batch=8, max_backward=4)
+    served = srv.serve(reqs, timeout=120)
     assert all(r.done is not None and r.done >= r.arrival for r in served)
     assert max(r.batch for r in served) > 1, "nothing was batched"
+    assert max(r.batch for r in served if r.backward) > 1, "no backward requests were batched together"
+    assert srv.peak_allocated <= 8 << 30
     check(scs, served)
 
 

@@ -1,7 +1,9 @@
 """The server's scheduling on CPU, with simulated jobs: every request is
-served once, admitted memory never exceeds the budget, forward-only
-requests of a scene are batched (up to max_batch), backward requests run
-alone, and a failing job surfaces as an exception instead of a hang."""
+served once, admitted memory never exceeds the budget (the estimates and
+the simulated device memory), forward-only requests are batched (up to
+max_batch, any scene), backward requests are batched among themselves (up
+to max_backward), and a failing job surfaces as an exception instead of a
+hang."""
 import threading
 import time
 
@@ -11,13 +13,13 @@ import torch
 
 
 
-def make(budget, streams, max_batch, job_time=0.004, fail=False):
+def make(budget, streams, max_batch, job_time=0.004, fail=False, max_backward=3):
     from msplat_gb300.serve import Server
 
     class Sim(Server):
         def __init__(self):
             super().__init__([{"shs": torch.zeros(1000, 3, 16)} for _ in range(3)], budget, streams, max_batch,
-                             device="cuda:0")
+                             device="cuda:0", max_backward=max_backward)
             self.lock = threading.Lock()
             self.in_use = 0
             self.peak = 0
@@ -25,6 +27,10 @@ def make(budget, streams, max_batch, job_time=0.004, fail=False):
 
         def _worker_stream(self):
             return None
+
+        def _device_memory(self):
+            with self.lock:
+                return self.in_use, self.in_use
 
         def _bytes(self, r):
             return 100 if r.backward else 60
@@ -57,15 +63,17 @@ def reqs(n, seed=0):
 def test_every_request_served_within_budget_and_batched():
     srv = make(budget=600, streams=3, max_batch=4)
     rs = reqs(120)
-    out = srv.serve(rs, timeout=30)
+    done = []
+    out = srv.serve(rs, timeout=30, on_done=done.append)
     assert len(out) == 120 and all(r.done is not None and r.done >= r.arrival for r in out)
-    assert srv.peak <= 600
+    assert sorted(map(id, done)) == sorted(map(id, rs))
+    assert srv.peak <= 600 and srv.peak_allocated <= 600
     for job in srv.jobs:
-        if any(b for _, b in job):
-            assert len(job) == 1
-        else:
-            assert len(job) <= 4 and len({s for s, _ in job}) == 1
-    assert max(len(j) for j in srv.jobs) > 1
+        kinds = {b for _, b in job}
+        assert len(kinds) == 1  # forward-only and backward requests never share a job
+        assert len(job) <= (3 if kinds == {True} else 4)
+    assert max(len(j) for j in srv.jobs if not j[0][1]) > 1
+    assert max(len(j) for j in srv.jobs if j[0][1]) > 1
     assert sum(len(j) for j in srv.jobs) == 120
 
 
