@@ -14,11 +14,16 @@
 // Gaussian's gradients over the cameras in registers (xyz, scale,
 // rotation, opacity) and in a shared-memory row (SH coefficients), so each
 // parameter gradient is written once instead of B times; camera gradients
-// are reduced per block and camera into partial rows [B][blocks][16].
+// are reduced per warp and camera (a reduce-scatter of shuffles) into
+// per-warp shared slots, which are summed in a fixed order into partial
+// rows [B][blocks][16] once per kCamChunk cameras (two block barriers per
+// chunk instead of two per camera).
 #include "geometry.cuh"
 #include "sh_basis.cuh"
 
 namespace msplat {
+
+constexpr int kCamChunk = 16;  // cameras per flush of the per-warp camera-gradient slots
 
 // cams: [B][16] = intr (fx, fy, cx, cy) then extr (3x4 row-major);
 // dims: [B][2] = (W, H).
@@ -116,7 +121,10 @@ batch_preprocess_bwd_kernel(int P, int B, int C, const float *__restrict__ xyz, 
     const int CD = C * D, stride = CD | 1;
     const int p0 = blockIdx.x * blockDim.x;
     const int n = min((int)blockDim.x, P - p0);
+    const int nwarps = blockDim.x >> 5, warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     float *grow_base = smem + (size_t)blockDim.x * stride;
+    // per-warp camera-gradient slots [kCamChunk][warps][16] after the rows
+    float *cslot = smem + (C > 0 ? (size_t)2 * blockDim.x * stride : 0);
     if (C > 0) {
         stage_rows(smem, shs + (size_t)p0 * CD, n, CD, stride);
         for (int e = threadIdx.x; e < n * stride; e += blockDim.x) grow_base[e] = 0.f;
@@ -211,8 +219,22 @@ batch_preprocess_bwd_kernel(int P, int B, int C, const float *__restrict__ xyz, 
         }
         if (active && dL_dop_cam) gop += dL_dop_cam[q];
         if (cam_grads) {
-            block_partial_16(acc, partials + (size_t)b * gridDim.x * kCamGradVals);
-            __syncthreads();  // the block's reduction buffer is reused next camera
+            const int cb = b % kCamChunk;
+            const float tot = warp_reduce_scatter_16(acc);
+            if ((lane & 1) == 0) cslot[((size_t)cb * nwarps + warp) * kCamGradVals + (lane >> 1)] = tot;
+            if (cb == kCamChunk - 1 || b == B - 1) {
+                __syncthreads();
+                // the block's partial row per camera of the chunk: its warps'
+                // slots in warp order
+                const int b0 = b - cb;
+                for (int e = threadIdx.x; e < (cb + 1) * kCamGradVals; e += blockDim.x) {
+                    const int c = e / kCamGradVals, k = e - c * kCamGradVals;
+                    float s = 0.f;
+                    for (int w = 0; w < nwarps; ++w) s += cslot[((size_t)c * nwarps + w) * kCamGradVals + k];
+                    partials[((size_t)(b0 + c) * gridDim.x + blockIdx.x) * kCamGradVals + k] = s;
+                }
+                __syncthreads();  // the slots are reused by the next chunk
+            }
         }
     }
     if (active) {
@@ -274,8 +296,9 @@ int batch_bwd_launch(int P, int B, int C, const float *xyz, const float *scales,
     const int CD = C * (DEG + 1) * (DEG + 1);
     const int nt = batch_block_points(CD, true);
     const int blocks = ceil_div(P, nt);
-    const size_t smem = C > 0 ? (size_t)2 * nt * (CD | 1) * sizeof(float) : 0;
     const bool cam = dL_dcams != nullptr;
+    const size_t smem = (C > 0 ? (size_t)2 * nt * (CD | 1) * sizeof(float) : 0) +
+                        (cam ? (size_t)kCamChunk * (nt / 32) * kCamGradVals * sizeof(float) : 0);
     cudaFuncSetAttribute(batch_preprocess_bwd_kernel<DEG>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     launch(batch_preprocess_bwd_kernel<DEG>, blocks, nt, smem, stream, P, B, C, xyz, scales, (const float4 *)uquats,
            shs, cams, depth, radius, (const float2 *)dL_duv, dL_dconic, dL_dcolor, dL_dop_cam, dL_dxyz, dL_dscales,

@@ -37,6 +37,25 @@ __device__ __forceinline__ void block_partial_16(float (&vals)[kCamGradVals],
     }
 }
 
+// Reduce-scatter of the 16 camera-gradient values over a warp: afterwards
+// lane l holds the warp total of value l >> 1 (lanes 2i and 2i + 1 the
+// same), after 8 + 4 + 2 + 1 + 1 shuffles instead of 16 x 5.
+__device__ __forceinline__ float warp_reduce_scatter_16(float (&v)[kCamGradVals]) {
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int o = 16, n = 16; o >= 2; o >>= 1, n >>= 1) {
+        const bool up = (lane & o) != 0;
+        const int h = n >> 1;
+#pragma unroll
+        for (int k = 0; k < h; ++k) {
+            const float send = up ? v[k] : v[k + h];
+            const float keep = up ? v[k + h] : v[k];
+            v[k] = keep + __shfl_xor_sync(0xffffffffu, send, o);
+        }
+    }
+    return v[0] + __shfl_xor_sync(0xffffffffu, v[0], 1);
+}
+
 // Fixed-order sum of `nblocks` partial rows; writes (does not accumulate)
 // dL_dintr[4] and dL_dextr[12], either of which may be null.  Thread t sums
 // column t % 16 over rows t / 16, t / 16 + 32, ... in double with four
