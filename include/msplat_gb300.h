@@ -280,6 +280,25 @@ MSPLAT_API int msplat_alpha_blending_forward(int P, int C, const float *uv,
                                   int H, float *out, float *final_T,
                                   int32_t *ncontrib, msplat_stream_t stream);
 
+/* Forward-blend variant and its bounded waits.  No counterpart in the
+ * reference (its blend gathers each batch with a block barrier,
+ * msplat/src/alpha_blending.cu:57-72).  With producer_warps = 2 or 4 the
+ * C <= 4 forward runs as a producer / consumer ring: that many warps gather
+ * each tile's batches into two shared-memory slots while eight warps blend,
+ * handed off through mbarriers; 0 selects the block-barrier kernel.
+ * batch_producer_warps does the same for the multi-camera grid.  Results
+ * are identical either way; the default is the tuned choice.  Process-wide
+ * setting (all devices, all threads). */
+MSPLAT_API int msplat_set_blend_ring(int producer_warps, int batch_producer_warps);
+/* Every wait of the ring gives up after `polls` polls of at most 1 us each
+ * (default 2^21, about 2 s), sets a device error word and lets the kernel
+ * finish with invalid results instead of hanging.  Process-wide. */
+MSPLAT_API int msplat_set_wait_limit(int polls);
+/* Reads (after synchronising `stream`) the current device's error word into
+ * *error (may be NULL), clears it when reset != 0, and returns
+ * MSPLAT_ERR_TIMEOUT if it was set, MSPLAT_OK otherwise. */
+MSPLAT_API int msplat_wait_error(int reset, int *error, msplat_stream_t stream);
+
 /* dL_duv [P,2], dL_dconic [P,3], dL_dopacity [P], dL_dfeature [P,C] must be
  * zero on entry (the kernels accumulate into them with atomics). */
 MSPLAT_API int msplat_alpha_blending_backward(int P, int C, const float *uv,

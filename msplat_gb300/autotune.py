@@ -7,8 +7,9 @@ gathered per thread x threads), the number of contributing lanes below
 which the backward sends a Gaussian's gradients as direct atomics instead
 of a warp reduction, the keys per thread of a radix tile (which sets the
 sort tile, 256 x items), optional register caps of the two blend kernels
-(more resident blocks per SM against spills) and whether a tile is blended
-by one block or by two of 8 rows each.  The tile itself stays 16x16: it is
+(more resident blocks per SM against spills), whether a tile is blended
+by one block or by two of 8 rows each, and whether the forward runs as a
+producer / consumer ring and with how many producer warps.  The tile itself stays 16x16: it is
 part of the reference's outputs (tiles_touched, tile_range).  The
 multi-camera blend grid has its own pixels-per-thread and batch parameters.
 
@@ -54,20 +55,23 @@ SPACE = {
     "MSPLAT_BLEND_BWD_REGS": [0, 64, 72],
     "MSPLAT_BLEND_SPLIT_FWD": [1, 2],
     "MSPLAT_BLEND_SPLIT_BWD": [1, 2],
+    "MSPLAT_BLEND_RING_FWD": [0, 2, 4],
 }
 DEFAULTS = {"MSPLAT_BLEND_NPIX_FWD": 1, "MSPLAT_BLEND_NPIX_BWD": 2, "MSPLAT_BLEND_GATHER_FWD": 1,
             "MSPLAT_BLEND_GATHER_BWD": 2, "MSPLAT_FEW_LANES": 12, "MSPLAT_SORT_ITEMS": 12,
             "MSPLAT_BLEND_FWD_REGS": 0, "MSPLAT_BLEND_BWD_REGS": 0, "MSPLAT_BLEND_SPLIT_FWD": 1,
-            "MSPLAT_BLEND_SPLIT_BWD": 1}
+            "MSPLAT_BLEND_SPLIT_BWD": 1, "MSPLAT_BLEND_RING_FWD": 0}
 # the multi-camera blend grid's own parameters (workload "batch")
 BATCH_SPACE = {
     "MSPLAT_BATCH_BLEND_NPIX_FWD": [1, 2],
     "MSPLAT_BATCH_BLEND_NPIX_BWD": [1, 2, 4],
     "MSPLAT_BATCH_BLEND_GATHER_FWD": [1, 2],
     "MSPLAT_BATCH_BLEND_GATHER_BWD": [1, 2, 4],
+    "MSPLAT_BATCH_BLEND_RING_FWD": [0, 2, 4],
 }
 BATCH_DEFAULTS = {"MSPLAT_BATCH_BLEND_NPIX_FWD": 1, "MSPLAT_BATCH_BLEND_NPIX_BWD": 2,
-                  "MSPLAT_BATCH_BLEND_GATHER_FWD": 1, "MSPLAT_BATCH_BLEND_GATHER_BWD": 2}
+                  "MSPLAT_BATCH_BLEND_GATHER_FWD": 1, "MSPLAT_BATCH_BLEND_GATHER_BWD": 2,
+                  "MSPLAT_BATCH_BLEND_RING_FWD": 0}
 TUNE_DIR = os.path.join(_build.PKG_DIR, "_build", "tune")
 
 

@@ -485,6 +485,33 @@ __device__ __forceinline__ PixPow<NPIX> blend_power_n(float a, float b, float c,
     return out;
 }
 
+// One entry of a tile's list: its record (uv, conic, opacity, power bound,
+// list index), features and warp-block mask, and whether the tile cull (the
+// box of ROWS rows from by0) keeps it.
+template <int C, int NPIX, int ROWS>
+__device__ __forceinline__ bool gather_entry(int j, const int32_t *__restrict__ idx_sorted,
+                                             const float2 *__restrict__ uv, const float *__restrict__ conic,
+                                             const float *__restrict__ opacity, const float *__restrict__ feature,
+                                             float bx0, float by0, float4 &A, float4 &B, float4 &F, int &G,
+                                             unsigned &M) {
+    const int g = idx_sorted[j];
+    const float2 p = uv[g];
+    const float ca = conic[3 * g], cb = conic[3 * g + 1], cc = conic[3 * g + 2];
+    const float op = opacity[g];
+    float L;
+    const bool keep = !cull_box(p.x, p.y, ca, cb, cc, op, bx0, by0, bx0 + (float)(kTile - 1),
+                                by0 + (float)(ROWS - 1), L);
+    M = keep ? warp_block_mask<4 * NPIX, ROWS>(p.x, p.y, ca, cb, cc, L, bx0, by0) : 0u;
+    A = make_float4(p.x, p.y, ca, cb);
+    B = make_float4(cc, op, power_bound(op), __int_as_float(j));
+    float f[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+    for (int q = 0; q < C; ++q) f[q] = feature[(size_t)g * C + q];
+    F = make_float4(f[0], f[1], f[2], f[3]);
+    G = g;
+    return keep;
+}
+
 // Gathers GE entries per thread (thread t owns list positions
 // base + dir * (t * GE + r)) and compacts the kept ones into shared
 // memory in list order, with the mask of the warp blocks (8 columns by
@@ -514,23 +541,9 @@ __device__ __forceinline__ int gather_small(int base, int dir, int lo, int hi,
     for (int r = 0; r < GE; ++r) {
         const int j = base + dir * ((int)threadIdx.x * GE + r);
         keep[r] = false;
-        if (j >= lo && j < hi) {
-            const int g = idx_sorted[j];
-            const float2 p = uv[g];
-            const float ca = conic[3 * g], cb = conic[3 * g + 1], cc = conic[3 * g + 2];
-            const float op = opacity[g];
-            float L;
-            keep[r] = !cull_box(p.x, p.y, ca, cb, cc, op, bx0, by0, bx0 + (float)(kTile - 1),
-                                by0 + (float)(ROWS - 1), L);
-            M[r] = keep[r] ? warp_block_mask<4 * NPIX, ROWS>(p.x, p.y, ca, cb, cc, L, bx0, by0) : 0u;
-            A[r] = make_float4(p.x, p.y, ca, cb);
-            B[r] = make_float4(cc, op, power_bound(op), __int_as_float(j));
-            float f[4] = {0.f, 0.f, 0.f, 0.f};
-#pragma unroll
-            for (int q = 0; q < C; ++q) f[q] = feature[(size_t)g * C + q];
-            F[r] = make_float4(f[0], f[1], f[2], f[3]);
-            G[r] = g;
-        }
+        if (j >= lo && j < hi)
+            keep[r] = gather_entry<C, NPIX, ROWS>(j, idx_sorted, uv, conic, opacity, feature, bx0, by0, A[r], B[r],
+                                                  F[r], G[r], M[r]);
         nk += keep[r];
     }
     // Block exclusive scan of the per-thread counts (NT <= 256 threads).
@@ -564,6 +577,57 @@ __device__ __forceinline__ int gather_small(int base, int dir, int lo, int hi,
     }
     __syncthreads();
     return total;
+}
+
+// The forward's walk over one gathered batch of n entries: each warp walks,
+// 32 entries at a time, only the entries whose warp-block mask has its bit
+// (a warp-uniform bit set from one ballot), and leaves the batch once all
+// of its pixels are done.  list0: the list index of the tile's first entry.
+template <int C, int NPIX>
+__device__ __forceinline__ void fwd_walk_batch(int n, const float4 *sA, const float4 *sB, const float4 *sF,
+                                               const unsigned char *sM, unsigned wbit, float fx,
+                                               const float (&fy)[NPIX], bool (&done)[NPIX], float (&T)[NPIX],
+                                               float (&F)[NPIX][4], int (&last)[NPIX], int list0) {
+    const int lane = threadIdx.x & 31;
+    bool warp_done = false;
+    for (int kw = 0; kw < n && !warp_done; kw += 32) {
+        unsigned bits = __ballot_sync(0xffffffffu, kw + lane < n && (sM[kw + lane] & wbit));
+        while (bits) {
+            bool ad = true;
+#pragma unroll
+            for (int i = 0; i < NPIX; ++i) ad &= done[i];
+            if (__all_sync(0xffffffffu, ad)) {
+                warp_done = true;
+                break;
+            }
+            const int k = kw + __ffs(bits) - 1;
+            bits &= bits - 1u;
+            const float4 A = sA[k], B = sB[k];
+            const float dx = A.x - fx;
+            float dy[NPIX];
+#pragma unroll
+            for (int i = 0; i < NPIX; ++i) dy[i] = A.y - fy[i];
+            const PixPow<NPIX> pw = blend_power_n<NPIX>(A.z, A.w, B.x, dx, dy);
+            const float4 f = sF[k];
+            const float fv[4] = {f.x, f.y, f.z, f.w};
+#pragma unroll
+            for (int i = 0; i < NPIX; ++i) {
+                const float power = pw.v[i];
+                if (done[i] || power > 0.0f || power < B.z) continue;
+                const float alpha = fminf(0.99f, B.y * __expf(power));
+                if (alpha < 1.0f / 255.0f) continue;
+                const float nT = T[i] * (1.0f - alpha);
+                if (nT < 0.0001f) {
+                    done[i] = true;
+                    continue;
+                }
+#pragma unroll
+                for (int q = 0; q < C; ++q) F[i][q] += fv[q] * alpha * T[i];
+                T[i] = nT;
+                last[i] = __float_as_int(B.w) - list0 + 1;
+            }
+        }
+    }
 }
 
 // SPLIT: a tile is rendered by SPLIT blocks of kTile / SPLIT rows each
@@ -627,48 +691,7 @@ blend_fwd_small_kernel(int P, const float2 *__restrict__ uv, const float *__rest
                                                          opacity, feature, bx0, by0, sA, sB, sF, nullptr, sM, scan,
                                                          all_done);
         if (n < 0) break;  // every pixel of the block is done
-        // Each warp walks, 32 entries at a time, only the entries whose row
-        // mask has its bit (a warp-uniform bit set from one ballot), and
-        // leaves the batch once all of its pixels are done.
-        bool warp_done = false;
-        for (int kw = 0; kw < n && !warp_done; kw += 32) {
-          unsigned bits = __ballot_sync(0xffffffffu, kw + lane < n && (sM[kw + lane] & wbit));
-          while (bits) {
-            bool ad = true;
-#pragma unroll
-            for (int i = 0; i < NPIX; ++i) ad &= done[i];
-            if (__all_sync(0xffffffffu, ad)) {
-                warp_done = true;
-                break;
-            }
-            const int k = kw + __ffs(bits) - 1;
-            bits &= bits - 1u;
-            const float4 A = sA[k], B = sB[k];
-            const float dx = A.x - fx;
-            float dy[NPIX];
-#pragma unroll
-            for (int i = 0; i < NPIX; ++i) dy[i] = A.y - fy[i];
-            const PixPow<NPIX> pw = blend_power_n<NPIX>(A.z, A.w, B.x, dx, dy);
-            const float4 f = sF[k];
-            const float fv[4] = {f.x, f.y, f.z, f.w};
-#pragma unroll
-            for (int i = 0; i < NPIX; ++i) {
-                const float power = pw.v[i];
-                if (done[i] || power > 0.0f || power < B.z) continue;
-                const float alpha = fminf(0.99f, B.y * __expf(power));
-                if (alpha < 1.0f / 255.0f) continue;
-                const float nT = T[i] * (1.0f - alpha);
-                if (nT < 0.0001f) {
-                    done[i] = true;
-                    continue;
-                }
-#pragma unroll
-                for (int q = 0; q < C; ++q) F[i][q] += fv[q] * alpha * T[i];
-                T[i] = nT;
-                last[i] = __float_as_int(B.w) - range.x + 1;
-            }
-          }
-        }
+        fwd_walk_batch<C, NPIX>(n, sA, sB, sF, sM, wbit, fx, fy, done, T, F, last, range.x);
     }
 #pragma unroll
     for (int i = 0; i < NPIX; ++i) {
@@ -680,6 +703,217 @@ blend_fwd_small_kernel(int P, const float2 *__restrict__ uv, const float *__rest
 #pragma unroll
             for (int q = 0; q < C; ++q) out[(size_t)q * H * W + pix] = F[i][q] + T[i] * bg;
         }
+    }
+}
+
+// ===================================================================
+// Forward blend as a producer / consumer ring (C <= 4, one pixel per
+// consumer thread).
+//
+// NP producer warps gather, cull and mask each 256-entry batch of a tile's
+// list (the same per-entry work as gather_small, compacted in list order)
+// into one of two shared-memory slots; the 8 consumer warps (one pixel per
+// thread, the warp blocks of blend_fwd_small_kernel) blend a slot while the
+// producers fill the other.  The hand-off is two mbarriers per slot: "full"
+// (the producers' threads arrive once their records are written) and
+// "empty" (each consumer warp arrives once done with the slot), so there is
+// no block-wide barrier between batches and consumer warps with little work
+// in a batch run on into the next one.  The producers stop at the end of
+// the list or once every consumer warp's pixels are done (a shared count),
+// and publish an end marker.  Results equal blend_fwd_small_kernel's bit
+// for bit (same entries in the same order, same per-pair code).
+//
+// Every wait is bounded: after `wait_limit` polls (each suspends for at most
+// kWaitHintNs) the thread sets the device error word g_wait_error and
+// leaves its loop, so a lost hand-off ends the kernel with an error the
+// host reads (msplat_wait_error) instead of a hang.
+// ===================================================================
+
+static __device__ int g_wait_error;  // 1 after a bounded wait of a blend gave up
+constexpr uint32_t kWaitHintNs = 1000;
+#ifndef MSPLAT_WAIT_LIMIT
+#define MSPLAT_WAIT_LIMIT (1 << 21)  // polls of <= 1 us each: about 2 s at most
+#endif
+static int g_wait_limit = MSPLAT_WAIT_LIMIT;
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
+    asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.shared::cta.b64 st, [%0];\n\t}" ::"r"(smem_u32(bar))
+                 : "memory");
+}
+
+__device__ __forceinline__ uint32_t mbar_try_wait(uint32_t addr, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(addr), "r"(parity), "r"(kWaitHintNs)
+        : "memory");
+    return ok;
+}
+
+// One thread waits for the completion of the barrier's phase of parity
+// `parity`; false (and the error word set) after `limit` polls.
+__device__ __forceinline__ bool mbar_wait_one(uint64_t *bar, uint32_t parity, int limit) {
+    const uint32_t a = smem_u32(bar);
+    for (int it = 0; it < limit; ++it)
+        if (mbar_try_wait(a, parity)) return true;
+    atomicExch(&g_wait_error, 1);
+    return false;
+}
+
+// The whole warp waits (every lane polls, so every lane acquires the
+// producers' writes), and the outcome is the same in every lane: a phase
+// stays complete until this warp itself takes part in the next one, so once
+// any lane sees it, all do within an iteration.  Bounded by `limit` polls.
+__device__ __forceinline__ bool mbar_wait_warp(uint64_t *bar, uint32_t parity, int limit) {
+    const uint32_t a = smem_u32(bar);
+    for (int it = 0; it < limit; ++it)
+        if (__all_sync(0xffffffffu, mbar_try_wait(a, parity) != 0)) return true;
+    if ((threadIdx.x & 31) == 0) atomicExch(&g_wait_error, 1);
+    return false;
+}
+
+// Barrier 1 among the NP producer warps only (the consumers never use it).
+template <int NP>
+__device__ __forceinline__ void producer_sync() {
+    asm volatile("bar.sync 1, %0;" ::"n"(NP * 32) : "memory");
+}
+
+template <int C, int NP, bool BATCH = false>
+__global__ void __launch_bounds__(kTilePixels + 32 * NP)
+blend_fwd_ring_kernel(int P, const float2 *__restrict__ uv, const float *__restrict__ conic,
+                      const float *__restrict__ opacity, const float *__restrict__ feature,
+                      const int32_t *__restrict__ idx_sorted, const int2 *__restrict__ tile_range, float bg, int W,
+                      int H, float *__restrict__ out, float *__restrict__ final_T, int32_t *__restrict__ ncontrib,
+                      BlendBatch bb, int wait_limit) {
+    constexpr int NC = kTilePixels / 32;       // consumer warps (one pixel per thread)
+    constexpr int SLOT = kTilePixels;          // entries per batch
+    constexpr int PER = SLOT / (32 * NP);      // gather rounds per producer warp
+    static_assert(SLOT % (32 * NP) == 0, "producer warps must split a batch evenly");
+    __shared__ float4 sA[2][SLOT], sB[2][SLOT], sF[2][SLOT];
+    __shared__ unsigned char sM[2][SLOT];
+    __shared__ int scount[2], sstop[2], pcount[2][NP];
+    __shared__ int ndone;
+    __shared__ __align__(8) uint64_t full_bar[2], empty_bar[2];
+
+    const BlendSite site = blend_site<BATCH, 1>(bb, W, H);
+    if (BATCH) {
+        W = site.W;
+        H = site.H;
+        uv += site.row_off;
+        conic += 3 * site.row_off;
+        opacity += site.op_off;
+        feature += (size_t)C * site.feat_off;
+        out += (size_t)C * site.pix_off;
+        final_T += site.pix_off;
+        ncontrib += site.pix_off;
+    }
+    const int2 range = tile_range[site.tidx];
+    const float bx0 = (float)(site.tx * kTile), by0 = (float)(site.ty * kTile);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (threadIdx.x == 0) {
+        mbar_init(&full_bar[0], 32 * NP);
+        mbar_init(&full_bar[1], 32 * NP);
+        mbar_init(&empty_bar[0], NC);
+        mbar_init(&empty_bar[1], NC);
+        ndone = 0;
+    }
+    __syncthreads();
+
+    if (warp >= NC) {
+        // ------------------------------------------------------- producers
+        const int pw = warp - NC;
+        for (int k = 0, start = range.x;; ++k, start += SLOT) {
+            const int s = k & 1;
+            // One producer thread waits for the slot and decides for all
+            // (so a timeout never splits the producers at their barrier).
+            if (pw == 0 && lane == 0) {
+                if (!mbar_wait_one(&empty_bar[s], ((k >> 1) & 1) ^ 1, wait_limit)) sstop[s] = 2;
+                else sstop[s] = (start >= range.y || *(volatile int *)&ndone >= NC) ? 1 : 0;
+            }
+            producer_sync<NP>();
+            if (sstop[s] == 2) return;  // gave up waiting: the consumers time out too
+            const bool stop = sstop[s] != 0;
+            int n = -1;
+            if (!stop) {
+                float4 A[PER], B[PER], F[PER];
+                int G[PER];
+                unsigned M[PER], ballots[PER];
+                int kept = 0;
+#pragma unroll
+                for (int r = 0; r < PER; ++r) {
+                    const int j = start + pw * (32 * PER) + r * 32 + lane;  // list order: warp, round, lane
+                    bool keep = false;
+                    if (j < range.y)
+                        keep = gather_entry<C, 1, kTile>(j, idx_sorted, uv, conic, opacity, feature, bx0, by0, A[r],
+                                                         B[r], F[r], G[r], M[r]);
+                    ballots[r] = __ballot_sync(0xffffffffu, keep);
+                    kept += __popc(ballots[r]);
+                }
+                if (lane == 0) pcount[s][pw] = kept;
+                producer_sync<NP>();
+                int base = 0;
+                n = 0;
+#pragma unroll
+                for (int q = 0; q < NP; ++q) {
+                    const int c = pcount[s][q];
+                    base += q < pw ? c : 0;
+                    n += c;
+                }
+#pragma unroll
+                for (int r = 0; r < PER; ++r) {
+                    if ((ballots[r] >> lane) & 1u) {
+                        const int pos = base + __popc(ballots[r] & ((1u << lane) - 1u));
+                        sA[s][pos] = A[r];
+                        sB[s][pos] = B[r];
+                        sF[s][pos] = F[r];
+                        sM[s][pos] = (unsigned char)M[r];
+                    }
+                    base += __popc(ballots[r]);
+                }
+            }
+            if (pw == 0 && lane == 0) scount[s] = n;
+            mbar_arrive(&full_bar[s]);  // releases this thread's slot writes
+            if (stop) return;
+        }
+    }
+
+    // ------------------------------------------------------------ consumers
+    const int px = site.tx * kTile + 8 * (warp & 1) + (lane & 7);
+    const int py = site.ty * kTile + 4 * (warp >> 1) + (lane >> 3);
+    const unsigned wbit = 1u << warp;
+    const float fx = (float)px;
+    const float fy[1] = {(float)py};
+    float T[1] = {1.0f}, F[1][4] = {{0.f, 0.f, 0.f, 0.f}};
+    int last[1] = {0};
+    bool done[1] = {!(px < W && py < H)};
+    bool counted = false;
+    for (int k = 0;; ++k) {
+        const int s = k & 1;
+        if (!mbar_wait_warp(&full_bar[s], (k >> 1) & 1, wait_limit)) break;
+        const int n = scount[s];
+        if (n < 0) break;
+        fwd_walk_batch<C, 1>(n, sA[s], sB[s], sF[s], sM[s], wbit, fx, fy, done, T, F, last, range.x);
+        if (!counted && __all_sync(0xffffffffu, done[0])) {
+            counted = true;
+            if (lane == 0) atomicAdd(&ndone, 1);
+        }
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&empty_bar[s]);
+    }
+    if (px < W && py < H) {
+        const int pix = py * W + px;
+        final_T[pix] = T[0];
+        ncontrib[pix] = last[0];
+#pragma unroll
+        for (int q = 0; q < C; ++q) out[(size_t)q * H * W + pix] = F[0][q] + T[0] * bg;
     }
 }
 
@@ -1005,6 +1239,17 @@ constexpr int kGatherFwd = MSPLAT_BLEND_GATHER_FWD, kGatherBwd = MSPLAT_BLEND_GA
 #define MSPLAT_BATCH_BLEND_GATHER_BWD MSPLAT_BATCH_BLEND_NPIX_BWD
 #endif
 constexpr int kBatchNpixFwd = MSPLAT_BATCH_BLEND_NPIX_FWD, kBatchNpixBwd = MSPLAT_BATCH_BLEND_NPIX_BWD;
+// The C <= 4 forward as a producer / consumer ring (blend_fwd_ring_kernel)
+// with this many producer warps (2 or 4), or the gather-barrier kernel (0);
+// the default is a tunable, msplat_set_blend_ring changes it at run time.
+#ifndef MSPLAT_BLEND_RING_FWD
+#define MSPLAT_BLEND_RING_FWD 0
+#endif
+#ifndef MSPLAT_BATCH_BLEND_RING_FWD
+#define MSPLAT_BATCH_BLEND_RING_FWD MSPLAT_BLEND_RING_FWD
+#endif
+static int g_fwd_ring = MSPLAT_BLEND_RING_FWD;
+static int g_batch_fwd_ring = MSPLAT_BATCH_BLEND_RING_FWD;
 constexpr int kBatchGatherFwd = MSPLAT_BATCH_BLEND_GATHER_FWD, kBatchGatherBwd = MSPLAT_BATCH_BLEND_GATHER_BWD;
 // Blocks per tile of the C <= 4 kernels (1 or 2: whole tiles, or halves of
 // 8 rows with their own gather, cull and end; compile-time tunables).
@@ -1023,7 +1268,13 @@ void launch_small(bool bwd, dim3 grid, cudaStream_t stream, int P, const float2 
                   const float *dout, float *duv, float *dcon, float *dop, float *dfeat) {
     const dim3 gf(grid.x, grid.y * kSplitFwd), gb(grid.x, grid.y * kSplitBwd);
     constexpr int tf = kTilePixels / kBlendNpixFwd / kSplitFwd, tb = kTilePixels / kBlendNpixBwd / kSplitBwd;
-    if (!bwd)
+    if (!bwd && g_fwd_ring == 2)
+        launch(blend_fwd_ring_kernel<C, 2>, grid, kTilePixels + 64, 0, stream, P, uv, conic, opacity, feature, idx,
+               tr, bg, W, H, out, final_T, nc, BlendBatch{}, g_wait_limit);
+    else if (!bwd && g_fwd_ring == 4)
+        launch(blend_fwd_ring_kernel<C, 4>, grid, kTilePixels + 128, 0, stream, P, uv, conic, opacity, feature, idx,
+               tr, bg, W, H, out, final_T, nc, BlendBatch{}, g_wait_limit);
+    else if (!bwd)
         launch(blend_fwd_small_kernel<C, kBlendNpixFwd, kSplitFwd, false, kGatherFwd>, gf, tf, 0, stream,
             P, uv, conic, opacity, feature, idx, tr, bg, W, H, out, final_T, nc, BlendBatch{});
     else if (bg != 0.0f)
@@ -1128,7 +1379,13 @@ void launch_small_batch(bool bwd, int tiles, cudaStream_t stream, const BlendBat
                         const int2 *tr, float bg, float *out, float *final_T, int32_t *nc, const float *fT,
                         const int32_t *nci, const float *dout, float *duv, float *dcon, float *dop, float *dfeat) {
     constexpr int tf = kTilePixels / kBatchNpixFwd, tb = kTilePixels / kBatchNpixBwd;
-    if (!bwd)
+    if (!bwd && g_batch_fwd_ring == 2)
+        launch(blend_fwd_ring_kernel<C, 2, true>, tiles, kTilePixels + 64, 0, stream, 0, uv, conic, opacity, feature,
+               idx, tr, bg, 1, 1, out, final_T, nc, bb, g_wait_limit);
+    else if (!bwd && g_batch_fwd_ring == 4)
+        launch(blend_fwd_ring_kernel<C, 4, true>, tiles, kTilePixels + 128, 0, stream, 0, uv, conic, opacity,
+               feature, idx, tr, bg, 1, 1, out, final_T, nc, bb, g_wait_limit);
+    else if (!bwd)
         launch(blend_fwd_small_kernel<C, kBatchNpixFwd, 1, true, kBatchGatherFwd>, tiles, tf, 0, stream, 0, uv,
                conic, opacity, feature, idx, tr, bg, 1, 1, out, final_T, nc, bb);
     else if (bg != 0.0f)
@@ -1221,4 +1478,33 @@ extern "C" int msplat_batch_alpha_blending_backward(const void *plan, int B, int
                opacity, feature, idx_sorted, (const int2 *)tile_range, bg, 1, 1, final_T, ncontrib, dL_dout, dL_duv,
                dL_dconic, dL_dopacity, dL_dfeature, bb);
     return check_launch("batch_alpha_blending_backward");
+}
+
+extern "C" int msplat_set_blend_ring(int producer_warps, int batch_producer_warps) {
+    if ((producer_warps != 0 && producer_warps != 2 && producer_warps != 4) ||
+        (batch_producer_warps != 0 && batch_producer_warps != 2 && batch_producer_warps != 4))
+        return set_error(MSPLAT_ERR_INVALID_ARGUMENT, "set_blend_ring: producer warps must be 0, 2 or 4");
+    g_fwd_ring = producer_warps;
+    g_batch_fwd_ring = batch_producer_warps;
+    return MSPLAT_OK;
+}
+
+extern "C" int msplat_set_wait_limit(int polls) {
+    if (polls < 0) return set_error(MSPLAT_ERR_INVALID_ARGUMENT, "set_wait_limit: polls < 0");
+    g_wait_limit = polls;
+    return MSPLAT_OK;
+}
+
+extern "C" int msplat_wait_error(int reset, int *error, msplat_stream_t stream) {
+    int h = 0;
+    cudaError_t e = cudaMemcpyFromSymbolAsync(&h, g_wait_error, sizeof(int), 0, cudaMemcpyDeviceToHost, stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+    if (e == cudaSuccess && reset) {
+        const int zero = 0;
+        e = cudaMemcpyToSymbolAsync(g_wait_error, &zero, sizeof(int), 0, cudaMemcpyHostToDevice, stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+    }
+    if (e != cudaSuccess) return set_error(MSPLAT_ERR_LAUNCH, "wait_error: %s", cudaGetErrorString(e));
+    if (error) *error = h;
+    return h ? set_error(MSPLAT_ERR_TIMEOUT, "a bounded device-side wait of a blend gave up") : MSPLAT_OK;
 }
