@@ -103,10 +103,41 @@ batch_preprocess_fwd_kernel(int P, int B, int C, const float *__restrict__ xyz, 
     }
 }
 
+// One camera's per-Gaussian inputs of the adjoint (zeros where the
+// Gaussian is inactive or a pointer is null; the first 4 colour gradients).
+struct BatchBwdIn {
+    float depth;
+    int radius;
+    float2 duv;
+    float dconic[3];
+    float dcol[kShChanBlock];
+    float dop;
+};
+
+__device__ __forceinline__ BatchBwdIn load_batch_bwd_in(bool active, size_t q, int C, const float *__restrict__ depth,
+                                                        const int32_t *__restrict__ radius,
+                                                        const float2 *__restrict__ dL_duv,
+                                                        const float *__restrict__ dL_dconic,
+                                                        const float *__restrict__ dL_dcolor,
+                                                        const float *__restrict__ dL_dop_cam) {
+    BatchBwdIn in;
+    in.depth = active ? depth[q] : 0.0f;
+    in.radius = active ? radius[q] : 0;
+    in.duv = active ? dL_duv[q] : make_float2(0.f, 0.f);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) in.dconic[k] = active ? dL_dconic[3 * q + k] : 0.f;
+#pragma unroll
+    for (int k = 0; k < kShChanBlock; ++k) in.dcol[k] = (active && k < C) ? dL_dcolor[q * C + k] : 0.f;
+    in.dop = (active && dL_dop_cam) ? dL_dop_cam[q] : 0.f;
+    return in;
+}
+
 // Shared memory per block: the coefficient rows, then (backward) one
 // gradient-accumulator row per Gaussian.
+// Up to degree 3 the adjoint fits 128 registers without spilling (4 blocks
+// of 128 threads per SM); higher degrees keep the compiler's choice.
 template <int DEG>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, DEG <= 3 ? 2 : 1)
 batch_preprocess_bwd_kernel(int P, int B, int C, const float *__restrict__ xyz, const float *__restrict__ scales,
                             const float4 *__restrict__ quats, const float *__restrict__ shs,
                             const float *__restrict__ cams, const float *__restrict__ depth,
@@ -150,20 +181,26 @@ batch_preprocess_bwd_kernel(int P, int B, int C, const float *__restrict__ xyz, 
     }
     float gxyz[3] = {0.f, 0.f, 0.f}, gs[3] = {0.f, 0.f, 0.f}, gop = 0.f;
     float4 gq = make_float4(0.f, 0.f, 0.f, 0.f);
+    // The inputs of camera b + 1 are loaded while camera b is computed (the
+    // loop is latency bound at this occupancy otherwise).
+    BatchBwdIn cur = load_batch_bwd_in(active, (size_t)p, C, depth, radius, dL_duv, dL_dconic, dL_dcolor, dL_dop_cam);
     for (int b = 0; b < B; ++b) {
+        const BatchBwdIn in = cur;
+        if (b + 1 < B) cur = load_batch_bwd_in(active, (size_t)(b + 1) * P + p, C, depth, radius, dL_duv, dL_dconic,
+                                                 dL_dcolor, dL_dop_cam);
         float acc[kCamGradVals];
 #pragma unroll
         for (int k = 0; k < kCamGradVals; ++k) acc[k] = 0.f;
         const size_t q = (size_t)b * P + p;
-        if (active && depth[q] != 0.0f) {
+        if (active && in.depth != 0.0f) {
             const Cam c = load_batch_cam(cams, b);
             float g[3] = {0.f, 0.f, 0.f};
-            project_bwd_one(c, px, py, pz, dL_duv[q], 0.0f, g, cam_grads, acc);
-            if (radius[q] > 0) {
+            project_bwd_one(c, px, py, pz, in.duv, 0.0f, g, cam_grads, acc);
+            if (in.radius > 0) {
                 float ge[3], dV[6], ds[3];
                 float4 dq;
-                if (ewa_bwd_one(c, px, py, pz, cov, dL_dconic[3 * q], dL_dconic[3 * q + 1], dL_dconic[3 * q + 2], ge,
-                                dV, cam_grads, acc)) {
+                if (ewa_bwd_one(c, px, py, pz, cov, in.dconic[0], in.dconic[1], in.dconic[2], ge, dV, cam_grads,
+                                acc)) {
                     cov3d_bwd_one(s, qt, dV, ds, dq);
 #pragma unroll
                     for (int k = 0; k < 3; ++k) {
@@ -186,7 +223,12 @@ batch_preprocess_bwd_kernel(int P, int B, int C, const float *__restrict__ xyz, 
                 for (int c0 = 0; c0 < C; c0 += kShChanBlock) {
                     float gc[kShChanBlock] = {0.f, 0.f, 0.f, 0.f};
                     const int nc = min(kShChanBlock, C - c0);
-                    for (int cb = 0; cb < nc; ++cb) gc[cb] = dL_dcolor[q * C + c0 + cb];
+                    if (c0 == 0) {
+#pragma unroll
+                        for (int cb = 0; cb < kShChanBlock; ++cb) gc[cb] = in.dcol[cb];
+                    } else {
+                        for (int cb = 0; cb < nc; ++cb) gc[cb] = dL_dcolor[q * C + c0 + cb];
+                    }
                     sh_basis<DEG, true>(d[0], d[1], d[2], [&](int i, float Y, float yx, float yy, float yz) {
 #pragma unroll
                         for (int cb = 0; cb < kShChanBlock; ++cb) {
@@ -217,7 +259,7 @@ batch_preprocess_bwd_kernel(int P, int B, int C, const float *__restrict__ xyz, 
 #pragma unroll
             for (int k = 0; k < 3; ++k) gxyz[k] += g[k];
         }
-        if (active && dL_dop_cam) gop += dL_dop_cam[q];
+        gop += in.dop;
         if (cam_grads) {
             const int cb = b % kCamChunk;
             const float tot = warp_reduce_scatter_16(acc);
