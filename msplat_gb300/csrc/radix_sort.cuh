@@ -155,6 +155,27 @@ radix_rowscan_kernel(uint32_t *__restrict__ hist, uint32_t *__restrict__ totals,
     if (threadIdx.x == 0) totals[d] = carry;
 }
 
+// Segmented row scan, one warp per (digit, segment): the segment's part of
+// the digit's row scanned in place (exclusive) and its total to
+// totals[s][d].  Any number of segments at the cost of their tiles.
+static __global__ void __launch_bounds__(256)
+radix_rowscan_warp_kernel(uint32_t *__restrict__ hist, uint32_t *__restrict__ totals, int ntiles, SortSegs segs) {
+    const int gw = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
+    if (gw >= kRadix * segs.nseg) return;  // whole warps
+    const int s = gw / kRadix, d = gw - s * kRadix;
+    const int t0 = segs.tile_start[s], t1 = segs.tile_start[s + 1];
+    uint32_t *row = hist + (size_t)d * ntiles;
+    uint32_t carry = 0;
+    for (int c0 = t0; c0 < t1; c0 += 32) {
+        const int i = c0 + lane;
+        const uint32_t v = i < t1 ? row[i] : 0u;
+        const uint32_t inc = warp_inclusive_scan(v);
+        if (i < t1) row[i] = carry + inc - v;
+        carry += __shfl_sync(0xffffffffu, inc, 31);
+    }
+    if (lane == 0) totals[(size_t)s * kRadix + d] = carry;
+}
+
 // -------------------------------------------------------------- downsweep
 inline size_t radix_downsweep_smem(size_t key_bytes) {
     return kSortTile * (key_bytes + 4) + (size_t)(kSortWarps * kRadix + 2 * kRadix) * 4;
@@ -360,7 +381,8 @@ int radix_sort_segmented(int ntiles, const SortSegs &segs, int begin_bit, int pa
         uint32_t *tot = totals + (size_t)p * segs.nseg * kRadix;
         launch(radix_upsweep_kernel<K, false, true>, ntiles, kSortThreads, 0, stream, ksrc, (int64_t)0, shift,
                ntiles, hist, (const int64_t *)nullptr, segs);
-        launch(radix_rowscan_kernel, dim3(kRadix, segs.nseg), 1024, 0, stream, hist, tot, ntiles, segs);
+        launch(radix_rowscan_warp_kernel, (unsigned)ceil_div64((int64_t)kRadix * segs.nseg, 8), 256, 0, stream,
+               hist, tot, ntiles, segs);
         launch(down, ntiles, kSortThreads, smem, stream, ksrc, vsrc, kdst, vdst, (int64_t)0, shift, ntiles, hist,
                (const uint32_t *)tot, (const int64_t *)nullptr, segs);
         ksrc = kdst;
