@@ -267,30 +267,6 @@ MSPLAT_API int msplat_sort_gaussian_finish_capacity(int P, const float *uv, cons
                                  void *workspace, size_t workspace_bytes,
                                  msplat_stream_t stream);
 
-/* The culled lists through tile-row segments (the fused path's sort; no
- * counterpart in the reference).  The prepare is the culled prepare plus,
- * per tile row, each 256-Gaussian block's intersections in that row;
- * counts (device, int64 [3]): [0] intersections, [1] as for the culled
- * prepare (tiles[] disagreeing with the rectangles: the reference layout is
- * needed), [2] the padded length a finish needs.  The finish emits every
- * intersection straight into its tile row's segment (rows start on
- * 3072-entry sort tiles), in depth order, and sorts each row by tile
- * column with one 8-bit radix pass: each tile's list equals the culled
- * finish's, but idx_sorted [capacity] has unused slots between rows (never
- * inside a tile's range).  capacity: a multiple of 3072; status (device
- * int32, may be NULL) = 1 if it is below counts[2] or counts[1] != 0.  No
- * host read.  Grids up to 256 x 4096 tiles (else MSPLAT_ERR_UNSUPPORTED). */
-MSPLAT_API size_t msplat_sort_rows_prepare_workspace_size(int P, int W, int H);
-MSPLAT_API int msplat_sort_gaussian_prepare_rows(int P, const float *depth, const int32_t *radius,
-                                                 const int32_t *tiles, const float *uv, const float *conic,
-                                                 const float *opacity, int W, int H, int64_t *counts,
-                                                 void *workspace, size_t workspace_bytes, msplat_stream_t stream);
-MSPLAT_API size_t msplat_sort_rows_finish_workspace_size(int W, int H, int64_t capacity);
-MSPLAT_API int msplat_sort_gaussian_finish_rows(int P, int W, int H, int64_t capacity, const int64_t *counts,
-                                                const void *prepare_workspace, int32_t *idx_sorted,
-                                                int32_t *tile_range, int32_t *status, void *workspace,
-                                                size_t workspace_bytes, msplat_stream_t stream);
-
 /* ------------------------------------------------------------------------ */
 /* Alpha blending: replaces alphaBlendingForward / alphaBlendingBackward
  * (msplat/src/alpha_blending.cu:248-394, :396-573; ext.cpp:24-25).

@@ -65,10 +65,6 @@ _SIGNATURES = {
         _I, [_I, _I, _P, _P, _P, _P, _P, _F, _F, _I, _I, _P, _P, _P, _P, _P, _P, _P, _P]),
     "msplat_batch_preprocess_backward": (
         _I, [_I, _I, _P, _P, _P, _P, _I, _I, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _SZ, _P]),
-    "msplat_sort_rows_prepare_workspace_size": (_SZ, [_I, _I, _I]),
-    "msplat_sort_gaussian_prepare_rows": (_I, [_I, _P, _P, _P, _P, _P, _P, _I, _I, _P, _P, _SZ, _P]),
-    "msplat_sort_rows_finish_workspace_size": (_SZ, [_I, _I, _I64]),
-    "msplat_sort_gaussian_finish_rows": (_I, [_I, _I, _I, _I64, _P, _P, _P, _P, _P, _P, _SZ, _P]),
     "msplat_set_blend_ring": (_I, [_I, _I]),
     "msplat_set_wait_limit": (_I, [_I]),
     "msplat_wait_error": (_I, [_I, _P, _P]),

@@ -24,7 +24,6 @@
 //   (the reference writes their range out of bounds; we skip that write).
 #include <mutex>
 
-#include "batch_plan.cuh"
 #include "cull.cuh"
 #include "radix_sort.cuh"
 
@@ -88,22 +87,14 @@ depth_key_kernel(int P, const float *__restrict__ depth, const int32_t *__restri
 // rectangle is first shrunk by shrink_rect, negative-depth Gaussians (which
 // no tile range includes) emit nothing, and the rectangle used is stored in
 // depth order in rects[j] for emit_kernel.
-// With rowcnt (the tile-row lists of the fused path) it also writes, per
-// tile row, the intersections of the block's Gaussians in that row:
-// rowcnt[row][block] (dynamic shared memory of gy ints).
 __global__ void __launch_bounds__(256)
 depth_order_count_kernel(int P, const uint32_t *__restrict__ order, const float2 *__restrict__ uv,
                          const float *__restrict__ depth, const int32_t *__restrict__ radius,
                          const int32_t *__restrict__ tiles, const float *__restrict__ conic,
                          const float *__restrict__ opacity, int gx, int gy, int64_t *__restrict__ bsum,
                          int64_t *__restrict__ counts, unsigned long long *__restrict__ neg,
-                         short4 *__restrict__ rects, int64_t *__restrict__ rowcnt) {
+                         short4 *__restrict__ rects) {
     __shared__ int64_t scratch[33];
-    extern __shared__ int srow[];
-    if (rowcnt) {
-        for (int i = threadIdx.x; i < gy; i += blockDim.x) srow[i] = 0;
-        __syncthreads();
-    }
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     bool bad = false, isneg = false;
     int c = 0;
@@ -130,12 +121,6 @@ depth_order_count_kernel(int P, const uint32_t *__restrict__ order, const float2
         }
         if (conic) rects[j] = make_short4((short)x0, (short)y0, (short)x1, (short)y1);
         bad = cref != tiles[g];
-        if (rowcnt && c > 0)
-            for (int ty = y0; ty < y1; ++ty) atomicAdd(&srow[ty], x1 - x0);
-    }
-    if (rowcnt) {
-        __syncthreads();
-        for (int i = threadIdx.x; i < gy; i += blockDim.x) rowcnt[(size_t)i * gridDim.x + blockIdx.x] = srow[i];
     }
     const unsigned mb = __ballot_sync(0xffffffffu, bad), mn = __ballot_sync(0xffffffffu, isneg);
     if ((threadIdx.x & 31) == 0) {
@@ -531,7 +516,7 @@ static int prepare_impl(int P, const float *depth, const int32_t *radius, const 
     const int nb = ceil_div(P, 256);
     launch(depth_order_count_kernel, nb, 256, 0, stream,
         P, ws.order, (const float2 *)uv, depth, radius, tiles, conic, opacity, gx, gy, ws.bsum, counts, ws.neg,
-        ws.rects, (int64_t *)nullptr);
+        ws.rects);
     launch(block_offsets_kernel, 1, 1024, 0, stream, nb, ws.bsum, counts);
     return check_launch("sort_gaussian_prepare");
 }
@@ -633,307 +618,3 @@ extern "C" int msplat_sort_gaussian_finish_capacity(int P, const float *uv, cons
                        workspace, workspace_bytes, stream);
 }
 
-// ------------------------------------------------------- tile-row lists
-// The fused path's culled lists sorted by bucketing: the intersections are
-// emitted straight into one segment per tile row (each Gaussian's run in a
-// row is x0..x1 of its rectangle, so its count per row is its width and the
-// emission needs no key for the row), in depth order within each row, and
-// one stable 8-bit pass per row segment sorts them by tile column -- one
-// radix pass over the intersections instead of two (13-bit tile keys at
-// 1080p).  Each tile's list is the same as after the two-pass sort.  Row
-// segments start on sort tiles, so the lists have unused slots between
-// rows (never inside a tile's range).  Grids up to 256 tiles wide.
-namespace msplat {
-
-constexpr int kRowsMaxGx = 256;   // tile columns fit one 8-bit pass
-constexpr int kRowsMaxGy = 4096;  // the count kernel's per-row histogram in shared memory
-
-// One block per tile row: exclusive scan of its per-block counts in place
-// and the row's total.
-__global__ void __launch_bounds__(1024)
-row_offsets_kernel(int nb, int64_t *__restrict__ rowcnt, int64_t *__restrict__ rowtot) {
-    __shared__ int64_t scratch[33];
-    int64_t *row = rowcnt + (size_t)blockIdx.x * nb;
-    int64_t carry = 0;
-    for (int c0 = 0; c0 < nb; c0 += blockDim.x) {
-        const int i = c0 + threadIdx.x;
-        const int64_t v = i < nb ? row[i] : 0;
-        int64_t tot;
-        const int64_t ex = block_exclusive_scan<int64_t>(v, scratch, &tot);
-        if (i < nb) row[i] = carry + ex;
-        carry += tot;
-    }
-    if (threadIdx.x == 0) rowtot[blockIdx.x] = carry;
-}
-
-// Row segments (in sort tiles) and the counts the caller reads:
-// counts[0] = intersections, counts[2] = the padded length a finish needs.
-__global__ void __launch_bounds__(32)
-row_layout_kernel(int gy, const int64_t *__restrict__ rowtot, int32_t *__restrict__ rstart,
-                  int64_t *__restrict__ counts) {
-    if (threadIdx.x != 0) return;
-    int64_t tiles = 0, total = 0;
-    for (int r = 0; r < gy; ++r) {
-        rstart[r] = (int32_t)min(tiles, (int64_t)INT32_MAX);
-        tiles += ceil_div64(rowtot[r], kSortTile);
-        total += rowtot[r];
-    }
-    rstart[gy] = (int32_t)min(tiles, (int64_t)INT32_MAX);
-    counts[0] = total;
-    counts[2] = tiles * kSortTile;
-}
-
-// The row segments clipped to a capacity of ntiles sort tiles, and the
-// status word: 1 when the capacity is exceeded or the tiles[] entries
-// disagree with the rectangles.
-__global__ void __launch_bounds__(256)
-row_segs_kernel(int gy, int ntiles, const int32_t *__restrict__ rstart, const int64_t *__restrict__ rowtot,
-                const int64_t *__restrict__ counts, int32_t *__restrict__ seg_start, int64_t *__restrict__ seg_count,
-                int32_t *__restrict__ status) {
-    const int r = blockIdx.x * blockDim.x + threadIdx.x;
-    if (r <= gy) seg_start[r] = min(rstart[r], ntiles);
-    if (r < gy) {
-        const int64_t room = (int64_t)(ntiles - min(rstart[r], ntiles)) * kSortTile;
-        seg_count[r] = max((int64_t)0, min(rowtot[r], room));
-    }
-    if (r == 0 && status) status[0] = (rstart[gy] > ntiles || counts[1] != 0) ? 1 : 0;
-}
-
-// Emits the intersections of 256 depth-ordered Gaussians per block into the
-// row segments: warp w takes rows rlo + w, rlo + w + 8, ... of the block's
-// row span; per row it scans the widths of the 256 Gaussians' runs in that
-// row (32 at a time, in depth order) and writes each run (keys = tile
-// columns, values = Gaussian ids) with its lanes spread over the run.
-// Nothing at or past the capacity `cap` is written.
-__global__ void __launch_bounds__(256)
-emit_rows_kernel(int P, int nb, const uint32_t *__restrict__ order, const short4 *__restrict__ rects,
-                 const int64_t *__restrict__ rowcnt, const int32_t *__restrict__ seg_start,
-                 uint32_t *__restrict__ tkeys, uint32_t *__restrict__ tvals, int64_t cap) {
-    __shared__ short4 srect[256];
-    __shared__ int sgid[256];
-    __shared__ int rlo, rhi;
-    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
-    const int j = blockIdx.x * 256 + t;
-    short4 r = make_short4(0, 0, 0, 0);
-    int g = 0;
-    if (j < P) {
-        r = rects[j];
-        g = (int)order[j];
-    }
-    srect[t] = r;
-    sgid[t] = g;
-    if (t == 0) {
-        rlo = kRowsMaxGy;
-        rhi = -1;
-    }
-    __syncthreads();
-    if (r.z > r.x && r.w > r.y) {
-        atomicMin(&rlo, (int)r.y);
-        atomicMax(&rhi, (int)r.w - 1);
-    }
-    __syncthreads();
-    if (rlo > rhi) return;  // no Gaussian of the block emits (uniform over the block)
-    for (int row = rlo + warp; row <= rhi; row += 8) {
-        const int64_t base = (int64_t)seg_start[row] * kSortTile + rowcnt[(size_t)row * nb + blockIdx.x];
-        int64_t run = 0;
-#pragma unroll 1
-        for (int c = 0; c < 256; c += 32) {
-            const short4 q = srect[c + lane];
-            const int w = (q.y <= row && row < q.w) ? q.z - q.x : 0;
-            const int inc = warp_inclusive_scan(w);
-            const int off = inc - w;
-            unsigned todo = __ballot_sync(0xffffffffu, w > 0);
-            while (todo) {
-                const int sl = __ffs(todo) - 1;
-                todo &= todo - 1;
-                const int sw = __shfl_sync(0xffffffffu, w, sl);
-                const int sx0 = __shfl_sync(0xffffffffu, (int)q.x, sl);
-                const int64_t p0 = base + run + __shfl_sync(0xffffffffu, off, sl);
-                const uint32_t sg = (uint32_t)sgid[c + sl];
-                for (int k = lane; k < sw; k += 32) {
-                    const int64_t p = p0 + k;
-                    if (p < cap) {
-                        tkeys[p] = (uint32_t)(sx0 + k);
-                        tvals[p] = sg;
-                    }
-                }
-            }
-            run += __shfl_sync(0xffffffffu, inc, 31);
-        }
-    }
-}
-
-// Tile ranges from the sorted row segments: each thread reads 8 keys (tile
-// columns) of one row segment with a neighbour on each side; a neighbour
-// outside the segment's items counts as "outside".
-__global__ void __launch_bounds__(256)
-range_rows_kernel(int gx, int gy, int ntiles_sort, const int32_t *__restrict__ seg_start,
-                  const int64_t *__restrict__ seg_count, const uint32_t *__restrict__ keys,
-                  int2 *__restrict__ range) {
-    constexpr int K = 8;
-    const int64_t i0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) * K;
-    if (i0 >= (int64_t)ntiles_sort * kSortTile) return;
-    const int st = (int)(i0 / kSortTile);
-    if (st >= seg_start[gy]) return;
-    const int row = upper_index(seg_start, gy, st);
-    const int64_t s0 = (int64_t)seg_start[row] * kSortTile, s1 = s0 + seg_count[row];
-    if (i0 >= s1) return;
-    constexpr uint32_t kOut = 0xffffffffu;
-    uint32_t k[K + 2];
-#pragma unroll
-    for (int u = -1; u <= K; ++u) {
-        const int64_t i = i0 + u;
-        k[u + 1] = (i >= s0 && i < s1) ? keys[i] : kOut;
-    }
-#pragma unroll
-    for (int u = 1; u <= K; ++u) {
-        const uint32_t key = k[u];
-        if (key == kOut) continue;
-        const int64_t i = i0 + u - 1;
-        const int tile = row * gx + (int)key;
-        if (k[u - 1] != key) range[tile].x = (int)i;
-        if (k[u + 1] != key) range[tile].y = (int)(i + 1);
-    }
-}
-
-struct RowsWs {
-    int64_t *rowcnt = nullptr;  // [gy][nb] per-block counts, then their scan within the row
-    int64_t *rowtot = nullptr;  // [gy]
-    int32_t *rstart = nullptr;  // [gy + 1] row segments in sort tiles
-};
-
-template <typename WS>
-inline void rows_carve(WS &w, int P, int gy, RowsWs &rw) {
-    rw.rowcnt = w.template take<int64_t>((size_t)gy * ceil_div(P, 256));
-    rw.rowtot = w.template take<int64_t>(gy);
-    rw.rstart = w.template take<int32_t>(gy + 1);
-}
-
-inline size_t prepare_rows_bytes(int P, int gy) {
-    SizeOnly z;
-    PrepareWs ws;
-    prepare_carve(z, P, ws);
-    RowsWs rw;
-    rows_carve(z, P, gy, rw);
-    return z.s.used;
-}
-
-struct FinishRowsWs {
-    uint32_t *ka = nullptr, *kb = nullptr, *vt = nullptr, *hist = nullptr, *totals = nullptr;
-    int32_t *seg_start = nullptr;
-    int64_t *seg_count = nullptr;
-};
-
-template <typename WS>
-inline void finish_rows_carve(WS &w, int64_t cap, int gy, FinishRowsWs &f) {
-    f.ka = w.template take<uint32_t>(cap);
-    f.kb = w.template take<uint32_t>(cap);
-    f.vt = w.template take<uint32_t>(cap);
-    f.hist = w.template take<uint32_t>((size_t)kRadix * (cap / kSortTile));
-    f.totals = w.template take<uint32_t>((size_t)kRadix * gy);
-    f.seg_start = w.template take<int32_t>(gy + 1);
-    f.seg_count = w.template take<int64_t>(gy);
-}
-
-}  // namespace msplat
-
-extern "C" size_t msplat_sort_rows_prepare_workspace_size(int P, int W, int H) {
-    if (P < 0 || W <= 0 || H <= 0) return 0;
-    return prepare_rows_bytes(P, ceil_div(H, kTile));
-}
-
-extern "C" int msplat_sort_gaussian_prepare_rows(int P, const float *depth, const int32_t *radius,
-                                                 const int32_t *tiles, const float *uv, const float *conic,
-                                                 const float *opacity, int W, int H, int64_t *counts,
-                                                 void *workspace, size_t workspace_bytes, msplat_stream_t stream) {
-    if (P < 0 || W <= 0 || H <= 0)
-        return set_error(MSPLAT_ERR_INVALID_ARGUMENT, "sort_gaussian_prepare_rows: bad sizes");
-    const int gx = ceil_div(W, kTile), gy = ceil_div(H, kTile);
-    if (gx > kRowsMaxGx || gy > kRowsMaxGy)
-        return set_error(MSPLAT_ERR_UNSUPPORTED,
-                         "sort_gaussian_prepare_rows: a grid of %d x %d tiles (at most %d x %d)", gx, gy, kRowsMaxGx,
-                         kRowsMaxGy);
-    if (!counts) return set_error(MSPLAT_ERR_INVALID_ARGUMENT, "sort_gaussian_prepare_rows: null counts");
-    if (P > 0 && (!depth || !radius || !tiles || !uv || !conic || !opacity))
-        return set_error(MSPLAT_ERR_INVALID_ARGUMENT, "sort_gaussian_prepare_rows: null pointer");
-    Workspace w(workspace, workspace_bytes);
-    PrepareWs ws;
-    prepare_carve(w, P, ws);
-    RowsWs rw;
-    rows_carve(w, P, gy, rw);
-    if (w.overflow)
-        return set_error(MSPLAT_ERR_WORKSPACE, "sort_gaussian_prepare_rows: workspace of %zu bytes < %zu",
-                         workspace_bytes, prepare_rows_bytes(P, gy));
-    cudaMemsetAsync(counts, 0, 3 * sizeof(int64_t), stream);
-    cudaMemsetAsync(ws.neg, 0, 2 * sizeof(unsigned long long), stream);
-    cudaMemsetAsync(ws.culled, 0xff, sizeof(int), stream);
-    if (P == 0) {
-        cudaMemsetAsync(rw.rowtot, 0, sizeof(int64_t) * gy, stream);
-        launch(row_layout_kernel, 1, 32, 0, stream, gy, (const int64_t *)rw.rowtot, rw.rstart, counts);
-        return check_launch("sort_gaussian_prepare_rows");
-    }
-    launch(depth_key_kernel, ceil_div(P, 256), 256, 0, stream, P, depth, radius, ws.ka);
-    int st = radix_sort_pairs<uint32_t, false>(P, 0, kDepthPasses, ws.ka, nullptr, ws.ka, ws.order, ws.kb, ws.vt,
-                                               ws.rb, stream);
-    if (st) return st;
-    const int nb = ceil_div(P, 256);
-    launch(depth_order_count_kernel, nb, 256, (size_t)gy * sizeof(int), stream, P, ws.order, (const float2 *)uv,
-           depth, radius, tiles, conic, opacity, gx, gy, ws.bsum, counts, ws.neg, ws.rects, rw.rowcnt);
-    launch(row_offsets_kernel, gy, 1024, 0, stream, nb, rw.rowcnt, rw.rowtot);
-    launch(row_layout_kernel, 1, 32, 0, stream, gy, (const int64_t *)rw.rowtot, rw.rstart, counts);
-    return check_launch("sort_gaussian_prepare_rows");
-}
-
-extern "C" size_t msplat_sort_rows_finish_workspace_size(int W, int H, int64_t capacity) {
-    if (W <= 0 || H <= 0 || capacity < 0) return 0;
-    SizeOnly z;
-    FinishRowsWs f;
-    finish_rows_carve(z, ceil_div64(capacity, kSortTile) * kSortTile, ceil_div(H, kTile), f);
-    return z.s.used;
-}
-
-extern "C" int msplat_sort_gaussian_finish_rows(int P, int W, int H, int64_t capacity, const int64_t *counts,
-                                                const void *prepare_workspace, int32_t *idx_sorted,
-                                                int32_t *tile_range, int32_t *status, void *workspace,
-                                                size_t workspace_bytes, msplat_stream_t stream) {
-    if (P < 0 || W <= 0 || H <= 0 || capacity < 0 || capacity % kSortTile != 0)
-        return set_error(MSPLAT_ERR_INVALID_ARGUMENT,
-                         "sort_gaussian_finish_rows: bad sizes (capacity must be a multiple of %d)", kSortTile);
-    if (capacity > INT32_MAX)
-        return set_error(MSPLAT_ERR_CAPACITY, "sort_gaussian_finish_rows: capacity %lld exceeds int32",
-                         (long long)capacity);
-    const int gx = ceil_div(W, kTile), gy = ceil_div(H, kTile);
-    if (gx > kRowsMaxGx || gy > kRowsMaxGy)
-        return set_error(MSPLAT_ERR_UNSUPPORTED, "sort_gaussian_finish_rows: grid too large");
-    if (!counts || !prepare_workspace || !tile_range || (capacity > 0 && !idx_sorted))
-        return set_error(MSPLAT_ERR_INVALID_ARGUMENT, "sort_gaussian_finish_rows: null pointer");
-    Workspace pw(const_cast<void *>(prepare_workspace), prepare_rows_bytes(P, gy));
-    PrepareWs prep;
-    prepare_carve(pw, P, prep);
-    RowsWs rw;
-    rows_carve(pw, P, gy, rw);
-    Workspace w(workspace, workspace_bytes);
-    FinishRowsWs f;
-    finish_rows_carve(w, capacity, gy, f);
-    if (w.overflow)
-        return set_error(MSPLAT_ERR_WORKSPACE, "sort_gaussian_finish_rows: workspace of %zu bytes < %zu",
-                         workspace_bytes, msplat_sort_rows_finish_workspace_size(W, H, capacity));
-    const int ntiles = (int)(capacity / kSortTile);
-    cudaMemsetAsync(tile_range, 0, sizeof(int32_t) * 2 * (size_t)gx * gy, stream);
-    launch(row_segs_kernel, ceil_div(gy + 1, 256), 256, 0, stream, gy, ntiles, (const int32_t *)rw.rstart,
-           (const int64_t *)rw.rowtot, counts, f.seg_start, f.seg_count, status);
-    if (P == 0 || capacity == 0) return check_launch("sort_gaussian_finish_rows");
-    const int nb = ceil_div(P, 256);
-    launch(emit_rows_kernel, nb, 256, 0, stream, P, nb, (const uint32_t *)prep.order, (const short4 *)prep.rects,
-           (const int64_t *)rw.rowcnt, (const int32_t *)f.seg_start, f.ka, f.vt, capacity);
-    SortSegs segs;
-    segs.tile_start = f.seg_start;
-    segs.count = f.seg_count;
-    segs.nseg = gy;
-    int st = radix_sort_segmented<uint32_t>(ntiles, segs, 0, 1, f.ka, f.vt, f.kb, (uint32_t *)idx_sorted, f.ka,
-                                            f.vt, f.hist, f.totals, stream);
-    if (st) return st;
-    launch(range_rows_kernel, (unsigned)ceil_div64(capacity / 8, 256), 256, 0, stream, gx, gy, ntiles,
-           (const int32_t *)f.seg_start, (const int64_t *)f.seg_count, (const uint32_t *)f.kb, (int2 *)tile_range);
-    return check_launch("sort_gaussian_finish_rows");
-}

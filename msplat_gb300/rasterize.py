@@ -19,7 +19,7 @@ from torch import Tensor
 from . import _lib
 from . import _tensors as tt
 from .alpha_blending import alpha_blending
-from .sort_gaussian import rows_supported, sort_gaussian, sort_gaussian_capacity, sort_gaussian_rows
+from .sort_gaussian import sort_gaussian, sort_gaussian_capacity
 
 
 class _Preprocess(torch.autograd.Function):
@@ -106,10 +106,7 @@ def preprocess(xyz: Tensor, scale: Tensor, rotate: Tensor, intr: Tensor, extr: T
 
 def _sort(uv, depth, W, H, radius, tiles, capacity, status, cull):
     # The fused calls sort culled lists: only the image and gradients leave
-    # them, and those equal the reference lists' (see sort_gaussian's cull);
-    # through tile-row segments where the grid allows (one radix pass).
-    if rows_supported(W, H):
-        return sort_gaussian_rows(uv, depth, W, H, radius, tiles, cull, capacity, status)
+    # them, and those equal the reference lists' (see sort_gaussian's cull).
     if capacity is None:
         return sort_gaussian(uv, depth, W, H, radius, tiles, cull=cull)
     if status is None:

@@ -161,68 +161,3 @@ def sort_gaussian_capacity(uv: Tensor, depth: Tensor, W: int, H: int, radius: Te
             "sort_gaussian_finish_capacity")
     return idx_sorted, tile_range
 
-
-ROWS_MAX_GX, ROWS_MAX_GY = 256, 4096  # tile grid the tile-row lists support
-SORT_TILE = 3072
-
-
-def rows_supported(W: int, H: int) -> bool:
-    return (int(W) + 15) // 16 <= ROWS_MAX_GX and (int(H) + 15) // 16 <= ROWS_MAX_GY
-
-
-def sort_gaussian_rows(uv: Tensor, depth: Tensor, W: int, H: int, radius: Tensor, tiles: Tensor,
-                       cull: Tuple[Tensor, Tensor], capacity: int | None = None,
-                       status: Tensor | None = None) -> Tuple[Tensor, Tensor]:
-    """The culled lists of ``sort_gaussian(..., cull=...)`` sorted through
-    tile-row segments: the intersections are emitted straight into one
-    segment per tile row, in depth order, and one 8-bit radix pass per row
-    sorts them by tile column (one pass over the intersections instead of
-    two).  Every tile's list is the same; idx_sorted has unused slots
-    between the rows (never inside a tile's range), so use it only through
-    tile_range.  With `capacity` (intersections) and a [1] int32 `status`
-    there is no host read: status = 1 if the capacity (plus the rows'
-    padding) was too small or the reference layout is needed.  Grids up to
-    256 x 4096 tiles (``rows_supported``)."""
-    u = tt.f32(uv, "uv", 2)
-    d = tt.f32(depth, "depth")
-    r = tt.i32(radius, "radius").view(-1)
-    t = tt.cuda(tiles, "tiles")
-    if t.dtype != torch.int32:
-        t = t.to(torch.int32)
-    t = t.contiguous().view(-1)
-    conic = tt.f32(cull[0], "conic", 3)
-    opacity = tt.f32(cull[1], "opacity")
-    P = u.shape[0]
-    if d.numel() != P or r.numel() != P or t.numel() != P or conic.shape[0] != P or opacity.numel() != P:
-        raise RuntimeError("uv, depth, radius, tiles, conic and opacity must describe the same number of points")
-    W, H = int(W), int(H)
-    dev = u.device
-    lib = _lib.load()
-    st = _lib.stream(dev)
-    counts = torch.empty(3, dtype=torch.int64, device=dev)
-    ws_prep = _lib.workspace(lib.msplat_sort_rows_prepare_workspace_size(P, W, H), dev)
-    with _lib.stage("sort_gaussian_prepare"):
-        _lib.check(lib.msplat_sort_gaussian_prepare_rows(
-            P, _lib.ptr(d), _lib.ptr(r), _lib.ptr(t), _lib.ptr(u), _lib.ptr(conic), _lib.ptr(opacity), W, H,
-            _lib.ptr(counts), _lib.ptr(ws_prep), ws_prep.numel(), st), "sort_gaussian_prepare_rows")
-    gy = (H + 15) // 16
-    if capacity is None:
-        I, n_mismatch, cap = (int(v) for v in counts.tolist())
-        if n_mismatch:
-            return _sort_reference_layout(u, d, W, H, r, t)
-        st_t = None
-    else:
-        if status is None:
-            raise RuntimeError("a capacity-bounded sort needs a status tensor to report overflow in")
-        st_t = tt.i32(status, "status")
-        cap = -(-(int(capacity) + gy * SORT_TILE) // SORT_TILE) * SORT_TILE  # + the rows' padding
-    if cap > 2**31 - 1:
-        raise RuntimeError(f"sort_gaussian: {cap} intersection slots exceed the int32 range")
-    idx_sorted = torch.empty((max(cap, 1),), dtype=torch.int32, device=dev)
-    tile_range = torch.empty((tt.ntiles(W, H), 2), dtype=torch.int32, device=dev)
-    ws = _lib.workspace(lib.msplat_sort_rows_finish_workspace_size(W, H, cap), dev)
-    with _lib.stage("sort_gaussian_finish"):
-        _lib.check(lib.msplat_sort_gaussian_finish_rows(
-            P, W, H, cap, _lib.ptr(counts), _lib.ptr(ws_prep), _lib.ptr(idx_sorted), _lib.ptr(tile_range),
-            _lib.ptr(st_t), _lib.ptr(ws), ws.numel(), st), "sort_gaussian_finish_rows")
-    return idx_sorted, tile_range
