@@ -1036,6 +1036,9 @@ def main():
     ap.add_argument("--cameras", type=int, default=64)
     ap.add_argument("--no-sub", action="store_true",
                     help="skip the batch / serve / 36-channel sub-results of the default run")
+    ap.add_argument("--blend-ring", type=int, default=None, choices=[0, 2, 4],
+                    help="run the forward blend as the producer / consumer ring with this many producer warps "
+                         "(0: the barrier kernel); default: the tuned choice")
     ap.add_argument("--rate", type=float, default=2000.0, help="serve: Poisson arrival rate (requests/s)")
     ap.add_argument("--duration", type=float, default=10.0, help="serve: seconds of arrivals")
     ap.add_argument("--streams", type=int, default=4, help="serve: worker streams")
@@ -1052,8 +1055,10 @@ def main():
     device = torch.device("cuda", local)
     if world > 1:
         torch.distributed.init_process_group("nccl", device_id=device)
-    from msplat_gb300 import _build
+    from msplat_gb300 import _build, _lib
     _build.build()
+    if args.blend_ring is not None:
+        _lib.check(_lib.load().msplat_set_blend_ring(args.blend_ring, args.blend_ring), "set_blend_ring")
     if args.workload in ("batch", "serve", "config2"):
         if rank == 0:
             run = {"batch": lambda: run_batch(args, device), "serve": lambda: run_serve(args),

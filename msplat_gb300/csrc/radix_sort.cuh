@@ -201,10 +201,9 @@ radix_downsweep_kernel(const K *__restrict__ kin, const uint32_t *__restrict__ v
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int64_t base = (int64_t)blockIdx.x * kSortTile;
-    int tile_n;
+    int tile_n, sg = 0;
     int64_t out_base = 0;  // first item of the segment in the arrays
     if (SEG) {
-        int sg;
         tile_n = seg_tile_items(segs, blockIdx.x, sg);
         if (sg < 0) return;  // past the last segment: nothing to move (uniform over the block)
         totals += (size_t)sg * kRadix;
@@ -216,9 +215,21 @@ radix_downsweep_kernel(const K *__restrict__ kin, const uint32_t *__restrict__ v
     for (int i = tid; i < kSortWarps * kRadix; i += kSortThreads) whist[i] = 0;
     // start of this tile's bucket of digit tid: the digit's start (scan of
     // the totals of the smaller digits) + the tile's offset within the digit
-    const uint32_t dbase = block_exclusive_scan<uint32_t>(totals[tid], scan_scratch, nullptr);
+    const uint32_t dtot = totals[tid];
+    const uint32_t dbase = block_exclusive_scan<uint32_t>(dtot, scan_scratch, nullptr);
     gstart[tid] = dbase + hist[(size_t)tid * ntiles + blockIdx.x];
-    __syncthreads();
+    // A digit that every key of the sort (segment) shares makes the pass the
+    // identity (stable): the tile is copied straight through.
+    const int64_t n_all = SEG ? segs.count[sg] : n;
+    if (__syncthreads_or(n_all > 0 && (int64_t)dtot == n_all)) {
+        for (int i = tid; i < tile_n; i += kSortThreads) {
+            K k = __ldcs(kin + base + i);
+            if (FLIP_IN != FLIP_OUT) k ^= sign_bit<K>();
+            if (kout) kout[base + i] = k;
+            vout[base + i] = vin ? __ldcs(vin + base + i) : (uint32_t)(base + i - out_base);
+        }
+        return;
+    }
 
     K key[kSortItems];
     uint32_t val[kSortItems];

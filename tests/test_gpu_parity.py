@@ -313,6 +313,27 @@ def test_radix_sort_i64_matches_stable_sort():
     np.testing.assert_array_equal(N(vo), vals[order])
 
 
+def test_radix_sort_i64_with_constant_digits():
+    """Passes whose digit every key shares copy the tiles straight through
+    (the identity is the stable result): keys below 2^20 sorted over all 64
+    bits, five of the eight passes constant, with duplicates."""
+    from msplat_gb300 import _lib
+    lib = _lib.load()
+    n = 200_003
+    rng = np.random.default_rng(5)
+    keys = rng.integers(0, 2**20, size=n, dtype=np.int64)
+    keys[::7] = keys[3::7][: len(keys[::7])]
+    vals = np.arange(n, dtype=np.int32)
+    tk, tv = T(keys), T(vals)
+    ko, vo = torch.empty_like(tk), torch.empty_like(tv)
+    ws = _lib.workspace(lib.msplat_radix_sort_i64_workspace_size(n), tk.device)
+    _lib.check(lib.msplat_radix_sort_i64_pairs(n, tk.data_ptr(), tv.data_ptr(), ko.data_ptr(), vo.data_ptr(), 0, 64,
+                                               ws.data_ptr(), ws.numel(), _lib.stream()), "sort")
+    order = np.argsort(keys, kind="stable")
+    np.testing.assert_array_equal(N(ko), keys[order])
+    np.testing.assert_array_equal(N(vo), vals[order])
+
+
 # ----------------------------------------------------------------- blend
 def blend_inputs(n=10000, W=256, H=256, C=3, seed=0):
     s = scene(n, seed, C=C)
