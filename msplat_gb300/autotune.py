@@ -9,7 +9,8 @@ of a warp reduction, the keys per thread of a radix tile (which sets the
 sort tile, 256 x items), optional register caps of the two blend kernels
 (more resident blocks per SM against spills), whether a tile is blended
 by one block or by two of 8 rows each, and whether the forward runs as a
-producer / consumer ring and with how many producer warps.  The tile itself stays 16x16: it is
+producer / consumer ring, with how many producer warps and with what
+minimum of resident ring blocks per SM.  The tile itself stays 16x16: it is
 part of the reference's outputs (tiles_touched, tile_range).  The
 multi-camera blend grid has its own pixels-per-thread and batch parameters.
 
@@ -56,11 +57,12 @@ SPACE = {
     "MSPLAT_BLEND_SPLIT_FWD": [1, 2],
     "MSPLAT_BLEND_SPLIT_BWD": [1, 2],
     "MSPLAT_BLEND_RING_FWD": [0, 2, 4],
+    "MSPLAT_RING_MIN_BLOCKS": [0, 5],
 }
 DEFAULTS = {"MSPLAT_BLEND_NPIX_FWD": 1, "MSPLAT_BLEND_NPIX_BWD": 2, "MSPLAT_BLEND_GATHER_FWD": 1,
             "MSPLAT_BLEND_GATHER_BWD": 2, "MSPLAT_FEW_LANES": 12, "MSPLAT_SORT_ITEMS": 12,
             "MSPLAT_BLEND_FWD_REGS": 0, "MSPLAT_BLEND_BWD_REGS": 0, "MSPLAT_BLEND_SPLIT_FWD": 1,
-            "MSPLAT_BLEND_SPLIT_BWD": 1, "MSPLAT_BLEND_RING_FWD": 0}
+            "MSPLAT_BLEND_SPLIT_BWD": 1, "MSPLAT_BLEND_RING_FWD": 0, "MSPLAT_RING_MIN_BLOCKS": 0}
 # the multi-camera blend grid's own parameters (workload "batch")
 BATCH_SPACE = {
     "MSPLAT_BATCH_BLEND_NPIX_FWD": [1, 2],
@@ -272,11 +274,17 @@ def main() -> None:
 def write_tuning(path: str, workload: str, best: dict, best_ms: float, shape: dict, evaluated: list) -> None:
     """Stores a workload's choice in the tuning file: the frame's under
     "defines" (the single-camera kernels), every other workload's under
-    "workloads"[name]["defines"]; the other sections are kept."""
+    "workloads"[name]["defines"]; the other sections are kept, and so are
+    the settings earlier searches of the workload evaluated (a setting timed
+    again keeps its new time)."""
     data = {}
     if os.path.exists(path):
         with open(path) as f:
             data = json.load(f)
+    before = data.get("evaluated", []) if workload == "frame" else \
+        data.get("workloads", {}).get(workload, {}).get("evaluated", [])
+    fresh = {json.dumps(e["defines"], sort_keys=True) for e in evaluated}
+    evaluated = [e for e in before if json.dumps(e["defines"], sort_keys=True) not in fresh] + list(evaluated)
     if workload == "frame":
         data.update({"defines": best, "ms_per_frame": round(best_ms, 4),
                      "workload": {k: shape[k] for k in ("gaussians", "width", "height")}, "evaluated": evaluated})

@@ -711,8 +711,8 @@ blend_fwd_small_kernel(int P, const float2 *__restrict__ uv, const float *__rest
 // consumer thread).
 //
 // NP producer warps gather, cull and mask each 256-entry batch of a tile's
-// list (the same per-entry work as gather_small, compacted in list order)
-// into one of two shared-memory slots; the 8 consumer warps (one pixel per
+// list (the same per-entry work as gather_small), each compacting its share
+// in list order into its own part of one of two shared-memory slots; the 8 consumer warps (one pixel per
 // thread, the warp blocks of blend_fwd_small_kernel) blend a slot while the
 // producers fill the other.  The hand-off is two mbarriers per slot: "full"
 // (the producers' threads arrive once their records are written) and
@@ -728,6 +728,17 @@ blend_fwd_small_kernel(int P, const float2 *__restrict__ uv, const float *__rest
 // leaves its loop, so a lost hand-off ends the kernel with an error the
 // host reads (msplat_wait_error) instead of a hang.
 // ===================================================================
+
+// Minimum resident ring blocks per SM (compile-time tunable; 0 = the
+// compiler's choice).
+#ifndef MSPLAT_RING_MIN_BLOCKS
+#define MSPLAT_RING_MIN_BLOCKS 0
+#endif
+#if MSPLAT_RING_MIN_BLOCKS > 0
+#define MSPLAT_RING_BOUNDS(T) __launch_bounds__(T, MSPLAT_RING_MIN_BLOCKS)
+#else
+#define MSPLAT_RING_BOUNDS(T) __launch_bounds__(T)
+#endif
 
 static __device__ int g_wait_error;  // 1 after a bounded wait of a blend gave up
 constexpr uint32_t kWaitHintNs = 1000;
@@ -787,7 +798,7 @@ __device__ __forceinline__ void producer_sync() {
 }
 
 template <int C, int NP, bool BATCH = false>
-__global__ void __launch_bounds__(kTilePixels + 32 * NP)
+__global__ void MSPLAT_RING_BOUNDS(kTilePixels + 32 * NP)
 blend_fwd_ring_kernel(int P, const float2 *__restrict__ uv, const float *__restrict__ conic,
                       const float *__restrict__ opacity, const float *__restrict__ feature,
                       const int32_t *__restrict__ idx_sorted, const int2 *__restrict__ tile_range, float bg, int W,
@@ -795,11 +806,12 @@ blend_fwd_ring_kernel(int P, const float2 *__restrict__ uv, const float *__restr
                       BlendBatch bb, int wait_limit) {
     constexpr int NC = kTilePixels / 32;       // consumer warps (one pixel per thread)
     constexpr int SLOT = kTilePixels;          // entries per batch
-    constexpr int PER = SLOT / (32 * NP);      // gather rounds per producer warp
+    constexpr int SUB = SLOT / NP;             // entries per producer warp (its own part of the slot)
+    constexpr int PER = SUB / 32;              // gather rounds per producer warp
     static_assert(SLOT % (32 * NP) == 0, "producer warps must split a batch evenly");
     __shared__ float4 sA[2][SLOT], sB[2][SLOT], sF[2][SLOT];
     __shared__ unsigned char sM[2][SLOT];
-    __shared__ int scount[2], sstop[2], pcount[2][NP];
+    __shared__ int scount[2][NP], sstop[2];
     __shared__ int ndone;
     __shared__ __align__(8) uint64_t full_bar[2], empty_bar[2];
 
@@ -829,6 +841,11 @@ blend_fwd_ring_kernel(int P, const float2 *__restrict__ uv, const float *__restr
 
     if (warp >= NC) {
         // ------------------------------------------------------- producers
+        // Producer warp pw gathers list positions [start + pw SUB, start +
+        // (pw + 1) SUB) and compacts the kept ones, in list order, into its
+        // own part [pw SUB, pw SUB + count) of the slot: the parts follow one
+        // another in list order, so no prefix across producer warps is needed
+        // and each round is written as soon as it is culled.
         const int pw = warp - NC;
         for (int k = 0, start = range.x;; ++k, start += SLOT) {
             const int s = k & 1;
@@ -841,45 +858,33 @@ blend_fwd_ring_kernel(int P, const float2 *__restrict__ uv, const float *__restr
             producer_sync<NP>();
             if (sstop[s] == 2) return;  // gave up waiting: the consumers time out too
             const bool stop = sstop[s] != 0;
-            int n = -1;
+            int n = 0;
             if (!stop) {
-                float4 A[PER], B[PER], F[PER];
-                int G[PER];
-                unsigned M[PER], ballots[PER];
-                int kept = 0;
-#pragma unroll
+                const int j0 = start + pw * SUB;
+                float4 *dA = sA[s] + pw * SUB, *dB = sB[s] + pw * SUB, *dF = sF[s] + pw * SUB;
+                unsigned char *dM = sM[s] + pw * SUB;
+#pragma unroll 2
                 for (int r = 0; r < PER; ++r) {
-                    const int j = start + pw * (32 * PER) + r * 32 + lane;  // list order: warp, round, lane
+                    const int j = j0 + r * 32 + lane;  // list order: round, lane
+                    float4 A, B, F;
+                    int G;
+                    unsigned M;
                     bool keep = false;
                     if (j < range.y)
-                        keep = gather_entry<C, 1, kTile>(j, idx_sorted, uv, conic, opacity, feature, bx0, by0, A[r],
-                                                         B[r], F[r], G[r], M[r]);
-                    ballots[r] = __ballot_sync(0xffffffffu, keep);
-                    kept += __popc(ballots[r]);
-                }
-                if (lane == 0) pcount[s][pw] = kept;
-                producer_sync<NP>();
-                int base = 0;
-                n = 0;
-#pragma unroll
-                for (int q = 0; q < NP; ++q) {
-                    const int c = pcount[s][q];
-                    base += q < pw ? c : 0;
-                    n += c;
-                }
-#pragma unroll
-                for (int r = 0; r < PER; ++r) {
-                    if ((ballots[r] >> lane) & 1u) {
-                        const int pos = base + __popc(ballots[r] & ((1u << lane) - 1u));
-                        sA[s][pos] = A[r];
-                        sB[s][pos] = B[r];
-                        sF[s][pos] = F[r];
-                        sM[s][pos] = (unsigned char)M[r];
+                        keep = gather_entry<C, 1, kTile>(j, idx_sorted, uv, conic, opacity, feature, bx0, by0, A, B,
+                                                         F, G, M);
+                    const unsigned ballot = __ballot_sync(0xffffffffu, keep);
+                    if (keep) {
+                        const int pos = n + __popc(ballot & ((1u << lane) - 1u));
+                        dA[pos] = A;
+                        dB[pos] = B;
+                        dF[pos] = F;
+                        dM[pos] = (unsigned char)M;
                     }
-                    base += __popc(ballots[r]);
+                    n += __popc(ballot);
                 }
             }
-            if (pw == 0 && lane == 0) scount[s] = n;
+            if (lane == 0) scount[s][pw] = stop ? -1 : n;
             mbar_arrive(&full_bar[s]);  // releases this thread's slot writes
             if (stop) return;
         }
@@ -898,9 +903,11 @@ blend_fwd_ring_kernel(int P, const float2 *__restrict__ uv, const float *__restr
     for (int k = 0;; ++k) {
         const int s = k & 1;
         if (!mbar_wait_warp(&full_bar[s], (k >> 1) & 1, wait_limit)) break;
-        const int n = scount[s];
-        if (n < 0) break;
-        fwd_walk_batch<C, 1>(n, sA[s], sB[s], sF[s], sM[s], wbit, fx, fy, done, T, F, last, range.x);
+        if (scount[s][0] < 0) break;
+#pragma unroll
+        for (int q = 0; q < NP; ++q)
+            fwd_walk_batch<C, 1>(scount[s][q], sA[s] + q * SUB, sB[s] + q * SUB, sF[s] + q * SUB, sM[s] + q * SUB,
+                                 wbit, fx, fy, done, T, F, last, range.x);
         if (!counted && __all_sync(0xffffffffu, done[0])) {
             counted = true;
             if (lane == 0) atomicAdd(&ndone, 1);

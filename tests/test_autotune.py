@@ -74,3 +74,18 @@ def test_each_workload_keeps_its_own_section(tmp_path):
     assert not set(autotune.SPACE) & set(autotune.BATCH_SPACE)
     for k, v in autotune.BATCH_DEFAULTS.items():
         assert v in autotune.BATCH_SPACE[k]
+
+
+def test_searches_keep_earlier_evaluations(tmp_path):
+    """A search of a few parameters adds to the settings earlier searches
+    timed; a setting timed again keeps its new time."""
+    p = str(tmp_path / "tuning.json")
+    shape = {"gaussians": 1, "width": 2, "height": 3}
+    autotune.write_tuning(p, "frame", {"MSPLAT_FEW_LANES": 16}, 1.9, shape,
+                          [{"defines": {"MSPLAT_FEW_LANES": 16}, "ms": 1.9},
+                           {"defines": {"MSPLAT_FEW_LANES": 12}, "ms": 2.0}])
+    autotune.write_tuning(p, "frame", {"MSPLAT_FEW_LANES": 16}, 1.85, shape,
+                          [{"defines": {"MSPLAT_FEW_LANES": 16}, "ms": 1.85},
+                           {"defines": {"MSPLAT_FEW_LANES": 8}, "ms": 2.1}])
+    ev = {e["defines"]["MSPLAT_FEW_LANES"]: e["ms"] for e in json.load(open(p))["evaluated"]}
+    assert ev == {12: 2.0, 16: 1.85, 8: 2.1}
