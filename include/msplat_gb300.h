@@ -204,6 +204,18 @@ MSPLAT_API int msplat_radix_sort_i64_pairs(int64_t n, const int64_t *keys_in,
                                 size_t workspace_bytes,
                                 msplat_stream_t stream);
 
+/* How every radix sort of the library runs its 8-bit passes (no
+ * counterpart in the reference, which calls torch.sort,
+ * msplat/sort_gaussian.py:42-50).  on == 0 (the default): three launches
+ * per pass (upsweep, row scan, downsweep), no device-side waits.  on != 0:
+ * one histogram kernel for all passes, then one kernel per pass that finds
+ * its tile's output offsets by decoupled look-back; every look-back wait is
+ * bounded by the limit of msplat_set_wait_limit and reported by
+ * msplat_wait_error.  Results are identical either way; on GB300 the
+ * three-launch passes are faster for the tile lists of a 1080p frame and
+ * of a 64-camera batch.  Process-wide. */
+MSPLAT_API int msplat_set_sort_onesweep(int on);
+
 /* Fast drop-in for the whole of sort_gaussian (msplat/sort_gaussian.py:
  * 8-54) in two calls with one host read in between:
  *   1. _prepare: depth-sorts the Gaussians and scans their tile counts in
@@ -290,13 +302,15 @@ MSPLAT_API int msplat_alpha_blending_forward(int P, int C, const float *uv,
  * are identical either way; the default is the tuned choice.  Process-wide
  * setting (all devices, all threads). */
 MSPLAT_API int msplat_set_blend_ring(int producer_warps, int batch_producer_warps);
-/* Every wait of the ring gives up after `polls` polls of at most 1 us each
- * (default 2^21, about 2 s), sets a device error word and lets the kernel
- * finish with invalid results instead of hanging.  Process-wide. */
+/* Every device-side wait -- the ring's hand-offs, the sort's look-back --
+ * gives up after `polls` polls of at most about 1 us each (default 2^21,
+ * about 2 s), sets a device error word and lets the kernel finish with
+ * invalid results instead of hanging.  Process-wide. */
 MSPLAT_API int msplat_set_wait_limit(int polls);
-/* Reads (after synchronising `stream`) the current device's error word into
- * *error (may be NULL), clears it when reset != 0, and returns
- * MSPLAT_ERR_TIMEOUT if it was set, MSPLAT_OK otherwise. */
+/* Reads (after synchronising `stream`) the current device's error words of
+ * the bounded waits into *error (1 if any is set; may be NULL), clears them
+ * when reset != 0, and returns MSPLAT_ERR_TIMEOUT if one was set,
+ * MSPLAT_OK otherwise. */
 MSPLAT_API int msplat_wait_error(int reset, int *error, msplat_stream_t stream);
 
 /* dL_duv [P,2], dL_dconic [P,3], dL_dopacity [P], dL_dfeature [P,C] must be

@@ -67,6 +67,7 @@ _SIGNATURES = {
         _I, [_I, _I, _P, _P, _P, _P, _I, _I, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _SZ, _P]),
     "msplat_set_blend_ring": (_I, [_I, _I]),
     "msplat_set_wait_limit": (_I, [_I]),
+    "msplat_set_sort_onesweep": (_I, [_I]),
     "msplat_wait_error": (_I, [_I, _P, _P]),
     "msplat_batch_plan_bytes": (_SZ, [_I]),
     "msplat_batch_plan": (_I, [_I, _P, _P, _P, _P, _SZ, _P]),

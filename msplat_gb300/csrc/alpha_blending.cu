@@ -43,12 +43,12 @@ struct BlendBatch {
 // part), the image size, and in a multi-camera batch (BATCH) the offsets of
 // the tile's camera into the stacked arrays (zero for a single camera).
 struct BlendSite {
-    int tx, ty, tidx, part, W, H;
+    int tx, ty, tidx, part, W, H, P;  // P: the Gaussians (rows) list ids index
     int64_t row_off, op_off, feat_off, pix_off;
 };
 
 template <bool BATCH, int SPLIT>
-__device__ __forceinline__ BlendSite blend_site(const BlendBatch &bb, int W, int H) {
+__device__ __forceinline__ BlendSite blend_site(const BlendBatch &bb, int P, int W, int H) {
     BlendSite s;
     if (BATCH) {
         const int t = blockIdx.x;
@@ -56,6 +56,7 @@ __device__ __forceinline__ BlendSite blend_site(const BlendBatch &bb, int W, int
         const BatchCam &c = bb.pv.cams[b];
         s.W = c.W;
         s.H = c.H;
+        s.P = c.P;
         const int lt = t - c.tile_off;
         s.ty = lt / c.gx;
         s.tx = lt - s.ty * c.gx;
@@ -69,6 +70,7 @@ __device__ __forceinline__ BlendSite blend_site(const BlendBatch &bb, int W, int
         const int gxn = (W + kTile - 1) / kTile;
         s.W = W;
         s.H = H;
+        s.P = P;
         s.tx = blockIdx.x;
         s.ty = blockIdx.y / SPLIT;
         s.part = blockIdx.y % SPLIT;
@@ -174,7 +176,7 @@ __device__ __forceinline__ float power_bound(float op) {
 // Gathers entry `j` (when valid) and compacts the kept entries of the block
 // into shared memory in thread order.  Returns the number kept.
 template <int CMAX>
-__device__ __forceinline__ int gather_batch(bool valid, int j, const int32_t *__restrict__ idx_sorted,
+__device__ __forceinline__ int gather_batch(bool valid, int j, int P, const int32_t *__restrict__ idx_sorted,
                                             const float2 *__restrict__ uv, const float *__restrict__ conic,
                                             const float *__restrict__ opacity,
                                             const float *__restrict__ feature, int C, int c0, int nc,
@@ -184,8 +186,8 @@ __device__ __forceinline__ int gather_batch(bool valid, int j, const int32_t *__
     BlendRec r;
     int g = 0;
     bool keep = false;
-    if (valid) {
-        g = idx_sorted[j];
+    if (valid) g = idx_sorted[j];
+    if (valid && (unsigned)g < (unsigned)P) {  // (an id outside the rows is never read)
         const float2 p = uv[g];
         const float ca = conic[3 * g], cb = conic[3 * g + 1], cc = conic[3 * g + 2];
         const float op = opacity[g];
@@ -228,7 +230,7 @@ blend_fwd_kernel(int P, int C, int c0, const float2 *__restrict__ uv, const floa
     __shared__ int sgid[kBatch];
     __shared__ int swarp[kBlendThreads / 32];
     const int nc = min(CMAX, C - c0);
-    const BlendSite site = blend_site<BATCH, 1>(bb, W, H);
+    const BlendSite site = blend_site<BATCH, 1>(bb, P, W, H);
     if (BATCH) {
         W = site.W;
         H = site.H;
@@ -257,7 +259,7 @@ blend_fwd_kernel(int P, int C, int c0, const float2 *__restrict__ uv, const floa
     for (int start = range.x; start < range.y; start += kBatch) {
         if (__syncthreads_count(done) == kBlendThreads) break;
         const int j = start + (int)threadIdx.x;
-        const int n = gather_batch<CMAX>(j < range.y, j, idx_sorted, uv, conic, opacity, feature, C, c0,
+        const int n = gather_batch<CMAX>(j < range.y, j, site.P, idx_sorted, uv, conic, opacity, feature, C, c0,
                                          nc, bx0, by0, srec, sfeat, sgid, swarp);
         for (int k = 0; k < n && !done; ++k) {
             const BlendRec r = srec[k];
@@ -325,7 +327,7 @@ blend_bwd_kernel(int P, int C, int c0, const float2 *__restrict__ uv, const floa
     __shared__ int swarp[kBlendThreads / 32];
     __shared__ int smax;
     const int nc = min(kBwdC, C - c0);
-    const BlendSite site = blend_site<BATCH, 1>(bb, W, H);
+    const BlendSite site = blend_site<BATCH, 1>(bb, P, W, H);
     if (BATCH) {
         W = site.W;
         H = site.H;
@@ -377,7 +379,7 @@ blend_bwd_kernel(int P, int C, int c0, const float2 *__restrict__ uv, const floa
     for (int bend = end; bend > range.x; bend -= kBatch) {
         const int bstart = max(range.x, bend - kBatch);
         const int j = bend - 1 - (int)threadIdx.x;
-        const int n = gather_batch<kBwdC>(j >= bstart, j, idx_sorted, uv, conic, opacity, feature, C, c0,
+        const int n = gather_batch<kBwdC>(j >= bstart, j, site.P, idx_sorted, uv, conic, opacity, feature, C, c0,
                                           nc, bx0, by0, srec, sfeat, sgid, swarp);
         for (int k = 0; k < n; ++k) {
             const BlendRec r = srec[k];
@@ -489,12 +491,18 @@ __device__ __forceinline__ PixPow<NPIX> blend_power_n(float a, float b, float c,
 // list index), features and warp-block mask, and whether the tile cull (the
 // box of ROWS rows from by0) keeps it.
 template <int C, int NPIX, int ROWS>
-__device__ __forceinline__ bool gather_entry(int j, const int32_t *__restrict__ idx_sorted,
+__device__ __forceinline__ bool gather_entry(int j, int P, const int32_t *__restrict__ idx_sorted,
                                              const float2 *__restrict__ uv, const float *__restrict__ conic,
                                              const float *__restrict__ opacity, const float *__restrict__ feature,
                                              float bx0, float by0, float4 &A, float4 &B, float4 &F, int &G,
                                              unsigned &M) {
     const int g = idx_sorted[j];
+    if ((unsigned)g >= (unsigned)P) {  // an id outside the rows is never read
+        A = B = F = make_float4(0.f, 0.f, 0.f, 0.f);
+        G = 0;
+        M = 0u;
+        return false;
+    }
     const float2 p = uv[g];
     const float ca = conic[3 * g], cb = conic[3 * g + 1], cc = conic[3 * g + 2];
     const float op = opacity[g];
@@ -524,7 +532,7 @@ __device__ __forceinline__ bool gather_entry(int j, const int32_t *__restrict__ 
 // previous batch, so a warp that finishes a batch early issues the next
 // batch's loads and cull tests while the others still blend.
 template <int C, int NPIX, bool WITH_ID, int ROWS = kTile, int GE = NPIX>
-__device__ __forceinline__ int gather_small(int base, int dir, int lo, int hi,
+__device__ __forceinline__ int gather_small(int base, int dir, int lo, int hi, int P,
                                             const int32_t *__restrict__ idx_sorted,
                                             const float2 *__restrict__ uv, const float *__restrict__ conic,
                                             const float *__restrict__ opacity,
@@ -542,7 +550,7 @@ __device__ __forceinline__ int gather_small(int base, int dir, int lo, int hi,
         const int j = base + dir * ((int)threadIdx.x * GE + r);
         keep[r] = false;
         if (j >= lo && j < hi)
-            keep[r] = gather_entry<C, NPIX, ROWS>(j, idx_sorted, uv, conic, opacity, feature, bx0, by0, A[r], B[r],
+            keep[r] = gather_entry<C, NPIX, ROWS>(j, P, idx_sorted, uv, conic, opacity, feature, bx0, by0, A[r], B[r],
                                                   F[r], G[r], M[r]);
         nk += keep[r];
     }
@@ -647,7 +655,7 @@ blend_fwd_small_kernel(int P, const float2 *__restrict__ uv, const float *__rest
     __shared__ float4 sA[BATCH_N], sB[BATCH_N], sF[BATCH_N];
     __shared__ unsigned char sM[BATCH_N];
     __shared__ int scan[NT / 32];
-    const BlendSite site = blend_site<BATCH, SPLIT>(bb, W, H);
+    const BlendSite site = blend_site<BATCH, SPLIT>(bb, P, W, H);
     if (BATCH) {
         W = site.W;
         H = site.H;
@@ -687,7 +695,7 @@ blend_fwd_small_kernel(int P, const float2 *__restrict__ uv, const float *__rest
         bool all_done = true;
 #pragma unroll
         for (int i = 0; i < NPIX; ++i) all_done &= done[i];
-        const int n = gather_small<C, NPIX, false, ROWS, GE>(start, 1, range.x, range.y, idx_sorted, uv, conic,
+        const int n = gather_small<C, NPIX, false, ROWS, GE>(start, 1, range.x, range.y, site.P, idx_sorted, uv, conic,
                                                          opacity, feature, bx0, by0, sA, sB, sF, nullptr, sM, scan,
                                                          all_done);
         if (n < 0) break;  // every pixel of the block is done
@@ -815,7 +823,7 @@ blend_fwd_ring_kernel(int P, const float2 *__restrict__ uv, const float *__restr
     __shared__ int ndone;
     __shared__ __align__(8) uint64_t full_bar[2], empty_bar[2];
 
-    const BlendSite site = blend_site<BATCH, 1>(bb, W, H);
+    const BlendSite site = blend_site<BATCH, 1>(bb, P, W, H);
     if (BATCH) {
         W = site.W;
         H = site.H;
@@ -871,7 +879,7 @@ blend_fwd_ring_kernel(int P, const float2 *__restrict__ uv, const float *__restr
                     unsigned M;
                     bool keep = false;
                     if (j < range.y)
-                        keep = gather_entry<C, 1, kTile>(j, idx_sorted, uv, conic, opacity, feature, bx0, by0, A, B,
+                        keep = gather_entry<C, 1, kTile>(j, site.P, idx_sorted, uv, conic, opacity, feature, bx0, by0, A, B,
                                                          F, G, M);
                     const unsigned ballot = __ballot_sync(0xffffffffu, keep);
                     if (keep) {
@@ -1000,7 +1008,7 @@ blend_bwd_small_kernel(int P, const float2 *__restrict__ uv, const float *__rest
     __shared__ unsigned char sM[BATCH_N];
     __shared__ int scan[NT / 32];
     __shared__ int smax;
-    const BlendSite site = blend_site<BATCH, SPLIT>(bb, W, H);
+    const BlendSite site = blend_site<BATCH, SPLIT>(bb, P, W, H);
     if (BATCH) {
         W = site.W;
         H = site.H;
@@ -1069,7 +1077,7 @@ blend_bwd_small_kernel(int P, const float2 *__restrict__ uv, const float *__rest
 
     for (int bend = end; bend > range.x; bend -= BATCH_N) {
         const int bstart = max(range.x, bend - BATCH_N);
-        const int n = gather_small<C, NPIX, true, ROWS, GE>(bend - 1, -1, bstart, bend, idx_sorted, uv, conic,
+        const int n = gather_small<C, NPIX, true, ROWS, GE>(bend - 1, -1, bstart, bend, site.P, idx_sorted, uv, conic,
                                                         opacity, feature, bx0, by0, sA, sB, sF, sG, sM, scan,
                                                         false);
         // Each warp walks only the entries that reach its rows and precede
@@ -1502,6 +1510,13 @@ extern "C" int msplat_set_wait_limit(int polls) {
     return MSPLAT_OK;
 }
 
+namespace msplat {
+int wait_limit_polls() { return g_wait_limit; }
+// The look-back error words of the two translation units that sort.
+cudaError_t sort_wait_error_single(int reset, int *value, cudaStream_t stream);
+cudaError_t sort_wait_error_batch(int reset, int *value, cudaStream_t stream);
+}  // namespace msplat
+
 extern "C" int msplat_wait_error(int reset, int *error, msplat_stream_t stream) {
     int h = 0;
     cudaError_t e = cudaMemcpyFromSymbolAsync(&h, g_wait_error, sizeof(int), 0, cudaMemcpyDeviceToHost, stream);
@@ -1511,7 +1526,13 @@ extern "C" int msplat_wait_error(int reset, int *error, msplat_stream_t stream) 
         e = cudaMemcpyToSymbolAsync(g_wait_error, &zero, sizeof(int), 0, cudaMemcpyHostToDevice, stream);
         if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
     }
+    int s1 = 0, s2 = 0;
+    if (e == cudaSuccess) e = sort_wait_error_single(reset, &s1, stream);
+    if (e == cudaSuccess) e = sort_wait_error_batch(reset, &s2, stream);
     if (e != cudaSuccess) return set_error(MSPLAT_ERR_LAUNCH, "wait_error: %s", cudaGetErrorString(e));
-    if (error) *error = h;
-    return h ? set_error(MSPLAT_ERR_TIMEOUT, "a bounded device-side wait of a blend gave up") : MSPLAT_OK;
+    const int any = h | s1 | s2;
+    if (error) *error = any;
+    if (!any) return MSPLAT_OK;
+    return set_error(MSPLAT_ERR_TIMEOUT, "a bounded device-side wait gave up (%s)",
+                     h ? "blend ring" : "sort look-back");
 }

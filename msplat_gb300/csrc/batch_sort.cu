@@ -7,12 +7,13 @@
 // reference's order restricted to the culled lists): Gaussians sorted by
 // depth (stable, ties by id), intersections emitted in that order, then
 // stably sorted by tile.  Batched:
-//   prepare  depth keys of every camera's Gaussians in one array of padded
-//            segments (one per camera), one segmented 4-pass radix sort,
-//            the culled rectangles and tile counts in depth order, block
-//            offsets scanned per camera (one block per camera), and the
-//            camera segments of the intersection list (each padded to a
-//            sort tile) -- all on the device;
+//   prepare  depth keys and culled rectangles of every camera's Gaussians
+//            in one array of padded segments (one per camera), one
+//            segmented 4-pass radix sort, the rectangles and tile counts
+//            gathered into depth order, block offsets scanned per camera
+//            (one block per camera), and the camera segments of the
+//            intersection list (each padded to a sort tile) -- all on the
+//            device;
 //   finish   emit every camera's (local tile + 1, Gaussian) pairs into its
 //            segment, one segmented radix sort by local tile (2 passes at
 //            1080p), and the tile ranges in the global tile numbering.
@@ -23,6 +24,7 @@
 
 #include "batch_plan.cuh"
 #include "cull.cuh"
+#include "emit.cuh"
 #include "radix_sort.cuh"
 
 namespace msplat {
@@ -31,48 +33,55 @@ constexpr int kBatchDepthPasses = 4;
 constexpr int kBlocksPerSortTile = kSortTile / 256;
 
 // Depth keys of every camera's Gaussians in its padded segment (sign-flipped
-// float bits; Gaussians that emit nothing sort last).
+// float bits; Gaussians that emit nothing sort last), and their culled
+// rectangles in the same layout (as the single-camera culled prepare:
+// negative depths emit nothing, rectangles shrunk by shrink_rect).  Rows are
+// read in order here, so the count after the depth sort gathers one 8-byte
+// rectangle per Gaussian instead of its projected values.
 __global__ void __launch_bounds__(256)
-batch_depth_key_kernel(BatchPlanView pv, int64_t n, const float *__restrict__ depth,
-                       const int32_t *__restrict__ radius, uint32_t *__restrict__ keys) {
+batch_key_rect_kernel(BatchPlanView pv, int64_t n, const float2 *__restrict__ uv, const float *__restrict__ depth,
+                      const int32_t *__restrict__ radius, const float *__restrict__ conic,
+                      const float *__restrict__ opacity, uint32_t *__restrict__ keys, short4 *__restrict__ rects) {
     const int64_t pos = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (pos >= n) return;
     const int b = upper_index(pv.dtile_start, pv.B, pos / kSortTile);
     const BatchCam &c = pv.cams[b];
     const int64_t j = pos - (int64_t)pv.dtile_start[b] * kSortTile;
-    if (j >= c.P) return;  // padding: never read by the segmented sort
+    if (j >= c.P) return;  // padding: never read by the segmented sort or the count
     const int64_t q = c.row_off + j;
-    keys[pos] = radius[q] > 0 ? (__float_as_uint(depth[q]) ^ 0x80000000u) : 0xffffffffu;
+    const int rad = radius[q];
+    const float d = depth[q];
+    keys[pos] = rad > 0 ? (__float_as_uint(d) ^ 0x80000000u) : 0xffffffffu;
+    int x0 = 0, y0 = 0, x1 = 0, y1 = 0;
+    if (rad > 0 && (__float_as_uint(d) >> 31) == 0) {
+        const float2 p = uv[q];
+        tile_rect(p.x, p.y, rad, c.gx, c.gy, x0, y0, x1, y1);
+        shrink_rect(p.x, p.y, conic[3 * q], conic[3 * q + 1], conic[3 * q + 2], opacity[c.op_off + j], x0, y0, x1,
+                    y1);
+    }
+    rects[pos] = make_short4((short)x0, (short)y0, (short)x1, (short)y1);
 }
 
-// Culled rectangles (as the single-camera culled prepare: negative depths
-// emit nothing, rectangles shrunk by shrink_rect) and tile counts of every
-// camera's Gaussians in depth order; the sum per block of 256 (blocks never
-// straddle cameras: segments are padded to sort tiles of 12 blocks).
+// The culled rectangles and tile counts of every camera's Gaussians in depth
+// order (gathered from the position layout of batch_key_rect_kernel); the
+// sum per block of 256 (blocks never straddle cameras: segments are padded
+// to sort tiles of 12 blocks).
 __global__ void __launch_bounds__(256)
-batch_count_kernel(BatchPlanView pv, const uint32_t *__restrict__ order, const float2 *__restrict__ uv,
-                   const float *__restrict__ depth, const int32_t *__restrict__ radius,
-                   const float *__restrict__ conic, const float *__restrict__ opacity, short4 *__restrict__ rects,
-                   int64_t *__restrict__ bsum) {
+batch_count_kernel(BatchPlanView pv, const uint32_t *__restrict__ order, const short4 *__restrict__ rect_at,
+                   short4 *__restrict__ rects, int64_t *__restrict__ bsum) {
     __shared__ int64_t scratch[33];
     const int64_t pos = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const int b = upper_index(pv.dtile_start, pv.B, (int64_t)blockIdx.x / kBlocksPerSortTile);
     const BatchCam &c = pv.cams[b];
-    const int64_t j = pos - (int64_t)pv.dtile_start[b] * kSortTile;
-    int x0 = 0, y0 = 0, x1 = 0, y1 = 0;
-    if (j < c.P) {
-        const int g = (int)order[pos];
-        const int64_t q = c.row_off + g;
-        if (radius[q] > 0 && (__float_as_uint(depth[q]) >> 31) == 0) {
-            const float2 p = uv[q];
-            tile_rect(p.x, p.y, radius[q], c.gx, c.gy, x0, y0, x1, y1);
-            shrink_rect(p.x, p.y, conic[3 * q], conic[3 * q + 1], conic[3 * q + 2], opacity[c.op_off + g], x0, y0,
-                        x1, y1);
-        }
+    const int64_t s0 = (int64_t)pv.dtile_start[b] * kSortTile;
+    short4 r = make_short4(0, 0, 0, 0);
+    if (pos - s0 < c.P) {
+        const uint32_t g = order[pos];
+        if (g < (uint32_t)c.P) r = rect_at[s0 + g];  // (an id outside the camera's rows is never read)
     }
-    rects[pos] = make_short4((short)x0, (short)y0, (short)x1, (short)y1);
+    rects[pos] = r;
     int64_t total;
-    block_exclusive_scan<int64_t>((int64_t)((x1 - x0) * (y1 - y0)), scratch, &total);
+    block_exclusive_scan<int64_t>((int64_t)((r.z - r.x) * (r.w - r.y)), scratch, &total);
     if (threadIdx.x == 0) bsum[blockIdx.x] = total;
 }
 
@@ -131,14 +140,13 @@ batch_finish_segs_kernel(int B, int ntiles, const int32_t *__restrict__ fin_star
 }
 
 // Emits each camera's (local tile + 1, Gaussian id) pairs into its segment,
-// in depth order (as emit_kernel: a warp writes each Gaussian's run with
-// its lanes spread over the run); nothing at or past the capacity `cap`.
+// in depth order (as emit_kernel: a block's runs written together with
+// coalesced stores, emit.cuh); nothing at or past the capacity `cap`.
 __global__ void __launch_bounds__(256)
 batch_emit_kernel(BatchPlanView pv, const uint32_t *__restrict__ order, const short4 *__restrict__ rects,
                   const int64_t *__restrict__ boff, const int32_t *__restrict__ seg_start,
                   uint32_t *__restrict__ tkeys, uint32_t *__restrict__ tvals, int64_t cap) {
-    __shared__ int64_t scratch[33];
-    const int lane = threadIdx.x & 31;
+    __shared__ EmitShared sm;
     const int64_t pos = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const int b = upper_index(pv.dtile_start, pv.B, (int64_t)blockIdx.x / kBlocksPerSortTile);
     const BatchCam &c = pv.cams[b];
@@ -150,27 +158,8 @@ batch_emit_kernel(BatchPlanView pv, const uint32_t *__restrict__ order, const sh
         r = rects[pos];
     }
     const int w = r.z - r.x, n = w * (r.w - r.y);
-    const int64_t start = (int64_t)seg_start[b] * kSortTile + boff[blockIdx.x] +
-                          block_exclusive_scan<int64_t>((int64_t)n, scratch, nullptr);
-    unsigned todo = __ballot_sync(0xffffffffu, n > 0);
-    while (todo) {
-        const int sl = __ffs(todo) - 1;
-        todo &= todo - 1;
-        const int sg = __shfl_sync(0xffffffffu, g, sl);
-        const int sx0 = __shfl_sync(0xffffffffu, (int)r.x, sl), sy0 = __shfl_sync(0xffffffffu, (int)r.y, sl);
-        const int sw = __shfl_sync(0xffffffffu, w, sl), sn = __shfl_sync(0xffffffffu, n, sl);
-        const int64_t sstart = __shfl_sync(0xffffffffu, (long long)start, sl);
-        const float inv = 1.0f / (float)sw;
-        const int64_t room = cap - sstart;
-        const int kmax = room <= 0 ? 0 : (int)min((int64_t)sn, room);
-        for (int k = lane; k < kmax; k += 32) {
-            int ry = (int)(((float)k + 0.5f) * inv);  // k / sw, corrected below
-            ry -= (ry * sw > k);
-            ry += ((ry + 1) * sw <= k);
-            tkeys[sstart + k] = (uint32_t)((sy0 + ry) * c.gx + sx0 + (k - ry * sw) + 1);
-            tvals[sstart + k] = (uint32_t)sg;
-        }
-    }
+    emit_block_runs(sm, (int64_t)seg_start[b] * kSortTile + boff[blockIdx.x], n, g, r.x, r.y, w, false, c.gx, tkeys,
+                    tvals, cap);
 }
 
 // Tile ranges in the global tile numbering from the sorted segments: each
@@ -197,10 +186,11 @@ batch_range_kernel(BatchPlanView pv, int ntiles, const int32_t *__restrict__ seg
         k[u + 1] = (i >= s0 && i < s1) ? keys[i] : kOut;
     }
     const int toff = pv.cams[b].tile_off;
+    const uint32_t nkeys = (uint32_t)(pv.cams[b].gx * pv.cams[b].gy);  // keys of the camera: [1, nkeys]
 #pragma unroll
     for (int u = 1; u <= K; ++u) {
         const uint32_t key = k[u];
-        if (key == 0 || key == kOut) continue;
+        if (key == 0 || key > nkeys) continue;  // (kOut too)
         const int64_t i = i0 + u - 1;
         if (k[u - 1] != key) range[toff + key - 1].x = (int)i;
         if (k[u + 1] != key) range[toff + key - 1].y = (int)(i + 1);
@@ -209,10 +199,10 @@ batch_range_kernel(BatchPlanView pv, int ntiles, const int32_t *__restrict__ seg
 
 struct BatchPrepareWs {
     uint32_t *ka, *kb, *vt, *order;
-    short4 *rects;
+    short4 *rects, *rect_at;
     int64_t *bsum, *cam_count;
     int32_t *fin_start;
-    uint32_t *hist, *totals;
+    RadixBuffers rb;
 };
 
 template <typename WS>
@@ -222,15 +212,16 @@ inline void batch_prepare_carve(WS &w, int B, int64_t dn, BatchPrepareWs &ws) {
     ws.vt = w.template take<uint32_t>(dn);
     ws.order = w.template take<uint32_t>(dn);
     ws.rects = w.template take<short4>(dn);
+    ws.rect_at = w.template take<short4>(dn);
     ws.bsum = w.template take<int64_t>((size_t)(dn / 256));
     ws.cam_count = w.template take<int64_t>(B);
     ws.fin_start = w.template take<int32_t>(B + 1);
-    ws.hist = w.template take<uint32_t>((size_t)kRadix * (dn / kSortTile));
-    ws.totals = w.template take<uint32_t>((size_t)kRadix * kBatchDepthPasses * B);
+    radix_carve(w, dn / kSortTile, B, kBatchDepthPasses, ws.rb);
 }
 
 struct BatchFinishWs {
-    uint32_t *ka, *kb, *vt, *hist, *totals;
+    uint32_t *ka, *kb, *vt;
+    RadixBuffers rb;
     int32_t *seg_start;
     int64_t *seg_count;
 };
@@ -240,8 +231,7 @@ inline void batch_finish_carve(WS &w, int B, int64_t cap, int passes, BatchFinis
     f.ka = w.template take<uint32_t>(cap);
     f.kb = w.template take<uint32_t>(cap);
     f.vt = w.template take<uint32_t>(cap);
-    f.hist = w.template take<uint32_t>((size_t)kRadix * (cap / kSortTile));
-    f.totals = w.template take<uint32_t>((size_t)kRadix * passes * B);
+    radix_carve(w, cap / kSortTile, B, passes, f.rb);
     f.seg_start = w.template take<int32_t>(B + 1);
     f.seg_count = w.template take<int64_t>(B);
 }
@@ -257,6 +247,12 @@ inline int batch_tile_passes(int max_tiles) {
     return ceil_div(bits > 0 ? bits : 1, kRadixBits);
 }
 
+}  // namespace msplat
+
+namespace msplat {
+cudaError_t sort_wait_error_batch(int reset, int *value, cudaStream_t stream) {
+    return sort_wait_error_read(reset, value, stream);
+}
 }  // namespace msplat
 
 using namespace msplat;
@@ -347,18 +343,18 @@ extern "C" int msplat_batch_sort_prepare(const void *plan, int B, int64_t depth_
     if (!uv || !depth || !radius || !conic || !opacity)
         return set_error(MSPLAT_ERR_INVALID_ARGUMENT, "batch_sort_prepare: null pointer");
     const int dtiles = (int)(depth_items / kSortTile);
-    launch(batch_depth_key_kernel, (unsigned)ceil_div64(depth_items, 256), 256, 0, stream, pv, depth_items, depth,
-           radius, ws.ka);
+    launch(batch_key_rect_kernel, (unsigned)ceil_div64(depth_items, 256), 256, 0, stream, pv, depth_items,
+           (const float2 *)uv, depth, radius, conic, opacity, ws.ka, ws.rect_at);
     SortSegs segs;
     segs.tile_start = pv.dtile_start;
     segs.count = pv.dcount;
     segs.nseg = B;
     // 4 passes (even): ka -> kb -> ka ... the values land in order
     int st = radix_sort_segmented<uint32_t>(dtiles, segs, 0, kBatchDepthPasses, ws.ka, nullptr, ws.ka, ws.order,
-                                            ws.kb, ws.vt, ws.hist, ws.totals, stream);
+                                            ws.kb, ws.vt, ws.rb, stream);
     if (st) return st;
     launch(batch_count_kernel, (unsigned)(depth_items / 256), 256, 0, stream, pv, (const uint32_t *)ws.order,
-           (const float2 *)uv, depth, radius, conic, opacity, ws.rects, ws.bsum);
+           (const short4 *)ws.rect_at, ws.rects, ws.bsum);
     launch(batch_block_offsets_kernel, B, 1024, 0, stream, pv, ws.bsum, ws.cam_count);
     launch(batch_layout_kernel, 1, 32, 0, stream, B, (const int64_t *)ws.cam_count, ws.fin_start, counts);
     return check_launch("batch_sort_prepare");
@@ -416,7 +412,7 @@ extern "C" int msplat_batch_sort_finish(const void *plan, int B, int64_t depth_i
     segs.nseg = B;
     uint32_t *kout = even ? f.ka : f.kb;
     int st = radix_sort_segmented<uint32_t>(ntiles, segs, 0, passes, f.ka, vemit, kout, out, even ? f.kb : f.ka,
-                                            f.vt, f.hist, f.totals, stream);
+                                            f.vt, f.rb, stream);
     if (st) return st;
     launch(batch_range_kernel, (unsigned)ceil_div64(capacity / 8, 256), 256, 0, stream, pv, ntiles,
            (const int32_t *)f.seg_start, (const int64_t *)f.seg_count, (const uint32_t *)kout, (int2 *)tile_range);

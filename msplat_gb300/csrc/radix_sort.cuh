@@ -1,17 +1,26 @@
 // LSD radix sort of (key, uint32 value) pairs and int32 scans, written for
 // sm_103a without library calls.
 //
-// One 8-bit pass = three launches with no device-side waiting:
-//   upsweep   per-tile digit histogram (per-warp shared atomics), stored
-//             digit-major [256][tiles]
-//   row scan  one block per digit: exclusive scan of its row (the start of
-//             each (digit, tile) bucket among the digit's items) and the
-//             digit's total
-//   downsweep adds the exclusive scan of the 256 totals (the start of each
-//             digit), re-reads the tile, ranks each item among equal digits with a
-//             warp-level multisplit (stable: items are ranked in index
-//             order), reorders the tile in shared memory and writes each
-//             digit run contiguously (coalesced).
+// Two implementations of an 8-bit pass, with identical results:
+//
+// Three launches per pass (the default): upsweep (per-tile digit
+// histogram, stored digit-major [256][tiles]), row scan (one block per
+// digit: exclusive scan of its row and the digit's total), downsweep
+// (re-reads the tile, ranks each item among equal digits with a warp-level
+// multisplit -- stable: items are ranked in index order -- reorders the
+// tile in shared memory and writes each digit run contiguously).
+//
+// One kernel per pass (msplat_set_sort_onesweep): a histogram kernel reads
+// the keys once and counts the digits of every pass (per segment); then
+// each pass is one onesweep kernel.  Its blocks take sort tiles in order
+// from an atomic counter, rank and reorder them as the downsweep does,
+// publish the tile's count of every digit and find each digit's count in
+// all earlier tiles by decoupled look-back over the published words (a
+// tile's predecessors were taken by blocks that already run, so every wait
+// ends; each is also bounded, see below).  Measured slower on GB300 for
+// the tile lists (its kernel spills more at the same 64-register cap, and
+// small sorts wait along long look-back chains), so it is not the default.
+//
 // Tiles are 3072 items (256 threads x 12).
 #pragma once
 
@@ -72,16 +81,21 @@ __device__ __forceinline__ int seg_tile_items(const SortSegs &sg, int t, int &se
     return (int)max((int64_t)0, min((int64_t)kSortTile, left));
 }
 
-// Lanes of `valid` holding the same 8-bit digit as this lane, from eight
-// ballots (much cheaper than __match_any_sync, whose throughput limits a
-// ranking loop).  Every lane of the warp must call it.
-__device__ __forceinline__ unsigned digit_peers(uint32_t d, unsigned valid) {
+// Lanes of `valid` holding the same digit as this lane, from one ballot
+// per significant digit bit (much cheaper than __match_any_sync, whose
+// throughput limits a ranking loop).  `dbits` (<= 8, the same in every
+// lane): only digit bits below it can be set in any key of the pass (the
+// others are zero in every key and need no ballot).  Every lane of the
+// warp must call it.
+__device__ __forceinline__ unsigned digit_peers(uint32_t d, unsigned valid, int dbits = kRadixBits) {
     unsigned peers = valid;
 #pragma unroll
     for (int b = 0; b < kRadixBits; ++b) {
-        const bool bit = (d >> b) & 1u;
-        const unsigned bb = __ballot_sync(0xffffffffu, bit);
-        peers &= bit ? bb : ~bb;
+        if (b < dbits) {
+            const bool bit = (d >> b) & 1u;
+            const unsigned bb = __ballot_sync(0xffffffffu, bit);
+            peers &= bit ? bb : ~bb;
+        }
     }
     return peers;
 }
@@ -301,38 +315,413 @@ radix_downsweep_kernel(const K *__restrict__ kin, const uint32_t *__restrict__ v
     }
 }
 
-// Workspace of one sort of n items over `passes` digits.
-struct RadixBuffers {
-    uint32_t *hist;    // [radix][tiles]
-    uint32_t *totals;  // [passes][radix]
-};
+// ------------------------------------------------------------- onesweep
+// Status word of a (tile, digit) in a pass's look-back array: a flag in the
+// top two bits (0: not yet published), the count below.
+constexpr unsigned long long kLbAggregate = 1ull << 62;  // the digit's count in this tile
+constexpr unsigned long long kLbInclusive = 2ull << 62;  // ... in this tile and every earlier one of its segment
+constexpr unsigned long long kLbCount = (1ull << 62) - 1;
+constexpr int kHistTilesPerBlock = 16;  // sort tiles counted per block of the histogram kernel
+constexpr int kLbWindow = 8;            // earlier tiles' words a look-back step reads at once
+#ifndef MSPLAT_LB_BACKOFF_NS
+#define MSPLAT_LB_BACKOFF_NS 256
+#endif
+constexpr unsigned kLbBackoffNs = MSPLAT_LB_BACKOFF_NS;  // sleep after a poll that found a word unpublished
 
-inline void radix_size(WorkspaceSizer &s, int64_t n, int passes) {
-    s.take<uint32_t>((size_t)kRadix * sort_tiles(n));
-    s.take<uint32_t>((size_t)kRadix * passes);
+// Set when a look-back wait of a onesweep pass gave up (see
+// radix_onesweep_kernel); read and cleared through sort_wait_error.
+static __device__ int g_sort_wait_error;
+
+// Polls a look-back wait makes before it gives up (process-wide, shared
+// with the blend's ring; set by msplat_set_wait_limit).
+int wait_limit_polls();
+// Whether the passes run as one kernel each (default) or as three launches
+// (process-wide; msplat_set_sort_onesweep).
+bool sort_onesweep_enabled();
+
+__device__ __forceinline__ void st_relaxed_u64(unsigned long long *p, unsigned long long v) {
+    asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
 }
 
-inline bool radix_take(Workspace &w, int64_t n, int passes, RadixBuffers &b) {
-    b.hist = w.take<uint32_t>((size_t)kRadix * sort_tiles(n));
-    b.totals = w.take<uint32_t>((size_t)kRadix * passes);
-    return !w.overflow;
+__device__ __forceinline__ unsigned long long ld_relaxed_u64(const unsigned long long *p) {
+    unsigned long long v;
+    asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+
+// Digit counts of every pass, per segment: totals[(p * nseg + s) * 256 + d]
+// += the items of segment s whose digit in pass p is d (totals cleared by
+// the caller).  Each block counts kHistTilesPerBlock consecutive sort tiles
+// in per-warp shared histograms and adds them to the totals once per
+// segment it covers.  Also clears the first pass's look-back words of its
+// tiles and (block 0) the passes' tile counters.
+template <typename K, bool FLIP, bool SEG>
+__global__ void __launch_bounds__(kSortThreads)
+radix_hist_kernel(const K *__restrict__ keys, int64_t n, int begin_bit, int passes, int ntiles,
+                  uint32_t *__restrict__ totals, unsigned long long *__restrict__ status0, int *__restrict__ counters,
+                  const int64_t *__restrict__ n_dev, SortSegs segs) {
+    extern __shared__ uint32_t hcnt[];  // [warps][passes][radix]
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int nseg = SEG ? segs.nseg : 1;
+    if (!SEG && n_dev) n = min(n, *n_dev);
+    if (blockIdx.x == 0 && tid < passes) counters[tid] = 0;
+    const int t0 = blockIdx.x * kHistTilesPerBlock, t1 = min(ntiles, t0 + kHistTilesPerBlock);
+    for (int64_t i = (int64_t)t0 * kRadix + tid; i < (int64_t)t1 * kRadix; i += kSortThreads) status0[i] = 0ull;
+    const int hsize = kSortWarps * passes * kRadix;
+    for (int i = tid; i < hsize; i += kSortThreads) hcnt[i] = 0u;
+    __syncthreads();
+    auto flush = [&](int sg) {
+        __syncthreads();
+        for (int p = 0; p < passes; ++p) {
+            uint32_t c = 0;
+#pragma unroll
+            for (int w = 0; w < kSortWarps; ++w) {
+                uint32_t &h = hcnt[(w * passes + p) * kRadix + tid];
+                c += h;
+                h = 0u;
+            }
+            if (c) atomicAdd(&totals[((size_t)p * nseg + sg) * kRadix + tid], c);
+        }
+        __syncthreads();
+    };
+    int cur = -1;  // the segment being counted (the same in every thread)
+    for (int t = t0; t < t1; ++t) {
+        int sg = 0, items;
+        if (SEG) items = seg_tile_items(segs, t, sg);
+        else items = (int)max((int64_t)0, min((int64_t)kSortTile, n - (int64_t)t * kSortTile));
+        if (sg != cur) {
+            if (cur >= 0) flush(cur);
+            cur = sg;
+        }
+        if (sg < 0 || items <= 0) continue;
+        const int64_t base = (int64_t)t * kSortTile;
+        K k[kSortItems];
+#pragma unroll
+        for (int r = 0; r < kSortItems; ++r) {
+            const int li = warp * (32 * kSortItems) + r * 32 + lane;
+            k[r] = li < items ? __ldcs(keys + base + li) : K(0);
+            if (FLIP) k[r] ^= sign_bit<K>();
+        }
+        for (int p = 0; p < passes; ++p) {
+            uint32_t *h = hcnt + (warp * passes + p) * kRadix;
+#pragma unroll
+            for (int r = 0; r < kSortItems; ++r) {
+                const int li = warp * (32 * kSortItems) + r * 32 + lane;
+                if (li < items) atomicAdd(&h[digit_of(k[r], begin_bit + p * kRadixBits)], 1u);
+            }
+        }
+    }
+    if (cur >= 0) flush(cur);
+}
+
+inline size_t radix_hist_smem(int passes) { return (size_t)kSortWarps * passes * kRadix * sizeof(uint32_t); }
+
+// One 8-bit pass in one kernel.  `totals` = this pass's digit counts of the
+// block's segment ([nseg][radix]), `status` = this pass's look-back words
+// ([tiles][radix], cleared), `status_next` = the next pass's (cleared here,
+// row by row, for the tiles this pass covers; null after the last pass),
+// `counter` = this pass's tile counter (zero).  A tile's items, ranks and
+// output positions are those of radix_downsweep_kernel.
+//
+// Look-back (thread = digit d): the block publishes its count of d as an
+// aggregate as soon as it is known, then walks back over the earlier tiles
+// of its segment adding their published counts until it meets an inclusive
+// one, and publishes its own inclusive count.  The walk gives up once it
+// has polled wait_limit times without finding a word published (a limit of
+// 0: before the first poll): it sets g_sort_wait_error and counts the rest
+// as zero, so the kernel always finishes, with output positions that are
+// wrong but in bounds (every count it adds is a true count of an earlier
+// tile), and the host reports MSPLAT_ERR_TIMEOUT.
+#ifndef MSPLAT_ONESWEEP_TRIM
+#define MSPLAT_ONESWEEP_TRIM 1  // rank with one ballot per digit bit present in the segment's pass
+#endif
+#ifndef MSPLAT_ONESWEEP_MIN_BLOCKS
+#define MSPLAT_ONESWEEP_MIN_BLOCKS 4  // resident onesweep blocks per SM asked of the compiler (32-bit keys)
+#endif
+template <typename K, bool FLIP_IN, bool FLIP_OUT, bool SEG>
+__global__ void __launch_bounds__(kSortThreads, sizeof(K) == 4 ? MSPLAT_ONESWEEP_MIN_BLOCKS : 3)
+radix_onesweep_kernel(const K *__restrict__ kin, const uint32_t *__restrict__ vin, K *__restrict__ kout,
+                      uint32_t *__restrict__ vout, int64_t n, int shift,
+                      const uint32_t *__restrict__ totals, unsigned long long *__restrict__ status,
+                      unsigned long long *__restrict__ status_next, int *__restrict__ counter,
+                      const int64_t *__restrict__ n_dev, SortSegs segs, int wait_limit) {
+    extern __shared__ __align__(16) unsigned char sm_raw[];
+    K *skeys = reinterpret_cast<K *>(sm_raw);
+    uint32_t *svals = reinterpret_cast<uint32_t *>(skeys + kSortTile);
+    uint32_t *whist = svals + kSortTile;             // [warps][radix]
+    uint32_t *lstart = whist + kSortWarps * kRadix;  // [radix]
+    uint32_t *gofs = lstart + kRadix;                // [radix]
+    __shared__ uint32_t scan_scratch[33];
+    __shared__ int s_tile;
+    __shared__ unsigned s_digits;
+
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    if (tid == 0) {
+        s_tile = atomicAdd(counter, 1);
+        s_digits = 0u;
+    }
+    __syncthreads();
+    const int tile = s_tile;
+    const int64_t base = (int64_t)tile * kSortTile;
+    if (status_next) status_next[(size_t)tile * kRadix + tid] = 0ull;
+    int tile_n, sg = 0, first = 0;
+    int64_t out_base = 0;  // first item of the segment in the arrays
+    if (SEG) {
+        tile_n = seg_tile_items(segs, tile, sg);
+        if (sg < 0) return;  // past the last segment: nothing to move
+        totals += (size_t)sg * kRadix;
+        first = segs.tile_start[sg];
+        out_base = (int64_t)first * kSortTile;
+    } else {
+        if (n_dev) n = min(n, *n_dev);
+        tile_n = (int)max((int64_t)0, min((int64_t)kSortTile, n - base));
+    }
+    // Empty tiles come after every non-empty one of their segment, so no
+    // tile that looks back ever reaches one.
+    if (tile_n <= 0) return;
+    for (int i = tid; i < kSortWarps * kRadix; i += kSortThreads) whist[i] = 0;
+    const uint32_t dtot = totals[tid];
+    // The digit bits any key of the segment has set in this pass: those of
+    // the OR of the digits present (the largest digit's bits).
+    if (dtot) atomicOr(&s_digits, (unsigned)tid);
+    const uint32_t dbase = block_exclusive_scan<uint32_t>(dtot, scan_scratch, nullptr);
+#if MSPLAT_ONESWEEP_TRIM
+    const int dbits = 32 - __clz((int)s_digits);
+#else
+    const int dbits = kRadixBits;
+#endif
+    // A digit that every key of the segment shares makes the pass the
+    // identity (stable): every tile of the segment copies itself through.
+    const int64_t n_all = SEG ? segs.count[sg] : n;
+    if (__syncthreads_or(n_all > 0 && (int64_t)dtot == n_all)) {
+        for (int i = tid; i < tile_n; i += kSortThreads) {
+            K k = __ldcs(kin + base + i);
+            if (FLIP_IN != FLIP_OUT) k ^= sign_bit<K>();
+            kout[base + i] = k;
+            vout[base + i] = vin ? __ldcs(vin + base + i) : (uint32_t)(base + i - out_base);
+        }
+        return;
+    }
+
+    K key[kSortItems];
+    uint32_t val[kSortItems];
+    uint32_t rank[kSortItems];
+    uint32_t *my_hist = whist + warp * kRadix;
+#pragma unroll
+    for (int r = 0; r < kSortItems; ++r) {
+        const int li = warp * (32 * kSortItems) + r * 32 + lane;
+        const bool valid = li < tile_n;
+        K k = K(0);
+        uint32_t v = 0;
+        if (valid) {
+            k = __ldcs(kin + base + li);
+            if (FLIP_IN) k ^= sign_bit<K>();
+            v = vin ? __ldcs(vin + base + li) : (uint32_t)(base + li - out_base);
+        }
+        key[r] = k;
+        val[r] = v;
+    }
+#pragma unroll
+    for (int r = 0; r < kSortItems; ++r) {
+        const int li = warp * (32 * kSortItems) + r * 32 + lane;
+        const bool valid = li < tile_n;
+        const unsigned vmask = __ballot_sync(0xffffffffu, valid);
+        const uint32_t d = digit_of(key[r], shift);
+        const unsigned peers = digit_peers(d, vmask, dbits);
+        uint32_t b0 = 0;
+        if (valid) b0 = my_hist[d];
+        __syncwarp();
+        if (valid) {
+            rank[r] = b0 + __popc(peers & ((1u << lane) - 1u));
+            if (lane == 31 - __clz(peers)) my_hist[d] = b0 + __popc(peers);
+        }
+        __syncwarp();
+    }
+    __syncthreads();
+    uint32_t tot = 0;
+#pragma unroll
+    for (int w = 0; w < kSortWarps; ++w) {
+        const uint32_t c = whist[w * kRadix + tid];
+        whist[w * kRadix + tid] = tot;
+        tot += c;
+    }
+    // publish this tile's count of digit tid before anything else
+    unsigned long long *mine = status + (size_t)tile * kRadix + tid;
+    st_relaxed_u64(mine, (tile == first ? kLbInclusive : kLbAggregate) | (unsigned long long)tot);
+    const uint32_t ex = block_exclusive_scan<uint32_t>(tot, scan_scratch, nullptr);
+    lstart[tid] = ex;
+    __syncthreads();
+#pragma unroll
+    for (int r = 0; r < kSortItems; ++r) {
+        const int li = warp * (32 * kSortItems) + r * 32 + lane;
+        if (li < tile_n) {
+            const uint32_t d = digit_of(key[r], shift);
+            const uint32_t pos = lstart[d] + my_hist[d] + rank[r];
+            skeys[pos] = key[r];
+            svals[pos] = val[r];
+        }
+    }
+    // count of digit tid in the segment's earlier tiles: the walk reads
+    // kLbWindow earlier words at a time (independent loads), adds them from
+    // the nearest back while they are aggregates, and stops at the first
+    // inclusive one; a word not yet published ends the window there and
+    // the walk polls again from it
+    uint32_t before = 0;
+    if (tile != first) {
+        int polls = 0;
+        for (int t = tile - 1;;) {
+            if (polls >= wait_limit) {
+                atomicExch(&g_sort_wait_error, 1);
+                break;
+            }
+            unsigned long long w[kLbWindow];
+#pragma unroll
+            for (int k = 0; k < kLbWindow; ++k)
+                w[k] = t - k >= first ? ld_relaxed_u64(status + (size_t)(t - k) * kRadix + tid) : 0ull;
+            int used = 0;
+            bool done = false, blocked = false;
+#pragma unroll
+            for (int k = 0; k < kLbWindow; ++k) {
+                if (done || blocked) continue;
+                const unsigned long long f = w[k] & ~kLbCount;
+                if (t - k < first || f == 0ull) {  // (the segment's first tile publishes an inclusive word)
+                    blocked = true;
+                    continue;
+                }
+                before += (uint32_t)(w[k] & kLbCount);
+                ++used;
+                done = f == kLbInclusive;
+            }
+            if (done) break;
+            t -= used;
+            if (blocked) {
+                ++polls;
+                __nanosleep(kLbBackoffNs);
+            }
+        }
+        st_relaxed_u64(mine, kLbInclusive | (unsigned long long)(before + tot));
+    }
+    // output position of the tile's i-th reordered item with digit d:
+    // out_base + gofs[d] + i (uint32 arithmetic; the sum is below 2^31)
+    gofs[tid] = dbase + before - ex;
+    __syncthreads();
+    for (int i = tid; i < tile_n; i += kSortThreads) {
+        K k = skeys[i];
+        const uint32_t d = digit_of(k, shift);
+        const size_t o = (size_t)out_base + (size_t)(uint32_t)(gofs[d] + (uint32_t)i);
+        if (FLIP_OUT) k ^= sign_bit<K>();
+        kout[o] = k;
+        vout[o] = svals[i];
+    }
+}
+
+inline size_t radix_onesweep_smem(size_t key_bytes) {
+    return kSortTile * (key_bytes + 4) + (size_t)(kSortWarps * kRadix + 2 * kRadix) * 4;
+}
+
+// Reads (after synchronising `stream`) this translation unit's look-back
+// error word, clearing it when reset != 0.
+static inline cudaError_t sort_wait_error_read(int reset, int *value, cudaStream_t stream) {
+    int h = 0;
+    cudaError_t e = cudaMemcpyFromSymbolAsync(&h, g_sort_wait_error, sizeof(int), 0, cudaMemcpyDeviceToHost, stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+    if (e == cudaSuccess && reset && h) {
+        const int zero = 0;
+        e = cudaMemcpyToSymbolAsync(g_sort_wait_error, &zero, sizeof(int), 0, cudaMemcpyHostToDevice, stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+    }
+    *value = h;
+    return e;
+}
+
+// Workspace of a sort over `ntiles` sort tiles, `nseg` segments (1 when
+// not segmented) and `passes` digits.  The three-launch passes use the
+// first quarter of the look-back words' bytes as their digit-major
+// histogram.
+struct RadixBuffers {
+    uint32_t *hist = nullptr;                // [radix][tiles]           (three launches per pass)
+    unsigned long long *status = nullptr;    // [2][tiles][radix]        (one kernel per pass)
+    uint32_t *totals = nullptr;              // [passes][nseg][radix]
+    int *counters = nullptr;                 // [passes]
+};
+
+template <typename WS>
+inline void radix_carve(WS &w, int64_t ntiles, int nseg, int passes, RadixBuffers &b) {
+    b.status = w.template take<unsigned long long>((size_t)2 * kRadix * ntiles);
+    b.hist = reinterpret_cast<uint32_t *>(b.status);
+    b.totals = w.template take<uint32_t>((size_t)kRadix * passes * nseg);
+    b.counters = w.template take<int>((size_t)passes);
+}
+
+// The one-kernel passes of a sort (segmented when segs.nseg > 0): the
+// histogram of every pass, then one onesweep launch per pass along the
+// pass chain of radix_sort_pairs.  ntiles = the sort tiles the launches
+// cover.  Graph-capturable (a memset and launches only).
+template <typename K, bool FLIP>
+int radix_onesweep_passes(int ntiles, int64_t n, const int64_t *n_dev, const SortSegs &segs, int begin_bit,
+                          int passes, const K *kin, const uint32_t *vin, K *kout, uint32_t *vout,
+                          K *ktmp, uint32_t *vtmp, const RadixBuffers &b, cudaStream_t stream) {
+    const bool seg = segs.nseg > 0;
+    const int nseg = seg ? segs.nseg : 1;
+    cudaMemsetAsync(b.totals, 0, sizeof(uint32_t) * kRadix * passes * nseg, stream);
+    const size_t hsm = radix_hist_smem(passes);
+    const unsigned hblocks = (unsigned)ceil_div(ntiles, kHistTilesPerBlock);
+    auto hist = seg ? radix_hist_kernel<K, FLIP, true> : radix_hist_kernel<K, FLIP, false>;
+    if (hsm > 48 * 1024) cudaFuncSetAttribute(hist, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)hsm);
+    launch(hist, hblocks, kSortThreads, hsm, stream, kin, n, begin_bit, passes, ntiles, b.totals, b.status,
+           b.counters, n_dev, segs);
+    const size_t smem = radix_onesweep_smem(sizeof(K));
+    const int limit = wait_limit_polls();
+    const K *ksrc = kin;
+    const uint32_t *vsrc = vin;
+    for (int p = 0; p < passes; ++p) {
+        const int shift = begin_bit + p * kRadixBits;
+        const bool to_out = ((passes - 1 - p) & 1) == 0;
+        K *kdst = to_out ? kout : ktmp;
+        uint32_t *vdst = to_out ? vout : vtmp;
+        const bool first = p == 0, last = p == passes - 1;
+        unsigned long long *st = b.status + (size_t)(p & 1) * kRadix * ntiles;
+        unsigned long long *st_next = last ? nullptr : b.status + (size_t)((p + 1) & 1) * kRadix * ntiles;
+        const uint32_t *tot = b.totals + (size_t)p * nseg * kRadix;
+#define MSPLAT_ONESWEEP(FI, FO, SG)                                                                             \
+    do {                                                                                                        \
+        auto kern = radix_onesweep_kernel<K, FI, FO, SG>;                                                       \
+        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);                     \
+        launch(kern, ntiles, kSortThreads, smem, stream, ksrc, vsrc, kdst, vdst, n, shift, tot, st, st_next,    \
+               b.counters + p, n_dev, segs, limit);                                                             \
+    } while (0)
+        if (seg) MSPLAT_ONESWEEP(false, false, true);
+        else if (FLIP && first && last) MSPLAT_ONESWEEP(true, true, false);
+        else if (FLIP && first) MSPLAT_ONESWEEP(true, false, false);
+        else if (FLIP && last) MSPLAT_ONESWEEP(false, true, false);
+        else MSPLAT_ONESWEEP(false, false, false);
+#undef MSPLAT_ONESWEEP
+        ksrc = kdst;
+        vsrc = vdst;
+    }
+    return check_launch("radix_onesweep_passes");
 }
 
 // Stable sort of n (key, value) pairs by key bits [begin_bit, begin_bit +
-// 8 * passes).  Pass p reads `src` and writes `dst`; the chain is
+// 8 * passes).  Pass p
+// reads `src` and writes `dst`; the chain is
 //   in -> out -> tmp -> out ...   (odd pass count)
 //   in -> tmp -> out -> tmp -> out (even pass count)
 // so the result always lands in (kout, vout) and `in` is only read.
 // Aliasing allowed: for an even pass count `in` may alias `out`, for an odd
 // count `in` may alias `tmp`.  vin == nullptr means value = index.  kout may
 // not be null.  FLIP: keys are signed integers (sign bit flipped on the
-// first load and restored on the last store).
+// first load and restored on the last store).  n_dev: the length is on the
+// device (n is then the capacity the buffers hold).
 template <typename K, bool FLIP>
 int radix_sort_pairs(int64_t n, int begin_bit, int passes, const K *kin, const uint32_t *vin,
                      K *kout, uint32_t *vout, K *ktmp, uint32_t *vtmp, const RadixBuffers &b,
                      cudaStream_t stream, const int64_t *n_dev = nullptr) {
     if (n <= 0 || passes <= 0) return MSPLAT_OK;
     const int nt = sort_tiles(n);
+    if (sort_onesweep_enabled())
+        return radix_onesweep_passes<K, FLIP>(nt, n, n_dev, SortSegs{}, begin_bit, passes, kin, vin, kout, vout,
+                                              ktmp, vtmp, b, stream);
     const size_t smem = radix_downsweep_smem(sizeof(K));
     const K *ksrc = kin;
     const uint32_t *vsrc = vin;
@@ -371,14 +760,17 @@ int radix_sort_pairs(int64_t n, int begin_bit, int passes, const K *kin, const u
 // Segmented stable sort of unsigned keys (see SortSegs): every segment's
 // items sorted by key bits [begin_bit, begin_bit + 8 * passes) in place of
 // the same layout, with the pass chain of radix_sort_pairs.  ntiles = the
-// sort tiles the launches cover (at least segs.tile_start[nseg]); hist
-// [radix][ntiles], totals [passes][nseg][radix].  vin == nullptr means value
-// = index within the segment.
+// sort tiles the launches cover (at least segs.tile_start[nseg]); the
+// buffers are carved by radix_carve(ntiles, segs.nseg, passes).  vin ==
+// nullptr means value = index within the segment.
 template <typename K>
 int radix_sort_segmented(int ntiles, const SortSegs &segs, int begin_bit, int passes, const K *kin,
-                         const uint32_t *vin, K *kout, uint32_t *vout, K *ktmp, uint32_t *vtmp, uint32_t *hist,
-                         uint32_t *totals, cudaStream_t stream) {
+                         const uint32_t *vin, K *kout, uint32_t *vout, K *ktmp, uint32_t *vtmp,
+                         const RadixBuffers &b, cudaStream_t stream) {
     if (ntiles <= 0 || passes <= 0 || segs.nseg <= 0) return MSPLAT_OK;
+    if (sort_onesweep_enabled())
+        return radix_onesweep_passes<K, false>(ntiles, 0, nullptr, segs, begin_bit, passes, kin, vin, kout, vout,
+                                               ktmp, vtmp, b, stream);
     const size_t smem = radix_downsweep_smem(sizeof(K));
     const K *ksrc = kin;
     const uint32_t *vsrc = vin;
@@ -389,12 +781,12 @@ int radix_sort_segmented(int ntiles, const SortSegs &segs, int begin_bit, int pa
         const bool to_out = ((passes - 1 - p) & 1) == 0;
         K *kdst = to_out ? kout : ktmp;
         uint32_t *vdst = to_out ? vout : vtmp;
-        uint32_t *tot = totals + (size_t)p * segs.nseg * kRadix;
+        uint32_t *tot = b.totals + (size_t)p * segs.nseg * kRadix;
         launch(radix_upsweep_kernel<K, false, true>, ntiles, kSortThreads, 0, stream, ksrc, (int64_t)0, shift,
-               ntiles, hist, (const int64_t *)nullptr, segs);
+               ntiles, b.hist, (const int64_t *)nullptr, segs);
         launch(radix_rowscan_warp_kernel, (unsigned)ceil_div64((int64_t)kRadix * segs.nseg, 8), 256, 0, stream,
-               hist, tot, ntiles, segs);
-        launch(down, ntiles, kSortThreads, smem, stream, ksrc, vsrc, kdst, vdst, (int64_t)0, shift, ntiles, hist,
+               b.hist, tot, ntiles, segs);
+        launch(down, ntiles, kSortThreads, smem, stream, ksrc, vsrc, kdst, vdst, (int64_t)0, shift, ntiles, b.hist,
                (const uint32_t *)tot, (const int64_t *)nullptr, segs);
         ksrc = kdst;
         vsrc = vdst;

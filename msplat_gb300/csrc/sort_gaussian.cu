@@ -25,6 +25,7 @@
 #include <mutex>
 
 #include "cull.cuh"
+#include "emit.cuh"
 #include "radix_sort.cuh"
 
 namespace msplat {
@@ -101,7 +102,7 @@ depth_order_count_kernel(int P, const uint32_t *__restrict__ order, const float2
     if (j < P) {
         const int g = (int)order[j];
         int x0 = 0, y0 = 0, x1 = 0, y1 = 0, cref = 0;
-        if (radius[g] > 0) {
+        if ((unsigned)g < (unsigned)P && radius[g] > 0) {  // (an id outside [0, P) is never read)
             const float2 p = uv[g];
             tile_rect(p.x, p.y, radius[g], gx, gy, x0, y0, x1, y1);
             cref = (x1 - x0) * (y1 - y0);
@@ -120,7 +121,7 @@ depth_order_count_kernel(int P, const uint32_t *__restrict__ order, const float2
             if (isneg && c > 0) atomicAdd(neg + 1, (unsigned long long)c);
         }
         if (conic) rects[j] = make_short4((short)x0, (short)y0, (short)x1, (short)y1);
-        bad = cref != tiles[g];
+        bad = (unsigned)g < (unsigned)P && cref != tiles[g];
     }
     const unsigned mb = __ballot_sync(0xffffffffu, bad), mn = __ballot_sync(0xffffffffu, isneg);
     if ((threadIdx.x & 31) == 0) {
@@ -162,9 +163,9 @@ __device__ __forceinline__ void for_rect_tiles(int g, const float2 *__restrict__
         for (int tx = x0; tx < x1; ++tx) f(ty * gx + tx);
 }
 
-// Emits the intersections of 32 depth-ordered Gaussians per warp: each lane
-// loads one Gaussian, then the whole warp writes each Gaussian's run of
-// (tile key, id) pairs with the lanes spread over its tiles (coalesced).
+// Emits the intersections of 256 depth-ordered Gaussians per block: each
+// thread loads one Gaussian, then the block writes all their runs of
+// (tile key, id) pairs together with coalesced stores (emit_block_runs).
 // Tile key 0 marks negative-depth Gaussians, t + 1 tile t.
 // A Gaussian's first slot is its block's base (boff, from the block sums)
 // plus the exclusive scan of the tile counts within the block.
@@ -174,8 +175,7 @@ emit_kernel(int P, const uint32_t *__restrict__ order, const int64_t *__restrict
             const float2 *__restrict__ uv, const float *__restrict__ depth,
             const int32_t *__restrict__ radius, const short4 *__restrict__ rects, const int *__restrict__ culled,
             int gx, int gy, uint32_t *__restrict__ tkeys, uint32_t *__restrict__ tvals, int64_t cap) {
-    __shared__ int64_t scratch[33];
-    const int lane = threadIdx.x & 31;
+    __shared__ EmitShared sm;
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     int g = -1, x0 = 0, y0 = 0, x1 = 0, y1 = 0;
     bool neg = false;
@@ -187,7 +187,7 @@ emit_kernel(int P, const uint32_t *__restrict__ order, const int64_t *__restrict
             y0 = r.y;
             x1 = r.z;
             y1 = r.w;
-        } else if (radius[g] > 0) {
+        } else if ((unsigned)g < (unsigned)P && radius[g] > 0) {
             const float2 p = uv[g];
             tile_rect(p.x, p.y, radius[g], gx, gy, x0, y0, x1, y1);
             neg = (__float_as_uint(depth[g]) >> 31) != 0;
@@ -196,27 +196,7 @@ emit_kernel(int P, const uint32_t *__restrict__ order, const int64_t *__restrict
     const int w = x1 - x0, n = w * (y1 - y0);
     // Offsets stay 64-bit: with a capacity-bounded finish the true count (and
     // so boff) may pass 2^31 while only the first `cap` slots exist.
-    const int64_t start = boff[blockIdx.x] + block_exclusive_scan<int64_t>((int64_t)n, scratch, nullptr);
-    unsigned todo = __ballot_sync(0xffffffffu, n > 0);
-    while (todo) {
-        const int sl = __ffs(todo) - 1;
-        todo &= todo - 1;
-        const int sg = __shfl_sync(0xffffffffu, g, sl);
-        const int sx0 = __shfl_sync(0xffffffffu, x0, sl), sy0 = __shfl_sync(0xffffffffu, y0, sl);
-        const int sw = __shfl_sync(0xffffffffu, w, sl), sn = __shfl_sync(0xffffffffu, n, sl);
-        const int64_t sstart = __shfl_sync(0xffffffffu, (long long)start, sl);
-        const bool sneg = __shfl_sync(0xffffffffu, (int)neg, sl) != 0;
-        const float inv = 1.0f / (float)sw;
-        const int64_t room = cap - sstart;  // slots left in the output (may be <= 0)
-        const int kmax = room <= 0 ? 0 : (int)min((int64_t)sn, room);
-        for (int k = lane; k < kmax; k += 32) {
-            int ry = (int)(((float)k + 0.5f) * inv);  // k / sw, corrected below
-            ry -= (ry * sw > k);
-            ry += ((ry + 1) * sw <= k);
-            tkeys[sstart + k] = sneg ? 0u : (uint32_t)((sy0 + ry) * gx + sx0 + (k - ry * sw) + 1);
-            tvals[sstart + k] = (uint32_t)sg;
-        }
-    }
+    emit_block_runs(sm, boff[blockIdx.x], n, g, x0, y0, w, neg, gx, tkeys, tvals, cap);
 }
 
 // Ranges from the sorted tile keys (key 0 = no tile, key t + 1 = tile t).
@@ -227,7 +207,7 @@ emit_kernel(int P, const uint32_t *__restrict__ order, const int64_t *__restrict
 constexpr int kRangeKeys = 8;
 
 __global__ void __launch_bounds__(256)
-range_from_tilekey_kernel(int64_t I, const uint32_t *__restrict__ keys, int2 *__restrict__ range,
+range_from_tilekey_kernel(int64_t I, const uint32_t *__restrict__ keys, int ntiles, int2 *__restrict__ range,
                           const int64_t *__restrict__ I_dev) {
     if (I_dev) I = min(I, *I_dev);  // the length is on the device; I is the capacity
     const int64_t i0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) * kRangeKeys;
@@ -248,7 +228,7 @@ range_from_tilekey_kernel(int64_t I, const uint32_t *__restrict__ keys, int2 *__
 #pragma unroll
     for (int u = 1; u <= kRangeKeys; ++u) {
         const uint32_t key = k[u];
-        if (key == 0 || key == kOut) continue;
+        if (key == 0 || key > (uint32_t)ntiles) continue;  // (kOut too)
         const int64_t i = i0 + u - 1;
         if (k[u - 1] != key) range[key - 1].x = (int)i;
         if (k[u + 1] != key) range[key - 1].y = (int)(i + 1);
@@ -285,8 +265,7 @@ inline void prepare_carve(WS &w, int P, PrepareWs &ws) {
     ws.ka = w.template take<uint32_t>(P);
     ws.kb = w.template take<uint32_t>(P);
     ws.vt = w.template take<uint32_t>(P);
-    ws.rb.hist = w.template take<uint32_t>((size_t)kRadix * sort_tiles(P));
-    ws.rb.totals = w.template take<uint32_t>((size_t)kRadix * kDepthPasses);
+    radix_carve(w, sort_tiles(P), 1, kDepthPasses, ws.rb);
 }
 
 struct SizeOnly {
@@ -317,8 +296,7 @@ inline void finish_carve(WS &w, int64_t I, int passes, FinishWs &f) {
     f.ka = w.template take<uint32_t>(I);
     f.kb = w.template take<uint32_t>(I);
     f.vt = w.template take<uint32_t>(I);
-    f.rb.hist = w.template take<uint32_t>((size_t)kRadix * sort_tiles(I));
-    f.rb.totals = w.template take<uint32_t>((size_t)kRadix * passes);
+    radix_carve(w, sort_tiles(I), 1, passes, f.rb);
 }
 
 inline size_t finish_bytes(int64_t I, int W, int H) {
@@ -328,14 +306,30 @@ inline size_t finish_bytes(int64_t I, int W, int H) {
     return z.s.used;
 }
 
-inline size_t radix_i64_bytes(int64_t n) {
-    WorkspaceSizer s;
-    s.take<uint64_t>(n);
-    s.take<uint32_t>(n);
-    radix_size(s, n, 8);
-    return s.used;
+template <typename WS>
+inline void radix_i64_carve(WS &w, int64_t n, int passes, uint64_t *&kt, uint32_t *&vt, RadixBuffers &rb) {
+    kt = w.template take<uint64_t>(n);
+    vt = w.template take<uint32_t>(n);
+    radix_carve(w, sort_tiles(n), 1, passes, rb);
 }
 
+inline size_t radix_i64_bytes(int64_t n) {
+    SizeOnly z;
+    uint64_t *kt;
+    uint32_t *vt;
+    RadixBuffers rb;
+    radix_i64_carve(z, n, 8, kt, vt, rb);
+    return z.s.used;
+}
+
+}  // namespace msplat
+
+namespace msplat {
+static int g_sort_onesweep = 0;  // three launches per pass: measured faster on the tile lists (see the header)
+bool sort_onesweep_enabled() { return g_sort_onesweep != 0; }
+cudaError_t sort_wait_error_single(int reset, int *value, cudaStream_t stream) {
+    return sort_wait_error_read(reset, value, stream);
+}
 }  // namespace msplat
 
 using namespace msplat;
@@ -470,10 +464,11 @@ extern "C" int msplat_radix_sort_i64_pairs(int64_t n, const int64_t *keys_in, co
         return check_launch("radix_sort_i64_pairs");
     }
     Workspace w(workspace, workspace_bytes);
-    uint64_t *kt = w.take<uint64_t>(n);
-    uint32_t *vt = w.take<uint32_t>(n);
+    uint64_t *kt;
+    uint32_t *vt;
     RadixBuffers rb;
-    if (!radix_take(w, n, passes, rb))
+    radix_i64_carve(w, n, 8, kt, vt, rb);  // sized for 8 passes, as the size query
+    if (w.overflow)
         return set_error(MSPLAT_ERR_WORKSPACE, "radix_sort_i64_pairs: workspace of %zu bytes < %zu",
                          workspace_bytes, msplat_radix_sort_i64_workspace_size(n));
     return radix_sort_pairs<uint64_t, true>(n, begin_bit, passes, (const uint64_t *)keys_in,
@@ -584,7 +579,7 @@ static int finish_impl(int P, const float *uv, const float *depth, const int32_t
                                                f.rb, stream, I_dev);
     if (st) return st;
     launch(range_from_tilekey_kernel, (unsigned)ceil_div64(ceil_div64(I, kRangeKeys), 256), 256, 0, stream, I, kout,
-           (int2 *)tile_range, I_dev);
+           nt, (int2 *)tile_range, I_dev);
     return check_launch("sort_gaussian_finish");
 }
 
@@ -618,3 +613,7 @@ extern "C" int msplat_sort_gaussian_finish_capacity(int P, const float *uv, cons
                        workspace, workspace_bytes, stream);
 }
 
+extern "C" int msplat_set_sort_onesweep(int on) {
+    g_sort_onesweep = on ? 1 : 0;
+    return MSPLAT_OK;
+}
