@@ -223,8 +223,9 @@ MSPLAT_API int msplat_set_sort_onesweep(int on);
  *      counts[1] = number of "filler" slots (tiles[i] larger than the
  *      Gaussian's rectangle, or radius <= 0 with tiles > 0).
  *   2. _finish (only valid when counts[1] == 0): emits (tile, id) pairs in
- *      depth order, stable-sorts them by tile, writes idx_sorted [I] and
- *      tile_range [ntiles,2].  Bit-identical to the reference's output.
+ *      depth order, stable-sorts them by tile, writes idx_sorted [I] (16-byte
+ *      aligned) and tile_range [ntiles,2].  Bit-identical to the reference's
+ *      output.
  * When counts[1] != 0 the caller uses the reference-layout path
  * (compute_gaussian_key + radix_sort_i64_pairs + tile range), which
  * reproduces the zero-filled slots exactly.                                */
@@ -432,8 +433,8 @@ MSPLAT_API int msplat_batch_sort_prepare(const void *plan, int B, int64_t depth_
                                          size_t workspace_bytes, msplat_stream_t stream);
 
 /* Emission and a segmented stable sort by tile of every camera's list, and
- * the tile ranges [total_tiles, 2] (positions in idx_sorted [capacity]).
- * capacity: a multiple of 3072, at least counts[1] of the prepare for a
+ * the tile ranges [total_tiles, 2] (positions in idx_sorted [capacity],
+ * 16-byte aligned).  capacity: a multiple of 3072, at least counts[1] of the prepare for a
  * valid result; no host read happens.  status (device int32, may be NULL)
  * is set to 1 when the capacity was too small (the result is then not
  * valid), else 0. */

@@ -383,6 +383,8 @@ extern "C" int msplat_batch_sort_finish(const void *plan, int B, int64_t depth_i
                          (long long)capacity);
     if (!plan || !prepare_workspace || !tile_range || (capacity > 0 && !idx_sorted))
         return set_error(MSPLAT_ERR_INVALID_ARGUMENT, "batch_sort_finish: null pointer");
+    if (((uintptr_t)idx_sorted & 15) != 0)  // the emit writes it with 16-byte stores
+        return set_error(MSPLAT_ERR_INVALID_ARGUMENT, "batch_sort_finish: idx_sorted is not 16-byte aligned");
     Workspace pw(const_cast<void *>(prepare_workspace), msplat_batch_sort_prepare_workspace_size(B, depth_items));
     BatchPrepareWs prep;
     batch_prepare_carve(pw, B, depth_items, prep);

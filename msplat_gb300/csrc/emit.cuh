@@ -6,10 +6,11 @@
 // are consecutive in the output (their order is the threads' order, which
 // is depth order), so the block's entries form one contiguous range.  The
 // threads scan the run lengths into shared memory and then walk that range
-// together, entry e + thread for e = 0, kEmitThreads, ...: each finds the
-// run holding its entry by binary search over the scanned offsets and
-// writes one key and one value, so every store instruction of a warp covers
-// 32 consecutive slots, whatever the runs' lengths.  (Spreading one run
+// together in groups of four consecutive slots per thread: each finds the
+// run holding its group's first entry by binary search over the scanned
+// offsets and writes four keys and four values with 16-byte stores, so
+// every store instruction of a warp covers 128 consecutive slots, whatever
+// the runs' lengths.  (Spreading one run
 // at a time over a warp's lanes, the common alternative, leaves most lanes
 // idle when runs are a few tiles long, as most are.)
 #pragma once
@@ -21,48 +22,85 @@ namespace msplat {
 constexpr int kEmitThreads = 256;
 
 struct EmitShared {
-    int64_t off[kEmitThreads + 1];  // exclusive prefix of the run lengths; off[kEmitThreads] = block total
+    int32_t off[kEmitThreads + 1];  // exclusive prefix of the run lengths (saturated at INT32_MAX)
     int g[kEmitThreads];            // Gaussian id written as the value
     uint32_t xy[kEmitThreads];      // x0 | y0 << 16 (tile units)
     int w[kEmitThreads];            // run width in tiles; < 0: a run of key 0 ("no tile")
     int64_t scratch[33];
 };
 
+// Key and value of entry k of run r.
+__device__ __forceinline__ void emit_entry(const EmitShared &sm, int r, int k, int gx, uint32_t &key, uint32_t &val) {
+    const int rw = sm.w[r];
+    key = 0u;
+    if (rw > 0) {
+        int ry = (int)(((float)k + 0.5f) / (float)rw);  // k / rw, corrected below
+        ry -= (ry * rw > k);
+        ry += ((ry + 1) * rw <= k);
+        const uint32_t xy = sm.xy[r];
+        key = (uint32_t)(((int)(xy >> 16) + ry) * gx + (int)(xy & 0xffffu) + (k - ry * rw) + 1);
+    }
+    val = (uint32_t)sm.g[r];
+}
+
 // Emits the block's runs into tkeys / tvals starting at `base` (the first
 // slot of the block's range); key = y * gx + x + 1 for tile (x, y), or 0
 // for a run with zero_key.  Slots at or past `cap` are not written.  Every
 // thread of the block (blockDim.x == kEmitThreads) must call it.
+// tkeys / tvals must be 16-byte aligned.  Each thread takes groups of four
+// consecutive slots starting on a multiple of four (16-byte stores); the
+// run of a group's first entry is found by binary search over the scanned
+// offsets, the next three by stepping past the runs that end before them.
+// Written slots lie below cap <= INT32_MAX, so offsets saturated there
+// still compare correctly with every entry that is written.
 __device__ __forceinline__ void emit_block_runs(EmitShared &sm, int64_t base, int n, int g, int x0, int y0, int w,
                                                 bool zero_key, int gx, uint32_t *__restrict__ tkeys,
                                                 uint32_t *__restrict__ tvals, int64_t cap) {
     const int t = threadIdx.x;
     int64_t total;
     const int64_t ex = block_exclusive_scan<int64_t>((int64_t)n, sm.scratch, &total);
-    sm.off[t] = ex;
-    if (t == 0) sm.off[kEmitThreads] = total;
+    sm.off[t] = (int32_t)min(ex, (int64_t)INT32_MAX);
+    if (t == 0) sm.off[kEmitThreads] = (int32_t)min(total, (int64_t)INT32_MAX);
     sm.g[t] = g;
     sm.xy[t] = ((uint32_t)x0 & 0xffffu) | ((uint32_t)y0 << 16);
     sm.w[t] = zero_key ? -max(w, 1) : w;
     __syncthreads();
-    const int64_t lim = min(total, cap - base);  // entries of the block that fit (may be <= 0)
-    for (int64_t e = t; e < lim; e += kEmitThreads) {
-        // the last run starting at or before e (it holds e: the next starts after it)
+    const int lim = (int)max((int64_t)0, min(total, cap - base));  // entries of the block that fit
+    // entries before the first slot on a multiple of four, one per thread
+    const int head = min(lim, (int)((4 - (base & 3)) & 3));
+    if (t < head) {
         int r = 0;
 #pragma unroll
         for (int step = kEmitThreads / 2; step > 0; step >>= 1)
-            if (sm.off[r + step] <= e) r += step;
-        const int k = (int)(e - sm.off[r]);
-        const int rw = sm.w[r];
-        uint32_t key = 0u;
-        if (rw > 0) {
-            int ry = (int)(((float)k + 0.5f) / (float)rw);  // k / rw, corrected below
-            ry -= (ry * rw > k);
-            ry += ((ry + 1) * rw <= k);
-            const uint32_t xy = sm.xy[r];
-            key = (uint32_t)(((int)(xy >> 16) + ry) * gx + (int)(xy & 0xffffu) + (k - ry * rw) + 1);
+            if (sm.off[r + step] <= t) r += step;
+        uint32_t key, val;
+        emit_entry(sm, r, t - sm.off[r], gx, key, val);
+        tkeys[base + t] = key;
+        tvals[base + t] = val;
+    }
+    for (int e0 = head + 4 * t; e0 < lim; e0 += 4 * kEmitThreads) {
+        int r = 0;
+#pragma unroll
+        for (int step = kEmitThreads / 2; step > 0; step >>= 1)
+            if (sm.off[r + step] <= e0) r += step;
+        uint32_t key[4], val[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const int e = e0 + u;
+            if (e < lim) {
+                while (sm.off[r + 1] <= e) ++r;  // (skips runs of no entries too)
+                emit_entry(sm, r, e - sm.off[r], gx, key[u], val[u]);
+            }
         }
-        tkeys[base + e] = key;
-        tvals[base + e] = (uint32_t)sm.g[r];
+        if (e0 + 4 <= lim) {
+            *reinterpret_cast<uint4 *>(tkeys + base + e0) = make_uint4(key[0], key[1], key[2], key[3]);
+            *reinterpret_cast<uint4 *>(tvals + base + e0) = make_uint4(val[0], val[1], val[2], val[3]);
+        } else {
+            for (int u = 0; u < lim - e0; ++u) {
+                tkeys[base + e0 + u] = key[u];
+                tvals[base + e0 + u] = val[u];
+            }
+        }
     }
 }
 

@@ -557,6 +557,8 @@ static int finish_impl(int P, const float *uv, const float *depth, const int32_t
     if (P == 0 || I == 0) return check_launch("sort_gaussian_finish");
     if (!uv || !depth || !radius || !prepare_workspace || !idx_sorted)
         return set_error(MSPLAT_ERR_INVALID_ARGUMENT, "sort_gaussian_finish: null pointer");
+    if (((uintptr_t)idx_sorted & 15) != 0)  // the emit writes it with 16-byte stores
+        return set_error(MSPLAT_ERR_INVALID_ARGUMENT, "sort_gaussian_finish: idx_sorted is not 16-byte aligned");
     Workspace pw(const_cast<void *>(prepare_workspace), prepare_bytes(P));
     PrepareWs prep;
     prepare_carve(pw, P, prep);

@@ -569,3 +569,27 @@ def small_vs_general(uv, conic, op, f3, idx, tr, W, H):
         rel_close(a, b, rtol=1e-5, what="grad")
     rel_close(res[3][3][3], res[5][3][3][:, :3], rtol=1e-5, what="dL/dfeature")
     return res[3]
+
+
+def test_sort_finish_rejects_a_misaligned_output():
+    """The emit writes idx_sorted with 16-byte stores: an output that is
+    not 16-byte aligned is refused on the host (nothing is launched)."""
+    from msplat_gb300 import _lib
+    lib = _lib.load()
+    uv, d, radius, tiles, W, H = sort_inputs(2000, seed=3)
+    P = uv.shape[0]
+    u, dd, r, t = T(uv), T(d), T(radius, torch.int32), T(tiles, torch.int32)
+    st = _lib.stream()
+    counts = torch.empty(2, dtype=torch.int64, device=u.device)
+    ws_prep = _lib.workspace(lib.msplat_sort_prepare_workspace_size(P, W, H), u.device)
+    _lib.check(lib.msplat_sort_gaussian_prepare(P, _lib.ptr(dd), _lib.ptr(r), _lib.ptr(t), _lib.ptr(u), W, H,
+                                                _lib.ptr(counts), _lib.ptr(ws_prep), ws_prep.numel(), st), "prepare")
+    I = int(counts[0].item())
+    assert I > 0 and int(counts[1].item()) == 0
+    idx = torch.empty(I + 4, dtype=torch.int32, device=u.device)
+    tr = torch.empty((-(-W // 16)) * (-(-H // 16)), 2, dtype=torch.int32, device=u.device)
+    ws = _lib.workspace(lib.msplat_sort_finish_workspace_size(P, I, W, H), u.device)
+    rc = lib.msplat_sort_gaussian_finish(P, _lib.ptr(u), _lib.ptr(dd), _lib.ptr(r), W, H, I, _lib.ptr(ws_prep),
+                                         idx.data_ptr() + 4, _lib.ptr(tr), _lib.ptr(ws), ws.numel(), st)
+    assert rc == 1  # MSPLAT_ERR_INVALID_ARGUMENT
+    assert b"16-byte" in lib.msplat_last_error()
