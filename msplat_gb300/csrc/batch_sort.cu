@@ -33,15 +33,23 @@ constexpr int kBatchDepthPasses = 4;
 constexpr int kBlocksPerSortTile = kSortTile / 256;
 
 // Depth keys of every camera's Gaussians in its padded segment (sign-flipped
-// float bits; Gaussians that emit nothing sort last), and their culled
-// rectangles in the same layout (as the single-camera culled prepare:
-// negative depths emit nothing, rectangles shrunk by shrink_rect).  Rows are
-// read in order here, so the count after the depth sort gathers one 8-byte
-// rectangle per Gaussian instead of its projected values.
+// float bits; Gaussians that emit nothing sort last), their culled
+// rectangles, per-row reaches and kept-tile counts in the same layout (as
+// the single-camera culled prepare: negative depths emit nothing,
+// rectangles shrunk by shrink_rect, each row cut to row_span).  Rows are
+// read in order here, so the count after the depth sort gathers one
+// 16-byte record per Gaussian instead of its projected values.
+struct BatchRect {
+    short4 rect;
+    int count;  // tiles the per-row reach keeps
+    int pad;
+};
+
 __global__ void __launch_bounds__(256)
 batch_key_rect_kernel(BatchPlanView pv, int64_t n, const float2 *__restrict__ uv, const float *__restrict__ depth,
                       const int32_t *__restrict__ radius, const float *__restrict__ conic,
-                      const float *__restrict__ opacity, uint32_t *__restrict__ keys, short4 *__restrict__ rects) {
+                      const float *__restrict__ opacity, uint32_t *__restrict__ keys, BatchRect *__restrict__ rects,
+                      RowReach *__restrict__ reach) {
     const int64_t pos = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (pos >= n) return;
     const int b = upper_index(pv.dtile_start, pv.B, pos / kSortTile);
@@ -52,36 +60,45 @@ batch_key_rect_kernel(BatchPlanView pv, int64_t n, const float2 *__restrict__ uv
     const int rad = radius[q];
     const float d = depth[q];
     keys[pos] = rad > 0 ? (__float_as_uint(d) ^ 0x80000000u) : 0xffffffffu;
-    int x0 = 0, y0 = 0, x1 = 0, y1 = 0;
+    int x0 = 0, y0 = 0, x1 = 0, y1 = 0, cnt = 0;
     if (rad > 0 && (__float_as_uint(d) >> 31) == 0) {
         const float2 p = uv[q];
+        const float ca = conic[3 * q], cb = conic[3 * q + 1], cc = conic[3 * q + 2], op = opacity[c.op_off + j];
         tile_rect(p.x, p.y, rad, c.gx, c.gy, x0, y0, x1, y1);
-        shrink_rect(p.x, p.y, conic[3 * q], conic[3 * q + 1], conic[3 * q + 2], opacity[c.op_off + j], x0, y0, x1,
-                    y1);
+        shrink_rect(p.x, p.y, ca, cb, cc, op, x0, y0, x1, y1);
+        if (x0 < x1 && y0 < y1) {
+            if (row_cut_enabled(c.gx, c.gy)) {
+                const RowReach rr = row_reach(p.x, p.y, ca, cb, cc, op, x0, y0, x1, y1);
+                reach[pos] = rr;
+                cnt = row_span_count(rr, x0, y0, x1, y1);
+            } else {
+                cnt = (x1 - x0) * (y1 - y0);
+            }
+        }
     }
-    rects[pos] = make_short4((short)x0, (short)y0, (short)x1, (short)y1);
+    rects[pos] = BatchRect{make_short4((short)x0, (short)y0, (short)x1, (short)y1), cnt, 0};
 }
 
-// The culled rectangles and tile counts of every camera's Gaussians in depth
-// order (gathered from the position layout of batch_key_rect_kernel); the
-// sum per block of 256 (blocks never straddle cameras: segments are padded
-// to sort tiles of 12 blocks).
+// The culled rectangles and kept-tile counts of every camera's Gaussians in
+// depth order (gathered from the position layout of
+// batch_key_rect_kernel); the sum per block of 256 (blocks never straddle
+// cameras: segments are padded to sort tiles of 12 blocks).
 __global__ void __launch_bounds__(256)
-batch_count_kernel(BatchPlanView pv, const uint32_t *__restrict__ order, const short4 *__restrict__ rect_at,
+batch_count_kernel(BatchPlanView pv, const uint32_t *__restrict__ order, const BatchRect *__restrict__ rect_at,
                    short4 *__restrict__ rects, int64_t *__restrict__ bsum) {
     __shared__ int64_t scratch[33];
     const int64_t pos = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const int b = upper_index(pv.dtile_start, pv.B, (int64_t)blockIdx.x / kBlocksPerSortTile);
     const BatchCam &c = pv.cams[b];
     const int64_t s0 = (int64_t)pv.dtile_start[b] * kSortTile;
-    short4 r = make_short4(0, 0, 0, 0);
+    BatchRect r{make_short4(0, 0, 0, 0), 0, 0};
     if (pos - s0 < c.P) {
         const uint32_t g = order[pos];
         if (g < (uint32_t)c.P) r = rect_at[s0 + g];  // (an id outside the camera's rows is never read)
     }
-    rects[pos] = r;
+    rects[pos] = r.rect;
     int64_t total;
-    block_exclusive_scan<int64_t>((int64_t)((r.z - r.x) * (r.w - r.y)), scratch, &total);
+    block_exclusive_scan<int64_t>((int64_t)r.count, scratch, &total);
     if (threadIdx.x == 0) bsum[blockIdx.x] = total;
 }
 
@@ -140,26 +157,45 @@ batch_finish_segs_kernel(int B, int ntiles, const int32_t *__restrict__ fin_star
 }
 
 // Emits each camera's (local tile + 1, Gaussian id) pairs into its segment,
-// in depth order (as emit_kernel: a block's runs written together with
-// coalesced stores, emit.cuh); nothing at or past the capacity `cap`.
+// in depth order, as the culled emit_kernel: on cameras of at least
+// kRowCutMinTiles tiles each rectangle's rows cut to their spans
+// (emit_block_rows, on the reach batch_key_rect_kernel recorded), whole
+// rectangles otherwise (emit_block_runs); nothing at or past the capacity
+// `cap`, nor past the slots the count gave the block.
 __global__ void __launch_bounds__(256)
 batch_emit_kernel(BatchPlanView pv, const uint32_t *__restrict__ order, const short4 *__restrict__ rects,
-                  const int64_t *__restrict__ boff, const int32_t *__restrict__ seg_start,
+                  const RowReach *__restrict__ reach_at, const int64_t *__restrict__ boff,
+                  const int64_t *__restrict__ cam_count, const int32_t *__restrict__ seg_start,
                   uint32_t *__restrict__ tkeys, uint32_t *__restrict__ tvals, int64_t cap) {
-    __shared__ EmitShared sm;
+    __shared__ union {
+        EmitShared runs;
+        EmitRowShared rows;
+    } sm;
     const int64_t pos = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const int b = upper_index(pv.dtile_start, pv.B, (int64_t)blockIdx.x / kBlocksPerSortTile);
     const BatchCam &c = pv.cams[b];
-    const int64_t j = pos - (int64_t)pv.dtile_start[b] * kSortTile;
+    const int64_t s0 = (int64_t)pv.dtile_start[b] * kSortTile;
+    const int64_t j = pos - s0;
+    const bool cut = row_cut_enabled(c.gx, c.gy);  // the same for the whole block (one camera)
     int g = 0;
     short4 r = make_short4(0, 0, 0, 0);
+    RowReach rr{};
     if (j < c.P) {
         g = (int)order[pos];
         r = rects[pos];
+        if (cut && r.x < r.z && r.y < r.w) rr = reach_at[s0 + g];  // (a non-empty rectangle has a valid id)
     }
-    const int w = r.z - r.x, n = w * (r.w - r.y);
-    emit_block_runs(sm, (int64_t)seg_start[b] * kSortTile + boff[blockIdx.x], n, g, r.x, r.y, w, false, c.gx, tkeys,
-                    tvals, cap);
+    if (!cut) {
+        const int w = r.z - r.x, n = w * (r.w - r.y);
+        emit_block_runs(sm.runs, (int64_t)seg_start[b] * kSortTile + boff[blockIdx.x], n, g, r.x, r.y, w, false,
+                        c.gx, tkeys, tvals, cap);
+        return;
+    }
+    // the block's slots: up to the next block of the camera, or its count
+    const int64_t last_block = (int64_t)pv.dtile_start[b + 1] * kBlocksPerSortTile - 1;
+    const int64_t next = (int64_t)blockIdx.x < last_block ? boff[blockIdx.x + 1] : cam_count[b];
+    emit_block_rows(sm.rows, (int64_t)seg_start[b] * kSortTile + boff[blockIdx.x], next - boff[blockIdx.x], j < c.P, rr,
+                    r.x, r.y, r.z, r.w, g, c.gx, tkeys, tvals, cap);
 }
 
 // Tile ranges in the global tile numbering from the sorted segments: each
@@ -199,7 +235,9 @@ batch_range_kernel(BatchPlanView pv, int ntiles, const int32_t *__restrict__ seg
 
 struct BatchPrepareWs {
     uint32_t *ka, *kb, *vt, *order;
-    short4 *rects, *rect_at;
+    short4 *rects;
+    BatchRect *rect_at;
+    RowReach *reach_at;
     int64_t *bsum, *cam_count;
     int32_t *fin_start;
     RadixBuffers rb;
@@ -212,7 +250,8 @@ inline void batch_prepare_carve(WS &w, int B, int64_t dn, BatchPrepareWs &ws) {
     ws.vt = w.template take<uint32_t>(dn);
     ws.order = w.template take<uint32_t>(dn);
     ws.rects = w.template take<short4>(dn);
-    ws.rect_at = w.template take<short4>(dn);
+    ws.rect_at = w.template take<BatchRect>(dn);
+    ws.reach_at = w.template take<RowReach>(dn);
     ws.bsum = w.template take<int64_t>((size_t)(dn / 256));
     ws.cam_count = w.template take<int64_t>(B);
     ws.fin_start = w.template take<int32_t>(B + 1);
@@ -344,7 +383,7 @@ extern "C" int msplat_batch_sort_prepare(const void *plan, int B, int64_t depth_
         return set_error(MSPLAT_ERR_INVALID_ARGUMENT, "batch_sort_prepare: null pointer");
     const int dtiles = (int)(depth_items / kSortTile);
     launch(batch_key_rect_kernel, (unsigned)ceil_div64(depth_items, 256), 256, 0, stream, pv, depth_items,
-           (const float2 *)uv, depth, radius, conic, opacity, ws.ka, ws.rect_at);
+           (const float2 *)uv, depth, radius, conic, opacity, ws.ka, ws.rect_at, ws.reach_at);
     SortSegs segs;
     segs.tile_start = pv.dtile_start;
     segs.count = pv.dcount;
@@ -354,7 +393,7 @@ extern "C" int msplat_batch_sort_prepare(const void *plan, int B, int64_t depth_
                                             ws.kb, ws.vt, ws.rb, stream);
     if (st) return st;
     launch(batch_count_kernel, (unsigned)(depth_items / 256), 256, 0, stream, pv, (const uint32_t *)ws.order,
-           (const short4 *)ws.rect_at, ws.rects, ws.bsum);
+           (const BatchRect *)ws.rect_at, ws.rects, ws.bsum);
     launch(batch_block_offsets_kernel, B, 1024, 0, stream, pv, ws.bsum, ws.cam_count);
     launch(batch_layout_kernel, 1, 32, 0, stream, B, (const int64_t *)ws.cam_count, ws.fin_start, counts);
     return check_launch("batch_sort_prepare");
@@ -406,8 +445,8 @@ extern "C" int msplat_batch_sort_finish(const void *plan, int B, int64_t depth_i
     const bool even = passes % 2 == 0;
     uint32_t *vemit = even ? out : f.vt;
     launch(batch_emit_kernel, (unsigned)(depth_items / 256), 256, 0, stream, pv, (const uint32_t *)prep.order,
-           (const short4 *)prep.rects, (const int64_t *)prep.bsum, (const int32_t *)f.seg_start, f.ka, vemit,
-           capacity);
+           (const short4 *)prep.rects, (const RowReach *)prep.reach_at, (const int64_t *)prep.bsum,
+           (const int64_t *)prep.cam_count, (const int32_t *)f.seg_start, f.ka, vemit, capacity);
     SortSegs segs;
     segs.tile_start = f.seg_start;
     segs.count = f.seg_count;

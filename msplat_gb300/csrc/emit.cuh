@@ -16,6 +16,7 @@
 #pragma once
 
 #include "block_scan.cuh"
+#include "cull.cuh"
 
 namespace msplat {
 
@@ -101,6 +102,113 @@ __device__ __forceinline__ void emit_block_runs(EmitShared &sm, int64_t base, in
                 tvals[base + e0 + u] = val[u];
             }
         }
+    }
+}
+
+// ------------------------------------------------------------------------
+// The same for runs culled row by row (row_span): a run is the tiles its
+// reach keeps in each row of its rectangle, row after row.  Two levels:
+// the rows of the block's runs are numbered (a scan of the row counts),
+// and taken 256 at a time; each thread evaluates one row's span, the
+// spans' lengths are scanned, and the chunk's entries are written four
+// consecutive slots per thread (binary search over the chunk's row offsets
+// for the group's first entry, as emit_block_runs does over runs).
+struct EmitRowShared {
+    RowReach reach[kEmitThreads];   // per run: centre, conic, threshold
+    int x0[kEmitThreads], x1[kEmitThreads], y0[kEmitThreads];
+    int g[kEmitThreads];
+    int ru[kEmitThreads + 1];       // exclusive prefix of the runs' row counts
+    int e[kEmitThreads + 1];        // per row of the chunk: exclusive prefix of the span lengths
+    uint32_t kb[kEmitThreads];      // per row of the chunk: key of its first entry
+    int rg[kEmitThreads];           // per row of the chunk: its run's Gaussian id
+    int64_t scratch[33];
+};
+
+// `allotted` = the slots the count kernel gave the block (its runs' row
+// span sums); entries past it, or at or past `cap`, are not written, so a
+// disagreement could never write outside the block's range (the span is
+// evaluated identically in both kernels, so none arises).
+__device__ __forceinline__ void emit_block_rows(EmitRowShared &sm, int64_t base, int64_t allotted, bool valid,
+                                                const RowReach &reach, int x0, int y0, int x1, int y1, int g, int gx,
+                                                uint32_t *__restrict__ tkeys, uint32_t *__restrict__ tvals,
+                                                int64_t cap) {
+    const int t = threadIdx.x;
+    const int h = valid && x0 < x1 ? max(0, y1 - y0) : 0;
+    int64_t rows64;
+    const int64_t ru = block_exclusive_scan<int64_t>((int64_t)h, sm.scratch, &rows64);
+    sm.ru[t] = (int)ru;
+    if (t == 0) sm.ru[kEmitThreads] = (int)rows64;
+    sm.reach[t] = reach;
+    sm.x0[t] = x0;
+    sm.x1[t] = x1;
+    sm.y0[t] = y0;
+    sm.g[t] = g;
+    __syncthreads();
+    const int rows = (int)rows64;
+    const int64_t lim_all = max((int64_t)0, min(allotted, cap - base));
+    int64_t done = 0;  // entries of the earlier chunks (the same in every thread)
+    for (int u0 = 0; u0 < rows; u0 += kEmitThreads) {
+        const int u = u0 + t;
+        int w = 0;
+        uint32_t kb = 0u;
+        int rg = 0;
+        if (u < rows) {
+            int r = 0;
+#pragma unroll
+            for (int step = kEmitThreads / 2; step > 0; step >>= 1)
+                if (sm.ru[r + step] <= u) r += step;
+            const int ty = sm.y0[r] + (u - sm.ru[r]);
+            int xa, xb;
+            row_span(sm.reach[r], ty, sm.x0[r], sm.x1[r], xa, xb);
+            w = xb - xa;
+            kb = (uint32_t)(ty * gx + xa + 1);
+            rg = sm.g[r];
+        }
+        int64_t tot64;
+        const int64_t ex = block_exclusive_scan<int64_t>((int64_t)w, sm.scratch, &tot64);
+        sm.e[t] = (int)ex;
+        sm.kb[t] = kb;
+        sm.rg[t] = rg;
+        if (t == 0) sm.e[kEmitThreads] = (int)tot64;
+        __syncthreads();
+        const int64_t cbase = base + done;
+        const int lim = (int)max((int64_t)0, min(tot64, lim_all - done));
+        const int head = min(lim, (int)((4 - (cbase & 3)) & 3));
+        if (t < head) {
+            int q = 0;
+#pragma unroll
+            for (int step = kEmitThreads / 2; step > 0; step >>= 1)
+                if (sm.e[q + step] <= t) q += step;
+            tkeys[cbase + t] = sm.kb[q] + (uint32_t)(t - sm.e[q]);
+            tvals[cbase + t] = (uint32_t)sm.rg[q];
+        }
+        for (int e0 = head + 4 * t; e0 < lim; e0 += 4 * kEmitThreads) {
+            int q = 0;
+#pragma unroll
+            for (int step = kEmitThreads / 2; step > 0; step >>= 1)
+                if (sm.e[q + step] <= e0) q += step;
+            uint32_t key[4], val[4];
+#pragma unroll
+            for (int v = 0; v < 4; ++v) {
+                const int e = e0 + v;
+                if (e < lim) {
+                    while (sm.e[q + 1] <= e) ++q;  // (skips rows of no entries too)
+                    key[v] = sm.kb[q] + (uint32_t)(e - sm.e[q]);
+                    val[v] = (uint32_t)sm.rg[q];
+                }
+            }
+            if (e0 + 4 <= lim) {
+                *reinterpret_cast<uint4 *>(tkeys + cbase + e0) = make_uint4(key[0], key[1], key[2], key[3]);
+                *reinterpret_cast<uint4 *>(tvals + cbase + e0) = make_uint4(val[0], val[1], val[2], val[3]);
+            } else {
+                for (int v = 0; v < lim - e0; ++v) {
+                    tkeys[cbase + e0 + v] = key[v];
+                    tvals[cbase + e0 + v] = val[v];
+                }
+            }
+        }
+        done += tot64;
+        __syncthreads();  // the chunk's rows are rewritten by the next chunk
     }
 }
 

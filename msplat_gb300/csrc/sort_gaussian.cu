@@ -85,16 +85,19 @@ depth_key_kernel(int P, const float *__restrict__ depth, const int32_t *__restri
 // reference layout), the negative-depth emitters (they come first in depth
 // order) and their intersections.
 // With conic and opacity (the culled lists of the fused path) each
-// rectangle is first shrunk by shrink_rect, negative-depth Gaussians (which
-// no tile range includes) emit nothing, and the rectangle used is stored in
-// depth order in rects[j] for emit_kernel.
+// rectangle is first shrunk by shrink_rect and, on images of at least
+// kRowCutMinTiles tiles, each of its rows then cut to the columns the
+// ellipse reaches there (row_span); negative-depth
+// Gaussians (which no tile range includes) emit nothing; the rectangle and
+// the reach are stored in depth order in rects[j] and reach[j] for
+// emit_kernel, which evaluates the same spans.
 __global__ void __launch_bounds__(256)
 depth_order_count_kernel(int P, const uint32_t *__restrict__ order, const float2 *__restrict__ uv,
                          const float *__restrict__ depth, const int32_t *__restrict__ radius,
                          const int32_t *__restrict__ tiles, const float *__restrict__ conic,
                          const float *__restrict__ opacity, int gx, int gy, int64_t *__restrict__ bsum,
                          int64_t *__restrict__ counts, unsigned long long *__restrict__ neg,
-                         short4 *__restrict__ rects) {
+                         short4 *__restrict__ rects, RowReach *__restrict__ reach) {
     __shared__ int64_t scratch[33];
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     bool bad = false, isneg = false;
@@ -113,11 +116,18 @@ depth_order_count_kernel(int P, const uint32_t *__restrict__ order, const float2
                     x1 = x0;
                     y1 = y0;
                 } else {
-                    shrink_rect(p.x, p.y, conic[3 * g], conic[3 * g + 1], conic[3 * g + 2], opacity[g], x0, y0, x1,
-                                y1);
+                    const float ca = conic[3 * g], cb = conic[3 * g + 1], cc = conic[3 * g + 2], op = opacity[g];
+                    shrink_rect(p.x, p.y, ca, cb, cc, op, x0, y0, x1, y1);
+                    if (row_cut_enabled(gx, gy)) {
+                        const RowReach rr = row_reach(p.x, p.y, ca, cb, cc, op, x0, y0, x1, y1);
+                        reach[j] = rr;
+                        c = row_span_count(rr, x0, y0, x1, y1);
+                    } else {
+                        c = (x1 - x0) * (y1 - y0);
+                    }
                 }
             }
-            c = (x1 - x0) * (y1 - y0);
+            if (!conic || isneg) c = (x1 - x0) * (y1 - y0);
             if (isneg && c > 0) atomicAdd(neg + 1, (unsigned long long)c);
         }
         if (conic) rects[j] = make_short4((short)x0, (short)y0, (short)x1, (short)y1);
@@ -169,16 +179,40 @@ __device__ __forceinline__ void for_rect_tiles(int g, const float2 *__restrict__
 // Tile key 0 marks negative-depth Gaussians, t + 1 tile t.
 // A Gaussian's first slot is its block's base (boff, from the block sums)
 // plus the exclusive scan of the tile counts within the block.
-// With *culled set (by a culled prepare) the rectangles come from rects[j].
+// With *culled set (by a culled prepare) the rectangles come from
+// rects[j]; on images of at least kRowCutMinTiles tiles the reaches from
+// reach[j], each row cut to its span (emit_block_rows), where `total` (or
+// *total_dev when given, the device count) bounds the last block's slots.
 __global__ void __launch_bounds__(256)
 emit_kernel(int P, const uint32_t *__restrict__ order, const int64_t *__restrict__ boff,
             const float2 *__restrict__ uv, const float *__restrict__ depth,
             const int32_t *__restrict__ radius, const short4 *__restrict__ rects, const int *__restrict__ culled,
-            int gx, int gy, uint32_t *__restrict__ tkeys, uint32_t *__restrict__ tvals, int64_t cap) {
-    __shared__ EmitShared sm;
+            const RowReach *__restrict__ reach, int gx, int gy, uint32_t *__restrict__ tkeys,
+            uint32_t *__restrict__ tvals, int64_t cap, int64_t total, const int64_t *__restrict__ total_dev) {
+    __shared__ union {
+        EmitShared runs;
+        EmitRowShared rows;
+    } sm;
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     int g = -1, x0 = 0, y0 = 0, x1 = 0, y1 = 0;
     bool neg = false;
+    if (*culled && row_cut_enabled(gx, gy)) {  // rows cut to the ellipse's reach (as the count kernel)
+        RowReach rr{};
+        if (j < P) {
+            g = (int)order[j];
+            const short4 r = rects[j];
+            x0 = r.x;
+            y0 = r.y;
+            x1 = r.z;
+            y1 = r.w;
+            if (x0 < x1 && y0 < y1) rr = reach[j];
+        }
+        if (total_dev) total = min(total, *total_dev);
+        const int64_t next = blockIdx.x + 1 < gridDim.x ? boff[blockIdx.x + 1] : total;
+        emit_block_rows(sm.rows, boff[blockIdx.x], next - boff[blockIdx.x], j < P, rr, x0, y0, x1, y1, g, gx, tkeys,
+                        tvals, cap);
+        return;
+    }
     if (j < P) {
         g = (int)order[j];
         if (*culled) {
@@ -196,7 +230,7 @@ emit_kernel(int P, const uint32_t *__restrict__ order, const int64_t *__restrict
     const int w = x1 - x0, n = w * (y1 - y0);
     // Offsets stay 64-bit: with a capacity-bounded finish the true count (and
     // so boff) may pass 2^31 while only the first `cap` slots exist.
-    emit_block_runs(sm, boff[blockIdx.x], n, g, x0, y0, w, neg, gx, tkeys, tvals, cap);
+    emit_block_runs(sm.runs, boff[blockIdx.x], n, g, x0, y0, w, neg, gx, tkeys, tvals, cap);
 }
 
 // Ranges from the sorted tile keys (key 0 = no tile, key t + 1 = tile t).
@@ -250,6 +284,7 @@ struct PrepareWs {
     int64_t *bsum = nullptr;    // [P/256] tile counts per block of 256 in depth order, then their scan
     unsigned long long *neg = nullptr;  // [0] negative emitters, [1] their intersections
     short4 *rects = nullptr;    // [P] rectangles in depth order (culled prepare)
+    RowReach *reach = nullptr;  // [P] per-row reach parameters in depth order (culled prepare)
     int *culled = nullptr;      // [1] nonzero after a culled prepare
     uint32_t *ka = nullptr, *kb = nullptr, *vt = nullptr;
     RadixBuffers rb{};
@@ -261,6 +296,7 @@ inline void prepare_carve(WS &w, int P, PrepareWs &ws) {
     ws.bsum = w.template take<int64_t>((size_t)ceil_div(P, 256));
     ws.neg = w.template take<unsigned long long>(2);
     ws.rects = w.template take<short4>(P);
+    ws.reach = w.template take<RowReach>(P);
     ws.culled = w.template take<int>(1);
     ws.ka = w.template take<uint32_t>(P);
     ws.kb = w.template take<uint32_t>(P);
@@ -511,7 +547,7 @@ static int prepare_impl(int P, const float *depth, const int32_t *radius, const 
     const int nb = ceil_div(P, 256);
     launch(depth_order_count_kernel, nb, 256, 0, stream,
         P, ws.order, (const float2 *)uv, depth, radius, tiles, conic, opacity, gx, gy, ws.bsum, counts, ws.neg,
-        ws.rects);
+        ws.rects, ws.reach);
     launch(block_offsets_kernel, 1, 1024, 0, stream, nb, ws.bsum, counts);
     return check_launch("sort_gaussian_prepare");
 }
@@ -575,7 +611,8 @@ static int finish_impl(int P, const float *uv, const float *depth, const int32_t
     const bool even = passes % 2 == 0;
     uint32_t *vemit = even ? out : f.vt;
     launch(emit_kernel, ceil_div(P, 256), 256, 0, stream, P, prep.order, prep.bsum, (const float2 *)uv, depth,
-           radius, (const short4 *)prep.rects, (const int *)prep.culled, gx, gy, f.ka, vemit, I);
+           radius, (const short4 *)prep.rects, (const int *)prep.culled, (const RowReach *)prep.reach, gx, gy, f.ka,
+           vemit, I, I, I_dev);
     uint32_t *kout = even ? f.ka : f.kb;
     int st = radix_sort_pairs<uint32_t, false>(I, 0, passes, f.ka, vemit, kout, out, even ? f.kb : f.ka, f.vt,
                                                f.rb, stream, I_dev);

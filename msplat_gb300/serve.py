@@ -59,13 +59,14 @@ class Request:
 
 def request_bytes(P: int, W: int, H: int, C: int, D: int, backward: bool) -> int:
     """Device memory a request may hold while it runs (an upper estimate):
-    per-Gaussian preprocess outputs and sort scratch, the intersections
+    per-Gaussian preprocess outputs and sort scratch (keys, ids, the
+    rectangle records and the per-row reach records), the intersections
     (about 29 tiles per Gaussian at 1080p and f = 1500, scaling with the
     image area), the image and blend state, and for a backward request the
     per-Gaussian gradients."""
     tiles_per = max(2.0, 29.0 * (W * H) / (1920 * 1080)) * 1.5
     inter = int(P * tiles_per)
-    b = P * (44 + 4 * C + 48) + inter * 20 + W * H * (4 * C + 8)
+    b = P * (44 + 4 * C + 100) + inter * 20 + W * H * (4 * C + 8)
     if backward:
         b += P * (4 * (6 + C) + 4 * (14 + C * D)) + W * H * 4 * C
     return int(b)

@@ -537,6 +537,25 @@ def test_culled_lists_blend_like_the_exact_lists():
                            s["feat"].numpy(), W, H)
 
 
+def test_row_cut_lists_blend_like_the_exact_lists():
+    """From about 720p up (3,000 tiles) the culled lists also cut each
+    rectangle row by row to the columns the ellipse's band reaches: on
+    strongly elongated, rotated and faint 2-D Gaussians at 1280x720 the
+    lists are still subsequences of the exact lists (fewer entries than the
+    whole-rectangle cut of the same Gaussians at a size below the
+    threshold would keep), the image is bit-identical and the gradients
+    agree; and the same on a projected scene."""
+    W, H = 1280, 720
+    uv, conic, op, feat, _, _, (depth, radius, tiles) = elongated_2d(6000, W, H, seed=8)
+    op = op.copy()
+    op[5::61] = 0.003  # below 1/255: reaches no pixel
+    n_full, n_cull = check_culled_lists(uv, depth, radius, tiles, conic, op, feat, W, H)
+    assert n_cull < 0.8 * n_full
+    s, it, _, _ = blend_inputs(n=30000, W=W, H=H, C=3, seed=4)
+    check_culled_lists(it["uv"], it["depth"], it["radius"], it["tiles"], it["conic"], s["opacity"].numpy(),
+                       s["feat"].numpy(), W, H)
+
+
 def small_vs_general(uv, conic, op, f3, idx, tr, W, H):
     from msplat_gb300 import _lib
     lib = _lib.load()
