@@ -66,6 +66,7 @@ _SIGNATURES = {
     "msplat_batch_preprocess_backward": (
         _I, [_I, _I, _P, _P, _P, _P, _I, _I, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _SZ, _P]),
     "msplat_set_blend_ring": (_I, [_I, _I]),
+    "msplat_set_blend_ring_bwd": (_I, [_I, _I]),
     "msplat_set_wait_limit": (_I, [_I]),
     "msplat_set_sort_onesweep": (_I, [_I]),
     "msplat_wait_error": (_I, [_I, _P, _P]),

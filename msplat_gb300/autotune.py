@@ -10,7 +10,8 @@ sort tile, 256 x items), optional register caps of the two blend kernels
 (more resident blocks per SM against spills), whether a tile is blended
 by one block or by two of 8 rows each, and whether the forward runs as a
 producer / consumer ring, with how many producer warps and with what
-minimum of resident ring blocks per SM.  The tile itself stays 16x16: it is
+minimum of resident ring blocks per SM, and whether the backward runs as
+a ring and with how many producer warps.  The tile itself stays 16x16: it is
 part of the reference's outputs (tiles_touched, tile_range).  The
 multi-camera blend grid has its own pixels-per-thread and batch parameters.
 
@@ -58,11 +59,13 @@ SPACE = {
     "MSPLAT_BLEND_SPLIT_BWD": [1, 2],
     "MSPLAT_BLEND_RING_FWD": [0, 2, 4],
     "MSPLAT_RING_MIN_BLOCKS": [0, 5],
+    "MSPLAT_BLEND_RING_BWD": [0, 1, 2],
 }
 DEFAULTS = {"MSPLAT_BLEND_NPIX_FWD": 1, "MSPLAT_BLEND_NPIX_BWD": 2, "MSPLAT_BLEND_GATHER_FWD": 1,
             "MSPLAT_BLEND_GATHER_BWD": 2, "MSPLAT_FEW_LANES": 12, "MSPLAT_SORT_ITEMS": 12,
             "MSPLAT_BLEND_FWD_REGS": 0, "MSPLAT_BLEND_BWD_REGS": 0, "MSPLAT_BLEND_SPLIT_FWD": 1,
-            "MSPLAT_BLEND_SPLIT_BWD": 1, "MSPLAT_BLEND_RING_FWD": 0, "MSPLAT_RING_MIN_BLOCKS": 0}
+            "MSPLAT_BLEND_SPLIT_BWD": 1, "MSPLAT_BLEND_RING_FWD": 0, "MSPLAT_RING_MIN_BLOCKS": 0,
+            "MSPLAT_BLEND_RING_BWD": 0}
 # the multi-camera blend grid's own parameters (workload "batch")
 BATCH_SPACE = {
     "MSPLAT_BATCH_BLEND_NPIX_FWD": [1, 2],
@@ -70,10 +73,11 @@ BATCH_SPACE = {
     "MSPLAT_BATCH_BLEND_GATHER_FWD": [1, 2],
     "MSPLAT_BATCH_BLEND_GATHER_BWD": [1, 2, 4],
     "MSPLAT_BATCH_BLEND_RING_FWD": [0, 2, 4],
+    "MSPLAT_BATCH_BLEND_RING_BWD": [0, 1, 2],
 }
 BATCH_DEFAULTS = {"MSPLAT_BATCH_BLEND_NPIX_FWD": 1, "MSPLAT_BATCH_BLEND_NPIX_BWD": 2,
                   "MSPLAT_BATCH_BLEND_GATHER_FWD": 1, "MSPLAT_BATCH_BLEND_GATHER_BWD": 2,
-                  "MSPLAT_BATCH_BLEND_RING_FWD": 0}
+                  "MSPLAT_BATCH_BLEND_RING_FWD": 0, "MSPLAT_BATCH_BLEND_RING_BWD": 0}
 TUNE_DIR = os.path.join(_build.PKG_DIR, "_build", "tune")
 
 

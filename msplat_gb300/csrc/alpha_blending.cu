@@ -988,6 +988,114 @@ __device__ __forceinline__ int scatter_slot(int lane) {
 #endif
 constexpr int kFewLanes = MSPLAT_FEW_LANES;
 
+// The backward's walk over one gathered batch (entries in reverse list
+// order): each warp walks only the entries that reach its rows and precede
+// its largest ncontrib (a warp-uniform bit set per 32 entries), per pixel
+// undoes the transmittance, accumulates dL/dalpha from the colour
+// recursion carried as two scalars, and per entry sends the moments of
+// h = G dL/dalpha and the colour gradients (few lanes: direct atomics;
+// otherwise a reduce-scatter and one atomic per value per warp).  Shared
+// by blend_bwd_small_kernel and blend_bwd_ring_kernel.
+template <int C, int NPIX, bool BG>
+__device__ __forceinline__ void bwd_walk_batch(int n, const float4 *sA, const float4 *sB, const float4 *sF,
+                                               const int *sG, const unsigned char *sM, unsigned wbit, int warp_last,
+                                               int list0, float fx, const float (&fy)[NPIX], float (&T)[NPIX],
+                                               const float (&Tf)[NPIX], float (&la)[NPIX], const float (&bgd)[NPIX],
+                                               float (&ad)[NPIX], float (&lfd)[NPIX], const float (&dp)[NPIX][4],
+                                               const int (&last)[NPIX], int vi, float *__restrict__ dL_duv,
+                                               float *__restrict__ dL_dconic, float *__restrict__ dL_dopacity,
+                                               float *__restrict__ dL_dfeature) {
+    constexpr int NV = 6 + C;
+    const int lane = threadIdx.x & 31;
+        for (int kw = 0; kw < n; kw += 32) {
+          const int kk = kw + lane;
+          unsigned bits = __ballot_sync(0xffffffffu, kk < n && (sM[kk] & wbit) &&
+                                                         __float_as_int(sB[kk].w) - list0 < warp_last);
+          while (bits) {
+            const int k = kw + __ffs(bits) - 1;
+            bits &= bits - 1u;
+            const float4 A = sA[k], B = sB[k];
+            const int jl = __float_as_int(B.w) - list0;
+            const float dx = A.x - fx;
+            float dy[NPIX];
+#pragma unroll
+            for (int i = 0; i < NPIX; ++i) dy[i] = A.y - fy[i];
+            const PixPow<NPIX> pw = blend_power_n<NPIX>(A.z, A.w, B.x, dx, dy);
+            const float4 f = sF[k];
+            const float fv[4] = {f.x, f.y, f.z, f.w};
+            const float op = B.y;
+            float v[NV];
+#pragma unroll
+            for (int q = 0; q < NV; ++q) v[q] = 0.0f;
+            bool any = false;
+#pragma unroll
+            for (int i = 0; i < NPIX; ++i) {
+                const float power = pw.v[i];
+                if (jl >= last[i] || power > 0.0f || power < B.z) continue;
+                const float G = __expf(power);
+                const float alpha = fminf(0.99f, op * G);
+                if (alpha < 1.0f / 255.0f) continue;
+                any = true;
+                const float inv1m = __fdividef(1.f, 1.f - alpha);
+                T[i] = T[i] * inv1m;
+                const float dcol = alpha * T[i];
+                float fd = 0.0f;  // colour . dL/dpix
+#pragma unroll
+                for (int q = 0; q < C; ++q) {
+                    fd += fv[q] * dp[i][q];
+                    v[6 + q] += dcol * dp[i][q];
+                }
+                ad[i] = la[i] * lfd[i] + (1.f - la[i]) * ad[i];
+                lfd[i] = fd;
+                float dL_dalpha = fd - ad[i];
+                dL_dalpha *= T[i];
+                la[i] = alpha;
+                if (BG) dL_dalpha += (-Tf[i] * inv1m) * bgd[i];
+                // Moments of h = G dL/dalpha over the pixels; the uv, conic
+                // and opacity gradients are linear in them (finished per
+                // Gaussian by blend_grad_finish_kernel).
+                const float h = G * dL_dalpha;
+                const float hdx = h * dx, hdy = h * dy[i];
+                v[0] += h;
+                v[1] += hdx;
+                v[2] += hdy;
+                v[3] += hdx * dx;
+                v[4] += hdx * dy[i];
+                v[5] += hdy * dy[i];
+            }
+            const unsigned am = __ballot_sync(0xffffffffu, any);
+            if (am) {
+                // moments land in the gradient slots: S -> opacity, (Sx, Sy)
+                // -> uv, (Sxx, Sxy, Syy) -> conic (finished per Gaussian later)
+                const int g = sG[k];
+                if (__popc(am) <= kFewLanes) {
+                    if (any) {
+                        atomicAdd(dL_dopacity + g, v[0]);
+                        atomicAdd(dL_duv + 2 * g, v[1]);
+                        atomicAdd(dL_duv + 2 * g + 1, v[2]);
+                        atomicAdd(dL_dconic + 3 * g, v[3]);
+                        atomicAdd(dL_dconic + 3 * g + 1, v[4]);
+                        atomicAdd(dL_dconic + 3 * g + 2, v[5]);
+#pragma unroll
+                        for (int q = 0; q < C; ++q) atomicAdd(dL_dfeature + (size_t)g * C + q, v[6 + q]);
+                    }
+                } else {
+                    ReduceScatter<NV, 16>::run(v, lane);
+                    const float s = v[0];
+                    if (vi >= 0) {
+                        float *dst;
+                        if (vi == 0) dst = dL_dopacity + g;
+                        else if (vi < 3) dst = dL_duv + 2 * g + (vi - 1);
+                        else if (vi < 6) dst = dL_dconic + 3 * g + (vi - 3);
+                        else dst = dL_dfeature + (size_t)g * C + (vi - 6);
+                        atomicAdd(dst, s);
+                    }
+                }
+            }
+          }
+        }
+}
+
 // BG: the background is nonzero, so dL/dalpha has the term
 // -T_final / (1 - alpha) * sum_c bg dL/dpix_c (compiled out for bg == 0).
 template <int C, int NPIX, bool BG, int SPLIT, bool BATCH = false, int GE = NPIX>
@@ -1080,96 +1188,170 @@ blend_bwd_small_kernel(int P, const float2 *__restrict__ uv, const float *__rest
         const int n = gather_small<C, NPIX, true, ROWS, GE>(bend - 1, -1, bstart, bend, site.P, idx_sorted, uv, conic,
                                                         opacity, feature, bx0, by0, sA, sB, sF, sG, sM, scan,
                                                         false);
-        // Each warp walks only the entries that reach its rows and precede
-        // its largest ncontrib (a warp-uniform bit set per 32 entries).
-        for (int kw = 0; kw < n; kw += 32) {
-          const int kk = kw + lane;
-          unsigned bits = __ballot_sync(0xffffffffu, kk < n && (sM[kk] & wbit) &&
-                                                         __float_as_int(sB[kk].w) - range.x < warp_last);
-          while (bits) {
-            const int k = kw + __ffs(bits) - 1;
-            bits &= bits - 1u;
-            const float4 A = sA[k], B = sB[k];
-            const int jl = __float_as_int(B.w) - range.x;
-            const float dx = A.x - fx;
-            float dy[NPIX];
-#pragma unroll
-            for (int i = 0; i < NPIX; ++i) dy[i] = A.y - fy[i];
-            const PixPow<NPIX> pw = blend_power_n<NPIX>(A.z, A.w, B.x, dx, dy);
-            const float4 f = sF[k];
-            const float fv[4] = {f.x, f.y, f.z, f.w};
-            const float op = B.y;
-            float v[NV];
-#pragma unroll
-            for (int q = 0; q < NV; ++q) v[q] = 0.0f;
-            bool any = false;
-#pragma unroll
-            for (int i = 0; i < NPIX; ++i) {
-                const float power = pw.v[i];
-                if (jl >= last[i] || power > 0.0f || power < B.z) continue;
-                const float G = __expf(power);
-                const float alpha = fminf(0.99f, op * G);
-                if (alpha < 1.0f / 255.0f) continue;
-                any = true;
-                const float inv1m = __fdividef(1.f, 1.f - alpha);
-                T[i] = T[i] * inv1m;
-                const float dcol = alpha * T[i];
-                float fd = 0.0f;  // colour . dL/dpix
-#pragma unroll
-                for (int q = 0; q < C; ++q) {
-                    fd += fv[q] * dp[i][q];
-                    v[6 + q] += dcol * dp[i][q];
-                }
-                ad[i] = la[i] * lfd[i] + (1.f - la[i]) * ad[i];
-                lfd[i] = fd;
-                float dL_dalpha = fd - ad[i];
-                dL_dalpha *= T[i];
-                la[i] = alpha;
-                if (BG) dL_dalpha += (-Tf[i] * inv1m) * bgd[i];
-                // Moments of h = G dL/dalpha over the pixels; the uv, conic
-                // and opacity gradients are linear in them (finished per
-                // Gaussian by blend_grad_finish_kernel).
-                const float h = G * dL_dalpha;
-                const float hdx = h * dx, hdy = h * dy[i];
-                v[0] += h;
-                v[1] += hdx;
-                v[2] += hdy;
-                v[3] += hdx * dx;
-                v[4] += hdx * dy[i];
-                v[5] += hdy * dy[i];
-            }
-            const unsigned am = __ballot_sync(0xffffffffu, any);
-            if (am) {
-                // moments land in the gradient slots: S -> opacity, (Sx, Sy)
-                // -> uv, (Sxx, Sxy, Syy) -> conic (finished per Gaussian later)
-                const int g = sG[k];
-                if (__popc(am) <= kFewLanes) {
-                    if (any) {
-                        atomicAdd(dL_dopacity + g, v[0]);
-                        atomicAdd(dL_duv + 2 * g, v[1]);
-                        atomicAdd(dL_duv + 2 * g + 1, v[2]);
-                        atomicAdd(dL_dconic + 3 * g, v[3]);
-                        atomicAdd(dL_dconic + 3 * g + 1, v[4]);
-                        atomicAdd(dL_dconic + 3 * g + 2, v[5]);
-#pragma unroll
-                        for (int q = 0; q < C; ++q) atomicAdd(dL_dfeature + (size_t)g * C + q, v[6 + q]);
-                    }
-                } else {
-                    ReduceScatter<NV, 16>::run(v, lane);
-                    const float s = v[0];
-                    if (vi >= 0) {
-                        float *dst;
-                        if (vi == 0) dst = dL_dopacity + g;
-                        else if (vi < 3) dst = dL_duv + 2 * g + (vi - 1);
-                        else if (vi < 6) dst = dL_dconic + 3 * g + (vi - 3);
-                        else dst = dL_dfeature + (size_t)g * C + (vi - 6);
-                        atomicAdd(dst, s);
-                    }
-                }
-            }
-          }
-        }
+        bwd_walk_batch<C, NPIX, BG>(n, sA, sB, sF, sG, sM, wbit, warp_last, range.x, fx, fy, T, Tf, la, bgd, ad,
+                                    lfd, dp, last, vi, dL_duv, dL_dconic, dL_dopacity, dL_dfeature);
         // no barrier here: the next gather's first barrier orders the batches
+    }
+}
+
+// ===================================================================
+// Backward blend as a producer / consumer ring (C <= 4): NP producer warps
+// gather, cull and mask each 256-entry batch of a tile's list from its end
+// (the same per-entry work as gather_small with dir = -1), each compacting
+// its share, in reverse list order, into its own part of one of two
+// shared-memory slots; the consumer warps (NPIX pixels per thread, the
+// warp blocks of blend_bwd_small_kernel) walk the other slot part by part
+// with the same code (bwd_walk_batch).  Hand-off and bounded waits as in
+// blend_fwd_ring_kernel: per slot a "full" mbarrier (every producer thread
+// arrives after its writes) and an "empty" one (each consumer warp
+// arrives); the number of batches follows from the block's largest
+// ncontrib, known to all before the first.  Results equal
+// blend_bwd_small_kernel's up to the order of the gradient atomics (the
+// same entries reach each warp in the same order with the same per-pair
+// code).
+// ===================================================================
+template <int C, int NPIX, int NP, bool BG, bool BATCH = false>
+__global__ void MSPLAT_RING_BOUNDS(kTilePixels / NPIX + 32 * NP)
+blend_bwd_ring_kernel(int P, const float2 *__restrict__ uv, const float *__restrict__ conic,
+                      const float *__restrict__ opacity, const float *__restrict__ feature,
+                      const int32_t *__restrict__ idx_sorted, const int2 *__restrict__ tile_range, float bg, int W,
+                      int H, const float *__restrict__ final_T, const int32_t *__restrict__ ncontrib,
+                      const float *__restrict__ dL_dout, float *__restrict__ dL_duv, float *__restrict__ dL_dconic,
+                      float *__restrict__ dL_dopacity, float *__restrict__ dL_dfeature, BlendBatch bb,
+                      int wait_limit) {
+    constexpr int NT = kTilePixels / NPIX;  // consumer threads
+    constexpr int NCW = NT / 32;            // consumer warps
+    constexpr int SLOT = 256;               // entries per batch
+    constexpr int SUB = SLOT / NP;          // entries per producer warp (its own part of the slot)
+    constexpr int PER = SUB / 32;           // gather rounds per producer warp
+    constexpr int NV = 6 + C;
+    static_assert(SLOT % (32 * NP) == 0, "producer warps must split a batch evenly");
+    __shared__ float4 sA[2][SLOT], sB[2][SLOT], sF[2][SLOT];
+    __shared__ int sG[2][SLOT];
+    __shared__ unsigned char sM[2][SLOT];
+    __shared__ int scount[2][NP], sstop[2];
+    __shared__ int smax;
+    __shared__ __align__(8) uint64_t full_bar[2], empty_bar[2];
+
+    const BlendSite site = blend_site<BATCH, 1>(bb, P, W, H);
+    if (BATCH) {
+        W = site.W;
+        H = site.H;
+        uv += site.row_off;
+        conic += 3 * site.row_off;
+        opacity += site.op_off;
+        feature += (size_t)C * site.feat_off;
+        final_T += site.pix_off;
+        ncontrib += site.pix_off;
+        dL_dout += (size_t)C * site.pix_off;
+        dL_duv += 2 * site.row_off;
+        dL_dconic += 3 * site.row_off;
+        dL_dopacity += site.row_off;
+        dL_dfeature += (size_t)C * site.row_off;
+    }
+    const int2 range = tile_range[site.tidx];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const bool consumer = warp < NCW;
+    const float bx0 = (float)(site.tx * kTile), by0 = (float)(site.ty * kTile);
+    if (threadIdx.x == 0) {
+        smax = 0;
+        mbar_init(&full_bar[0], 32 * NP);
+        mbar_init(&full_bar[1], 32 * NP);
+        mbar_init(&empty_bar[0], NCW);
+        mbar_init(&empty_bar[1], NCW);
+    }
+    __syncthreads();
+
+    // consumer pixels and state (as blend_bwd_small_kernel)
+    const int px = site.tx * kTile + 8 * (warp & 1) + (lane & 7);
+    const int py0 = site.ty * kTile + 4 * NPIX * (warp >> 1) + (lane >> 3) * NPIX;
+    float fy[NPIX], T[NPIX], Tf[NPIX], la[NPIX], bgd[NPIX], ad[NPIX], lfd[NPIX];
+    float dp[NPIX][4];
+    int last[NPIX];
+    int mylast = 0;
+    if (consumer) {
+#pragma unroll
+        for (int i = 0; i < NPIX; ++i) {
+            const int py = py0 + i;
+            const bool in = px < W && py < H;
+            const int pix = py * W + px;
+            fy[i] = (float)py;
+            Tf[i] = in ? final_T[pix] : 0.0f;
+            T[i] = Tf[i];
+            last[i] = in ? ncontrib[pix] : 0;
+            mylast = max(mylast, last[i]);
+            la[i] = 0.0f;
+            bgd[i] = 0.0f;
+            ad[i] = 0.0f;
+            lfd[i] = 0.0f;
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                dp[i][q] = (in && q < C) ? dL_dout[(size_t)q * H * W + pix] : 0.0f;
+                if (q < C) bgd[i] += bg * dp[i][q];
+            }
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) mylast = max(mylast, __shfl_xor_sync(0xffffffffu, mylast, o));
+        if (lane == 0) atomicMax(&smax, mylast);
+    }
+    __syncthreads();
+    const int end = range.x + min(smax, range.y - range.x);
+    const int nb = end > range.x ? (end - range.x + SLOT - 1) / SLOT : 0;
+
+    if (!consumer) {
+        // ------------------------------------------------------- producers
+        const int pw = warp - NCW;
+        for (int k = 0; k < nb; ++k) {
+            const int s = k & 1;
+            if (pw == 0 && lane == 0) sstop[s] = mbar_wait_one(&empty_bar[s], ((k >> 1) & 1) ^ 1, wait_limit) ? 0 : 2;
+            producer_sync<NP>();
+            if (sstop[s] == 2) return;  // gave up waiting: the consumers time out too
+            const int bend = end - k * SLOT, bstart = max(range.x, bend - SLOT);
+            float4 *dA = sA[s] + pw * SUB, *dB = sB[s] + pw * SUB, *dF = sF[s] + pw * SUB;
+            int *dG = sG[s] + pw * SUB;
+            unsigned char *dM = sM[s] + pw * SUB;
+            int n = 0;
+#pragma unroll 2
+            for (int r = 0; r < PER; ++r) {
+                const int j = bend - 1 - (pw * SUB + r * 32 + lane);  // reverse list order: part, round, lane
+                float4 A, B, F;
+                int G;
+                unsigned M;
+                bool keep = false;
+                if (j >= bstart)
+                    keep = gather_entry<C, NPIX, kTile>(j, site.P, idx_sorted, uv, conic, opacity, feature, bx0, by0,
+                                                        A, B, F, G, M);
+                const unsigned ballot = __ballot_sync(0xffffffffu, keep);
+                if (keep) {
+                    const int pos = n + __popc(ballot & ((1u << lane) - 1u));
+                    dA[pos] = A;
+                    dB[pos] = B;
+                    dF[pos] = F;
+                    dG[pos] = G;
+                    dM[pos] = (unsigned char)M;
+                }
+                n += __popc(ballot);
+            }
+            if (lane == 0) scount[s][pw] = n;
+            mbar_arrive(&full_bar[s]);  // releases this thread's slot writes
+        }
+        return;
+    }
+
+    // ------------------------------------------------------------ consumers
+    const unsigned wbit = 1u << warp;
+    const float fx = (float)px;
+    const int vi = scatter_slot<NV>(lane);
+    for (int k = 0; k < nb; ++k) {
+        const int s = k & 1;
+        if (!mbar_wait_warp(&full_bar[s], (k >> 1) & 1, wait_limit)) break;
+#pragma unroll
+        for (int q = 0; q < NP; ++q)
+            bwd_walk_batch<C, NPIX, BG>(scount[s][q], sA[s] + q * SUB, sB[s] + q * SUB, sF[s] + q * SUB,
+                                        sG[s] + q * SUB, sM[s] + q * SUB, wbit, mylast, range.x, fx, fy, T, Tf, la,
+                                        bgd, ad, lfd, dp, last, vi, dL_duv, dL_dconic, dL_dopacity, dL_dfeature);
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&empty_bar[s]);
     }
 }
 
@@ -1265,6 +1447,16 @@ constexpr int kBatchNpixFwd = MSPLAT_BATCH_BLEND_NPIX_FWD, kBatchNpixBwd = MSPLA
 #endif
 static int g_fwd_ring = MSPLAT_BLEND_RING_FWD;
 static int g_batch_fwd_ring = MSPLAT_BATCH_BLEND_RING_FWD;
+// The backward as a ring with 1 or 2 producer warps (0: block-barrier
+// kernel); tunable default, msplat_set_blend_ring_bwd at run time.
+#ifndef MSPLAT_BLEND_RING_BWD
+#define MSPLAT_BLEND_RING_BWD 0
+#endif
+#ifndef MSPLAT_BATCH_BLEND_RING_BWD
+#define MSPLAT_BATCH_BLEND_RING_BWD MSPLAT_BLEND_RING_BWD
+#endif
+static int g_bwd_ring = MSPLAT_BLEND_RING_BWD;
+static int g_batch_bwd_ring = MSPLAT_BATCH_BLEND_RING_BWD;
 constexpr int kBatchGatherFwd = MSPLAT_BATCH_BLEND_GATHER_FWD, kBatchGatherBwd = MSPLAT_BATCH_BLEND_GATHER_BWD;
 // Blocks per tile of the C <= 4 kernels (1 or 2: whole tiles, or halves of
 // 8 rows with their own gather, cull and end; compile-time tunables).
@@ -1292,7 +1484,17 @@ void launch_small(bool bwd, dim3 grid, cudaStream_t stream, int P, const float2 
     else if (!bwd)
         launch(blend_fwd_small_kernel<C, kBlendNpixFwd, kSplitFwd, false, kGatherFwd>, gf, tf, 0, stream,
             P, uv, conic, opacity, feature, idx, tr, bg, W, H, out, final_T, nc, BlendBatch{});
-    else if (bg != 0.0f)
+    else if (g_bwd_ring == 1 || g_bwd_ring == 2) {
+        constexpr int tr0 = kTilePixels / kBlendNpixBwd;
+#define MSPLAT_BWD_RING(NP, BGV)                                                                                 \
+    launch(blend_bwd_ring_kernel<C, kBlendNpixBwd, NP, BGV>, grid, tr0 + 32 * NP, 0, stream, P, uv, conic, opacity, \
+           feature, idx, tr, bg, W, H, fT, nci, dout, duv, dcon, dop, dfeat, BlendBatch{}, g_wait_limit)
+        if (g_bwd_ring == 1 && bg != 0.0f) MSPLAT_BWD_RING(1, true);
+        else if (g_bwd_ring == 1) MSPLAT_BWD_RING(1, false);
+        else if (bg != 0.0f) MSPLAT_BWD_RING(2, true);
+        else MSPLAT_BWD_RING(2, false);
+#undef MSPLAT_BWD_RING
+    } else if (bg != 0.0f)
         launch(blend_bwd_small_kernel<C, kBlendNpixBwd, true, kSplitBwd, false, kGatherBwd>, gb, tb, 0, stream,
             P, uv, conic, opacity, feature, idx, tr, bg, W, H, fT, nci, dout, duv, dcon, dop, dfeat, BlendBatch{});
     else
@@ -1403,7 +1605,16 @@ void launch_small_batch(bool bwd, int tiles, cudaStream_t stream, const BlendBat
     else if (!bwd)
         launch(blend_fwd_small_kernel<C, kBatchNpixFwd, 1, true, kBatchGatherFwd>, tiles, tf, 0, stream, 0, uv,
                conic, opacity, feature, idx, tr, bg, 1, 1, out, final_T, nc, bb);
-    else if (bg != 0.0f)
+    else if (g_batch_bwd_ring == 1 || g_batch_bwd_ring == 2) {
+#define MSPLAT_BWD_RING(NP, BGV)                                                                                  \
+    launch(blend_bwd_ring_kernel<C, kBatchNpixBwd, NP, BGV, true>, tiles, tb + 32 * NP, 0, stream, 0, uv, conic,     \
+           opacity, feature, idx, tr, bg, 1, 1, fT, nci, dout, duv, dcon, dop, dfeat, bb, g_wait_limit)
+        if (g_batch_bwd_ring == 1 && bg != 0.0f) MSPLAT_BWD_RING(1, true);
+        else if (g_batch_bwd_ring == 1) MSPLAT_BWD_RING(1, false);
+        else if (bg != 0.0f) MSPLAT_BWD_RING(2, true);
+        else MSPLAT_BWD_RING(2, false);
+#undef MSPLAT_BWD_RING
+    } else if (bg != 0.0f)
         launch(blend_bwd_small_kernel<C, kBatchNpixBwd, true, 1, true, kBatchGatherBwd>, tiles, tb, 0, stream, 0, uv,
                conic, opacity, feature, idx, tr, bg, 1, 1, fT, nci, dout, duv, dcon, dop, dfeat, bb);
     else
@@ -1501,6 +1712,14 @@ extern "C" int msplat_set_blend_ring(int producer_warps, int batch_producer_warp
         return set_error(MSPLAT_ERR_INVALID_ARGUMENT, "set_blend_ring: producer warps must be 0, 2 or 4");
     g_fwd_ring = producer_warps;
     g_batch_fwd_ring = batch_producer_warps;
+    return MSPLAT_OK;
+}
+
+extern "C" int msplat_set_blend_ring_bwd(int producer_warps, int batch_producer_warps) {
+    if (producer_warps < 0 || producer_warps > 2 || batch_producer_warps < 0 || batch_producer_warps > 2)
+        return set_error(MSPLAT_ERR_INVALID_ARGUMENT, "set_blend_ring_bwd: producer warps must be 0, 1 or 2");
+    g_bwd_ring = producer_warps;
+    g_batch_bwd_ring = batch_producer_warps;
     return MSPLAT_OK;
 }
 
