@@ -251,19 +251,26 @@ def blend_pairs(ms, p, color_dim=3):
 # DRAM bytes per launch (read + write) of the blend kernels at the benchmark
 # size over the fused calls' culled lists: a constant taken from an earlier
 # ncu capture, not measured by this run (reported with that label).
-NCU_TRAFFIC_1M_1080P = {"alpha_blending_backward": 95.92e6 + 0.81e6,
-                        "alpha_blending_forward": 44.51e6 + 11.07e6}
+NCU_TRAFFIC_1M_1080P = {"alpha_blending_backward": 93.74e6 + 1.03e6,
+                        "alpha_blending_forward": 42.26e6 + 9.39e6}
 
 
-def roofline(stages, steps, pairs, inter, nvis, sm_mhz, peaks, peak_kind, C=3, n=None, D=16, full=None):
+def roofline(stages, steps, pairs, inter, nvis, sm_mhz, peaks, peak_kind, C=3, n=None, D=16, full=None,
+             pairs_ref=None):
     """Roofline entry for the stage with the largest share of the step (C
-    blended channels, n Gaussians, D SH coefficients per channel)."""
+    blended channels, n Gaussians, D SH coefficients per channel).  For a
+    blend the work is Q pixel-entry pairs: Q = sum of ncontrib over the
+    reference's tile lists (pairs_ref) when given -- the algorithm's pairs,
+    whatever entries the culled lists skip -- else over the lists blended
+    (pairs), and the fraction over the culled lists' pairs is reported
+    beside it."""
     name, (calls, total) = max(stages.items(), key=lambda kv: kv[1][1])
     per_launch_ms = total / max(calls, 1)
     N_G = N_GAUSS if n is None else n
     if name.startswith("alpha_blending"):
         fl = (12 + 2 * C) if name.endswith("forward") else (30 + 8 * C)
-        flops = pairs * (fl + 1)  # + one exponential per pair
+        q = pairs_ref if pairs_ref else pairs
+        flops = q * (fl + 1)  # + one exponential per pair
         ach = flops / (per_launch_ms * 1e-3) / 1e12
         peak = fp32_peak_tflops(sm_mhz)
         if full is None:
@@ -273,7 +280,11 @@ def roofline(stages, steps, pairs, inter, nvis, sm_mhz, peaks, peak_kind, C=3, n
         out = {"bound": "fp32", "achieved": round(ach, 3), "peak": round(peak, 2), "unit": "TFLOP/s",
                "frac": round(ach / peak, 4), "traffic": traffic,
                "peak_source": "nominal FP32 lanes x sampled SM clock (not measured)",
-               "kernel": name, "per_launch_ms": round(per_launch_ms, 4)}
+               "kernel": name, "per_launch_ms": round(per_launch_ms, 4),
+               "work": (f"Q = {q} pixel-entry pairs (sum of ncontrib over the "
+                        f"{'reference' if pairs_ref else 'blended'} tile lists) x {fl + 1} flop")}
+        if pairs_ref:
+            out["frac_over_culled_pairs"] = round(pairs * (fl + 1) / (per_launch_ms * 1e-3) / 1e12 / peak, 4)
         if traffic:
             # the same kernel against the memory roof: DRAM bytes per launch
             # (ncu) over the live launch time
@@ -483,7 +494,8 @@ def _finish(args, rank, world, ms, p, stages, clk, ms_step, e2e_ms, h2d, extra):
     # the fused calls the bench times sort and blend the culled lists
     pairs, inter, nvis = work["culled"]["blend_pairs"], work["culled"]["intersections"], work["visible_gaussians"]
     peaks, peak_kind = measured_peaks()
-    dom, roof = roofline(stages, args.steps, pairs, inter, nvis, clk.get("sm_mhz"), peaks, peak_kind)
+    dom, roof = roofline(stages, args.steps, pairs, inter, nvis, clk.get("sm_mhz"), peaks, peak_kind,
+                         pairs_ref=work["reference"]["blend_pairs"])
     in_mb = (sum(v.numel() * v.element_size() for v in p.values()) + 3 * W_IMG * H_IMG * 4) / 1e6
     stage_ms = {k: round(v[1] / args.steps, 4) for k, v in sorted(stages.items(), key=lambda kv: -kv[1][1])}
     out = {
