@@ -2,6 +2,8 @@
 (drop-in for msplat/alpha_blending.py)."""
 from __future__ import annotations
 
+import math
+
 import torch
 from torch import Tensor
 
@@ -39,6 +41,19 @@ def alpha_blending(
     """
     return _AlphaBlending.apply(uv, conic, opacity, feature, idx_sorted, tile_range, bg, W, H, ndc)
 
+
+
+def zeroed_views(dev, shapes):
+    """Zero-filled float32 tensors of the given shapes, carved from one
+    allocation (one fill instead of one per tensor), each contiguous and
+    starting on a 16-byte boundary."""
+    sizes = [math.prod(sh) for sh in shapes]
+    offs, total = [], 0
+    for n in sizes:
+        offs.append(total)
+        total += -(-n // 4) * 4
+    buf = torch.zeros(max(total, 1), dtype=torch.float32, device=dev)
+    return [buf[o:o + n].view(sh) for o, n, sh in zip(offs, sizes, shapes)]
 
 class _AlphaBlending(torch.autograd.Function):
     @staticmethod
@@ -78,10 +93,8 @@ class _AlphaBlending(torch.autograd.Function):
         P, C = f.shape
         dev = f.device
         g = dL_drendered.float().contiguous()
-        dL_duv = torch.zeros((P, 2), dtype=torch.float32, device=dev)
-        dL_dconic = torch.zeros((P, 3), dtype=torch.float32, device=dev)
-        dL_dopacity = torch.zeros(ctx.opacity_shape, dtype=torch.float32, device=dev)
-        dL_dfeature = torch.zeros((P, C), dtype=torch.float32, device=dev)
+        dL_duv, dL_dconic, dL_dopacity, dL_dfeature = zeroed_views(
+            dev, [(P, 2), (P, 3), tuple(ctx.opacity_shape), (P, C)])
         if C > 0 and P > 0:
             lib = _lib.load()
             with _lib.stage("alpha_blending_backward"):

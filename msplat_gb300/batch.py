@@ -34,6 +34,7 @@ from torch import Tensor
 
 from . import _lib
 from . import _tensors as tt
+from .alpha_blending import zeroed_views
 
 SORT_TILE = 3072  # items per sort tile: capacities are multiples of it
 
@@ -245,10 +246,7 @@ class _RasterizeScenes(torch.autograd.Function):
                 seg.zero_()
             else:
                 seg.copy_(g.reshape(-1))
-        dL_duv = torch.zeros((R, 2), dtype=torch.float32, device=dev)
-        dL_dconic = torch.zeros((R, 3), dtype=torch.float32, device=dev)
-        dL_dop = torch.zeros((R,), dtype=torch.float32, device=dev)
-        dL_dfeat = torch.zeros((R, C), dtype=torch.float32, device=dev)
+        dL_duv, dL_dconic, dL_dop, dL_dfeat = zeroed_views(dev, [(R, 2), (R, 3), (R,), (R, C)])
         with _lib.stage("alpha_blending_backward"):
             _lib.check(lib.msplat_batch_alpha_blending_backward(
                 _lib.ptr(plan.device), B, plan.tiles, R, C, 1 if use_sh else 0, _lib.ptr(uv), _lib.ptr(conic),
@@ -263,11 +261,8 @@ class _RasterizeScenes(torch.autograd.Function):
         with _lib.stage("batch_preprocess_backward"):
             for s, (xyz, scale, rot, op, sf) in enumerate(prep):
                 Bs, P = groups[s], xyz.shape[0]
-                gx = torch.zeros((P, 3), dtype=torch.float32, device=dev)
-                gs = torch.zeros((P, 3), dtype=torch.float32, device=dev)
-                gr = torch.zeros((P, 4), dtype=torch.float32, device=dev)
-                go = torch.zeros((P,), dtype=torch.float32, device=dev)
-                gsh = torch.zeros((P, C, D), dtype=torch.float32, device=dev) if use_sh else None
+                gx, gs, gr, go, gsh = zeroed_views(dev, [(P, 3), (P, 3), (P, 4), (P,), (P, C, D) if use_sh else (0,)])
+                gsh = gsh if use_sh else None
                 gf = None
                 if Bs > 0:
                     r0, r1 = plan.row_off[b0], plan.row_off[b0 + Bs]
