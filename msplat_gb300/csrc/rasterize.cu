@@ -11,6 +11,7 @@
 // to the stage-by-stage path; the covariance is recomputed in the backward
 // instead of being stored.
 #include "geometry.cuh"
+#include "sh_basis.cuh"
 #include "sh_dispatch.cuh"
 
 namespace msplat {
@@ -42,6 +43,77 @@ preprocess_fwd_kernel(int P, const float *__restrict__ xyz, const float *__restr
     conic[3 * i + 2] = o[2];
     radius[i] = rad;
     tiles[i] = nt;
+}
+
+// Geometry and view-direction SH colour in one kernel (SH degree <= 3,
+// C <= 4, the common case): the block's coefficient rows are staged in
+// shared memory as sh_fwd_kernel stages them, the geometry of
+// preprocess_fwd_kernel runs while those loads are in flight, and the
+// colour follows with sh_fwd_kernel's code (camera-centre view direction,
+// the same products in the same order), so every output is identical to
+// the two-kernel path.
+template <int DEG>
+__global__ void __launch_bounds__(256)
+preprocess_sh_fwd_kernel(int P, int C, const float *__restrict__ xyz, const float *__restrict__ scales,
+                         const float4 *__restrict__ quats, const float *__restrict__ intr,
+                         const float *__restrict__ extr, int W, int H, float nearest, float extent, int gx, int gy,
+                         const float *__restrict__ shs, float2 *__restrict__ uv, float *__restrict__ depth,
+                         float *__restrict__ conic, int32_t *__restrict__ radius, int32_t *__restrict__ tiles,
+                         float *__restrict__ color) {
+    constexpr int D = (DEG + 1) * (DEG + 1);
+    extern __shared__ float smem[];
+    const int CD = C * D, stride = CD | 1;
+    const int p0 = blockIdx.x * blockDim.x;
+    const int n = min((int)blockDim.x, P - p0);
+    stage_rows(smem, shs + (size_t)p0 * CD, n, CD, stride);
+    const int t = threadIdx.x;
+    const int i = p0 + t;
+    float px = 0.f, py = 0.f, pz = 0.f, d = 0.f;
+    if (t < n) {
+        const Cam c = load_cam(intr, extr);
+        px = xyz[3 * i];
+        py = xyz[3 * i + 1];
+        pz = xyz[3 * i + 2];
+        float2 u;
+        project_fwd_one(c, px, py, pz, W, H, nearest, extent, u, d);
+        uv[i] = u;
+        depth[i] = d;
+        float o[3] = {0.f, 0.f, 0.f};
+        int rad = 0, nt = 0;
+        if (d != 0.0f) {  // visible = depth != 0, as the reference's rasterization
+            float cov[6];
+            cov3d_fwd_one(scales[3 * i], scales[3 * i + 1], scales[3 * i + 2], quats[i], cov);
+            ewa_fwd_one(c, px, py, pz, cov, u, gx, gy, o, rad, nt);
+        }
+        conic[3 * i + 0] = o[0];
+        conic[3 * i + 1] = o[1];
+        conic[3 * i + 2] = o[2];
+        radius[i] = rad;
+        tiles[i] = nt;
+    }
+    __syncthreads();
+    if (t >= n) return;
+    float *out = color + (size_t)i * C;
+    if (d == 0.0f) {
+        for (int ch = 0; ch < C; ++ch) out[ch] = 0.f;
+        return;
+    }
+    float cc[3];
+    camera_centre(extr, cc);
+    const float dx = px - cc[0], dy = py - cc[1], dz = pz - cc[2];
+    const float len = sqrtf(dx * dx + dy * dy + dz * dz);
+    const float vx = dx / len, vy = dy / len, vz = dz / len;
+    const float *row = smem + t * stride;
+    for (int c0 = 0; c0 < C; c0 += kShChanBlock) {
+        float acc[kShChanBlock] = {0.f, 0.f, 0.f, 0.f};
+        const int nc = min(kShChanBlock, C - c0);
+        sh_basis<DEG, false>(vx, vy, vz, [&](int k, float Y) {
+#pragma unroll
+            for (int cb = 0; cb < kShChanBlock; ++cb)
+                if (cb < nc) acc[cb] += Y * row[(c0 + cb) * D + k];
+        });
+        for (int cb = 0; cb < nc; ++cb) out[c0 + cb] = acc[cb];
+    }
 }
 
 // dL/dxyz accumulates (projection + EWA) onto what the SH backward wrote
@@ -137,6 +209,21 @@ extern "C" int msplat_rasterize_preprocess_forward(int P, const float *xyz, cons
     if (sh && !color)
         return set_error(MSPLAT_ERR_INVALID_ARGUMENT, "rasterize_preprocess_forward: shs given without color");
     const int gx = ceil_div(W, kTile), gy = ceil_div(H, kTile);
+    if (sh && D <= 16 && C <= kShChanBlock) {  // one kernel: geometry and colour
+        const size_t smem = (size_t)256 * ((C * D) | 1) * sizeof(float);
+#define MSPLAT_PREP_SH(DG)                                                                                       \
+    case (DG + 1) * (DG + 1):                                                                                    \
+        cudaFuncSetAttribute(preprocess_sh_fwd_kernel<DG>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); \
+        launch(preprocess_sh_fwd_kernel<DG>, ceil_div(P, 256), 256, smem, stream, P, C, xyz, scales,             \
+               (const float4 *)uquats, intr, extr, W, H, nearest, extent, gx, gy, shs, (float2 *)uv, depth, conic, \
+               radius, tiles, color);                                                                            \
+        return check_launch("rasterize_preprocess_forward");
+        switch (D) {
+            MSPLAT_PREP_SH(0) MSPLAT_PREP_SH(1) MSPLAT_PREP_SH(2) MSPLAT_PREP_SH(3)
+            default: break;
+        }
+#undef MSPLAT_PREP_SH
+    }
     launch(preprocess_fwd_kernel, ceil_div(P, 256), 256, 0, stream, P, xyz, scales, (const float4 *)uquats, intr,
            extr, W, H, nearest, extent, gx, gy, (float2 *)uv, depth, conic, radius, tiles);
     int st = check_launch("rasterize_preprocess_forward");
