@@ -178,6 +178,119 @@ preprocess_bwd_kernel(int P, const float *__restrict__ xyz, const float *__restr
     if (cam_grads) block_partial_16(acc, partials);
 }
 
+// The SH adjoint and the geometry adjoint in one kernel (SH degree <= 3,
+// C <= 4): each step of preprocess_bwd_kernel's loop stages its block's
+// coefficient rows as sh_bwd_kernel does, evaluates the SH adjoint in
+// place (dL/dsh) and its view-direction gradient gv, then runs the
+// geometry adjoint with gv in registers instead of reading it back from
+// dL/dxyz, and streams the dL/dsh rows out.  The same Gaussians go to the
+// same threads in the same order, and every sum is taken in the same
+// order as in the two-kernel path, so all outputs are identical.
+template <int DEG>
+__global__ void __launch_bounds__(256, 3)
+preprocess_sh_bwd_kernel(int P, int C, const float *__restrict__ xyz, const float *__restrict__ scales,
+                         const float4 *__restrict__ quats, const float *__restrict__ intr,
+                         const float *__restrict__ extr, const float *__restrict__ shs,
+                         const float *__restrict__ depth, const int32_t *__restrict__ radius,
+                         const float2 *__restrict__ dL_duv, const float *__restrict__ dL_dconic,
+                         const float *__restrict__ dL_dcolor, float *__restrict__ dL_dxyz,
+                         float *__restrict__ dL_dscales, float4 *__restrict__ dL_dquats, float *__restrict__ dL_dshs,
+                         bool cam_grads, float *__restrict__ partials) {
+    constexpr int D = (DEG + 1) * (DEG + 1);
+    extern __shared__ float smem[];
+    const int CD = C * D, stride = CD | 1;
+    const Cam c = load_cam(intr, extr);
+    float cc[3];
+    camera_centre(extr, cc);
+    float acc[kCamGradVals];
+#pragma unroll
+    for (int k = 0; k < kCamGradVals; ++k) acc[k] = 0.0f;
+    const int t = threadIdx.x;
+    for (int p0 = blockIdx.x * blockDim.x; p0 < P; p0 += gridDim.x * blockDim.x) {
+        const int n = min((int)blockDim.x, P - p0);
+        stage_rows(smem, shs + (size_t)p0 * CD, n, CD, stride);
+        __syncthreads();
+        if (t < n) {
+            const int i = p0 + t;
+            float *row = smem + t * stride;
+            const float px = xyz[3 * i], py = xyz[3 * i + 1], pz = xyz[3 * i + 2];
+            const float dep = depth[i];
+            // SH adjoint (sh_bwd_kernel, camera mode)
+            float gv[3] = {0.f, 0.f, 0.f};
+            if (dep == 0.0f) {
+                for (int k = 0; k < CD; ++k) row[k] = 0.f;
+            } else {
+                const float dx = px - cc[0], dy = py - cc[1], dz = pz - cc[2];
+                const float len = sqrtf(dx * dx + dy * dy + dz * dz);
+                const float d[3] = {dx / len, dy / len, dz / len};
+                float gdx = 0.f, gdy = 0.f, gdz = 0.f;
+                for (int c0 = 0; c0 < C; c0 += kShChanBlock) {
+                    float g[kShChanBlock] = {0.f, 0.f, 0.f, 0.f};
+                    const int nc = min(kShChanBlock, C - c0);
+                    for (int cb = 0; cb < nc; ++cb) g[cb] = dL_dcolor[(size_t)i * C + c0 + cb];
+                    sh_basis<DEG, true>(d[0], d[1], d[2], [&](int k, float Y, float yx, float yy, float yz) {
+#pragma unroll
+                        for (int cb = 0; cb < kShChanBlock; ++cb) {
+                            if (cb < nc) {
+                                float *slot = row + (c0 + cb) * D + k;
+                                const float w = g[cb] * *slot;  // dL/dval * coefficient
+                                gdx += w * yx;
+                                gdy += w * yy;
+                                gdz += w * yz;
+                                *slot = g[cb] * Y;  // dL/dsh, written in place
+                            }
+                        }
+                    });
+                }
+                const float dg = d[0] * gdx + d[1] * gdy + d[2] * gdz;
+                gv[0] = (gdx - d[0] * dg) / len;
+                gv[1] = (gdy - d[1] * dg) / len;
+                gv[2] = (gdz - d[2] * dg) / len;
+            }
+            // geometry adjoint (preprocess_bwd_kernel with add_xyz)
+            float gx3[3] = {0.f, 0.f, 0.f};
+            float ds[3] = {0.f, 0.f, 0.f};
+            float4 dq = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (dep != 0.0f) {
+                project_bwd_one(c, px, py, pz, dL_duv[i], 0.0f, gx3, cam_grads, acc);
+                if (radius[i] > 0) {
+                    const float s3[3] = {scales[3 * i], scales[3 * i + 1], scales[3 * i + 2]};
+                    const float4 q = quats[i];
+                    float cov[6], ge[3], dV[6];
+                    cov3d_fwd_one(s3[0], s3[1], s3[2], q, cov);
+                    if (ewa_bwd_one(c, px, py, pz, cov, dL_dconic[3 * i], dL_dconic[3 * i + 1], dL_dconic[3 * i + 2],
+                                    ge, dV, cam_grads, acc)) {
+                        cov3d_bwd_one(s3, q, dV, ds, dq);
+#pragma unroll
+                        for (int k = 0; k < 3; ++k) gx3[k] += ge[k];
+                    }
+                }
+            }
+#pragma unroll
+            for (int k = 0; k < 3; ++k) gx3[k] += gv[k];
+            if (cam_grads) {
+#pragma unroll
+                for (int r = 0; r < 3; ++r) {
+#pragma unroll
+                    for (int j = 0; j < 3; ++j) acc[4 + 4 * r + j] += c.e[4 * r + 3] * gv[j];
+                    acc[4 + 4 * r + 3] += c.e[4 * r] * gv[0] + c.e[4 * r + 1] * gv[1] + c.e[4 * r + 2] * gv[2];
+                }
+            }
+            dL_dxyz[3 * i + 0] = gx3[0];
+            dL_dxyz[3 * i + 1] = gx3[1];
+            dL_dxyz[3 * i + 2] = gx3[2];
+            dL_dscales[3 * i + 0] = ds[0];
+            dL_dscales[3 * i + 1] = ds[1];
+            dL_dscales[3 * i + 2] = ds[2];
+            dL_dquats[i] = dq;
+        }
+        __syncthreads();
+        unstage_rows(dL_dshs + (size_t)p0 * CD, smem, n, CD, stride);
+        __syncthreads();  // the rows are staged again by the next step
+    }
+    if (cam_grads) block_partial_16(acc, partials);
+}
+
 inline int preprocess_bwd_blocks(int P) { return min(ceil_div(P, 256), kCamGradBlocks); }
 
 }  // namespace msplat
@@ -259,6 +372,24 @@ extern "C" int msplat_rasterize_preprocess_backward(
                          workspace_bytes, need);
     const int gblocks = preprocess_bwd_blocks(P);
     float *partials = (float *)workspace;
+    if (sh && D <= 16 && C <= kShChanBlock) {  // one kernel: SH and geometry adjoints
+        const size_t smem = (size_t)256 * ((C * D) | 1) * sizeof(float);
+#define MSPLAT_PREP_SH_BWD(DG)                                                                                   \
+    case (DG + 1) * (DG + 1):                                                                                    \
+        cudaFuncSetAttribute(preprocess_sh_bwd_kernel<DG>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); \
+        launch(preprocess_sh_bwd_kernel<DG>, gblocks, 256, smem, stream, P, C, xyz, scales, (const float4 *)uquats, \
+               intr, extr, shs, depth, radius, (const float2 *)dL_duv, dL_dconic, dL_dcolor, dL_dxyz, dL_dscales,  \
+               (float4 *)dL_duquats, dL_dshs, cam, partials);                                                   \
+        break;
+        switch (D) {
+            MSPLAT_PREP_SH_BWD(0) MSPLAT_PREP_SH_BWD(1) MSPLAT_PREP_SH_BWD(2) MSPLAT_PREP_SH_BWD(3)
+            default: break;
+        }
+#undef MSPLAT_PREP_SH_BWD
+        if (cam) launch(cam_grad_finalize_kernel, 1, kCamGradFinalizeThreads, 0, stream, gblocks, partials,
+                        dL_dintr, dL_dextr, 0);
+        return check_launch("rasterize_preprocess_backward");
+    }
     if (sh) {
         // writes dL/dxyz (view-direction part) first; the geometry kernel adds
         const ShDirs in{nullptr, nullptr, xyz, extr, depth, dL_dxyz};
