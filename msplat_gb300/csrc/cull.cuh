@@ -32,14 +32,11 @@ __device__ __forceinline__ float box_threshold(float gx, float gy, float a, floa
 // evaluation.  L receives the threshold it used: a pixel of the box can
 // contribute only where the exact q = a dx^2 + 2 b dx dy + c dy^2 is <= L
 // (INFINITY or NaN when the test gives no such bound).
-__device__ __forceinline__ bool cull_box(float gx, float gy, float a, float b, float c, float op, float bx0,
-                                         float by0, float bx1, float by1, float &L) {
+// cull_box for opacity > 0 with tau = 2 log(255 op) given (a caller that
+// tests several boxes of one Gaussian computes it once).
+__device__ __forceinline__ bool cull_box_tau(float gx, float gy, float a, float b, float c, float tau, float bx0,
+                                             float by0, float bx1, float by1, float &L) {
     L = INFINITY;
-    if (!(op > 0.0f)) {  // NaN opacity is never culled
-        L = op;
-        return op <= 0.0f;
-    }
-    const float tau = 2.0f * logf(255.0f * op);    // q <= tau  <=>  op e^{-q/2} >= 1/255
     const float det = a * c - b * b;
     if (!(a > 0.0f) || !(c > 0.0f) || !(det > 0.0f)) return false;  // not an ellipse
     const float lx = bx0 - gx, hx = bx1 - gx, ly = by0 - gy, hy = by1 - gy;  // pixel - centre
@@ -64,6 +61,16 @@ __device__ __forceinline__ bool cull_box(float gx, float gy, float a, float b, f
         }
     }
     return qmin > L;
+}
+
+__device__ __forceinline__ bool cull_box(float gx, float gy, float a, float b, float c, float op, float bx0,
+                                         float by0, float bx1, float by1, float &L) {
+    if (!(op > 0.0f)) {  // NaN opacity is never culled
+        L = op;
+        return op <= 0.0f;
+    }
+    const float tau = 2.0f * logf(255.0f * op);  // q <= tau  <=>  op e^{-q/2} >= 1/255
+    return cull_box_tau(gx, gy, a, b, c, tau, bx0, by0, bx1, by1, L);
 }
 
 // The same test for the 16 x 16 tile whose first pixel centre is (bx0, by0).
@@ -217,7 +224,7 @@ __device__ __forceinline__ void shrink_rect(float gx, float gy, float a, float b
     const float det = a * c - b * b;
     if (!(a > 0.0f) || !(c > 0.0f) || !(det > 0.0f)) return;
     if (!(tau > 0.0f)) {  // the ellipse is (nearly) empty: try the whole rectangle
-        if (cull_box(gx, gy, a, b, c, op, x0 * T, y0 * T, x1 * T - 1.0f, y1 * T - 1.0f, L)) {
+        if (cull_box_tau(gx, gy, a, b, c, tau, x0 * T, y0 * T, x1 * T - 1.0f, y1 * T - 1.0f, L)) {
             x1 = x0;
             y1 = y0;
         }
@@ -231,29 +238,29 @@ __device__ __forceinline__ void shrink_rect(float gx, float gy, float a, float b
     const int py0 = (int)fmaxf(fy0, (float)y0), py1 = (int)fminf(fy1, (float)y1);
     const int px0 = (int)fmaxf(fx0, (float)x0), px1 = (int)fminf(fx1, (float)x1);
     if (py0 >= py1 || px0 >= px1) {  // the box misses the rectangle: try all of it
-        if (cull_box(gx, gy, a, b, c, op, x0 * T, y0 * T, x1 * T - 1.0f, y1 * T - 1.0f, L)) {
+        if (cull_box_tau(gx, gy, a, b, c, tau, x0 * T, y0 * T, x1 * T - 1.0f, y1 * T - 1.0f, L)) {
             x1 = x0;
             y1 = y0;
         }
         return;
     }
     for (int k = py0; k > y0 && k >= py0 - 1; --k)
-        if (cull_box(gx, gy, a, b, c, op, x0 * T, y0 * T, x1 * T - 1.0f, k * T - 1.0f, L)) {
+        if (cull_box_tau(gx, gy, a, b, c, tau, x0 * T, y0 * T, x1 * T - 1.0f, k * T - 1.0f, L)) {
             y0 = k;
             break;
         }
     for (int k = py1; k < y1 && k <= py1 + 1; ++k)
-        if (cull_box(gx, gy, a, b, c, op, x0 * T, k * T, x1 * T - 1.0f, y1 * T - 1.0f, L)) {
+        if (cull_box_tau(gx, gy, a, b, c, tau, x0 * T, k * T, x1 * T - 1.0f, y1 * T - 1.0f, L)) {
             y1 = k;
             break;
         }
     for (int k = px0; k > x0 && k >= px0 - 1; --k)
-        if (cull_box(gx, gy, a, b, c, op, x0 * T, y0 * T, k * T - 1.0f, y1 * T - 1.0f, L)) {
+        if (cull_box_tau(gx, gy, a, b, c, tau, x0 * T, y0 * T, k * T - 1.0f, y1 * T - 1.0f, L)) {
             x0 = k;
             break;
         }
     for (int k = px1; k < x1 && k <= px1 + 1; ++k)
-        if (cull_box(gx, gy, a, b, c, op, k * T, y0 * T, x1 * T - 1.0f, y1 * T - 1.0f, L)) {
+        if (cull_box_tau(gx, gy, a, b, c, tau, k * T, y0 * T, x1 * T - 1.0f, y1 * T - 1.0f, L)) {
             x1 = k;
             break;
         }

@@ -121,7 +121,7 @@ struct EmitRowShared {
     int e[kEmitThreads + 1];        // per row of the chunk: exclusive prefix of the span lengths
     uint32_t kb[kEmitThreads];      // per row of the chunk: key of its first entry
     int rg[kEmitThreads];           // per row of the chunk: its run's Gaussian id
-    int64_t scratch[33];
+    int iscratch[33];
 };
 
 // `allotted` = the slots the count kernel gave the block (its runs' row
@@ -133,18 +133,17 @@ __device__ __forceinline__ void emit_block_rows(EmitRowShared &sm, int64_t base,
                                                 uint32_t *__restrict__ tkeys, uint32_t *__restrict__ tvals,
                                                 int64_t cap) {
     const int t = threadIdx.x;
-    const int h = valid && x0 < x1 ? max(0, y1 - y0) : 0;
-    int64_t rows64;
-    const int64_t ru = block_exclusive_scan<int64_t>((int64_t)h, sm.scratch, &rows64);
-    sm.ru[t] = (int)ru;
-    if (t == 0) sm.ru[kEmitThreads] = (int)rows64;
+    const int h = valid && x0 < x1 ? max(0, y1 - y0) : 0;  // rows: 256 x 32767 at most, within int
+    int rows;
+    const int ru = block_exclusive_scan<int>(h, sm.iscratch, &rows);
+    sm.ru[t] = ru;
+    if (t == 0) sm.ru[kEmitThreads] = rows;
     sm.reach[t] = reach;
     sm.x0[t] = x0;
     sm.x1[t] = x1;
     sm.y0[t] = y0;
     sm.g[t] = g;
     __syncthreads();
-    const int rows = (int)rows64;
     const int64_t lim_all = max((int64_t)0, min(allotted, cap - base));
     int64_t done = 0;  // entries of the earlier chunks (the same in every thread)
     for (int u0 = 0; u0 < rows; u0 += kEmitThreads) {
@@ -164,15 +163,15 @@ __device__ __forceinline__ void emit_block_rows(EmitRowShared &sm, int64_t base,
             kb = (uint32_t)(ty * gx + xa + 1);
             rg = sm.g[r];
         }
-        int64_t tot64;
-        const int64_t ex = block_exclusive_scan<int64_t>((int64_t)w, sm.scratch, &tot64);
-        sm.e[t] = (int)ex;
+        int tot;  // a chunk's entries: 256 rows of at most 32767 tiles, within int
+        const int ex = block_exclusive_scan<int>(w, sm.iscratch, &tot);
+        sm.e[t] = ex;
         sm.kb[t] = kb;
         sm.rg[t] = rg;
-        if (t == 0) sm.e[kEmitThreads] = (int)tot64;
+        if (t == 0) sm.e[kEmitThreads] = tot;
         __syncthreads();
         const int64_t cbase = base + done;
-        const int lim = (int)max((int64_t)0, min(tot64, lim_all - done));
+        const int lim = (int)max((int64_t)0, min((int64_t)tot, lim_all - done));
         const int head = min(lim, (int)((4 - (cbase & 3)) & 3));
         if (t < head) {
             int q = 0;
@@ -207,7 +206,7 @@ __device__ __forceinline__ void emit_block_rows(EmitRowShared &sm, int64_t base,
                 }
             }
         }
-        done += tot64;
+        done += tot;
         __syncthreads();  // the chunk's rows are rewritten by the next chunk
     }
 }

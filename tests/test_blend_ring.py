@@ -184,7 +184,10 @@ def test_ring_backward_on_elongated_faint_gaussians(lib):
     lib.msplat_set_blend_ring_bwd(2, 2)
     _, got = blend_grads(*t, 0.5, W, H)
     lib.msplat_set_blend_ring_bwd(*tuned_rings_bwd())
-    grads_close(got, ref)
+    # the gradient bar of the culled-list checks: 1e-4 of the largest (the uv
+    # gradients of these faint, elongated Gaussians are sums of opposite
+    # moments, and the float atomics arrive in another order)
+    grads_close(got, ref, rtol=1e-4)
 
 
 def test_ring_backward_in_the_multi_camera_grid(lib):
