@@ -13,6 +13,8 @@ bit-identical to the stage-by-stage calls.
 """
 from __future__ import annotations
 
+import threading
+
 import torch
 from torch import Tensor
 
@@ -104,14 +106,51 @@ def preprocess(xyz: Tensor, scale: Tensor, rotate: Tensor, intr: Tensor, extr: T
     return _Preprocess.apply(xyz, scale, rotate, shs, intr, extr, W, H, nearest, extent)
 
 
-def _sort(uv, depth, W, H, radius, tiles, capacity, status, cull):
-    # The fused calls sort culled lists: only the image and gradients leave
-    # them, and those equal the reference lists' (see sort_gaussian's cull).
-    if capacity is None:
-        return sort_gaussian(uv, depth, W, H, radius, tiles, cull=cull)
-    if status is None:
-        raise RuntimeError("a capacity-bounded sort needs a status tensor to report overflow in")
-    return sort_gaussian_capacity(uv, depth, W, H, radius, tiles, capacity, status, cull=cull)
+# Eager fused calls keep the true intersection count of their last call per
+# (device, Gaussians, image size), and sort the next call of that shape into
+# a capacity above it without waiting for the count (see _sort_and_blend).
+_CAP_LOCK = threading.Lock()
+_CAP_CACHE: dict = {}
+_CAP_MARGIN = 1.15
+
+
+def _remember(key, count: int) -> None:
+    with _CAP_LOCK:
+        _CAP_CACHE[key] = min(int(count * _CAP_MARGIN) + 3072, 2**31 - 1)
+
+
+def _sort_and_blend(uv, depth, conic, opacity, feature, radius, tiles, W, H, bg, ndc, capacity, status):
+    """Sort and blend of the fused calls, which sort culled lists: only the
+    image and gradients leave them, and those equal the reference lists'
+    (see sort_gaussian's cull).  With a capacity (CUDA-graph capture) the
+    caller's; eagerly, the first call of a shape reads the intersection
+    count before it allocates the lists, later calls sort into the
+    capacity their shape's last count suggests and check the true count
+    only after the blend is enqueued -- the wait covers the sort's prepare
+    alone, so the device never idles for it -- and redo the sort and blend
+    exactly in the rare case that it did not fit (the result is the same
+    either way)."""
+    cull = (conic.detach(), opacity.detach())
+    if capacity is not None:
+        if status is None:
+            raise RuntimeError("a capacity-bounded sort needs a status tensor to report overflow in")
+        idx, tr = sort_gaussian_capacity(uv, depth, W, H, radius, tiles, capacity, status, cull=cull)
+        return alpha_blending(uv, conic, opacity, feature, idx, tr, bg, W, H, ndc)
+    key = (uv.device, uv.shape[0], int(W), int(H))
+    with _CAP_LOCK:
+        cap = _CAP_CACHE.get(key)
+    if cap is not None and uv.is_cuda:
+        flag = torch.empty(1, dtype=torch.int32, device=uv.device)
+        idx, tr, pending = sort_gaussian_capacity(uv, depth, W, H, radius, tiles, cap, flag, cull=cull,
+                                                  deferred=True)
+        img = alpha_blending(uv, conic, opacity, feature, idx, tr, bg, W, H, ndc)
+        count, mismatch = pending.result()
+        _remember(key, count)
+        if count <= cap and mismatch == 0:
+            return img
+    idx, tr = sort_gaussian(uv, depth, W, H, radius, tiles, cull=cull)
+    _remember(key, idx.numel())
+    return alpha_blending(uv, conic, opacity, feature, idx, tr, bg, W, H, ndc)
 
 
 def rasterization(xyz: Tensor, scale: Tensor, rotate: Tensor, opacity: Tensor, feature: Tensor, intr: Tensor,
@@ -133,9 +172,7 @@ def rasterization(xyz: Tensor, scale: Tensor, rotate: Tensor, opacity: Tensor, f
     a capacity.
     """
     uv, depth, conic, radius, tiles, _ = preprocess(xyz, scale, rotate, intr, extr, W, H)
-    cull = (conic.detach(), opacity.detach())
-    idx_sorted, tile_range = _sort(uv, depth, W, H, radius, tiles, capacity, status, cull)
-    img = alpha_blending(uv, conic, opacity, feature, idx_sorted, tile_range, bg, W, H, ndc)
+    img = _sort_and_blend(uv, depth, conic, opacity, feature, radius, tiles, W, H, bg, ndc, capacity, status)
     return (img, radius) if return_radius else img
 
 
@@ -150,7 +187,5 @@ def rasterization_sh(xyz: Tensor, scale: Tensor, rotate: Tensor, opacity: Tensor
     [P] with return_radius=True).  `capacity` / `status` as for
     `rasterization`."""
     uv, depth, conic, radius, tiles, color = preprocess(xyz, scale, rotate, intr, extr, W, H, shs=shs)
-    cull = (conic.detach(), opacity.detach())
-    idx_sorted, tile_range = _sort(uv, depth, W, H, radius, tiles, capacity, status, cull)
-    img = alpha_blending(uv, conic, opacity, color, idx_sorted, tile_range, bg, W, H, ndc)
+    img = _sort_and_blend(uv, depth, conic, opacity, color, radius, tiles, W, H, bg, ndc, capacity, status)
     return (img, radius) if return_radius else img

@@ -125,15 +125,36 @@ def _sort_reference_layout(u, d, W, H, r, t):
     return idx_sorted, tile_range
 
 
+class DeferredCounts:
+    """The prepare's counts (intersections, rectangle mismatches) of a
+    capacity-bounded sort, copied to pinned host memory behind an event
+    recorded right after the prepare: result() waits for the prepare only,
+    not for the work enqueued after it."""
+
+    def __init__(self, counts: Tensor, stream):
+        self._host = torch.empty(2, dtype=torch.int64, pin_memory=True)
+        self._host.copy_(counts, non_blocking=True)
+        self._event = torch.cuda.Event()
+        self._event.record(stream)
+
+    def result(self) -> Tuple[int, int]:
+        self._event.synchronize()
+        return int(self._host[0]), int(self._host[1])
+
+
 def sort_gaussian_capacity(uv: Tensor, depth: Tensor, W: int, H: int, radius: Tensor, tiles: Tensor,
                            capacity: int, status: Tensor, *,
-                           cull: Tuple[Tensor, Tensor] | None = None) -> Tuple[Tensor, Tensor]:
+                           cull: Tuple[Tensor, Tensor] | None = None,
+                           deferred: bool = False):
     """`sort_gaussian` without a host read, for stream capture: idx_sorted has
     `capacity` entries (those past the true count are unused; the tile
     ranges index the valid ones) and status (a [1] int32 CUDA tensor) is set
     to 1 on the device when the result is not valid (more intersections than
     the capacity, or tiles[] disagreeing with the rectangles), else 0.
-    `cull` as for `sort_gaussian`."""
+    `cull` as for `sort_gaussian`.  With deferred=True a DeferredCounts is
+    returned as a third value (the true counts, readable once the prepare
+    has run, for a caller that checks the capacity after enqueueing the
+    work that uses the lists)."""
     u = tt.f32(uv, "uv", 2)
     d = tt.f32(depth, "depth")
     r = tt.i32(radius, "radius").view(-1)
@@ -151,6 +172,7 @@ def sort_gaussian_capacity(uv: Tensor, depth: Tensor, W: int, H: int, radius: Te
     ws_prep = _lib.workspace(lib.msplat_sort_prepare_workspace_size(P, W, H), dev)
     with _lib.stage("sort_gaussian_prepare"):
         _prepare(lib, P, d, r, t, u, W, H, counts, ws_prep, st, cull)
+    pending = DeferredCounts(counts, torch.cuda.current_stream(dev)) if deferred else None
     idx_sorted = torch.empty((capacity,), dtype=torch.int32, device=dev)
     tile_range = torch.empty((tt.ntiles(W, H), 2), dtype=torch.int32, device=dev)
     ws = _lib.workspace(lib.msplat_sort_finish_workspace_size(P, capacity, W, H), dev)
@@ -159,5 +181,7 @@ def sort_gaussian_capacity(uv: Tensor, depth: Tensor, W: int, H: int, radius: Te
             P, _lib.ptr(u), _lib.ptr(d), _lib.ptr(r), W, H, capacity, _lib.ptr(counts), _lib.ptr(ws_prep),
             _lib.ptr(idx_sorted), _lib.ptr(tile_range), _lib.ptr(st_t), _lib.ptr(ws), ws.numel(), st),
             "sort_gaussian_finish_capacity")
+    if deferred:
+        return idx_sorted, tile_range, pending
     return idx_sorted, tile_range
 
