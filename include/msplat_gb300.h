@@ -305,8 +305,9 @@ MSPLAT_API int msplat_alpha_blending_forward(int P, int C, const float *uv,
 MSPLAT_API int msplat_set_blend_ring(int producer_warps, int batch_producer_warps);
 /* The same for the C <= 4 backward: producer_warps = 1 or 2 runs it as a
  * ring (producer warps gather each tile's batches from the end of its list
- * while the backward's four consumer warps walk the other slot), 0 the
- * block-barrier kernel.  Gradients agree up to the order of float atomics.
+ * while the backward's four consumer warps walk the other slot) on
+ * single-camera images of at least 1,024 tiles, 0 the block-barrier kernel
+ * everywhere.  Gradients agree up to the order of float atomics.
  * Process-wide. */
 MSPLAT_API int msplat_set_blend_ring_bwd(int producer_warps, int batch_producer_warps);
 /* Every device-side wait -- the ring's hand-offs, the sort's look-back --

@@ -1457,6 +1457,11 @@ static int g_batch_fwd_ring = MSPLAT_BATCH_BLEND_RING_FWD;
 #endif
 static int g_bwd_ring = MSPLAT_BLEND_RING_BWD;
 static int g_batch_bwd_ring = MSPLAT_BATCH_BLEND_RING_BWD;
+// Single-camera images below this many tiles keep the barrier backward:
+// with a few hundred tiles of long lists (less than one wave of blocks) the
+// ring's single producer warp falls behind (256 x 256: 2.12 vs 1.96 ms;
+// from 512 x 512 up the ring is as fast or faster).
+constexpr int kBwdRingMinTiles = 1024;
 constexpr int kBatchGatherFwd = MSPLAT_BATCH_BLEND_GATHER_FWD, kBatchGatherBwd = MSPLAT_BATCH_BLEND_GATHER_BWD;
 // Blocks per tile of the C <= 4 kernels (1 or 2: whole tiles, or halves of
 // 8 rows with their own gather, cull and end; compile-time tunables).
@@ -1484,7 +1489,7 @@ void launch_small(bool bwd, dim3 grid, cudaStream_t stream, int P, const float2 
     else if (!bwd)
         launch(blend_fwd_small_kernel<C, kBlendNpixFwd, kSplitFwd, false, kGatherFwd>, gf, tf, 0, stream,
             P, uv, conic, opacity, feature, idx, tr, bg, W, H, out, final_T, nc, BlendBatch{});
-    else if (g_bwd_ring == 1 || g_bwd_ring == 2) {
+    else if ((g_bwd_ring == 1 || g_bwd_ring == 2) && (int)(grid.x * grid.y) >= kBwdRingMinTiles) {
         constexpr int tr0 = kTilePixels / kBlendNpixBwd;
 #define MSPLAT_BWD_RING(NP, BGV)                                                                                 \
     launch(blend_bwd_ring_kernel<C, kBlendNpixBwd, NP, BGV>, grid, tr0 + 32 * NP, 0, stream, P, uv, conic, opacity, \

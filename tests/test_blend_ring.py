@@ -162,7 +162,7 @@ def grads_close(got, ref, rtol=1e-5):
 
 @pytest.mark.parametrize("C,bg", [(1, 0.0), (3, 0.0), (3, 0.4), (4, 0.2)])
 def test_ring_backward_equals_the_barrier_kernel(lib, C, bg):
-    W, H = 320, 240
+    W, H = 640, 480  # the single-camera ring runs from 1,024 tiles
     uv, conic, op, feat, idx, tr = projected(30000, W, H, 21 + C, C=C)
     lib.msplat_set_blend_ring_bwd(0, 0)
     img0, ref = blend_grads(uv, conic, op, feat, idx, tr, bg, W, H)
@@ -176,7 +176,7 @@ def test_ring_backward_equals_the_barrier_kernel(lib, C, bg):
 
 def test_ring_backward_on_elongated_faint_gaussians(lib):
     import test_gpu_parity as tgp
-    W, H = 320, 240
+    W, H = 640, 480
     uv, conic, op, feat, idx, tr, _ = tgp.elongated_2d(5000, W, H, seed=10)
     t = [torch.as_tensor(x).to(DEV).contiguous() for x in (uv, conic, op.reshape(-1, 1), feat, idx, tr)]
     lib.msplat_set_blend_ring_bwd(0, 0)
@@ -213,7 +213,7 @@ def test_ring_backward_in_the_multi_camera_grid(lib):
 def test_ring_backward_wait_that_runs_out_reports_timeout(lib):
     import ctypes
     from msplat_gb300 import _lib
-    W, H = 128, 96
+    W, H = 640, 480
     uv, conic, op, feat, idx, tr = projected(8000, W, H, 6)
     err = ctypes.c_int(0)
     assert lib.msplat_wait_error(1, ctypes.byref(err), _lib.stream()) == 0  # clear
