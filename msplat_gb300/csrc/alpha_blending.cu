@@ -724,14 +724,14 @@ blend_fwd_small_kernel(int P, const float2 *__restrict__ uv, const float *__rest
 }
 
 // ===================================================================
-// Forward blend as a producer / consumer ring (C <= 4, one pixel per
+// Forward blend as a producer / consumer ring (C <= 4, NPIX pixels per
 // consumer thread).
 //
 // NP producer warps gather, cull and mask each 256-entry batch of a tile's
 // list (the same per-entry work as gather_small), each compacting its share
-// in list order into its own part of one of two shared-memory slots; the 8 consumer warps (one pixel per
-// thread, the warp blocks of blend_fwd_small_kernel) blend a slot while the
-// producers fill the other.  The hand-off is two mbarriers per slot: "full"
+// in list order into its own part of one of two shared-memory slots; the
+// 8 / NPIX consumer warps (NPIX pixels per thread, the warp blocks of
+// blend_fwd_small_kernel) blend a slot while the producers fill the other.  The hand-off is two mbarriers per slot: "full"
 // (the producers' threads arrive once their records are written) and
 // "empty" (each consumer warp arrives once done with the slot), so there is
 // no block-wide barrier between batches and consumer warps with little work
@@ -814,14 +814,14 @@ __device__ __forceinline__ void producer_sync() {
     asm volatile("bar.sync 1, %0;" ::"n"(NP * 32) : "memory");
 }
 
-template <int C, int NP, bool BATCH = false>
-__global__ void MSPLAT_RING_BOUNDS(kTilePixels + 32 * NP)
+template <int C, int NP, bool BATCH = false, int NPIX = 1>
+__global__ void MSPLAT_RING_BOUNDS(kTilePixels / NPIX + 32 * NP)
 blend_fwd_ring_kernel(int P, const float2 *__restrict__ uv, const float *__restrict__ conic,
                       const float *__restrict__ opacity, const float *__restrict__ feature,
                       const int32_t *__restrict__ idx_sorted, const int2 *__restrict__ tile_range, float bg, int W,
                       int H, float *__restrict__ out, float *__restrict__ final_T, int32_t *__restrict__ ncontrib,
                       BlendBatch bb, int wait_limit) {
-    constexpr int NC = kTilePixels / 32;       // consumer warps (one pixel per thread)
+    constexpr int NC = kTilePixels / NPIX / 32;  // consumer warps (NPIX pixels per thread)
     constexpr int SLOT = kTilePixels;          // entries per batch
     constexpr int SUB = SLOT / NP;             // entries per producer warp (its own part of the slot)
     constexpr int PER = SUB / 32;              // gather rounds per producer warp
@@ -888,8 +888,8 @@ blend_fwd_ring_kernel(int P, const float2 *__restrict__ uv, const float *__restr
                     unsigned M;
                     bool keep = false;
                     if (j < range.y)
-                        keep = gather_entry<C, 1, kTile>(j, site.P, idx_sorted, uv, conic, opacity, feature, bx0, by0, A, B,
-                                                         F, G, M);
+                        keep = gather_entry<C, NPIX, kTile>(j, site.P, idx_sorted, uv, conic, opacity, feature, bx0, by0, A,
+                                                            B, F, G, M);
                     const unsigned ballot = __ballot_sync(0xffffffffu, keep);
                     if (keep) {
                         const int pos = n + __popc(ballot & ((1u << lane) - 1u));
@@ -908,14 +908,23 @@ blend_fwd_ring_kernel(int P, const float2 *__restrict__ uv, const float *__restr
     }
 
     // ------------------------------------------------------------ consumers
+    // (the warp blocks of blend_fwd_small_kernel: 8 columns by 4 NPIX rows)
     const int px = site.tx * kTile + 8 * (warp & 1) + (lane & 7);
-    const int py = site.ty * kTile + 4 * (warp >> 1) + (lane >> 3);
+    const int py0 = site.ty * kTile + 4 * NPIX * (warp >> 1) + (lane >> 3) * NPIX;
     const unsigned wbit = 1u << warp;
     const float fx = (float)px;
-    const float fy[1] = {(float)py};
-    float T[1] = {1.0f}, F[1][4] = {{0.f, 0.f, 0.f, 0.f}};
-    int last[1] = {0};
-    bool done[1] = {!(px < W && py < H)};
+    float fy[NPIX], T[NPIX], F[NPIX][4];
+    int last[NPIX];
+    bool done[NPIX];
+#pragma unroll
+    for (int i = 0; i < NPIX; ++i) {
+        fy[i] = (float)(py0 + i);
+        T[i] = 1.0f;
+        last[i] = 0;
+        done[i] = !(px < W && py0 + i < H);
+#pragma unroll
+        for (int q = 0; q < 4; ++q) F[i][q] = 0.0f;
+    }
     bool counted = false;
     for (int k = 0;; ++k) {
         const int s = k & 1;
@@ -923,21 +932,28 @@ blend_fwd_ring_kernel(int P, const float2 *__restrict__ uv, const float *__restr
         if (scount[s][0] < 0) break;
 #pragma unroll
         for (int q = 0; q < NP; ++q)
-            fwd_walk_batch<C, 1>(scount[s][q], sA[s] + q * SUB, sB[s] + q * SUB, sF[s] + q * SUB, sM[s] + q * SUB,
-                                 wbit, fx, fy, done, T, F, last, range.x);
-        if (!counted && __all_sync(0xffffffffu, done[0])) {
+            fwd_walk_batch<C, NPIX>(scount[s][q], sA[s] + q * SUB, sB[s] + q * SUB, sF[s] + q * SUB,
+                                    sM[s] + q * SUB, wbit, fx, fy, done, T, F, last, range.x);
+        bool all_done = true;
+#pragma unroll
+        for (int i = 0; i < NPIX; ++i) all_done &= done[i];
+        if (!counted && __all_sync(0xffffffffu, all_done)) {
             counted = true;
             if (lane == 0) atomicAdd(&ndone, 1);
         }
         __syncwarp();
         if (lane == 0) mbar_arrive(&empty_bar[s]);
     }
-    if (px < W && py < H) {
-        const int pix = py * W + px;
-        final_T[pix] = T[0];
-        ncontrib[pix] = last[0];
 #pragma unroll
-        for (int q = 0; q < C; ++q) out[(size_t)q * H * W + pix] = F[0][q] + T[0] * bg;
+    for (int i = 0; i < NPIX; ++i) {
+        const int py = py0 + i;
+        if (px < W && py < H) {
+            const int pix = py * W + px;
+            final_T[pix] = T[i];
+            ncontrib[pix] = last[i];
+#pragma unroll
+            for (int q = 0; q < C; ++q) out[(size_t)q * H * W + pix] = F[i][q] + T[i] * bg;
+        }
     }
 }
 
@@ -1476,6 +1492,14 @@ static int g_batch_bwd_ring = MSPLAT_BATCH_BLEND_RING_BWD;
 // ring's single producer warp falls behind (256 x 256: 2.12 vs 1.96 ms;
 // from 512 x 512 up the ring is as fast or faster).
 constexpr int kBwdRingMinTiles = 1024;
+// The forward ring takes the tuned pixels per thread (MSPLAT_BLEND_NPIX_FWD)
+// on single-camera images of at least this many tiles and one pixel per
+// thread below: two pixels per thread halve the per-entry overhead but
+// coarsen the warp blocks (8 x 8 pixels instead of 8 x 4), which pays where
+// Gaussians cover many pixels (1920 x 1080: 0.265 -> 0.237 ms) and not on
+// smaller images of the same scene (1280 x 720: 0.199 -> 0.220 ms; 512 x
+// 512: 0.429 -> 0.548 ms).
+constexpr int kFwdRingWideMinTiles = 6000;
 constexpr int kBatchGatherFwd = MSPLAT_BATCH_BLEND_GATHER_FWD, kBatchGatherBwd = MSPLAT_BATCH_BLEND_GATHER_BWD;
 // Blocks per tile of the C <= 4 kernels (1 or 2: whole tiles, or halves of
 // 8 rows with their own gather, cull and end; compile-time tunables).
@@ -1494,13 +1518,18 @@ void launch_small(bool bwd, dim3 grid, cudaStream_t stream, int P, const float2 
                   const float *dout, float *duv, float *dcon, float *dop, float *dfeat) {
     const dim3 gf(grid.x, grid.y * kSplitFwd), gb(grid.x, grid.y * kSplitBwd);
     constexpr int tf = kTilePixels / kBlendNpixFwd / kSplitFwd, tb = kTilePixels / kBlendNpixBwd / kSplitBwd;
-    if (!bwd && g_fwd_ring == 2)
-        launch(blend_fwd_ring_kernel<C, 2>, grid, kTilePixels + 64, 0, stream, P, uv, conic, opacity, feature, idx,
-               tr, bg, W, H, out, final_T, nc, BlendBatch{}, g_wait_limit);
-    else if (!bwd && g_fwd_ring == 4)
-        launch(blend_fwd_ring_kernel<C, 4>, grid, kTilePixels + 128, 0, stream, P, uv, conic, opacity, feature, idx,
-               tr, bg, W, H, out, final_T, nc, BlendBatch{}, g_wait_limit);
-    else if (!bwd)
+    if (!bwd && (g_fwd_ring == 2 || g_fwd_ring == 4)) {
+        // the tuned pixels per thread on images of at least kFwdRingWideMinTiles tiles, one below
+        const bool wide = (int)(grid.x * grid.y) >= kFwdRingWideMinTiles;
+#define MSPLAT_FWD_RING(NP, NPX)                                                                                 \
+    launch(blend_fwd_ring_kernel<C, NP, false, NPX>, grid, kTilePixels / NPX + 32 * NP, 0, stream, P, uv, conic,    \
+           opacity, feature, idx, tr, bg, W, H, out, final_T, nc, BlendBatch{}, g_wait_limit)
+        if (g_fwd_ring == 2 && wide) MSPLAT_FWD_RING(2, kBlendNpixFwd);
+        else if (g_fwd_ring == 2) MSPLAT_FWD_RING(2, 1);
+        else if (wide) MSPLAT_FWD_RING(4, kBlendNpixFwd);
+        else MSPLAT_FWD_RING(4, 1);
+#undef MSPLAT_FWD_RING
+    } else if (!bwd)
         launch(blend_fwd_small_kernel<C, kBlendNpixFwd, kSplitFwd, false, kGatherFwd>, gf, tf, 0, stream,
             P, uv, conic, opacity, feature, idx, tr, bg, W, H, out, final_T, nc, BlendBatch{});
     else if ((g_bwd_ring == 1 || g_bwd_ring == 2) && (int)(grid.x * grid.y) >= kBwdRingMinTiles) {
@@ -1616,10 +1645,10 @@ void launch_small_batch(bool bwd, int tiles, cudaStream_t stream, const BlendBat
                         const int32_t *nci, const float *dout, float *duv, float *dcon, float *dop, float *dfeat) {
     constexpr int tf = kTilePixels / kBatchNpixFwd, tb = kTilePixels / kBatchNpixBwd;
     if (!bwd && g_batch_fwd_ring == 2)
-        launch(blend_fwd_ring_kernel<C, 2, true>, tiles, kTilePixels + 64, 0, stream, 0, uv, conic, opacity, feature,
+        launch(blend_fwd_ring_kernel<C, 2, true, kBatchNpixFwd>, tiles, kTilePixels / kBatchNpixFwd + 64, 0, stream, 0, uv, conic, opacity, feature,
                idx, tr, bg, 1, 1, out, final_T, nc, bb, g_wait_limit);
     else if (!bwd && g_batch_fwd_ring == 4)
-        launch(blend_fwd_ring_kernel<C, 4, true>, tiles, kTilePixels + 128, 0, stream, 0, uv, conic, opacity,
+        launch(blend_fwd_ring_kernel<C, 4, true, kBatchNpixFwd>, tiles, kTilePixels / kBatchNpixFwd + 128, 0, stream, 0, uv, conic, opacity,
                feature, idx, tr, bg, 1, 1, out, final_T, nc, bb, g_wait_limit);
     else if (!bwd)
         launch(blend_fwd_small_kernel<C, kBatchNpixFwd, 1, true, kBatchGatherFwd>, tiles, tf, 0, stream, 0, uv,

@@ -84,6 +84,22 @@ def test_ring_forward_equals_the_barrier_kernel(lib, C):
     lib.msplat_set_blend_ring(*tuned_rings())
 
 
+def test_ring_forward_on_a_large_image(lib):
+    """1600 x 1200 (7,500 tiles): the ring takes the tuned pixels per thread
+    there (one per thread below 6,000 tiles); results stay those of the
+    barrier kernel."""
+    W, H = 1600, 1200
+    args = projected(200000, W, H, 21, C=3)
+    lib.msplat_set_blend_ring(0, 0)
+    ref = blend(lib, *args, 0.0, W, H)
+    for np_ in (2, 4):
+        assert lib.msplat_set_blend_ring(np_, np_) == 0
+        got = blend(lib, *args, 0.0, W, H)
+        for a, b in zip(got, ref):
+            assert torch.equal(a, b), np_
+    lib.msplat_set_blend_ring(*tuned_rings())
+
+
 def test_ring_forward_on_elongated_faint_gaussians(lib):
     import test_gpu_parity as tgp
     W, H = 320, 240
