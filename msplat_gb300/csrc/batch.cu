@@ -11,8 +11,9 @@
 // outputs are bit-identical to a single-camera call.
 //
 // The adjoint reads the per-camera blend gradients [B, P, ...] and sums the
-// Gaussian's gradients over the cameras in registers (xyz, scale,
-// rotation, opacity) and in a shared-memory row (SH coefficients), so each
+// Gaussian's gradients over the cameras in registers (xyz, opacity, and
+// dL/dcov, whose adjoint -- linear in it -- then gives the scale and
+// rotation gradients once) and in a shared-memory row (SH coefficients), so each
 // parameter gradient is written once instead of B times; camera gradients
 // are reduced per warp and camera (a reduce-scatter of shuffles) into
 // per-warp shared slots, which are summed in a fixed order into partial
@@ -179,8 +180,9 @@ batch_preprocess_bwd_kernel(int P, int B, int C, const float *__restrict__ xyz, 
         qt = quats[p];
         cov3d_fwd_one(s[0], s[1], s[2], qt, cov);
     }
-    float gxyz[3] = {0.f, 0.f, 0.f}, gs[3] = {0.f, 0.f, 0.f}, gop = 0.f;
-    float4 gq = make_float4(0.f, 0.f, 0.f, 0.f);
+    // dL/dcov summed over the cameras: the covariance adjoint is linear in
+    // it, so it runs once per Gaussian after the loop instead of per camera
+    float gxyz[3] = {0.f, 0.f, 0.f}, gV[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f}, gop = 0.f;
     // The inputs of camera b + 1 are loaded while camera b is computed (the
     // loop is latency bound at this occupancy otherwise).
     BatchBwdIn cur = load_batch_bwd_in(active, (size_t)p, C, depth, radius, dL_duv, dL_dconic, dL_dcolor, dL_dop_cam);
@@ -197,20 +199,13 @@ batch_preprocess_bwd_kernel(int P, int B, int C, const float *__restrict__ xyz, 
             float g[3] = {0.f, 0.f, 0.f};
             project_bwd_one(c, px, py, pz, in.duv, 0.0f, g, cam_grads, acc);
             if (in.radius > 0) {
-                float ge[3], dV[6], ds[3];
-                float4 dq;
+                float ge[3], dV[6];
                 if (ewa_bwd_one(c, px, py, pz, cov, in.dconic[0], in.dconic[1], in.dconic[2], ge, dV, cam_grads,
                                 acc)) {
-                    cov3d_bwd_one(s, qt, dV, ds, dq);
 #pragma unroll
-                    for (int k = 0; k < 3; ++k) {
-                        g[k] += ge[k];
-                        gs[k] += ds[k];
-                    }
-                    gq.x += dq.x;
-                    gq.y += dq.y;
-                    gq.z += dq.z;
-                    gq.w += dq.w;
+                    for (int k = 0; k < 6; ++k) gV[k] += dV[k];
+#pragma unroll
+                    for (int k = 0; k < 3; ++k) g[k] += ge[k];
                 }
             }
             if (C > 0) {
@@ -280,6 +275,9 @@ batch_preprocess_bwd_kernel(int P, int B, int C, const float *__restrict__ xyz, 
         }
     }
     if (active) {
+        float gs[3];
+        float4 gq;
+        cov3d_bwd_one(s, qt, gV, gs, gq);
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
             dL_dxyz[3 * p + k] = gxyz[k];
