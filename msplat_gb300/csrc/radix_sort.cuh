@@ -107,7 +107,7 @@ __device__ __forceinline__ unsigned digit_peers(uint32_t d, unsigned valid, int 
 template <typename K, bool FLIP, bool SEG = false>
 __global__ void __launch_bounds__(kSortThreads)
 radix_upsweep_kernel(const K *__restrict__ keys, int64_t n, int shift, int ntiles,
-                     uint32_t *__restrict__ hist, const int64_t *__restrict__ n_dev, SortSegs segs = {}) {
+                     uint32_t *__restrict__ hist, const int64_t *__restrict__ n_dev, int nd, SortSegs segs = {}) {
     __shared__ uint32_t cnt[kSortWarps][kRadix];
     if (SEG) {
         // items of this tile within its segment, as a length relative to
@@ -136,7 +136,7 @@ radix_upsweep_kernel(const K *__restrict__ keys, int64_t n, int shift, int ntile
     uint32_t c = 0;
 #pragma unroll
     for (int w = 0; w < kSortWarps; ++w) c += cnt[w][threadIdx.x];
-    hist[(size_t)threadIdx.x * ntiles + blockIdx.x] = c;
+    if ((int)threadIdx.x < nd) hist[(size_t)threadIdx.x * ntiles + blockIdx.x] = c;  // (digits >= nd: none)
 }
 
 // --------------------------------------------------------------- row scan
@@ -173,10 +173,11 @@ radix_rowscan_kernel(uint32_t *__restrict__ hist, uint32_t *__restrict__ totals,
 // the digit's row scanned in place (exclusive) and its total to
 // totals[s][d].  Any number of segments at the cost of their tiles.
 static __global__ void __launch_bounds__(256)
-radix_rowscan_warp_kernel(uint32_t *__restrict__ hist, uint32_t *__restrict__ totals, int ntiles, SortSegs segs) {
+radix_rowscan_warp_kernel(uint32_t *__restrict__ hist, uint32_t *__restrict__ totals, int ntiles, int nd,
+                          SortSegs segs) {
     const int gw = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
-    if (gw >= kRadix * segs.nseg) return;  // whole warps
-    const int s = gw / kRadix, d = gw - s * kRadix;
+    if (gw >= nd * segs.nseg) return;  // whole warps
+    const int s = gw / nd, d = gw - s * nd;
     const int t0 = segs.tile_start[s], t1 = segs.tile_start[s + 1];
     uint32_t *row = hist + (size_t)d * ntiles;
     uint32_t carry = 0;
@@ -199,7 +200,10 @@ inline size_t radix_downsweep_smem(size_t key_bytes) {
 // the key's sign bit on load / store (signed-integer order).
 // 32-bit keys: capped at 64 registers for 4 blocks per SM (no spill); the
 // 64-bit keys of the reference-layout sort would spill there and keep 3.
-template <typename K, bool FLIP_IN, bool FLIP_OUT, bool SEG = false>
+// DB: the digit bits any key of the pass can have (the last pass of a sort
+// whose keys are known to stay below 2^(shift + DB)); the ranking takes one
+// ballot per such bit.
+template <typename K, bool FLIP_IN, bool FLIP_OUT, bool SEG = false, int DB = kRadixBits>
 __global__ void __launch_bounds__(kSortThreads, sizeof(K) == 4 ? 4 : 3)
 radix_downsweep_kernel(const K *__restrict__ kin, const uint32_t *__restrict__ vin,
                        K *__restrict__ kout, uint32_t *__restrict__ vout, int64_t n, int shift,
@@ -229,9 +233,11 @@ radix_downsweep_kernel(const K *__restrict__ kin, const uint32_t *__restrict__ v
     for (int i = tid; i < kSortWarps * kRadix; i += kSortThreads) whist[i] = 0;
     // start of this tile's bucket of digit tid: the digit's start (scan of
     // the totals of the smaller digits) + the tile's offset within the digit
-    const uint32_t dtot = totals[tid];
+    // (digits from 2^DB on occur in no key of the pass: no count, no row)
+    const bool used = tid < (1 << DB);
+    const uint32_t dtot = used ? totals[tid] : 0u;
     const uint32_t dbase = block_exclusive_scan<uint32_t>(dtot, scan_scratch, nullptr);
-    gstart[tid] = dbase + hist[(size_t)tid * ntiles + blockIdx.x];
+    gstart[tid] = dbase + (used ? hist[(size_t)tid * ntiles + blockIdx.x] : 0u);
     // A digit that every key of the sort (segment) shares makes the pass the
     // identity (stable): the tile is copied straight through.
     const int64_t n_all = SEG ? segs.count[sg] : n;
@@ -272,7 +278,7 @@ radix_downsweep_kernel(const K *__restrict__ kin, const uint32_t *__restrict__ v
         const K k = key[r];
         const unsigned vmask = __ballot_sync(0xffffffffu, valid);
         const uint32_t d = digit_of(k, shift);
-        const unsigned peers = digit_peers(d, vmask);
+        const unsigned peers = digit_peers(d, vmask, DB);
         uint32_t b0 = 0;
         if (valid) b0 = my_hist[d];
         __syncwarp();
@@ -716,7 +722,7 @@ int radix_onesweep_passes(int ntiles, int64_t n, const int64_t *n_dev, const Sor
 template <typename K, bool FLIP>
 int radix_sort_pairs(int64_t n, int begin_bit, int passes, const K *kin, const uint32_t *vin,
                      K *kout, uint32_t *vout, K *ktmp, uint32_t *vtmp, const RadixBuffers &b,
-                     cudaStream_t stream, const int64_t *n_dev = nullptr) {
+                     cudaStream_t stream, const int64_t *n_dev = nullptr, int last_bits = kRadixBits) {
     if (n <= 0 || passes <= 0) return MSPLAT_OK;
     const int nt = sort_tiles(n);
     if (sort_onesweep_enabled())
@@ -732,24 +738,32 @@ int radix_sort_pairs(int64_t n, int begin_bit, int passes, const K *kin, const u
         uint32_t *vdst = to_out ? vout : vtmp;
         uint32_t *tot = b.totals + p * kRadix;
         const bool first = p == 0, last = p == passes - 1;
+        // digits the pass can meet; the ranking is specialised for 5-7 bits (fewer round up to 5)
+        int dbits = last ? last_bits : kRadixBits;
+        if (FLIP || dbits < 1 || dbits > kRadixBits) dbits = kRadixBits;
+        else if (dbits < 5) dbits = 5;
+        const int nd = 1 << dbits;
         if (FLIP && first)
-            launch(radix_upsweep_kernel<K, true>, nt, kSortThreads, 0, stream, ksrc, n, shift, nt, b.hist, n_dev,
+            launch(radix_upsweep_kernel<K, true>, nt, kSortThreads, 0, stream, ksrc, n, shift, nt, b.hist, n_dev, nd,
                    SortSegs{});
         else
-            launch(radix_upsweep_kernel<K, false>, nt, kSortThreads, 0, stream, ksrc, n, shift, nt, b.hist, n_dev,
+            launch(radix_upsweep_kernel<K, false>, nt, kSortThreads, 0, stream, ksrc, n, shift, nt, b.hist, n_dev, nd,
                    SortSegs{});
-        launch(radix_rowscan_kernel, kRadix, 1024, 0, stream, b.hist, tot, nt, SortSegs{});
-#define MSPLAT_DOWNSWEEP(FI, FO)                                                                                \
+        launch(radix_rowscan_kernel, nd, 1024, 0, stream, b.hist, tot, nt, SortSegs{});
+#define MSPLAT_DOWNSWEEP(FI, FO, DBV)                                                                           \
     do {                                                                                                        \
-        auto kern = radix_downsweep_kernel<K, FI, FO>;                                                          \
+        auto kern = radix_downsweep_kernel<K, FI, FO, false, DBV>;                                              \
         cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);                     \
         launch(kern, nt, kSortThreads, smem, stream, ksrc, vsrc, kdst, vdst, n, shift, nt, b.hist, tot, n_dev,    \
-               SortSegs{});                                                                             \
+               SortSegs{});                                                                                     \
     } while (0)
-        if (FLIP && first && last) MSPLAT_DOWNSWEEP(true, true);
-        else if (FLIP && first) MSPLAT_DOWNSWEEP(true, false);
-        else if (FLIP && last) MSPLAT_DOWNSWEEP(false, true);
-        else MSPLAT_DOWNSWEEP(false, false);
+        if (FLIP && first && last) MSPLAT_DOWNSWEEP(true, true, kRadixBits);
+        else if (FLIP && first) MSPLAT_DOWNSWEEP(true, false, kRadixBits);
+        else if (FLIP && last) MSPLAT_DOWNSWEEP(false, true, kRadixBits);
+        else if (dbits == 5) MSPLAT_DOWNSWEEP(false, false, 5);
+        else if (dbits == 6) MSPLAT_DOWNSWEEP(false, false, 6);
+        else if (dbits == 7) MSPLAT_DOWNSWEEP(false, false, 7);
+        else MSPLAT_DOWNSWEEP(false, false, kRadixBits);
 #undef MSPLAT_DOWNSWEEP
         ksrc = kdst;
         vsrc = vdst;
@@ -766,7 +780,7 @@ int radix_sort_pairs(int64_t n, int begin_bit, int passes, const K *kin, const u
 template <typename K>
 int radix_sort_segmented(int ntiles, const SortSegs &segs, int begin_bit, int passes, const K *kin,
                          const uint32_t *vin, K *kout, uint32_t *vout, K *ktmp, uint32_t *vtmp,
-                         const RadixBuffers &b, cudaStream_t stream) {
+                         const RadixBuffers &b, cudaStream_t stream, int last_bits = kRadixBits) {
     if (ntiles <= 0 || passes <= 0 || segs.nseg <= 0) return MSPLAT_OK;
     if (sort_onesweep_enabled())
         return radix_onesweep_passes<K, false>(ntiles, 0, nullptr, segs, begin_bit, passes, kin, vin, kout, vout,
@@ -776,16 +790,18 @@ int radix_sort_segmented(int ntiles, const SortSegs &segs, int begin_bit, int pa
     const uint32_t *vsrc = vin;
     auto down = radix_downsweep_kernel<K, false, false, true>;
     cudaFuncSetAttribute(down, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    (void)last_bits;  // (the segmented passes rank all 8 bits)
     for (int p = 0; p < passes; ++p) {
         const int shift = begin_bit + p * kRadixBits;
         const bool to_out = ((passes - 1 - p) & 1) == 0;
         K *kdst = to_out ? kout : ktmp;
         uint32_t *vdst = to_out ? vout : vtmp;
         uint32_t *tot = b.totals + (size_t)p * segs.nseg * kRadix;
+        const int nd = kRadix;
         launch(radix_upsweep_kernel<K, false, true>, ntiles, kSortThreads, 0, stream, ksrc, (int64_t)0, shift,
-               ntiles, b.hist, (const int64_t *)nullptr, segs);
-        launch(radix_rowscan_warp_kernel, (unsigned)ceil_div64((int64_t)kRadix * segs.nseg, 8), 256, 0, stream,
-               b.hist, tot, ntiles, segs);
+               ntiles, b.hist, (const int64_t *)nullptr, nd, segs);
+        launch(radix_rowscan_warp_kernel, (unsigned)ceil_div64((int64_t)nd * segs.nseg, 8), 256, 0, stream,
+               b.hist, tot, ntiles, nd, segs);
         launch(down, ntiles, kSortThreads, smem, stream, ksrc, vsrc, kdst, vdst, (int64_t)0, shift, ntiles, b.hist,
                (const uint32_t *)tot, (const int64_t *)nullptr, segs);
         ksrc = kdst;

@@ -614,8 +614,10 @@ static int finish_impl(int P, const float *uv, const float *depth, const int32_t
            radius, (const short4 *)prep.rects, (const int *)prep.culled, (const RowReach *)prep.reach, gx, gy, f.ka,
            vemit, I, I, I_dev);
     uint32_t *kout = even ? f.ka : f.kb;
+    // the last pass meets only the digits of keys up to ntiles (5 bits of 8 at 1920 x 1080)
+    const int last_bits = max(1, bits_for((uint32_t)nt)) - kRadixBits * (passes - 1);
     int st = radix_sort_pairs<uint32_t, false>(I, 0, passes, f.ka, vemit, kout, out, even ? f.kb : f.ka, f.vt,
-                                               f.rb, stream, I_dev);
+                                               f.rb, stream, I_dev, last_bits);
     if (st) return st;
     launch(range_from_tilekey_kernel, (unsigned)ceil_div64(ceil_div64(I, kRangeKeys), 256), 256, 0, stream, I, kout,
            nt, (int2 *)tile_range, I_dev);
