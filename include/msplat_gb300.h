@@ -334,6 +334,37 @@ MSPLAT_API int msplat_alpha_blending_backward(int P, int C, const float *uv,
                                    float *dL_dconic, float *dL_dopacity,
                                    float *dL_dfeature, msplat_stream_t stream);
 
+/* The same two calls keeping each list entry's warp-block mask from the
+ * forward for the backward.  No counterpart in the reference (its backward
+ * re-gathers and re-tests every entry, msplat/src/alpha_blending.cu:166-182).
+ * entry_masks: one byte per entry of idx_sorted; the forward writes it for
+ * every entry it gathers (every entry up to each tile's last contributor),
+ * and the backward -- called with the same lists and C -- reads it instead
+ * of repeating the tile and warp-block culls.  Results are those of the
+ * plain calls.  For C > 4 (and builds that split tiles between blocks) the
+ * masks are neither written nor read. */
+MSPLAT_API int msplat_alpha_blending_forward_masks(int P, int C, const float *uv,
+                                        const float *conic, const float *opacity,
+                                        const float *feature,
+                                        const int32_t *idx_sorted,
+                                        const int32_t *tile_range, float bg,
+                                        int W, int H, float *out,
+                                        float *final_T, int32_t *ncontrib,
+                                        unsigned char *entry_masks,
+                                        msplat_stream_t stream);
+MSPLAT_API int msplat_alpha_blending_backward_masks(int P, int C, const float *uv,
+                                         const float *conic, const float *opacity,
+                                         const float *feature,
+                                         const int32_t *idx_sorted,
+                                         const int32_t *tile_range, float bg,
+                                         int W, int H, const float *final_T,
+                                         const int32_t *ncontrib,
+                                         const float *dL_dout, float *dL_duv,
+                                         float *dL_dconic, float *dL_dopacity,
+                                         float *dL_dfeature,
+                                         const unsigned char *entry_masks,
+                                         msplat_stream_t stream);
+
 /* ------------------------------------------------------------------------ */
 /* Fused preprocess of a rasterisation.  No single counterpart in the
  * reference: it is the composite project_point -> compute_cov3d ->

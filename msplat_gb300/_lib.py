@@ -56,6 +56,10 @@ _SIGNATURES = {
         _I, [_I, _I, _P, _P, _P, _P, _P, _P, _F, _I, _I, _P, _P, _P, _P]),
     "msplat_alpha_blending_backward": (
         _I, [_I, _I, _P, _P, _P, _P, _P, _P, _F, _I, _I, _P, _P, _P, _P, _P, _P, _P, _P]),
+    "msplat_alpha_blending_forward_masks": (
+        _I, [_I, _I, _P, _P, _P, _P, _P, _P, _F, _I, _I, _P, _P, _P, _P, _P]),
+    "msplat_alpha_blending_backward_masks": (
+        _I, [_I, _I, _P, _P, _P, _P, _P, _P, _F, _I, _I, _P, _P, _P, _P, _P, _P, _P, _P, _P]),
     "msplat_rasterize_preprocess_forward": (
         _I, [_I, _P, _P, _P, _P, _P, _I, _I, _F, _F, _I, _I, _P, _P, _P, _P, _P, _P, _P, _P]),
     "msplat_rasterize_preprocess_workspace_size": (_SZ, [_I, _I, _I]),

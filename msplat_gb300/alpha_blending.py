@@ -74,15 +74,22 @@ class _AlphaBlending(torch.autograd.Function):
         out = torch.empty((C, H, W), dtype=torch.float32, device=dev)
         final_T = torch.empty((H, W), dtype=torch.float32, device=dev)
         ncontrib = torch.empty((H, W), dtype=torch.int32, device=dev)
+        # With a backward to come (C <= 4) the forward keeps every list
+        # entry's warp-block mask for it (one byte per entry), so the
+        # backward repeats no cull arithmetic.
+        masks = None
+        if C <= 4 and any(ctx.needs_input_grad[:4]):
+            masks = torch.empty((max(ids.numel(), 1),), dtype=torch.uint8, device=dev)
         if C > 0:
             lib = _lib.load()
             with _lib.stage("alpha_blending_forward"):
-                _lib.check(lib.msplat_alpha_blending_forward(
+                _lib.check(lib.msplat_alpha_blending_forward_masks(
                     P, C, _lib.ptr(u), _lib.ptr(c), _lib.ptr(o), _lib.ptr(f), _lib.ptr(ids),
                     _lib.ptr(tr), float(bg), W, H, _lib.ptr(out), _lib.ptr(final_T),
-                    _lib.ptr(ncontrib), _lib.stream(dev)), "alpha_blending_forward")
+                    _lib.ptr(ncontrib), _lib.ptr(masks), _lib.stream(dev)), "alpha_blending_forward")
         ctx.W, ctx.H, ctx.bg = W, H, float(bg)
         ctx.has_ndc = ndc is not None
+        ctx.masks = masks
         ctx.save_for_backward(u, c, o, f, ids, tr, final_T, ncontrib)
         ctx.opacity_shape = opacity.shape
         return out
@@ -98,11 +105,11 @@ class _AlphaBlending(torch.autograd.Function):
         if C > 0 and P > 0:
             lib = _lib.load()
             with _lib.stage("alpha_blending_backward"):
-                _lib.check(lib.msplat_alpha_blending_backward(
+                _lib.check(lib.msplat_alpha_blending_backward_masks(
                     P, C, _lib.ptr(u), _lib.ptr(c), _lib.ptr(o), _lib.ptr(f), _lib.ptr(ids),
                     _lib.ptr(tr), ctx.bg, ctx.W, ctx.H, _lib.ptr(final_T), _lib.ptr(ncontrib),
                     _lib.ptr(g), _lib.ptr(dL_duv), _lib.ptr(dL_dconic), _lib.ptr(dL_dopacity),
-                    _lib.ptr(dL_dfeature), _lib.stream(dev)), "alpha_blending_backward")
+                    _lib.ptr(dL_dfeature), _lib.ptr(ctx.masks), _lib.stream(dev)), "alpha_blending_backward")
         dL_dndc = None
         if ctx.has_ndc:
             scale = torch.tensor([0.5 * ctx.W, 0.5 * ctx.H], dtype=u.dtype, device=dev)

@@ -488,30 +488,74 @@ __device__ __forceinline__ PixPow<NPIX> blend_power_n(float a, float b, float c,
     return out;
 }
 
+// The warp-block masks of a tile list's entries, as the forward computed
+// them, kept for the backward: emask[j] for list position j holds the
+// blocks of 8 columns by 4 NPB rows (the backward's warp blocks) entry j
+// can reach (0: the tile cull dropped it).  The forward writes them (out)
+// for every position it gathers -- every position up to the tile's last
+// contributor -- and the backward reads them (in) instead of repeating the
+// cull and mask arithmetic.  Either pointer may be null.
+struct EntryMasks {
+    const unsigned char *__restrict__ in = nullptr;
+    unsigned char *__restrict__ out = nullptr;
+};
+
+// A mask of warp blocks of RF rows as one of blocks of RT rows (RT a
+// multiple of RF): block g of RT rows covers blocks g K .. g K + K - 1.
+template <int RF, int RT, int ROWS>
+__device__ __forceinline__ unsigned merge_block_rows(unsigned m) {
+    constexpr int K = RT / RF, NB = ROWS / RT;
+    if (K == 1) return m;
+    unsigned out = 0u;
+#pragma unroll
+    for (int g = 0; g < NB; ++g)
+#pragma unroll
+        for (int k = 0; k < K; ++k) out |= ((m >> (2 * (g * K + k))) & 3u) << (2 * g);
+    return out;
+}
+
 // One entry of a tile's list: its record (uv, conic, opacity, list index),
 // features and warp-block mask, and whether the tile cull (the box of ROWS
 // rows from by0) keeps it.  (No power bound: the branch-free walks evaluate
-// every pair's alpha, which the bound only let them skip.)
-template <int C, int NPIX, int ROWS>
+// every pair's alpha, which the bound only let them skip.)  With em.in the
+// mask comes from there (kept: mask != 0) and no cull is evaluated; with
+// em.out the entry's mask in the geometry of NPB pixels per thread is
+// stored there.
+template <int C, int NPIX, int ROWS, int NPB = NPIX>
 __device__ __forceinline__ bool gather_entry(int j, int P, const int32_t *__restrict__ idx_sorted,
                                              const float2 *__restrict__ uv, const float *__restrict__ conic,
                                              const float *__restrict__ opacity, const float *__restrict__ feature,
                                              float bx0, float by0, float4 &A, float4 &B, float4 &F, int &G,
-                                             unsigned &M) {
+                                             unsigned &M, EntryMasks em = {}) {
     const int g = idx_sorted[j];
-    if ((unsigned)g >= (unsigned)P) {  // an id outside the rows is never read
+    unsigned mi = 1u;
+    if (em.in) mi = em.in[j];
+    if ((unsigned)g >= (unsigned)P || mi == 0u) {  // an id outside the rows is never read
         A = B = F = make_float4(0.f, 0.f, 0.f, 0.f);
         G = 0;
         M = 0u;
+        if (em.out) em.out[j] = 0;
         return false;
     }
     const float2 p = uv[g];
     const float ca = conic[3 * g], cb = conic[3 * g + 1], cc = conic[3 * g + 2];
     const float op = opacity[g];
-    float L;
-    const bool keep = !cull_box(p.x, p.y, ca, cb, cc, op, bx0, by0, bx0 + (float)(kTile - 1),
-                                by0 + (float)(ROWS - 1), L);
-    M = keep ? warp_block_mask<4 * NPIX, ROWS>(p.x, p.y, ca, cb, cc, L, bx0, by0) : 0u;
+    bool keep;
+    if (em.in) {
+        keep = true;
+        M = mi;
+    } else {
+        float L;
+        keep = !cull_box(p.x, p.y, ca, cb, cc, op, bx0, by0, bx0 + (float)(kTile - 1), by0 + (float)(ROWS - 1),
+                         L);
+        M = keep ? warp_block_mask<4 * NPIX, ROWS>(p.x, p.y, ca, cb, cc, L, bx0, by0) : 0u;
+        if (em.out) {
+            unsigned mo;
+            if (NPB % NPIX == 0) mo = merge_block_rows<4 * NPIX, 4 * NPB, ROWS>(M);
+            else mo = keep ? warp_block_mask<4 * NPB, ROWS>(p.x, p.y, ca, cb, cc, L, bx0, by0) : 0u;
+            em.out[j] = (unsigned char)mo;
+        }
+    }
     A = make_float4(p.x, p.y, ca, cb);
     B = make_float4(cc, op, 0.0f, __int_as_float(j));  // (z unused: the walks evaluate every alpha)
     float f[4] = {0.f, 0.f, 0.f, 0.f};
@@ -533,14 +577,14 @@ __device__ __forceinline__ bool gather_entry(int j, int P, const int32_t *__rest
 // are written after it, and every warp reaches it only once done with the
 // previous batch, so a warp that finishes a batch early issues the next
 // batch's loads and cull tests while the others still blend.
-template <int C, int NPIX, bool WITH_ID, int ROWS = kTile, int GE = NPIX>
+template <int C, int NPIX, bool WITH_ID, int ROWS = kTile, int GE = NPIX, int NPB = NPIX>
 __device__ __forceinline__ int gather_small(int base, int dir, int lo, int hi, int P,
                                             const int32_t *__restrict__ idx_sorted,
                                             const float2 *__restrict__ uv, const float *__restrict__ conic,
                                             const float *__restrict__ opacity,
                                             const float *__restrict__ feature, float bx0, float by0,
                                             float4 *sA, float4 *sB, float4 *sF, int *sG, unsigned char *sM,
-                                            int *scan, bool vote) {
+                                            int *scan, bool vote, EntryMasks em = {}) {
     constexpr int NT = kTile * ROWS / NPIX;
     float4 A[GE], B[GE], F[GE];
     int G[GE];
@@ -552,8 +596,8 @@ __device__ __forceinline__ int gather_small(int base, int dir, int lo, int hi, i
         const int j = base + dir * ((int)threadIdx.x * GE + r);
         keep[r] = false;
         if (j >= lo && j < hi)
-            keep[r] = gather_entry<C, NPIX, ROWS>(j, P, idx_sorted, uv, conic, opacity, feature, bx0, by0, A[r], B[r],
-                                                  F[r], G[r], M[r]);
+            keep[r] = gather_entry<C, NPIX, ROWS, NPB>(j, P, idx_sorted, uv, conic, opacity, feature, bx0, by0, A[r],
+                                                       B[r], F[r], G[r], M[r], em);
         nk += keep[r];
     }
     // Block exclusive scan of the per-thread counts (NT <= 256 threads).
@@ -650,13 +694,13 @@ __device__ __forceinline__ void fwd_walk_batch(int n, const float4 *sA, const fl
 // SPLIT: a tile is rendered by SPLIT blocks of kTile / SPLIT rows each
 // (grid.y = tiles down x SPLIT), each gathering the tile's list against
 // its own part.
-template <int C, int NPIX, int SPLIT, bool BATCH = false, int GE = NPIX>
+template <int C, int NPIX, int SPLIT, bool BATCH = false, int GE = NPIX, int NPB = NPIX>
 __global__ void MSPLAT_FWD_BOUNDS(kTilePixels / NPIX / SPLIT)
 blend_fwd_small_kernel(int P, const float2 *__restrict__ uv, const float *__restrict__ conic,
                        const float *__restrict__ opacity, const float *__restrict__ feature,
                        const int32_t *__restrict__ idx_sorted, const int2 *__restrict__ tile_range, float bg,
                        int W, int H, float *__restrict__ out, float *__restrict__ final_T,
-                       int32_t *__restrict__ ncontrib, BlendBatch bb = {}) {
+                       int32_t *__restrict__ ncontrib, unsigned char *__restrict__ emask, BlendBatch bb) {
     static_assert(!BATCH || SPLIT == 1, "batched blends render whole tiles");
     // GE entries gathered per thread: BATCH_N Gaussians per shared-memory batch
     constexpr int ROWS = kTile / SPLIT, NT = kTile * ROWS / NPIX, BATCH_N = NT * GE;
@@ -704,9 +748,9 @@ blend_fwd_small_kernel(int P, const float2 *__restrict__ uv, const float *__rest
         bool all_done = true;
 #pragma unroll
         for (int i = 0; i < NPIX; ++i) all_done &= done[i];
-        const int n = gather_small<C, NPIX, false, ROWS, GE>(start, 1, range.x, range.y, site.P, idx_sorted, uv, conic,
-                                                         opacity, feature, bx0, by0, sA, sB, sF, nullptr, sM, scan,
-                                                         all_done);
+        const int n = gather_small<C, NPIX, false, ROWS, GE, NPB>(start, 1, range.x, range.y, site.P, idx_sorted, uv,
+                                                              conic, opacity, feature, bx0, by0, sA, sB, sF, nullptr,
+                                                              sM, scan, all_done, EntryMasks{nullptr, emask});
         if (n < 0) break;  // every pixel of the block is done
         fwd_walk_batch<C, NPIX>(n, sA, sB, sF, sM, wbit, fx, fy, done, T, F, last, range.x);
     }
@@ -814,13 +858,13 @@ __device__ __forceinline__ void producer_sync() {
     asm volatile("bar.sync 1, %0;" ::"n"(NP * 32) : "memory");
 }
 
-template <int C, int NP, bool BATCH = false, int NPIX = 1>
+template <int C, int NP, bool BATCH = false, int NPIX = 1, int NPB = NPIX>
 __global__ void MSPLAT_RING_BOUNDS(kTilePixels / NPIX + 32 * NP)
 blend_fwd_ring_kernel(int P, const float2 *__restrict__ uv, const float *__restrict__ conic,
                       const float *__restrict__ opacity, const float *__restrict__ feature,
                       const int32_t *__restrict__ idx_sorted, const int2 *__restrict__ tile_range, float bg, int W,
                       int H, float *__restrict__ out, float *__restrict__ final_T, int32_t *__restrict__ ncontrib,
-                      BlendBatch bb, int wait_limit) {
+                      unsigned char *__restrict__ emask, BlendBatch bb, int wait_limit) {
     constexpr int NC = kTilePixels / NPIX / 32;  // consumer warps (NPIX pixels per thread)
     constexpr int SLOT = kTilePixels;          // entries per batch
     constexpr int SUB = SLOT / NP;             // entries per producer warp (its own part of the slot)
@@ -888,8 +932,8 @@ blend_fwd_ring_kernel(int P, const float2 *__restrict__ uv, const float *__restr
                     unsigned M;
                     bool keep = false;
                     if (j < range.y)
-                        keep = gather_entry<C, NPIX, kTile>(j, site.P, idx_sorted, uv, conic, opacity, feature, bx0, by0, A,
-                                                            B, F, G, M);
+                        keep = gather_entry<C, NPIX, kTile, NPB>(j, site.P, idx_sorted, uv, conic, opacity, feature, bx0,
+                                                                 by0, A, B, F, G, M, EntryMasks{nullptr, emask});
                     const unsigned ballot = __ballot_sync(0xffffffffu, keep);
                     if (keep) {
                         const int pos = n + __popc(ballot & ((1u << lane) - 1u));
@@ -1136,7 +1180,7 @@ blend_bwd_small_kernel(int P, const float2 *__restrict__ uv, const float *__rest
                        int W, int H, const float *__restrict__ final_T, const int32_t *__restrict__ ncontrib,
                        const float *__restrict__ dL_dout, float *__restrict__ dL_duv,
                        float *__restrict__ dL_dconic, float *__restrict__ dL_dopacity,
-                       float *__restrict__ dL_dfeature, BlendBatch bb = {}) {
+                       float *__restrict__ dL_dfeature, const unsigned char *__restrict__ emask, BlendBatch bb) {
     static_assert(!BATCH || SPLIT == 1, "batched blends render whole tiles");
     constexpr int ROWS = kTile / SPLIT, NT = kTile * ROWS / NPIX, BATCH_N = NT * GE;
     static_assert(4 * NPIX <= ROWS, "a warp block of 4 NPIX rows must fit the block's rows");
@@ -1217,7 +1261,7 @@ blend_bwd_small_kernel(int P, const float2 *__restrict__ uv, const float *__rest
         const int bstart = max(range.x, bend - BATCH_N);
         const int n = gather_small<C, NPIX, true, ROWS, GE>(bend - 1, -1, bstart, bend, site.P, idx_sorted, uv, conic,
                                                         opacity, feature, bx0, by0, sA, sB, sF, sG, sM, scan,
-                                                        false);
+                                                        false, EntryMasks{emask, nullptr});
         bwd_walk_batch<C, NPIX, BG>(n, sA, sB, sF, sG, sM, wbit, warp_last, range.x, fx, fy, T, Tf, la, bgd, ad,
                                     lfd, dp, last, vi, dL_duv, dL_dconic, dL_dopacity, dL_dfeature);
         // no barrier here: the next gather's first barrier orders the batches
@@ -1247,8 +1291,8 @@ blend_bwd_ring_kernel(int P, const float2 *__restrict__ uv, const float *__restr
                       const int32_t *__restrict__ idx_sorted, const int2 *__restrict__ tile_range, float bg, int W,
                       int H, const float *__restrict__ final_T, const int32_t *__restrict__ ncontrib,
                       const float *__restrict__ dL_dout, float *__restrict__ dL_duv, float *__restrict__ dL_dconic,
-                      float *__restrict__ dL_dopacity, float *__restrict__ dL_dfeature, BlendBatch bb,
-                      int wait_limit) {
+                      float *__restrict__ dL_dopacity, float *__restrict__ dL_dfeature,
+                      const unsigned char *__restrict__ emask, BlendBatch bb, int wait_limit) {
     constexpr int NT = kTilePixels / NPIX;  // consumer threads
     constexpr int NCW = NT / 32;            // consumer warps
     constexpr int SLOT = 256;               // entries per batch
@@ -1350,7 +1394,7 @@ blend_bwd_ring_kernel(int P, const float2 *__restrict__ uv, const float *__restr
                 bool keep = false;
                 if (j >= bstart)
                     keep = gather_entry<C, NPIX, kTile>(j, site.P, idx_sorted, uv, conic, opacity, feature, bx0, by0,
-                                                        A, B, F, G, M);
+                                                        A, B, F, G, M, EntryMasks{emask, nullptr});
                 const unsigned ballot = __ballot_sync(0xffffffffu, keep);
                 if (keep) {
                     const int pos = n + __popc(ballot & ((1u << lane) - 1u));
@@ -1510,33 +1554,36 @@ constexpr int kBatchGatherFwd = MSPLAT_BATCH_BLEND_GATHER_FWD, kBatchGatherBwd =
 #define MSPLAT_BLEND_SPLIT_BWD 1
 #endif
 constexpr int kSplitFwd = MSPLAT_BLEND_SPLIT_FWD, kSplitBwd = MSPLAT_BLEND_SPLIT_BWD;
+// The forward's entry masks carry over to the backward when both render whole tiles.
+constexpr bool kEntryMasks = kSplitFwd == 1 && kSplitBwd == 1;
 
 template <int C>
 void launch_small(bool bwd, dim3 grid, cudaStream_t stream, int P, const float2 *uv, const float *conic,
                   const float *opacity, const float *feature, const int32_t *idx, const int2 *tr, float bg, int W,
                   int H, float *out, float *final_T, int32_t *nc, const float *fT, const int32_t *nci,
-                  const float *dout, float *duv, float *dcon, float *dop, float *dfeat) {
+                  const float *dout, float *duv, float *dcon, float *dop, float *dfeat, unsigned char *emask) {
     const dim3 gf(grid.x, grid.y * kSplitFwd), gb(grid.x, grid.y * kSplitBwd);
+    if (!kEntryMasks) emask = nullptr;
     constexpr int tf = kTilePixels / kBlendNpixFwd / kSplitFwd, tb = kTilePixels / kBlendNpixBwd / kSplitBwd;
     if (!bwd && (g_fwd_ring == 2 || g_fwd_ring == 4)) {
         // the tuned pixels per thread on images of at least kFwdRingWideMinTiles tiles, one below
         const bool wide = (int)(grid.x * grid.y) >= kFwdRingWideMinTiles;
 #define MSPLAT_FWD_RING(NP, NPX)                                                                                 \
-    launch(blend_fwd_ring_kernel<C, NP, false, NPX>, grid, kTilePixels / NPX + 32 * NP, 0, stream, P, uv, conic,    \
-           opacity, feature, idx, tr, bg, W, H, out, final_T, nc, BlendBatch{}, g_wait_limit)
+    launch(blend_fwd_ring_kernel<C, NP, false, NPX, kBlendNpixBwd>, grid, kTilePixels / NPX + 32 * NP, 0, stream, P, \
+           uv, conic, opacity, feature, idx, tr, bg, W, H, out, final_T, nc, emask, BlendBatch{}, g_wait_limit)
         if (g_fwd_ring == 2 && wide) MSPLAT_FWD_RING(2, kBlendNpixFwd);
         else if (g_fwd_ring == 2) MSPLAT_FWD_RING(2, 1);
         else if (wide) MSPLAT_FWD_RING(4, kBlendNpixFwd);
         else MSPLAT_FWD_RING(4, 1);
 #undef MSPLAT_FWD_RING
     } else if (!bwd)
-        launch(blend_fwd_small_kernel<C, kBlendNpixFwd, kSplitFwd, false, kGatherFwd>, gf, tf, 0, stream,
-            P, uv, conic, opacity, feature, idx, tr, bg, W, H, out, final_T, nc, BlendBatch{});
+        launch(blend_fwd_small_kernel<C, kBlendNpixFwd, kSplitFwd, false, kGatherFwd, kBlendNpixBwd>, gf, tf, 0, stream,
+            P, uv, conic, opacity, feature, idx, tr, bg, W, H, out, final_T, nc, emask, BlendBatch{});
     else if ((g_bwd_ring == 1 || g_bwd_ring == 2) && (int)(grid.x * grid.y) >= kBwdRingMinTiles) {
         constexpr int tr0 = kTilePixels / kBlendNpixBwd;
 #define MSPLAT_BWD_RING(NP, BGV)                                                                                 \
     launch(blend_bwd_ring_kernel<C, kBlendNpixBwd, NP, BGV>, grid, tr0 + 32 * NP, 0, stream, P, uv, conic, opacity, \
-           feature, idx, tr, bg, W, H, fT, nci, dout, duv, dcon, dop, dfeat, BlendBatch{}, g_wait_limit)
+           feature, idx, tr, bg, W, H, fT, nci, dout, duv, dcon, dop, dfeat, emask, BlendBatch{}, g_wait_limit)
         if (g_bwd_ring == 1 && bg != 0.0f) MSPLAT_BWD_RING(1, true);
         else if (g_bwd_ring == 1) MSPLAT_BWD_RING(1, false);
         else if (bg != 0.0f) MSPLAT_BWD_RING(2, true);
@@ -1544,22 +1591,24 @@ void launch_small(bool bwd, dim3 grid, cudaStream_t stream, int P, const float2 
 #undef MSPLAT_BWD_RING
     } else if (bg != 0.0f)
         launch(blend_bwd_small_kernel<C, kBlendNpixBwd, true, kSplitBwd, false, kGatherBwd>, gb, tb, 0, stream,
-            P, uv, conic, opacity, feature, idx, tr, bg, W, H, fT, nci, dout, duv, dcon, dop, dfeat, BlendBatch{});
+            P, uv, conic, opacity, feature, idx, tr, bg, W, H, fT, nci, dout, duv, dcon, dop, dfeat, emask,
+            BlendBatch{});
     else
         launch(blend_bwd_small_kernel<C, kBlendNpixBwd, false, kSplitBwd, false, kGatherBwd>, gb, tb, 0, stream,
-            P, uv, conic, opacity, feature, idx, tr, bg, W, H, fT, nci, dout, duv, dcon, dop, dfeat, BlendBatch{});
+            P, uv, conic, opacity, feature, idx, tr, bg, W, H, fT, nci, dout, duv, dcon, dop, dfeat, emask,
+            BlendBatch{});
 }
 
 inline void dispatch_small(bool bwd, int C, dim3 grid, cudaStream_t stream, int P, const float2 *uv,
                            const float *conic, const float *opacity, const float *feature, const int32_t *idx,
                            const int2 *tr, float bg, int W, int H, float *out, float *final_T, int32_t *nc,
                            const float *fT, const int32_t *nci, const float *dout, float *duv, float *dcon,
-                           float *dop, float *dfeat) {
+                           float *dop, float *dfeat, unsigned char *emask) {
     switch (C) {
 #define MSPLAT_SMALL(CC)                                                                                       \
     case CC:                                                                                                   \
         launch_small<CC>(bwd, grid, stream, P, uv, conic, opacity, feature, idx, tr, bg, W, H, out, final_T,   \
-                         nc, fT, nci, dout, duv, dcon, dop, dfeat);                                           \
+                         nc, fT, nci, dout, duv, dcon, dop, dfeat, emask);                                    \
         break;
         MSPLAT_SMALL(1) MSPLAT_SMALL(2) MSPLAT_SMALL(3) MSPLAT_SMALL(4)
 #undef MSPLAT_SMALL
@@ -1571,11 +1620,9 @@ inline void dispatch_small(bool bwd, int C, dim3 grid, cudaStream_t stream, int 
 
 using namespace msplat;
 
-extern "C" int msplat_alpha_blending_forward(int P, int C, const float *uv, const float *conic,
-                                             const float *opacity, const float *feature,
-                                             const int32_t *idx_sorted, const int32_t *tile_range,
-                                             float bg, int W, int H, float *out, float *final_T,
-                                             int32_t *ncontrib, msplat_stream_t stream) {
+static int blend_forward(int P, int C, const float *uv, const float *conic, const float *opacity, const float *feature,
+                         const int32_t *idx_sorted, const int32_t *tile_range, float bg, int W, int H, float *out,
+                         float *final_T, int32_t *ncontrib, unsigned char *entry_masks, cudaStream_t stream) {
     if (P < 0 || C <= 0 || W <= 0 || H <= 0)
         return set_error(MSPLAT_ERR_INVALID_ARGUMENT, "alpha_blending_forward: bad sizes P=%d C=%d W=%d H=%d",
                          P, C, W, H);
@@ -1585,7 +1632,7 @@ extern "C" int msplat_alpha_blending_forward(int P, int C, const float *uv, cons
     if (C <= 4) {
         dispatch_small(false, C, grid, stream, P, (const float2 *)uv, conic, opacity, feature, idx_sorted,
                        (const int2 *)tile_range, bg, W, H, out, final_T, ncontrib, nullptr, nullptr, nullptr,
-                       nullptr, nullptr, nullptr, nullptr);
+                       nullptr, nullptr, nullptr, nullptr, entry_masks);
         return check_launch("alpha_blending_forward");
     }
     for (int c0 = 0; c0 < C; c0 += 32) {
@@ -1606,13 +1653,11 @@ extern "C" int msplat_alpha_blending_forward(int P, int C, const float *uv, cons
     return check_launch("alpha_blending_forward");
 }
 
-extern "C" int msplat_alpha_blending_backward(int P, int C, const float *uv, const float *conic,
-                                              const float *opacity, const float *feature,
-                                              const int32_t *idx_sorted, const int32_t *tile_range,
-                                              float bg, int W, int H, const float *final_T,
-                                              const int32_t *ncontrib, const float *dL_dout,
-                                              float *dL_duv, float *dL_dconic, float *dL_dopacity,
-                                              float *dL_dfeature, msplat_stream_t stream) {
+static int blend_backward(int P, int C, const float *uv, const float *conic, const float *opacity,
+                          const float *feature, const int32_t *idx_sorted, const int32_t *tile_range, float bg, int W,
+                          int H, const float *final_T, const int32_t *ncontrib, const float *dL_dout, float *dL_duv,
+                          float *dL_dconic, float *dL_dopacity, float *dL_dfeature, const unsigned char *entry_masks,
+                          cudaStream_t stream) {
     if (P < 0 || C <= 0 || W <= 0 || H <= 0)
         return set_error(MSPLAT_ERR_INVALID_ARGUMENT, "alpha_blending_backward: bad sizes");
     if (!tile_range || !final_T || !ncontrib || !dL_dout ||
@@ -1623,7 +1668,7 @@ extern "C" int msplat_alpha_blending_backward(int P, int C, const float *uv, con
     if (C <= 4) {
         dispatch_small(true, C, grid, stream, P, (const float2 *)uv, conic, opacity, feature, idx_sorted,
                        (const int2 *)tile_range, bg, W, H, nullptr, nullptr, nullptr, final_T, ncontrib, dL_dout,
-                       dL_duv, dL_dconic, dL_dopacity, dL_dfeature);
+                       dL_duv, dL_dconic, dL_dopacity, dL_dfeature, const_cast<unsigned char *>(entry_masks));
         launch(blend_grad_finish_kernel, ceil_div(P, 256), 256, 0, stream, P, conic, opacity, dL_duv, dL_dconic);
         return check_launch("alpha_blending_backward");
     }
@@ -1633,6 +1678,46 @@ extern "C" int msplat_alpha_blending_backward(int P, int C, const float *uv, con
                                                              ncontrib, dL_dout, dL_duv, dL_dconic, dL_dopacity,
                                                              dL_dfeature, BlendBatch{});
     return check_launch("alpha_blending_backward");
+}
+
+extern "C" int msplat_alpha_blending_forward(int P, int C, const float *uv, const float *conic,
+                                             const float *opacity, const float *feature,
+                                             const int32_t *idx_sorted, const int32_t *tile_range,
+                                             float bg, int W, int H, float *out, float *final_T,
+                                             int32_t *ncontrib, msplat_stream_t stream) {
+    return blend_forward(P, C, uv, conic, opacity, feature, idx_sorted, tile_range, bg, W, H, out, final_T, ncontrib,
+                         nullptr, stream);
+}
+
+extern "C" int msplat_alpha_blending_forward_masks(int P, int C, const float *uv, const float *conic,
+                                                   const float *opacity, const float *feature,
+                                                   const int32_t *idx_sorted, const int32_t *tile_range, float bg,
+                                                   int W, int H, float *out, float *final_T, int32_t *ncontrib,
+                                                   unsigned char *entry_masks, msplat_stream_t stream) {
+    return blend_forward(P, C, uv, conic, opacity, feature, idx_sorted, tile_range, bg, W, H, out, final_T, ncontrib,
+                         entry_masks, stream);
+}
+
+extern "C" int msplat_alpha_blending_backward(int P, int C, const float *uv, const float *conic,
+                                              const float *opacity, const float *feature,
+                                              const int32_t *idx_sorted, const int32_t *tile_range,
+                                              float bg, int W, int H, const float *final_T,
+                                              const int32_t *ncontrib, const float *dL_dout,
+                                              float *dL_duv, float *dL_dconic, float *dL_dopacity,
+                                              float *dL_dfeature, msplat_stream_t stream) {
+    return blend_backward(P, C, uv, conic, opacity, feature, idx_sorted, tile_range, bg, W, H, final_T, ncontrib,
+                          dL_dout, dL_duv, dL_dconic, dL_dopacity, dL_dfeature, nullptr, stream);
+}
+
+extern "C" int msplat_alpha_blending_backward_masks(int P, int C, const float *uv, const float *conic,
+                                                    const float *opacity, const float *feature,
+                                                    const int32_t *idx_sorted, const int32_t *tile_range, float bg,
+                                                    int W, int H, const float *final_T, const int32_t *ncontrib,
+                                                    const float *dL_dout, float *dL_duv, float *dL_dconic,
+                                                    float *dL_dopacity, float *dL_dfeature,
+                                                    const unsigned char *entry_masks, msplat_stream_t stream) {
+    return blend_backward(P, C, uv, conic, opacity, feature, idx_sorted, tile_range, bg, W, H, final_T, ncontrib,
+                          dL_dout, dL_duv, dL_dconic, dL_dopacity, dL_dfeature, entry_masks, stream);
 }
 
 // ------------------------------------------------------------ batches
@@ -1646,17 +1731,17 @@ void launch_small_batch(bool bwd, int tiles, cudaStream_t stream, const BlendBat
     constexpr int tf = kTilePixels / kBatchNpixFwd, tb = kTilePixels / kBatchNpixBwd;
     if (!bwd && g_batch_fwd_ring == 2)
         launch(blend_fwd_ring_kernel<C, 2, true, kBatchNpixFwd>, tiles, kTilePixels / kBatchNpixFwd + 64, 0, stream, 0, uv, conic, opacity, feature,
-               idx, tr, bg, 1, 1, out, final_T, nc, bb, g_wait_limit);
+               idx, tr, bg, 1, 1, out, final_T, nc, nullptr, bb, g_wait_limit);
     else if (!bwd && g_batch_fwd_ring == 4)
         launch(blend_fwd_ring_kernel<C, 4, true, kBatchNpixFwd>, tiles, kTilePixels / kBatchNpixFwd + 128, 0, stream, 0, uv, conic, opacity,
-               feature, idx, tr, bg, 1, 1, out, final_T, nc, bb, g_wait_limit);
+               feature, idx, tr, bg, 1, 1, out, final_T, nc, nullptr, bb, g_wait_limit);
     else if (!bwd)
         launch(blend_fwd_small_kernel<C, kBatchNpixFwd, 1, true, kBatchGatherFwd>, tiles, tf, 0, stream, 0, uv,
-               conic, opacity, feature, idx, tr, bg, 1, 1, out, final_T, nc, bb);
+               conic, opacity, feature, idx, tr, bg, 1, 1, out, final_T, nc, nullptr, bb);
     else if (g_batch_bwd_ring == 1 || g_batch_bwd_ring == 2) {
 #define MSPLAT_BWD_RING(NP, BGV)                                                                                  \
     launch(blend_bwd_ring_kernel<C, kBatchNpixBwd, NP, BGV, true>, tiles, tb + 32 * NP, 0, stream, 0, uv, conic,     \
-           opacity, feature, idx, tr, bg, 1, 1, fT, nci, dout, duv, dcon, dop, dfeat, bb, g_wait_limit)
+           opacity, feature, idx, tr, bg, 1, 1, fT, nci, dout, duv, dcon, dop, dfeat, nullptr, bb, g_wait_limit)
         if (g_batch_bwd_ring == 1 && bg != 0.0f) MSPLAT_BWD_RING(1, true);
         else if (g_batch_bwd_ring == 1) MSPLAT_BWD_RING(1, false);
         else if (bg != 0.0f) MSPLAT_BWD_RING(2, true);
@@ -1664,10 +1749,10 @@ void launch_small_batch(bool bwd, int tiles, cudaStream_t stream, const BlendBat
 #undef MSPLAT_BWD_RING
     } else if (bg != 0.0f)
         launch(blend_bwd_small_kernel<C, kBatchNpixBwd, true, 1, true, kBatchGatherBwd>, tiles, tb, 0, stream, 0, uv,
-               conic, opacity, feature, idx, tr, bg, 1, 1, fT, nci, dout, duv, dcon, dop, dfeat, bb);
+               conic, opacity, feature, idx, tr, bg, 1, 1, fT, nci, dout, duv, dcon, dop, dfeat, nullptr, bb);
     else
         launch(blend_bwd_small_kernel<C, kBatchNpixBwd, false, 1, true, kBatchGatherBwd>, tiles, tb, 0, stream, 0,
-               uv, conic, opacity, feature, idx, tr, bg, 1, 1, fT, nci, dout, duv, dcon, dop, dfeat, bb);
+               uv, conic, opacity, feature, idx, tr, bg, 1, 1, fT, nci, dout, duv, dcon, dop, dfeat, nullptr, bb);
 }
 
 void dispatch_small_batch(bool bwd, int C, int tiles, cudaStream_t stream, const BlendBatch &bb, const float2 *uv,
