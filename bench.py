@@ -251,8 +251,8 @@ def blend_pairs(ms, p, color_dim=3):
 # DRAM bytes per launch (read + write) of the blend kernels at the benchmark
 # size over the fused calls' culled lists: a constant taken from an earlier
 # ncu capture, not measured by this run (reported with that label).
-NCU_TRAFFIC_1M_1080P = {"alpha_blending_backward": 93.74e6 + 1.03e6,
-                        "alpha_blending_forward": 42.26e6 + 9.39e6}
+NCU_TRAFFIC_1M_1080P = {"alpha_blending_backward": 95.14e6 + 0.76e6,
+                        "alpha_blending_forward": 42.48e6 + 10.86e6}
 
 
 def roofline(stages, steps, pairs, inter, nvis, sm_mhz, peaks, peak_kind, C=3, n=None, D=16, full=None,

@@ -55,6 +55,7 @@ class _EWAProject(torch.autograd.Function):
         ctx.save_for_backward(x, c, intr_c, extr_c, radius)
         ctx.extr_shape = extr.shape
         ctx.mark_non_differentiable(radius, tiles)
+        ctx.set_materialize_grads(False)  # no zero-filled gradients for radius and tiles
         return conic, radius, tiles
 
     @staticmethod
@@ -62,6 +63,8 @@ class _EWAProject(torch.autograd.Function):
         x, c, intr, extr, radius = ctx.saved_tensors
         P = x.shape[0]
         dev = x.device
+        if dL_dconic is None:
+            dL_dconic = torch.zeros((P, 3), dtype=torch.float32, device=dev)
         g = dL_dconic.float().contiguous()
         want_i, want_e = ctx.needs_input_grad[2], ctx.needs_input_grad[3]
         dxyz = torch.empty((P, 3), dtype=torch.float32, device=dev)

@@ -59,6 +59,9 @@ class _Preprocess(torch.autograd.Function):
         ctx.intr_shape, ctx.extr_shape = intr.shape, extr.shape
         ctx.save_for_backward(xyz_c, scale_c, rot_c, shs_c, intr_c, extr_c, depth, radius)
         ctx.mark_non_differentiable(depth, radius, tiles)
+        # outputs without a gradient arrive as None (no zero-filled tensors
+        # for depth, radius and tiles); the backward fills what it needs
+        ctx.set_materialize_grads(False)
         return uv, depth, conic, radius, tiles, color
 
     @staticmethod
