@@ -505,6 +505,25 @@ MSPLAT_API int msplat_batch_alpha_blending_backward(const void *plan, int B, int
                                                     float *dL_dopacity, float *dL_dfeature,
                                                     msplat_stream_t stream);
 
+/* The same two calls keeping each list entry's warp-block mask from the
+ * forward for the backward (as msplat_alpha_blending_forward_masks /
+ * _backward_masks): entry_masks holds one byte per entry of idx_sorted. */
+MSPLAT_API int msplat_batch_alpha_blending_forward_masks(const void *plan, int B, int total_tiles, int C,
+                                                         int feature_per_camera, const float *uv, const float *conic,
+                                                         const float *opacity, const float *feature,
+                                                         const int32_t *idx_sorted, const int32_t *tile_range,
+                                                         float bg, float *out, float *final_T, int32_t *ncontrib,
+                                                         unsigned char *entry_masks, msplat_stream_t stream);
+MSPLAT_API int msplat_batch_alpha_blending_backward_masks(const void *plan, int B, int total_tiles, int64_t rows,
+                                                          int C, int feature_per_camera, const float *uv,
+                                                          const float *conic, const float *opacity,
+                                                          const float *feature, const int32_t *idx_sorted,
+                                                          const int32_t *tile_range, float bg, const float *final_T,
+                                                          const int32_t *ncontrib, const float *dL_dout,
+                                                          float *dL_duv, float *dL_dconic, float *dL_dopacity,
+                                                          float *dL_dfeature, const unsigned char *entry_masks,
+                                                          msplat_stream_t stream);
+
 /* ------------------------------------------------------------------------ */
 /* Density-control statistics after a backward pass.  No kernel counterpart
  * in the reference; accumulates the screen-space gradient that its

@@ -84,6 +84,10 @@ _SIGNATURES = {
         _I, [_P, _I, _I, _I, _I, _P, _P, _P, _P, _P, _P, _F, _P, _P, _P, _P]),
     "msplat_batch_alpha_blending_backward": (
         _I, [_P, _I, _I, _I64, _I, _I, _P, _P, _P, _P, _P, _P, _F, _P, _P, _P, _P, _P, _P, _P, _P]),
+    "msplat_batch_alpha_blending_forward_masks": (
+        _I, [_P, _I, _I, _I, _I, _P, _P, _P, _P, _P, _P, _F, _P, _P, _P, _P, _P]),
+    "msplat_batch_alpha_blending_backward_masks": (
+        _I, [_P, _I, _I, _I64, _I, _I, _P, _P, _P, _P, _P, _P, _F, _P, _P, _P, _P, _P, _P, _P, _P, _P]),
     "msplat_rasterize_preprocess_backward": (
         _I, [_I, _P, _P, _P, _P, _P, _I, _I, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _SZ, _P]),
 }

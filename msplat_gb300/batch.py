@@ -214,11 +214,16 @@ class _RasterizeScenes(torch.autograd.Function):
         out = torch.empty((C * plan.pixels,), dtype=torch.float32, device=dev)
         final_T = torch.empty((plan.pixels,), dtype=torch.float32, device=dev)
         ncontrib = torch.empty((plan.pixels,), dtype=torch.int32, device=dev)
+        # the forward keeps each list entry's warp-block mask for the backward
+        masks = None
+        if C <= 4 and any(ctx.needs_input_grad[1:]):
+            masks = torch.empty((max(idx.numel(), 1),), dtype=torch.uint8, device=dev)
         with _lib.stage("alpha_blending_forward"):
-            _lib.check(lib.msplat_batch_alpha_blending_forward(
+            _lib.check(lib.msplat_batch_alpha_blending_forward_masks(
                 _lib.ptr(plan.device), B, plan.tiles, C, 1 if use_sh else 0, _lib.ptr(uv), _lib.ptr(conic),
                 _lib.ptr(op_all), _lib.ptr(feat), _lib.ptr(idx), _lib.ptr(tr), float(bg), _lib.ptr(out),
-                _lib.ptr(final_T), _lib.ptr(ncontrib), st), "batch_alpha_blending_forward")
+                _lib.ptr(final_T), _lib.ptr(ncontrib), _lib.ptr(masks), st), "batch_alpha_blending_forward")
+        ctx.masks = masks
         imgs = tuple(out[C * plan.pix_off[b]:C * plan.pix_off[b + 1]].view(C, h, w)
                      for b, (w, h) in enumerate(plan.dims))
         ctx.meta = (groups, plan, bg, use_sh, C, D)
@@ -248,11 +253,11 @@ class _RasterizeScenes(torch.autograd.Function):
                 seg.copy_(g.reshape(-1))
         dL_duv, dL_dconic, dL_dop, dL_dfeat = zeroed_views(dev, [(R, 2), (R, 3), (R,), (R, C)])
         with _lib.stage("alpha_blending_backward"):
-            _lib.check(lib.msplat_batch_alpha_blending_backward(
+            _lib.check(lib.msplat_batch_alpha_blending_backward_masks(
                 _lib.ptr(plan.device), B, plan.tiles, R, C, 1 if use_sh else 0, _lib.ptr(uv), _lib.ptr(conic),
                 _lib.ptr(op_all), _lib.ptr(feat), _lib.ptr(idx), _lib.ptr(tr), float(bg), _lib.ptr(final_T),
                 _lib.ptr(ncontrib), _lib.ptr(gout), _lib.ptr(dL_duv), _lib.ptr(dL_dconic), _lib.ptr(dL_dop),
-                _lib.ptr(dL_dfeat), st), "batch_alpha_blending_backward")
+                _lib.ptr(dL_dfeat), _lib.ptr(ctx.masks), st), "batch_alpha_blending_backward")
         n_in = 5 * S + 2
         want_i, want_e = ctx.needs_input_grad[1 + 5 * S], ctx.needs_input_grad[2 + 5 * S]
         dL_dcams = torch.empty((B, 16), dtype=torch.float32, device=dev) if (want_i or want_e) else None

@@ -1727,21 +1727,22 @@ template <int C>
 void launch_small_batch(bool bwd, int tiles, cudaStream_t stream, const BlendBatch &bb, const float2 *uv,
                         const float *conic, const float *opacity, const float *feature, const int32_t *idx,
                         const int2 *tr, float bg, float *out, float *final_T, int32_t *nc, const float *fT,
-                        const int32_t *nci, const float *dout, float *duv, float *dcon, float *dop, float *dfeat) {
+                        const int32_t *nci, const float *dout, float *duv, float *dcon, float *dop, float *dfeat,
+                        unsigned char *emask) {
     constexpr int tf = kTilePixels / kBatchNpixFwd, tb = kTilePixels / kBatchNpixBwd;
     if (!bwd && g_batch_fwd_ring == 2)
-        launch(blend_fwd_ring_kernel<C, 2, true, kBatchNpixFwd>, tiles, kTilePixels / kBatchNpixFwd + 64, 0, stream, 0, uv, conic, opacity, feature,
-               idx, tr, bg, 1, 1, out, final_T, nc, nullptr, bb, g_wait_limit);
+        launch(blend_fwd_ring_kernel<C, 2, true, kBatchNpixFwd, kBatchNpixBwd>, tiles, kTilePixels / kBatchNpixFwd + 64, 0, stream, 0, uv, conic, opacity, feature,
+               idx, tr, bg, 1, 1, out, final_T, nc, emask, bb, g_wait_limit);
     else if (!bwd && g_batch_fwd_ring == 4)
-        launch(blend_fwd_ring_kernel<C, 4, true, kBatchNpixFwd>, tiles, kTilePixels / kBatchNpixFwd + 128, 0, stream, 0, uv, conic, opacity,
-               feature, idx, tr, bg, 1, 1, out, final_T, nc, nullptr, bb, g_wait_limit);
+        launch(blend_fwd_ring_kernel<C, 4, true, kBatchNpixFwd, kBatchNpixBwd>, tiles, kTilePixels / kBatchNpixFwd + 128, 0, stream, 0, uv, conic, opacity,
+               feature, idx, tr, bg, 1, 1, out, final_T, nc, emask, bb, g_wait_limit);
     else if (!bwd)
-        launch(blend_fwd_small_kernel<C, kBatchNpixFwd, 1, true, kBatchGatherFwd>, tiles, tf, 0, stream, 0, uv,
-               conic, opacity, feature, idx, tr, bg, 1, 1, out, final_T, nc, nullptr, bb);
+        launch(blend_fwd_small_kernel<C, kBatchNpixFwd, 1, true, kBatchGatherFwd, kBatchNpixBwd>, tiles, tf, 0,
+               stream, 0, uv, conic, opacity, feature, idx, tr, bg, 1, 1, out, final_T, nc, emask, bb);
     else if (g_batch_bwd_ring == 1 || g_batch_bwd_ring == 2) {
 #define MSPLAT_BWD_RING(NP, BGV)                                                                                  \
     launch(blend_bwd_ring_kernel<C, kBatchNpixBwd, NP, BGV, true>, tiles, tb + 32 * NP, 0, stream, 0, uv, conic,     \
-           opacity, feature, idx, tr, bg, 1, 1, fT, nci, dout, duv, dcon, dop, dfeat, nullptr, bb, g_wait_limit)
+           opacity, feature, idx, tr, bg, 1, 1, fT, nci, dout, duv, dcon, dop, dfeat, emask, bb, g_wait_limit)
         if (g_batch_bwd_ring == 1 && bg != 0.0f) MSPLAT_BWD_RING(1, true);
         else if (g_batch_bwd_ring == 1) MSPLAT_BWD_RING(1, false);
         else if (bg != 0.0f) MSPLAT_BWD_RING(2, true);
@@ -1749,21 +1750,22 @@ void launch_small_batch(bool bwd, int tiles, cudaStream_t stream, const BlendBat
 #undef MSPLAT_BWD_RING
     } else if (bg != 0.0f)
         launch(blend_bwd_small_kernel<C, kBatchNpixBwd, true, 1, true, kBatchGatherBwd>, tiles, tb, 0, stream, 0, uv,
-               conic, opacity, feature, idx, tr, bg, 1, 1, fT, nci, dout, duv, dcon, dop, dfeat, nullptr, bb);
+               conic, opacity, feature, idx, tr, bg, 1, 1, fT, nci, dout, duv, dcon, dop, dfeat, emask, bb);
     else
         launch(blend_bwd_small_kernel<C, kBatchNpixBwd, false, 1, true, kBatchGatherBwd>, tiles, tb, 0, stream, 0,
-               uv, conic, opacity, feature, idx, tr, bg, 1, 1, fT, nci, dout, duv, dcon, dop, dfeat, nullptr, bb);
+               uv, conic, opacity, feature, idx, tr, bg, 1, 1, fT, nci, dout, duv, dcon, dop, dfeat, emask, bb);
 }
 
 void dispatch_small_batch(bool bwd, int C, int tiles, cudaStream_t stream, const BlendBatch &bb, const float2 *uv,
                           const float *conic, const float *opacity, const float *feature, const int32_t *idx,
                           const int2 *tr, float bg, float *out, float *final_T, int32_t *nc, const float *fT,
-                          const int32_t *nci, const float *dout, float *duv, float *dcon, float *dop, float *dfeat) {
+                          const int32_t *nci, const float *dout, float *duv, float *dcon, float *dop, float *dfeat,
+                          unsigned char *emask) {
     switch (C) {
 #define MSPLAT_SMALL_B(CC)                                                                                   \
     case CC:                                                                                                 \
         launch_small_batch<CC>(bwd, tiles, stream, bb, uv, conic, opacity, feature, idx, tr, bg, out, final_T, \
-                               nc, fT, nci, dout, duv, dcon, dop, dfeat);                                    \
+                               nc, fT, nci, dout, duv, dcon, dop, dfeat, emask);                             \
         break;
         MSPLAT_SMALL_B(1) MSPLAT_SMALL_B(2) MSPLAT_SMALL_B(3) MSPLAT_SMALL_B(4)
 #undef MSPLAT_SMALL_B
@@ -1773,12 +1775,10 @@ void dispatch_small_batch(bool bwd, int C, int tiles, cudaStream_t stream, const
 
 }  // namespace
 
-extern "C" int msplat_batch_alpha_blending_forward(const void *plan, int B, int total_tiles, int C,
-                                                   int feature_per_camera, const float *uv, const float *conic,
-                                                   const float *opacity, const float *feature,
-                                                   const int32_t *idx_sorted, const int32_t *tile_range, float bg,
-                                                   float *out, float *final_T, int32_t *ncontrib,
-                                                   msplat_stream_t stream) {
+static int batch_blend_forward(const void *plan, int B, int total_tiles, int C, int feature_per_camera,
+                               const float *uv, const float *conic, const float *opacity, const float *feature,
+                               const int32_t *idx_sorted, const int32_t *tile_range, float bg, float *out,
+                               float *final_T, int32_t *ncontrib, unsigned char *entry_masks, cudaStream_t stream) {
     if (B <= 0 || total_tiles < 0 || C <= 0)
         return set_error(MSPLAT_ERR_INVALID_ARGUMENT, "batch_alpha_blending_forward: bad sizes B=%d C=%d", B, C);
     if (!plan || !uv || !conic || !opacity || !feature || !tile_range || !out || !final_T || !ncontrib)
@@ -1788,7 +1788,7 @@ extern "C" int msplat_batch_alpha_blending_forward(const void *plan, int B, int 
     if (C <= 4) {
         dispatch_small_batch(false, C, total_tiles, stream, bb, (const float2 *)uv, conic, opacity, feature, idx_sorted,
                              (const int2 *)tile_range, bg, out, final_T, ncontrib, nullptr, nullptr, nullptr, nullptr,
-                             nullptr, nullptr, nullptr);
+                             nullptr, nullptr, nullptr, entry_masks);
         return check_launch("batch_alpha_blending_forward");
     }
     for (int c0 = 0; c0 < C; c0 += 32) {
@@ -1809,14 +1809,12 @@ extern "C" int msplat_batch_alpha_blending_forward(const void *plan, int B, int 
     return check_launch("batch_alpha_blending_forward");
 }
 
-extern "C" int msplat_batch_alpha_blending_backward(const void *plan, int B, int total_tiles, int64_t rows, int C,
-                                                    int feature_per_camera, const float *uv, const float *conic,
-                                                    const float *opacity, const float *feature,
-                                                    const int32_t *idx_sorted, const int32_t *tile_range, float bg,
-                                                    const float *final_T, const int32_t *ncontrib,
-                                                    const float *dL_dout, float *dL_duv, float *dL_dconic,
-                                                    float *dL_dopacity, float *dL_dfeature,
-                                                    msplat_stream_t stream) {
+static int batch_blend_backward(const void *plan, int B, int total_tiles, int64_t rows, int C,
+                                int feature_per_camera, const float *uv, const float *conic, const float *opacity,
+                                const float *feature, const int32_t *idx_sorted, const int32_t *tile_range, float bg,
+                                const float *final_T, const int32_t *ncontrib, const float *dL_dout, float *dL_duv,
+                                float *dL_dconic, float *dL_dopacity, float *dL_dfeature,
+                                const unsigned char *entry_masks, cudaStream_t stream) {
     if (B <= 0 || total_tiles < 0 || C <= 0 || rows < 0)
         return set_error(MSPLAT_ERR_INVALID_ARGUMENT, "batch_alpha_blending_backward: bad sizes");
     if (!plan || !uv || !conic || !opacity || !feature || !tile_range || !final_T || !ncontrib || !dL_dout ||
@@ -1827,7 +1825,7 @@ extern "C" int msplat_batch_alpha_blending_backward(const void *plan, int B, int
     if (C <= 4) {
         dispatch_small_batch(true, C, total_tiles, stream, bb, (const float2 *)uv, conic, opacity, feature, idx_sorted,
                              (const int2 *)tile_range, bg, nullptr, nullptr, nullptr, final_T, ncontrib, dL_dout,
-                             dL_duv, dL_dconic, dL_dopacity, dL_dfeature);
+                             dL_duv, dL_dconic, dL_dopacity, dL_dfeature, const_cast<unsigned char *>(entry_masks));
         launch(batch_blend_grad_finish_kernel, (unsigned)ceil_div64(rows, 256), 256, 0, stream, bb.pv, rows, conic,
                opacity, dL_duv, dL_dconic);
         return check_launch("batch_alpha_blending_backward");
@@ -1837,6 +1835,53 @@ extern "C" int msplat_batch_alpha_blending_backward(const void *plan, int B, int
                opacity, feature, idx_sorted, (const int2 *)tile_range, bg, 1, 1, final_T, ncontrib, dL_dout, dL_duv,
                dL_dconic, dL_dopacity, dL_dfeature, bb);
     return check_launch("batch_alpha_blending_backward");
+}
+
+extern "C" int msplat_batch_alpha_blending_forward(const void *plan, int B, int total_tiles, int C,
+                                                   int feature_per_camera, const float *uv, const float *conic,
+                                                   const float *opacity, const float *feature,
+                                                   const int32_t *idx_sorted, const int32_t *tile_range, float bg,
+                                                   float *out, float *final_T, int32_t *ncontrib,
+                                                   msplat_stream_t stream) {
+    return batch_blend_forward(plan, B, total_tiles, C, feature_per_camera, uv, conic, opacity, feature, idx_sorted,
+                               tile_range, bg, out, final_T, ncontrib, nullptr, stream);
+}
+
+extern "C" int msplat_batch_alpha_blending_forward_masks(const void *plan, int B, int total_tiles, int C,
+                                                         int feature_per_camera, const float *uv, const float *conic,
+                                                         const float *opacity, const float *feature,
+                                                         const int32_t *idx_sorted, const int32_t *tile_range,
+                                                         float bg, float *out, float *final_T, int32_t *ncontrib,
+                                                         unsigned char *entry_masks, msplat_stream_t stream) {
+    return batch_blend_forward(plan, B, total_tiles, C, feature_per_camera, uv, conic, opacity, feature, idx_sorted,
+                               tile_range, bg, out, final_T, ncontrib, entry_masks, stream);
+}
+
+extern "C" int msplat_batch_alpha_blending_backward(const void *plan, int B, int total_tiles, int64_t rows, int C,
+                                                    int feature_per_camera, const float *uv, const float *conic,
+                                                    const float *opacity, const float *feature,
+                                                    const int32_t *idx_sorted, const int32_t *tile_range, float bg,
+                                                    const float *final_T, const int32_t *ncontrib,
+                                                    const float *dL_dout, float *dL_duv, float *dL_dconic,
+                                                    float *dL_dopacity, float *dL_dfeature,
+                                                    msplat_stream_t stream) {
+    return batch_blend_backward(plan, B, total_tiles, rows, C, feature_per_camera, uv, conic, opacity, feature,
+                                idx_sorted, tile_range, bg, final_T, ncontrib, dL_dout, dL_duv, dL_dconic,
+                                dL_dopacity, dL_dfeature, nullptr, stream);
+}
+
+extern "C" int msplat_batch_alpha_blending_backward_masks(const void *plan, int B, int total_tiles, int64_t rows,
+                                                          int C, int feature_per_camera, const float *uv,
+                                                          const float *conic, const float *opacity,
+                                                          const float *feature, const int32_t *idx_sorted,
+                                                          const int32_t *tile_range, float bg, const float *final_T,
+                                                          const int32_t *ncontrib, const float *dL_dout,
+                                                          float *dL_duv, float *dL_dconic, float *dL_dopacity,
+                                                          float *dL_dfeature, const unsigned char *entry_masks,
+                                                          msplat_stream_t stream) {
+    return batch_blend_backward(plan, B, total_tiles, rows, C, feature_per_camera, uv, conic, opacity, feature,
+                                idx_sorted, tile_range, bg, final_T, ncontrib, dL_dout, dL_duv, dL_dconic,
+                                dL_dopacity, dL_dfeature, entry_masks, stream);
 }
 
 extern "C" int msplat_set_blend_ring(int producer_warps, int batch_producer_warps) {
