@@ -481,6 +481,15 @@ MSPLAT_API int msplat_batch_sort_finish(const void *plan, int B, int64_t depth_i
                                         int64_t capacity, const void *prepare_workspace, int32_t *idx_sorted,
                                         int32_t *tile_range, int32_t *status, void *workspace,
                                         size_t workspace_bytes, msplat_stream_t stream);
+/* The same, told the digit bits of the last tile-key pass: every camera's
+ * local tile keys stay below 2^(8 (passes - 1) + last_pass_bits), so the
+ * last pass ranks only those bits (1..8; bits_for(largest camera tile
+ * count) - 8 (passes - 1)).  Same results as msplat_batch_sort_finish. */
+MSPLAT_API int msplat_batch_sort_finish_bits(const void *plan, int B, int64_t depth_items, int total_tiles,
+                                             int passes, int last_pass_bits, int64_t capacity,
+                                             const void *prepare_workspace, int32_t *idx_sorted,
+                                             int32_t *tile_range, int32_t *status, void *workspace,
+                                             size_t workspace_bytes, msplat_stream_t stream);
 
 /* One blend grid over every camera's tiles (the semantics of
  * msplat_alpha_blending_forward per camera).  feature_per_camera: 1 when

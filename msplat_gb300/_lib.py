@@ -80,6 +80,7 @@ _SIGNATURES = {
     "msplat_batch_sort_prepare": (_I, [_P, _I, _I64, _P, _P, _P, _P, _P, _P, _P, _SZ, _P]),
     "msplat_batch_sort_finish_workspace_size": (_SZ, [_I, _I64, _I]),
     "msplat_batch_sort_finish": (_I, [_P, _I, _I64, _I, _I, _I64, _P, _P, _P, _P, _P, _SZ, _P]),
+    "msplat_batch_sort_finish_bits": (_I, [_P, _I, _I64, _I, _I, _I, _I64, _P, _P, _P, _P, _P, _SZ, _P]),
     "msplat_batch_alpha_blending_forward": (
         _I, [_P, _I, _I, _I, _I, _P, _P, _P, _P, _P, _P, _F, _P, _P, _P, _P]),
     "msplat_batch_alpha_blending_backward": (

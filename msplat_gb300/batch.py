@@ -67,6 +67,9 @@ class _Plan:
         self.B = B
         self.dims = [(int(w), int(h)) for w, h in d]
         self.tiles, self.rows, self.pixels, self.depth_items, self.passes = (int(x) for x in sizes)
+        # digit bits of the last tile-key pass: local keys span [1, largest camera's tile count]
+        max_tiles = max((-(-w // 16)) * (-(-h // 16)) for w, h in self.dims)
+        self.last_pass_bits = max(1, int(max_tiles).bit_length() - 8 * (self.passes - 1))
         self.row_off = np.concatenate([[0], np.cumsum(n.astype(np.int64))]).tolist()
         self.pix_off = np.concatenate([[0], np.cumsum(d[:, 0].astype(np.int64) * d[:, 1])]).tolist()
         self.device = torch.from_numpy(host).to(dev)
@@ -139,9 +142,10 @@ def _sort(lib, plan, uv, depth, radius, conic, opacity, capacity, status, dev, s
     tr = torch.empty((plan.tiles, 2), dtype=torch.int32, device=dev)
     ws = _lib.workspace(lib.msplat_batch_sort_finish_workspace_size(B, cap, plan.passes), dev)
     with _lib.stage("sort_gaussian_finish"):
-        _lib.check(lib.msplat_batch_sort_finish(
-            _lib.ptr(plan.device), B, plan.depth_items, plan.tiles, plan.passes, cap, _lib.ptr(ws_prep),
-            _lib.ptr(idx), _lib.ptr(tr), _lib.ptr(status), _lib.ptr(ws), ws.numel(), st), "batch_sort_finish")
+        _lib.check(lib.msplat_batch_sort_finish_bits(
+            _lib.ptr(plan.device), B, plan.depth_items, plan.tiles, plan.passes, plan.last_pass_bits, cap,
+            _lib.ptr(ws_prep), _lib.ptr(idx), _lib.ptr(tr), _lib.ptr(status), _lib.ptr(ws), ws.numel(), st),
+            "batch_sort_finish")
     return idx, tr
 
 

@@ -407,10 +407,10 @@ extern "C" size_t msplat_batch_sort_finish_workspace_size(int B, int64_t capacit
     return z.s.used;
 }
 
-extern "C" int msplat_batch_sort_finish(const void *plan, int B, int64_t depth_items, int total_tiles, int passes,
-                                        int64_t capacity, const void *prepare_workspace, int32_t *idx_sorted,
-                                        int32_t *tile_range, int32_t *status, void *workspace,
-                                        size_t workspace_bytes, msplat_stream_t stream) {
+static int batch_sort_finish(const void *plan, int B, int64_t depth_items, int total_tiles, int passes,
+                             int last_pass_bits, int64_t capacity, const void *prepare_workspace,
+                             int32_t *idx_sorted, int32_t *tile_range, int32_t *status, void *workspace,
+                             size_t workspace_bytes, cudaStream_t stream) {
     if (B <= 0 || depth_items < 0 || depth_items % kSortTile != 0 || total_tiles < 0 || passes <= 0 ||
         passes > 4 || capacity < 0)
         return set_error(MSPLAT_ERR_INVALID_ARGUMENT, "batch_sort_finish: bad sizes");
@@ -453,9 +453,29 @@ extern "C" int msplat_batch_sort_finish(const void *plan, int B, int64_t depth_i
     segs.nseg = B;
     uint32_t *kout = even ? f.ka : f.kb;
     int st = radix_sort_segmented<uint32_t>(ntiles, segs, 0, passes, f.ka, vemit, kout, out, even ? f.kb : f.ka,
-                                            f.vt, f.rb, stream);
+                                            f.vt, f.rb, stream, last_pass_bits);
     if (st) return st;
     launch(batch_range_kernel, (unsigned)ceil_div64(capacity / 8, 256), 256, 0, stream, pv, ntiles,
            (const int32_t *)f.seg_start, (const int64_t *)f.seg_count, (const uint32_t *)kout, (int2 *)tile_range);
     return check_launch("batch_sort_finish");
+}
+
+extern "C" int msplat_batch_sort_finish(const void *plan, int B, int64_t depth_items, int total_tiles, int passes,
+                                        int64_t capacity, const void *prepare_workspace, int32_t *idx_sorted,
+                                        int32_t *tile_range, int32_t *status, void *workspace,
+                                        size_t workspace_bytes, msplat_stream_t stream) {
+    return batch_sort_finish(plan, B, depth_items, total_tiles, passes, kRadixBits, capacity, prepare_workspace,
+                             idx_sorted, tile_range, status, workspace, workspace_bytes, stream);
+}
+
+extern "C" int msplat_batch_sort_finish_bits(const void *plan, int B, int64_t depth_items, int total_tiles,
+                                             int passes, int last_pass_bits, int64_t capacity,
+                                             const void *prepare_workspace, int32_t *idx_sorted,
+                                             int32_t *tile_range, int32_t *status, void *workspace,
+                                             size_t workspace_bytes, msplat_stream_t stream) {
+    if (last_pass_bits < 1 || last_pass_bits > kRadixBits)
+        return set_error(MSPLAT_ERR_INVALID_ARGUMENT, "batch_sort_finish_bits: last_pass_bits = %d not in 1..8",
+                         last_pass_bits);
+    return batch_sort_finish(plan, B, depth_items, total_tiles, passes, last_pass_bits, capacity, prepare_workspace,
+                             idx_sorted, tile_range, status, workspace, workspace_bytes, stream);
 }

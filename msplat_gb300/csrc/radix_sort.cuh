@@ -790,20 +790,34 @@ int radix_sort_segmented(int ntiles, const SortSegs &segs, int begin_bit, int pa
     const uint32_t *vsrc = vin;
     auto down = radix_downsweep_kernel<K, false, false, true>;
     cudaFuncSetAttribute(down, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    (void)last_bits;  // (the segmented passes rank all 8 bits)
     for (int p = 0; p < passes; ++p) {
         const int shift = begin_bit + p * kRadixBits;
         const bool to_out = ((passes - 1 - p) & 1) == 0;
         K *kdst = to_out ? kout : ktmp;
         uint32_t *vdst = to_out ? vout : vtmp;
         uint32_t *tot = b.totals + (size_t)p * segs.nseg * kRadix;
-        const int nd = kRadix;
+        // digits the pass can meet (as radix_sort_pairs: 5-7 bits specialised, fewer round up to 5)
+        int dbits = p == passes - 1 ? last_bits : kRadixBits;
+        if (dbits < 1 || dbits > kRadixBits) dbits = kRadixBits;
+        else if (dbits < 5) dbits = 5;
+        const int nd = 1 << dbits;
         launch(radix_upsweep_kernel<K, false, true>, ntiles, kSortThreads, 0, stream, ksrc, (int64_t)0, shift,
                ntiles, b.hist, (const int64_t *)nullptr, nd, segs);
         launch(radix_rowscan_warp_kernel, (unsigned)ceil_div64((int64_t)nd * segs.nseg, 8), 256, 0, stream,
                b.hist, tot, ntiles, nd, segs);
-        launch(down, ntiles, kSortThreads, smem, stream, ksrc, vsrc, kdst, vdst, (int64_t)0, shift, ntiles, b.hist,
-               (const uint32_t *)tot, (const int64_t *)nullptr, segs);
+#define MSPLAT_SEG_DOWN(DBV)                                                                                    \
+    do {                                                                                                        \
+        auto kd = radix_downsweep_kernel<K, false, false, true, DBV>;                                           \
+        cudaFuncSetAttribute(kd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);                       \
+        launch(kd, ntiles, kSortThreads, smem, stream, ksrc, vsrc, kdst, vdst, (int64_t)0, shift, ntiles, b.hist, \
+               (const uint32_t *)tot, (const int64_t *)nullptr, segs);                                          \
+    } while (0)
+        if (dbits == 5) MSPLAT_SEG_DOWN(5);
+        else if (dbits == 6) MSPLAT_SEG_DOWN(6);
+        else if (dbits == 7) MSPLAT_SEG_DOWN(7);
+        else launch(down, ntiles, kSortThreads, smem, stream, ksrc, vsrc, kdst, vdst, (int64_t)0, shift, ntiles,
+                    b.hist, (const uint32_t *)tot, (const int64_t *)nullptr, segs);
+#undef MSPLAT_SEG_DOWN
         ksrc = kdst;
         vsrc = vdst;
     }
