@@ -22,8 +22,6 @@
 //   sign-extended keys the reference sorts first and keeps out of every
 //   range, get tile key 0 so they lead idx_sorted in depth order as there
 //   (the reference writes their range out of bounds; we skip that write).
-#include <mutex>
-
 #include "cull.cuh"
 #include "emit.cuh"
 #include "radix_sort.cuh"
@@ -434,30 +432,17 @@ extern "C" int msplat_inclusive_scan_i32(int n, const int32_t *in, int32_t *out,
 // Scratch of msplat_inclusive_scan_i32_noalloc: the partial sums of a scan of
 // up to MSPLAT_SCAN_NOALLOC_MAX_N elements, one int64 per 4096-element tile
 // plus one (131 KB).  Host code cannot use the symbol as a device address;
-// noalloc_scan_parts() looks the address up once per device.
+// noalloc_scan_parts() looks the address up.
 constexpr int kNoAllocScanParts = MSPLAT_SCAN_NOALLOC_MAX_N / kScanTile + 1;
 static __device__ __align__(256) int64_t g_noalloc_scan_parts[kNoAllocScanParts];
 
-// Device address of g_noalloc_scan_parts on the current device (looked up
-// with cudaGetSymbolAddress the first time each device is seen).
+// Device address of g_noalloc_scan_parts in the current context, looked up
+// on every call (no allocation; a cached address would go stale when a
+// device reset reloads the module).
 static int64_t *noalloc_scan_parts(cudaError_t *err) {
-    static std::mutex mu;
-    static int64_t *addr[128] = {nullptr};
-    int dev = 0;
-    *err = cudaGetDevice(&dev);
-    if (*err != cudaSuccess) return nullptr;
-    if (dev < 0 || dev >= 128) {
-        *err = cudaErrorInvalidDevice;
-        return nullptr;
-    }
-    std::lock_guard<std::mutex> lock(mu);
-    if (!addr[dev]) {
-        void *p = nullptr;
-        *err = cudaGetSymbolAddress(&p, g_noalloc_scan_parts);
-        if (*err != cudaSuccess) return nullptr;
-        addr[dev] = static_cast<int64_t *>(p);
-    }
-    return addr[dev];
+    void *p = nullptr;
+    *err = cudaGetSymbolAddress(&p, g_noalloc_scan_parts);
+    return *err == cudaSuccess ? static_cast<int64_t *>(p) : nullptr;
 }
 
 extern "C" int msplat_inclusive_scan_i32_noalloc(int n, const int32_t *in, int32_t *out, int64_t *total,
