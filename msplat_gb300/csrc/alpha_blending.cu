@@ -446,6 +446,153 @@ blend_bwd_kernel(int P, int C, int c0, const float2 *__restrict__ uv, const floa
 
 
 // ===================================================================
+// Backward for 4 < C <= CMAX channels in one walk.  The pair's geometry, its
+// transmittance and the colour recursion are evaluated once per pair for
+// all channels -- the recursion carried as two scalars, as in the C <= 4
+// kernels (the reference's per-channel accum_rec enters dL/dalpha only
+// through its dot product with dL/dpix) -- and the gradients go out in
+// groups of 16 values per warp reduce-scatter: the six geometry gradients
+// with the first 10 colour channels, then 16 channels at a time.  (Walking
+// the list once per 10 channels, as blend_bwd_kernel does, repeats the
+// pair's geometry and recursion per chunk.)  A pixel past its last
+// contributor, or where the pair's alpha is below 1/255, adds zeros.
+// ===================================================================
+template <int CMAX>
+inline size_t blend_bwd_wide_smem() {
+    return (size_t)kBatch * (sizeof(BlendRec) + sizeof(int)) + (size_t)CMAX * kBatch * sizeof(float);
+}
+
+template <int CMAX, bool BATCH = false>
+__global__ void __launch_bounds__(kBlendThreads)
+blend_bwd_wide_kernel(int P, int C, const float2 *__restrict__ uv, const float *__restrict__ conic,
+                      const float *__restrict__ opacity, const float *__restrict__ feature,
+                      const int32_t *__restrict__ idx_sorted, const int2 *__restrict__ tile_range, float bg, int W,
+                      int H, const float *__restrict__ final_T, const int32_t *__restrict__ ncontrib,
+                      const float *__restrict__ dL_dout, float *__restrict__ dL_duv, float *__restrict__ dL_dconic,
+                      float *__restrict__ dL_dopacity, float *__restrict__ dL_dfeature, BlendBatch bb) {
+    extern __shared__ __align__(16) unsigned char wide_raw[];
+    BlendRec *srec = reinterpret_cast<BlendRec *>(wide_raw);
+    int *sgid = reinterpret_cast<int *>(srec + kBatch);
+    float *sfeat = reinterpret_cast<float *>(sgid + kBatch);  // [CMAX][kBatch]
+    __shared__ int swarp[kBlendThreads / 32];
+    __shared__ int smax;
+    const BlendSite site = blend_site<BATCH, 1>(bb, P, W, H);
+    if (BATCH) {
+        W = site.W;
+        H = site.H;
+        uv += site.row_off;
+        conic += 3 * site.row_off;
+        opacity += site.op_off;
+        feature += (size_t)C * site.feat_off;
+        final_T += site.pix_off;
+        ncontrib += site.pix_off;
+        dL_dout += (size_t)C * site.pix_off;
+        dL_duv += 2 * site.row_off;
+        dL_dconic += 3 * site.row_off;
+        dL_dopacity += site.row_off;
+        dL_dfeature += (size_t)C * site.row_off;
+    }
+    const int px = site.tx * kTile + (threadIdx.x & (kTile - 1));
+    const int py = site.ty * kTile + (threadIdx.x >> 4);
+    const bool inside = px < W && py < H;
+    const float fx = (float)px, fy = (float)py;
+    const float bx0 = (float)(site.tx * kTile), by0 = (float)(site.ty * kTile);
+    const int2 range = tile_range[site.tidx];
+    const int pix = py * W + px;
+    const int lane = threadIdx.x & 31;
+
+    const float T_final = inside ? final_T[pix] : 0.0f;
+    const int last = inside ? ncontrib[pix] : 0;
+    float T = T_final, ad = 0.0f, lfd = 0.0f, la = 0.0f;
+    float dpix[CMAX];
+    float bg_dot = 0.0f;
+#pragma unroll
+    for (int q = 0; q < CMAX; ++q) {
+        dpix[q] = (inside && q < C) ? dL_dout[(size_t)q * H * W + pix] : 0.0f;
+        bg_dot += bg * dpix[q];
+    }
+
+    // Nothing past the tile's largest ncontrib contributes.
+    if (threadIdx.x == 0) smax = 0;
+    __syncthreads();
+    int wmax = last;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) wmax = max(wmax, __shfl_xor_sync(0xffffffffu, wmax, o));
+    if (lane == 0) atomicMax(&smax, wmax);
+    __syncthreads();
+    const int end = range.x + min(smax, range.y - range.x);
+
+    for (int bend = end; bend > range.x; bend -= kBatch) {
+        const int bstart = max(range.x, bend - kBatch);
+        const int j = bend - 1 - (int)threadIdx.x;
+        const int n = gather_batch<CMAX>(j >= bstart, j, site.P, idx_sorted, uv, conic, opacity, feature, C, 0, C,
+                                         bx0, by0, srec, sfeat, sgid, swarp);
+        for (int k = 0; k < n; ++k) {
+            const BlendRec r = srec[k];
+            const int jl = __float_as_int(r.b.w) - range.x;  // list position
+            const float dx = r.a.x - fx, dy = r.a.y - fy;
+            const float ca = r.a.z, cb = r.a.w, cc = r.b.x, op = r.b.y;
+            const float power = -0.5f * (ca * dx * dx + cc * dy * dy) - cb * dx * dy;
+            const float G = __expf(power);
+            const float alpha = fminf(0.99f, op * G);
+            const bool ok = jl < last && power <= 0.0f && !(alpha < 1.0f / 255.0f);
+            if (!__any_sync(0xffffffffu, ok)) continue;
+            const float inv1m = __fdividef(1.f, 1.f - alpha);
+            const float Tn = T * inv1m;
+            const float dcol = ok ? alpha * Tn : 0.0f;
+            float fd = 0.0f;  // colour . dL/dpix
+#pragma unroll
+            for (int q = 0; q < CMAX; ++q)
+                if (q < C) fd += sfeat[q * kBatch + k] * dpix[q];
+            const float adn = la * lfd + (1.f - la) * ad;
+            float dL_dalpha = (fd - adn) * Tn;
+            dL_dalpha += (-T_final * inv1m) * bg_dot;
+            const float dL_dG = ok ? op * dL_dalpha : 0.0f;
+            const float gdx = -G * dx * ca - G * dy * cb;
+            const float gdy = -G * dy * cc - G * dx * cb;
+            float v[16];
+            v[0] = dL_dG * gdx;
+            v[1] = dL_dG * gdy;
+            v[2] = -0.5f * G * dx * dx * dL_dG;
+            v[3] = -G * dx * dy * dL_dG;
+            v[4] = -0.5f * G * dy * dy * dL_dG;
+            v[5] = ok ? G * dL_dalpha : 0.0f;
+#pragma unroll
+            for (int i = 0; i < 10; ++i) v[6 + i] = dcol * dpix[i];
+            T = ok ? Tn : T;
+            ad = ok ? adn : ad;
+            lfd = ok ? fd : lfd;
+            la = ok ? alpha : la;
+            const int g = sgid[k];
+            {
+                const float s = warp_reduce_scatter16(v);
+                const int vi = lane >> 1;
+                if ((lane & 1) == 0 && vi < 6 + min(10, C)) {
+                    float *dst;
+                    if (vi < 2) dst = dL_duv + 2 * g + vi;
+                    else if (vi < 5) dst = dL_dconic + 3 * g + (vi - 2);
+                    else if (vi == 5) dst = dL_dopacity + g;
+                    else dst = dL_dfeature + (size_t)g * C + (vi - 6);
+                    atomicAdd(dst, s);
+                }
+            }
+#pragma unroll
+            for (int q0 = 10; q0 < CMAX; q0 += 16) {
+                if (q0 < C) {  // (uniform)
+                    float w[16];
+#pragma unroll
+                    for (int i = 0; i < 16; ++i) w[i] = q0 + i < CMAX ? dcol * dpix[q0 + i] : 0.0f;
+                    const float s = warp_reduce_scatter16(w);
+                    const int vi = lane >> 1;
+                    if ((lane & 1) == 0 && q0 + vi < C) atomicAdd(dL_dfeature + (size_t)g * C + q0 + vi, s);
+                }
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// ===================================================================
 // Several pixels per thread, C <= 4 channels (the common RGB case).
 //
 // A thread owns NPIX pixels of one tile column (rows ly, ly + 16/NPIX, ...),
@@ -1557,6 +1704,30 @@ constexpr int kSplitFwd = MSPLAT_BLEND_SPLIT_FWD, kSplitBwd = MSPLAT_BLEND_SPLIT
 // The forward's entry masks carry over to the backward when both render whole tiles.
 constexpr bool kEntryMasks = kSplitFwd == 1 && kSplitBwd == 1;
 
+
+// The one-walk backward for 4 < C <= 64 (blend_bwd_wide_kernel): the
+// smallest channel capacity that holds C.
+template <bool BATCH>
+inline void launch_bwd_wide(int C, dim3 grid, cudaStream_t stream, int P, const float2 *uv, const float *conic,
+                            const float *opacity, const float *feature, const int32_t *idx, const int2 *tr, float bg,
+                            int W, int H, const float *fT, const int32_t *nci, const float *dout, float *duv,
+                            float *dcon, float *dop, float *dfeat, const BlendBatch &bb) {
+#define MSPLAT_WIDE(CM)                                                                                          \
+    do {                                                                                                         \
+        const size_t smem = blend_bwd_wide_smem<CM>();                                                           \
+        cudaFuncSetAttribute(blend_bwd_wide_kernel<CM, BATCH>, cudaFuncAttributeMaxDynamicSharedMemorySize,       \
+                             (int)smem);                                                                         \
+        launch(blend_bwd_wide_kernel<CM, BATCH>, grid, kBlendThreads, smem, stream, P, C, uv, conic, opacity,      \
+               feature, idx, tr, bg, W, H, fT, nci, dout, duv, dcon, dop, dfeat, bb);                            \
+    } while (0)
+    if (C <= 16) MSPLAT_WIDE(16);
+    else if (C <= 32) MSPLAT_WIDE(32);
+    else if (C <= 40) MSPLAT_WIDE(40);
+    else MSPLAT_WIDE(64);
+#undef MSPLAT_WIDE
+}
+constexpr int kWideMaxC = 64;  // channels of the one-walk backward; more go through chunked walks
+
 template <int C>
 void launch_small(bool bwd, dim3 grid, cudaStream_t stream, int P, const float2 *uv, const float *conic,
                   const float *opacity, const float *feature, const int32_t *idx, const int2 *tr, float bg, int W,
@@ -1670,6 +1841,12 @@ static int blend_backward(int P, int C, const float *uv, const float *conic, con
                        (const int2 *)tile_range, bg, W, H, nullptr, nullptr, nullptr, final_T, ncontrib, dL_dout,
                        dL_duv, dL_dconic, dL_dopacity, dL_dfeature, const_cast<unsigned char *>(entry_masks));
         launch(blend_grad_finish_kernel, ceil_div(P, 256), 256, 0, stream, P, conic, opacity, dL_duv, dL_dconic);
+        return check_launch("alpha_blending_backward");
+    }
+    if (C <= kWideMaxC) {
+        launch_bwd_wide<false>(C, grid, stream, P, (const float2 *)uv, conic, opacity, feature, idx_sorted,
+                               (const int2 *)tile_range, bg, W, H, final_T, ncontrib, dL_dout, dL_duv, dL_dconic,
+                               dL_dopacity, dL_dfeature, BlendBatch{});
         return check_launch("alpha_blending_backward");
     }
     for (int c0 = 0; c0 < C; c0 += kBwdC)
@@ -1828,6 +2005,12 @@ static int batch_blend_backward(const void *plan, int B, int total_tiles, int64_
                              dL_duv, dL_dconic, dL_dopacity, dL_dfeature, const_cast<unsigned char *>(entry_masks));
         launch(batch_blend_grad_finish_kernel, (unsigned)ceil_div64(rows, 256), 256, 0, stream, bb.pv, rows, conic,
                opacity, dL_duv, dL_dconic);
+        return check_launch("batch_alpha_blending_backward");
+    }
+    if (C <= kWideMaxC) {
+        launch_bwd_wide<true>(C, dim3(total_tiles), stream, 0, (const float2 *)uv, conic, opacity, feature, idx_sorted,
+                              (const int2 *)tile_range, bg, 1, 1, final_T, ncontrib, dL_dout, dL_duv, dL_dconic,
+                              dL_dopacity, dL_dfeature, bb);
         return check_launch("batch_alpha_blending_backward");
     }
     for (int c0 = 0; c0 < C; c0 += kBwdC)
