@@ -226,7 +226,7 @@ blend_fwd_kernel(int P, int C, int c0, const float2 *__restrict__ uv, const floa
                  int W, int H, float *__restrict__ out, float *__restrict__ final_T,
                  int32_t *__restrict__ ncontrib, BlendBatch bb = {}) {
     __shared__ BlendRec srec[kBatch];
-    __shared__ float sfeat[CMAX * kBatch];
+    extern __shared__ float sfeat[];  // [CMAX][kBatch] (dynamic: up to 64 KB)
     __shared__ int sgid[kBatch];
     __shared__ int swarp[kBlendThreads / 32];
     const int nc = min(CMAX, C - c0);
@@ -1705,6 +1705,34 @@ constexpr int kSplitFwd = MSPLAT_BLEND_SPLIT_FWD, kSplitBwd = MSPLAT_BLEND_SPLIT
 constexpr bool kEntryMasks = kSplitFwd == 1 && kSplitBwd == 1;
 
 
+// The forward for C > 4: one walk over the list when the channels fit 64
+// (the smallest of 16 / 32 / 40 / 64 that holds them), else walks of 32
+// channels.  Every channel's colour is the same sum either way.
+template <bool BATCH>
+inline void launch_fwd_general(int C, dim3 grid, cudaStream_t stream, int P, const float2 *uv, const float *conic,
+                               const float *opacity, const float *feature, const int32_t *idx, const int2 *tr,
+                               float bg, int W, int H, float *out, float *final_T, int32_t *nc,
+                               const BlendBatch &bb) {
+#define MSPLAT_FWDG(CM, C0)                                                                                      \
+    do {                                                                                                         \
+        const size_t smem = (size_t)CM * kBatch * sizeof(float);                                                 \
+        cudaFuncSetAttribute(blend_fwd_kernel<CM, BATCH>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); \
+        launch(blend_fwd_kernel<CM, BATCH>, grid, kBlendThreads, smem, stream, P, C, C0, uv, conic, opacity,       \
+               feature, idx, tr, bg, W, H, out, final_T, nc, bb);                                                \
+    } while (0)
+    if (C <= 16) MSPLAT_FWDG(16, 0);
+    else if (C <= 32) MSPLAT_FWDG(32, 0);
+    else if (C <= 40) MSPLAT_FWDG(40, 0);
+    else if (C <= 64) MSPLAT_FWDG(64, 0);
+    else
+        for (int c0 = 0; c0 < C; c0 += 32) {
+            if (C - c0 <= 4) MSPLAT_FWDG(4, c0);
+            else if (C - c0 <= 16) MSPLAT_FWDG(16, c0);
+            else MSPLAT_FWDG(32, c0);
+        }
+#undef MSPLAT_FWDG
+}
+
 // The one-walk backward for 4 < C <= 64 (blend_bwd_wide_kernel): the
 // smallest channel capacity that holds C.
 template <bool BATCH>
@@ -1806,21 +1834,9 @@ static int blend_forward(int P, int C, const float *uv, const float *conic, cons
                        nullptr, nullptr, nullptr, nullptr, entry_masks);
         return check_launch("alpha_blending_forward");
     }
-    for (int c0 = 0; c0 < C; c0 += 32) {
-        const int nc = min(32, C - c0);
-        if (nc <= 4)
-            launch(blend_fwd_kernel<4>, grid, kBlendThreads, 0, stream, P, C, c0, (const float2 *)uv, conic, opacity,
-                                                                    feature, idx_sorted, (const int2 *)tile_range,
-                                                                    bg, W, H, out, final_T, ncontrib, BlendBatch{});
-        else if (nc <= 16)
-            launch(blend_fwd_kernel<16>, grid, kBlendThreads, 0, stream, P, C, c0, (const float2 *)uv, conic, opacity,
-                                                                     feature, idx_sorted, (const int2 *)tile_range,
-                                                                     bg, W, H, out, final_T, ncontrib, BlendBatch{});
-        else
-            launch(blend_fwd_kernel<32>, grid, kBlendThreads, 0, stream, P, C, c0, (const float2 *)uv, conic, opacity,
-                                                                     feature, idx_sorted, (const int2 *)tile_range,
-                                                                     bg, W, H, out, final_T, ncontrib, BlendBatch{});
-    }
+    // one walk for up to 64 channels, chunks of 32 beyond
+    launch_fwd_general<false>(C, grid, stream, P, (const float2 *)uv, conic, opacity, feature, idx_sorted,
+                              (const int2 *)tile_range, bg, W, H, out, final_T, ncontrib, BlendBatch{});
     return check_launch("alpha_blending_forward");
 }
 
@@ -1968,21 +1984,8 @@ static int batch_blend_forward(const void *plan, int B, int total_tiles, int C, 
                              nullptr, nullptr, nullptr, entry_masks);
         return check_launch("batch_alpha_blending_forward");
     }
-    for (int c0 = 0; c0 < C; c0 += 32) {
-        const int nc = min(32, C - c0);
-        if (nc <= 4)
-            launch(blend_fwd_kernel<4, true>, total_tiles, kBlendThreads, 0, stream, 0, C, c0, (const float2 *)uv,
-                   conic, opacity, feature, idx_sorted, (const int2 *)tile_range, bg, 1, 1, out, final_T, ncontrib,
-                   bb);
-        else if (nc <= 16)
-            launch(blend_fwd_kernel<16, true>, total_tiles, kBlendThreads, 0, stream, 0, C, c0, (const float2 *)uv,
-                   conic, opacity, feature, idx_sorted, (const int2 *)tile_range, bg, 1, 1, out, final_T, ncontrib,
-                   bb);
-        else
-            launch(blend_fwd_kernel<32, true>, total_tiles, kBlendThreads, 0, stream, 0, C, c0, (const float2 *)uv,
-                   conic, opacity, feature, idx_sorted, (const int2 *)tile_range, bg, 1, 1, out, final_T, ncontrib,
-                   bb);
-    }
+    launch_fwd_general<true>(C, dim3(total_tiles), stream, 0, (const float2 *)uv, conic, opacity, feature,
+                             idx_sorted, (const int2 *)tile_range, bg, 1, 1, out, final_T, ncontrib, bb);
     return check_launch("batch_alpha_blending_forward");
 }
 
