@@ -343,7 +343,7 @@ def blend_inputs(n=10000, W=256, H=256, C=3, seed=0):
     return s, inter, W, H
 
 
-@pytest.mark.parametrize("C", [1, 3, 4, 5, 16, 33, 40])
+@pytest.mark.parametrize("C", [1, 3, 4, 5, 16, 33, 40, 48, 64, 70])
 def test_alpha_blending_forward(C):
     s, it, W, H = blend_inputs(C=C, seed=C)
     bg = 0.25
@@ -382,8 +382,11 @@ def test_alpha_blending_golden():
                                    atol=1e-5 * max(1.0, np.abs(g[key]).max()))
 
 
-@pytest.mark.parametrize("C,bg", [(3, 0.0), (3, 0.7), (13, 0.3), (33, 1.0)])
+@pytest.mark.parametrize("C,bg", [(3, 0.0), (3, 0.7), (13, 0.3), (33, 1.0), (40, 0.2), (64, 0.5), (70, 0.1)])
 def test_alpha_blending_backward(C, bg):
+    """C <= 4: the several-pixels kernels; 4 < C <= 64: one walk over the
+    list for all channels (capacities 16, 32, 40, 64); C > 64: walks of 10
+    channels."""
     s, it, W, H = blend_inputs(n=6000, C=C, seed=20 + C)
     ins = [T(it["uv"]), T(it["conic"]), T(s["opacity"]), T(s["feat"])]
     for a in ins:
