@@ -310,10 +310,11 @@ MSPLAT_API int msplat_set_blend_ring(int producer_warps, int batch_producer_warp
  * everywhere.  Gradients agree up to the order of float atomics.
  * Process-wide. */
 MSPLAT_API int msplat_set_blend_ring_bwd(int producer_warps, int batch_producer_warps);
-/* Every device-side wait -- the ring's hand-offs, the sort's look-back --
- * gives up after `polls` polls of at most about 1 us each (default 2^21,
- * about 2 s), sets a device error word and lets the kernel finish with
- * invalid results instead of hanging.  Process-wide. */
+/* Every device-side wait -- the ring's hand-offs, the sort's look-back,
+ * the SH kernels' wait for a bulk copy of coefficient rows -- gives up
+ * after `polls` polls of at most about 1 us each (default 2^21, about
+ * 2 s), sets a device error word and lets the kernel finish with invalid
+ * results instead of hanging.  Process-wide. */
 MSPLAT_API int msplat_set_wait_limit(int polls);
 /* Reads (after synchronising `stream`) the current device's error words of
  * the bounded waits into *error (1 if any is set; may be NULL), clears them

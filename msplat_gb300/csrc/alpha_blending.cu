@@ -2098,6 +2098,8 @@ int wait_limit_polls() { return g_wait_limit; }
 // The look-back error words of the two translation units that sort.
 cudaError_t sort_wait_error_single(int reset, int *value, cudaStream_t stream);
 cudaError_t sort_wait_error_batch(int reset, int *value, cudaStream_t stream);
+// The bulk-staging error word of the SH kernels.
+cudaError_t sh_wait_error(int reset, int *value, cudaStream_t stream);
 }  // namespace msplat
 
 extern "C" int msplat_wait_error(int reset, int *error, msplat_stream_t stream) {
@@ -2109,13 +2111,14 @@ extern "C" int msplat_wait_error(int reset, int *error, msplat_stream_t stream) 
         e = cudaMemcpyToSymbolAsync(g_wait_error, &zero, sizeof(int), 0, cudaMemcpyHostToDevice, stream);
         if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
     }
-    int s1 = 0, s2 = 0;
+    int s1 = 0, s2 = 0, s3 = 0;
     if (e == cudaSuccess) e = sort_wait_error_single(reset, &s1, stream);
     if (e == cudaSuccess) e = sort_wait_error_batch(reset, &s2, stream);
+    if (e == cudaSuccess) e = sh_wait_error(reset, &s3, stream);
     if (e != cudaSuccess) return set_error(MSPLAT_ERR_LAUNCH, "wait_error: %s", cudaGetErrorString(e));
-    const int any = h | s1 | s2;
+    const int any = h | s1 | s2 | s3;
     if (error) *error = any;
     if (!any) return MSPLAT_OK;
     return set_error(MSPLAT_ERR_TIMEOUT, "a bounded device-side wait gave up (%s)",
-                     h ? "blend ring" : "sort look-back");
+                     h ? "blend ring" : (s1 | s2) ? "sort look-back" : "SH bulk staging");
 }

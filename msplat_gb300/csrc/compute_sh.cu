@@ -18,13 +18,105 @@
 // bands l >= 4; both are generated so that the direction gradient -- which
 // sees the off-sphere shape -- matches the reference as well.
 //
-// Coefficients are staged per block into shared memory with coalesced
-// loads (rows padded to an odd stride against bank conflicts); the
-// backward overwrites each row in place with dL/dsh and streams it out.
+// Coefficients are staged per block into shared memory; the backward
+// overwrites each row in place with dL/dsh and streams it out.  When a row
+// holds an odd number of floats (C * D odd: an even degree and an odd
+// channel count, e.g. degree 10 with 3 colours) thread t's word t*CD + k
+// falls in a different bank for each of 32 threads without padding, so the
+// block's chunk of contiguous rows arrives as ONE bulk copy
+// (cp.async.bulk, completing on an mbarrier) and the backward's gradient
+// rows leave as one: the whole chunk (up to 48 KB) is in flight at once.
+// Otherwise the rows are padded to an odd stride and moved by a coalesced
+// thread loop.
 #include "sh_basis.cuh"
 #include "sh_dispatch.cuh"
 
 namespace msplat {
+
+// ---- bulk staging ----------------------------------------------------------
+// The wait for a bulk copy is bounded like every other device-side wait:
+// after `limit` polls (each suspends for at most kShWaitHintNs) the thread
+// sets g_sh_wait_error, which the host reads through msplat_wait_error, and
+// the block waits once more, for at most kShDrainPolls polls whatever the
+// limit, for its copy before it leaves without computing.
+static __device__ int g_sh_wait_error;
+constexpr uint32_t kShWaitHintNs = 1000;
+constexpr int kShDrainPolls = 1 << 21;  // about 2 s at most
+
+int wait_limit_polls();  // process-wide poll limit (msplat_set_wait_limit)
+
+#ifndef MSPLAT_SH_BULK
+#define MSPLAT_SH_BULK 1  // bulk copies for odd row lengths (0: the thread loop for all)
+#endif
+#ifndef MSPLAT_SH_BULK_KB
+#define MSPLAT_SH_BULK_KB 48  // bytes of rows per block on the bulk path (32 Gaussians at degree 10, C = 3)
+#endif
+
+__device__ __forceinline__ uint32_t sh_smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ bool sh_bulk_wait(uint32_t bar, int limit) {
+    for (int it = 0; it < limit; ++it) {
+        uint32_t ok;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0, %2;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}"
+            : "=r"(ok)
+            : "r"(bar), "r"(kShWaitHintNs)
+            : "memory");
+        if (ok) return true;
+    }
+    atomicExch(&g_sh_wait_error, 1);
+    return false;
+}
+
+// The mbarrier of a bulk-staged chunk sits after the rows of `cap` floats.
+__device__ __forceinline__ uint64_t *sh_bulk_bar(float *rows, int cap) {
+    return reinterpret_cast<uint64_t *>(rows + ((cap + 1) & ~1));
+}
+
+// Copies `total` contiguous floats from global (16-byte aligned) into
+// shared memory: the largest multiple of 4 by one bulk copy that thread 0
+// starts, the rest by plain loads.  Returns (the same in every thread)
+// whether the data arrived; the caller leaves without computing if not.
+__device__ __forceinline__ bool stage_rows_bulk(float *dst, const float *__restrict__ src, int total, int cap,
+                                                int limit) {
+    const uint32_t bar = sh_smem_u32(sh_bulk_bar(dst, cap));
+    const int nv = total & ~3;
+    if (threadIdx.x == 0 && nv > 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n\t}" ::"r"(bar),
+                     "r"(nv * 4)
+                     : "memory");
+        asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                         sh_smem_u32(dst)),
+                     "l"(src), "r"(nv * 4), "r"(bar)
+                     : "memory");
+    }
+    for (int e = nv + threadIdx.x; e < total; e += blockDim.x) dst[e] = __ldcs(src + e);
+    __syncthreads();  // the barrier is initialised before any thread polls it
+    const bool ok = nv == 0 || sh_bulk_wait(bar, limit);
+    if (__syncthreads_and(ok)) return true;
+    if (!ok) sh_bulk_wait(bar, kShDrainPolls);  // the copy may still be writing this block's shared memory
+    return false;
+}
+
+// Writes `total` floats of shared memory back to global (16-byte aligned):
+// one bulk copy from thread 0 for the largest multiple of 4, plain stores
+// for the rest.  Every thread of the block calls it after its last write.
+__device__ __forceinline__ void unstage_rows_bulk(float *__restrict__ dst, const float *src, int total) {
+    const int nv = total & ~3;
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // this thread's writes, seen by the copy
+    __syncthreads();
+    if (threadIdx.x == 0 && nv > 0) {
+        asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(dst), "r"(sh_smem_u32(src)),
+                     "r"(nv * 4)
+                     : "memory");
+        asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+        asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");  // shared memory stays until it is read
+    }
+    for (int e = nv + threadIdx.x; e < total; e += blockDim.x) __stcs(dst + e, src[e]);
+}
 
 // Direction of point p and whether it is visible; n = |x - c| in camera mode.
 template <bool CAM>
@@ -47,16 +139,20 @@ __device__ __forceinline__ bool sh_direction(const ShDirs &in, int p, const floa
     return true;
 }
 
-template <int DEG, bool CAM>
+template <int DEG, bool CAM, bool BULK>
 __global__ void sh_fwd_kernel(int P, int C, const float *__restrict__ shs, ShDirs in,
-                              float *__restrict__ value) {
+                              float *__restrict__ value, int wait_limit) {
     constexpr int D = (DEG + 1) * (DEG + 1);
-    extern __shared__ float smem[];
-    const int CD = C * D, stride = CD | 1;
+    extern __shared__ __align__(16) float smem[];
+    const int CD = C * D, stride = BULK ? CD : (CD | 1);
     const int p0 = blockIdx.x * blockDim.x;
     const int n = min((int)blockDim.x, P - p0);
-    stage_rows(smem, shs + (size_t)p0 * CD, n, CD, stride);
-    __syncthreads();
+    if (BULK) {
+        if (!stage_rows_bulk(smem, shs + (size_t)p0 * CD, n * CD, (int)blockDim.x * CD, wait_limit)) return;
+    } else {
+        stage_rows(smem, shs + (size_t)p0 * CD, n, CD, stride);
+        __syncthreads();
+    }
     const int t = threadIdx.x;
     if (t >= n) return;
     const int p = p0 + t;
@@ -80,17 +176,21 @@ __global__ void sh_fwd_kernel(int P, int C, const float *__restrict__ shs, ShDir
     }
 }
 
-template <int DEG, bool CAM>
+template <int DEG, bool CAM, bool BULK>
 __global__ void sh_bwd_kernel(int P, int C, const float *__restrict__ shs, ShDirs in,
                               const float *__restrict__ dL_dval, float *__restrict__ dL_dshs,
-                              float *__restrict__ dL_ddirs) {
+                              float *__restrict__ dL_ddirs, int wait_limit) {
     constexpr int D = (DEG + 1) * (DEG + 1);
-    extern __shared__ float smem[];
-    const int CD = C * D, stride = CD | 1;
+    extern __shared__ __align__(16) float smem[];
+    const int CD = C * D, stride = BULK ? CD : (CD | 1);
     const int p0 = blockIdx.x * blockDim.x;
     const int n = min((int)blockDim.x, P - p0);
-    stage_rows(smem, shs + (size_t)p0 * CD, n, CD, stride);
-    __syncthreads();
+    if (BULK) {
+        if (!stage_rows_bulk(smem, shs + (size_t)p0 * CD, n * CD, (int)blockDim.x * CD, wait_limit)) return;
+    } else {
+        stage_rows(smem, shs + (size_t)p0 * CD, n, CD, stride);
+        __syncthreads();
+    }
     const int t = threadIdx.x;
     if (t < n) {
         const int p = p0 + t;
@@ -141,27 +241,34 @@ __global__ void sh_bwd_kernel(int P, int C, const float *__restrict__ shs, ShDir
             in.dxyz[3 * p + 2] = gv[2];
         }
     }
-    __syncthreads();
-    unstage_rows(dL_dshs + (size_t)p0 * CD, smem, n, CD, stride);
+    if (BULK) {
+        unstage_rows_bulk(dL_dshs + (size_t)p0 * CD, smem, n * CD);
+    } else {
+        __syncthreads();
+        unstage_rows(dL_dshs + (size_t)p0 * CD, smem, n, CD, stride);
+    }
 }
 
-template <int DEG>
-int sh_launch(bool backward, int P, int C, const float *shs, const ShDirs &in, const float *dval, float *out,
-              float *ddirs, cudaStream_t stream) {
-    constexpr int D = (DEG + 1) * (DEG + 1);
-    const int CD = C * D;
-    const int nt = sh_block_points(CD);
-    const size_t smem = (size_t)nt * (CD | 1) * sizeof(float);
-    if (smem > 200 * 1024)
-        return set_error(MSPLAT_ERR_UNSUPPORTED, "compute_sh: C*D = %d too large", CD);
-    const int blocks = ceil_div(P, nt);
-#define MSPLAT_SH_GO(CAM)                                                                                     \
-    if (!backward) {                                                                                          \
-        cudaFuncSetAttribute(sh_fwd_kernel<DEG, CAM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); \
-        launch(sh_fwd_kernel<DEG, CAM>, blocks, nt, smem, stream, P, C, shs, in, out);                        \
-    } else {                                                                                                  \
-        cudaFuncSetAttribute(sh_bwd_kernel<DEG, CAM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); \
-        launch(sh_bwd_kernel<DEG, CAM>, blocks, nt, smem, stream, P, C, shs, in, dval, out, ddirs);           \
+// Points per block on the bulk path: a power of two (32..256, a multiple of
+// 4 so that every chunk but the last starts 16-byte aligned) whose rows fit
+// in MSPLAT_SH_BULK_KB.
+inline int sh_bulk_block_points(int CD) {
+    int nt = 256;
+    while (nt > 32 && (size_t)nt * CD * sizeof(float) > (size_t)MSPLAT_SH_BULK_KB * 1024) nt >>= 1;
+    return nt;
+}
+
+template <int DEG, bool BULK>
+void sh_go(bool backward, int blocks, int nt, size_t smem, int P, int C, const float *shs, const ShDirs &in,
+           const float *dval, float *out, float *ddirs, cudaStream_t stream) {
+    const int limit = wait_limit_polls();
+#define MSPLAT_SH_GO(CAM)                                                                                           \
+    if (!backward) {                                                                                                \
+        cudaFuncSetAttribute(sh_fwd_kernel<DEG, CAM, BULK>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); \
+        launch(sh_fwd_kernel<DEG, CAM, BULK>, blocks, nt, smem, stream, P, C, shs, in, out, limit);                 \
+    } else {                                                                                                        \
+        cudaFuncSetAttribute(sh_bwd_kernel<DEG, CAM, BULK>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); \
+        launch(sh_bwd_kernel<DEG, CAM, BULK>, blocks, nt, smem, stream, P, C, shs, in, dval, out, ddirs, limit);    \
     }
     if (in.xyz) {
         MSPLAT_SH_GO(true)
@@ -169,7 +276,43 @@ int sh_launch(bool backward, int P, int C, const float *shs, const ShDirs &in, c
         MSPLAT_SH_GO(false)
     }
 #undef MSPLAT_SH_GO
+}
+
+template <int DEG>
+int sh_launch(bool backward, int P, int C, const float *shs, const ShDirs &in, const float *dval, float *out,
+              float *ddirs, cudaStream_t stream) {
+    constexpr int D = (DEG + 1) * (DEG + 1);
+    const int CD = C * D;
+    if constexpr ((D & 1) != 0 && MSPLAT_SH_BULK) {
+        const bool aligned = ((uintptr_t)shs & 15) == 0 && (!backward || ((uintptr_t)out & 15) == 0);
+        if ((C & 1) && aligned) {
+            const int nt = sh_bulk_block_points(CD);
+            const size_t smem = (size_t)((nt * CD + 1) & ~1) * sizeof(float) + sizeof(uint64_t);
+            if (smem <= 200 * 1024) {
+                sh_go<DEG, true>(backward, ceil_div(P, nt), nt, smem, P, C, shs, in, dval, out, ddirs, stream);
+                return check_launch(backward ? "compute_sh_backward" : "compute_sh_forward");
+            }
+        }
+    }
+    const int nt = sh_block_points(CD);
+    const size_t smem = (size_t)nt * (CD | 1) * sizeof(float);
+    if (smem > 200 * 1024)
+        return set_error(MSPLAT_ERR_UNSUPPORTED, "compute_sh: C*D = %d too large", CD);
+    sh_go<DEG, false>(backward, ceil_div(P, nt), nt, smem, P, C, shs, in, dval, out, ddirs, stream);
     return check_launch(backward ? "compute_sh_backward" : "compute_sh_forward");
+}
+
+cudaError_t sh_wait_error(int reset, int *value, cudaStream_t stream) {
+    int h = 0;
+    cudaError_t e = cudaMemcpyFromSymbolAsync(&h, g_sh_wait_error, sizeof(int), 0, cudaMemcpyDeviceToHost, stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+    if (e == cudaSuccess && reset && h) {
+        const int zero = 0;
+        e = cudaMemcpyToSymbolAsync(g_sh_wait_error, &zero, sizeof(int), 0, cudaMemcpyHostToDevice, stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+    }
+    if (value) *value = h;
+    return e;
 }
 
 int sh_dispatch(bool backward, int P, int C, int D, const float *shs, const ShDirs &in, const float *dval,
