@@ -28,6 +28,8 @@
 // rows leave as one: the whole chunk (up to 48 KB) is in flight at once.
 // Otherwise the rows are padded to an odd stride and moved by a coalesced
 // thread loop.
+#include <algorithm>
+
 #include "sh_basis.cuh"
 #include "sh_dispatch.cuh"
 
@@ -147,20 +149,23 @@ __global__ void sh_fwd_kernel(int P, int C, const float *__restrict__ shs, ShDir
     const int CD = C * D, stride = BULK ? CD : (CD | 1);
     const int p0 = blockIdx.x * blockDim.x;
     const int n = min((int)blockDim.x, P - p0);
+    const int t = threadIdx.x;
+    const int p = p0 + t;
+    // The view direction is read before the rows arrive, so that its
+    // latency overlaps the staging.
+    float cc[3] = {0.f, 0.f, 0.f}, d[3] = {0.f, 0.f, 0.f}, len = 1.f;
+    if (CAM) camera_centre(in.extr, cc);
+    const bool vis = t < n && sh_direction<CAM>(in, p, cc, d, len);
     if (BULK) {
         if (!stage_rows_bulk(smem, shs + (size_t)p0 * CD, n * CD, (int)blockDim.x * CD, wait_limit)) return;
     } else {
         stage_rows(smem, shs + (size_t)p0 * CD, n, CD, stride);
         __syncthreads();
     }
-    const int t = threadIdx.x;
     if (t >= n) return;
-    const int p = p0 + t;
     const float *row = smem + t * stride;
     float *out = value + (size_t)p * C;
-    float cc[3] = {0.f, 0.f, 0.f}, d[3], len;
-    if (CAM) camera_centre(in.extr, cc);
-    if (!sh_direction<CAM>(in, p, cc, d, len)) {
+    if (!vis) {
         for (int c = 0; c < C; ++c) out[c] = 0.f;
         return;
     }
@@ -185,27 +190,39 @@ __global__ void sh_bwd_kernel(int P, int C, const float *__restrict__ shs, ShDir
     const int CD = C * D, stride = BULK ? CD : (CD | 1);
     const int p0 = blockIdx.x * blockDim.x;
     const int n = min((int)blockDim.x, P - p0);
+    const int t = threadIdx.x;
+    const int p = p0 + t;
+    // The view direction and the first channels' dL/dval are read before
+    // the rows arrive, so that their latency overlaps the staging.
+    float cc[3] = {0.f, 0.f, 0.f}, d[3] = {0.f, 0.f, 0.f}, len = 1.f;
+    if (CAM) camera_centre(in.extr, cc);
+    const bool vis = t < n && sh_direction<CAM>(in, p, cc, d, len);
+    float g0[kShChanBlock] = {0.f, 0.f, 0.f, 0.f};
+    if (vis) {
+#pragma unroll
+        for (int cb = 0; cb < kShChanBlock; ++cb)
+            if (cb < C) g0[cb] = dL_dval[(size_t)p * C + cb];
+    }
     if (BULK) {
         if (!stage_rows_bulk(smem, shs + (size_t)p0 * CD, n * CD, (int)blockDim.x * CD, wait_limit)) return;
     } else {
         stage_rows(smem, shs + (size_t)p0 * CD, n, CD, stride);
         __syncthreads();
     }
-    const int t = threadIdx.x;
     if (t < n) {
-        const int p = p0 + t;
         float *row = smem + t * stride;
         float gdx = 0.f, gdy = 0.f, gdz = 0.f;
-        float cc[3] = {0.f, 0.f, 0.f}, d[3], len = 1.f;
-        if (CAM) camera_centre(in.extr, cc);
-        const bool vis = sh_direction<CAM>(in, p, cc, d, len);
         if (!vis) {
             for (int k = 0; k < CD; ++k) row[k] = 0.f;
         } else {
             for (int c0 = 0; c0 < C; c0 += kShChanBlock) {
-                float g[kShChanBlock] = {0.f, 0.f, 0.f, 0.f};
+                float g[kShChanBlock] = {g0[0], g0[1], g0[2], g0[3]};
                 const int nc = min(kShChanBlock, C - c0);
-                for (int cb = 0; cb < nc; ++cb) g[cb] = dL_dval[(size_t)p * C + c0 + cb];
+                if (c0 > 0) {
+#pragma unroll
+                    for (int cb = 0; cb < kShChanBlock; ++cb)
+                        g[cb] = cb < nc ? dL_dval[(size_t)p * C + c0 + cb] : 0.f;
+                }
                 sh_basis<DEG, true>(d[0], d[1], d[2], [&](int i, float Y, float yx, float yy, float yz) {
 #pragma unroll
                     for (int cb = 0; cb < kShChanBlock; ++cb) {
@@ -249,13 +266,12 @@ __global__ void sh_bwd_kernel(int P, int C, const float *__restrict__ shs, ShDir
     }
 }
 
-// Points per block on the bulk path: a power of two (32..256, a multiple of
-// 4 so that every chunk but the last starts 16-byte aligned) whose rows fit
-// in MSPLAT_SH_BULK_KB.
+// Points per block on the bulk path: the most (at most 256) whose rows fit
+// in MSPLAT_SH_BULK_KB, rounded down to a multiple of 4 so that every chunk
+// but the last starts 16-byte aligned; at least 4.
 inline int sh_bulk_block_points(int CD) {
-    int nt = 256;
-    while (nt > 32 && (size_t)nt * CD * sizeof(float) > (size_t)MSPLAT_SH_BULK_KB * 1024) nt >>= 1;
-    return nt;
+    const size_t fit = (size_t)MSPLAT_SH_BULK_KB * 1024 / ((size_t)CD * sizeof(float));
+    return (int)std::max<size_t>(4, std::min<size_t>(256, fit) & ~(size_t)3);
 }
 
 template <int DEG, bool BULK>
