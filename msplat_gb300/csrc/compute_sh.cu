@@ -25,7 +25,7 @@
 // falls in a different bank for each of 32 threads without padding, so the
 // block's chunk of contiguous rows arrives as ONE bulk copy
 // (cp.async.bulk, completing on an mbarrier) and the backward's gradient
-// rows leave as one: the whole chunk (up to 48 KB) is in flight at once.
+// rows leave as one: the whole chunk (24-36 KB) is in flight at once.
 // Otherwise the rows are padded to an odd stride and moved by a coalesced
 // thread loop.
 #include <algorithm>
@@ -50,8 +50,17 @@ int wait_limit_polls();  // process-wide poll limit (msplat_set_wait_limit)
 #ifndef MSPLAT_SH_BULK
 #define MSPLAT_SH_BULK 1  // bulk copies for odd row lengths (0: the thread loop for all)
 #endif
-#ifndef MSPLAT_SH_BULK_KB
-#define MSPLAT_SH_BULK_KB 48  // bytes of rows per block on the bulk path (32 Gaussians at degree 10, C = 3)
+// Bytes of rows per block on the bulk path, forward and backward (degree
+// 10, C = 3: 24 and 16 Gaussians, 6 and 9 one-warp blocks per SM).
+#ifndef MSPLAT_SH_BULK_KB_FWD
+#define MSPLAT_SH_BULK_KB_FWD 36
+#endif
+#ifndef MSPLAT_SH_BULK_KB_BWD
+#define MSPLAT_SH_BULK_KB_BWD 24
+#endif
+// Kernels with the channel count fixed at 3 (colour) for degrees >= 4.
+#ifndef MSPLAT_SH_FIXED_C3
+#define MSPLAT_SH_FIXED_C3 1
 #endif
 
 __device__ __forceinline__ uint32_t sh_smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -141,10 +150,12 @@ __device__ __forceinline__ bool sh_direction(const ShDirs &in, int p, const floa
     return true;
 }
 
-template <int DEG, bool CAM, bool BULK>
-__global__ void sh_fwd_kernel(int P, int C, const float *__restrict__ shs, ShDirs in,
+// FC > 0: the channel count, fixed at compile time (C is then FC).
+template <int DEG, bool CAM, bool BULK, int FC>
+__global__ void sh_fwd_kernel(int P, int C_, const float *__restrict__ shs, ShDirs in,
                               float *__restrict__ value, int wait_limit) {
     constexpr int D = (DEG + 1) * (DEG + 1);
+    const int C = FC > 0 ? FC : C_;
     extern __shared__ __align__(16) float smem[];
     const int CD = C * D, stride = BULK ? CD : (CD | 1);
     const int p0 = blockIdx.x * blockDim.x;
@@ -181,11 +192,12 @@ __global__ void sh_fwd_kernel(int P, int C, const float *__restrict__ shs, ShDir
     }
 }
 
-template <int DEG, bool CAM, bool BULK>
-__global__ void sh_bwd_kernel(int P, int C, const float *__restrict__ shs, ShDirs in,
+template <int DEG, bool CAM, bool BULK, int FC>
+__global__ void sh_bwd_kernel(int P, int C_, const float *__restrict__ shs, ShDirs in,
                               const float *__restrict__ dL_dval, float *__restrict__ dL_dshs,
                               float *__restrict__ dL_ddirs, int wait_limit) {
     constexpr int D = (DEG + 1) * (DEG + 1);
+    const int C = FC > 0 ? FC : C_;
     extern __shared__ __align__(16) float smem[];
     const int CD = C * D, stride = BULK ? CD : (CD | 1);
     const int p0 = blockIdx.x * blockDim.x;
@@ -267,24 +279,24 @@ __global__ void sh_bwd_kernel(int P, int C, const float *__restrict__ shs, ShDir
 }
 
 // Points per block on the bulk path: the most (at most 256) whose rows fit
-// in MSPLAT_SH_BULK_KB, rounded down to a multiple of 4 so that every chunk
-// but the last starts 16-byte aligned; at least 4.
-inline int sh_bulk_block_points(int CD) {
-    const size_t fit = (size_t)MSPLAT_SH_BULK_KB * 1024 / ((size_t)CD * sizeof(float));
+// in `kb` KB, rounded down to a multiple of 4 so that every chunk but the
+// last starts 16-byte aligned; at least 4.
+inline int sh_bulk_block_points(int CD, int kb) {
+    const size_t fit = (size_t)kb * 1024 / ((size_t)CD * sizeof(float));
     return (int)std::max<size_t>(4, std::min<size_t>(256, fit) & ~(size_t)3);
 }
 
-template <int DEG, bool BULK>
+template <int DEG, bool BULK, int FC>
 void sh_go(bool backward, int blocks, int nt, size_t smem, int P, int C, const float *shs, const ShDirs &in,
            const float *dval, float *out, float *ddirs, cudaStream_t stream) {
     const int limit = wait_limit_polls();
 #define MSPLAT_SH_GO(CAM)                                                                                           \
     if (!backward) {                                                                                                \
-        cudaFuncSetAttribute(sh_fwd_kernel<DEG, CAM, BULK>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); \
-        launch(sh_fwd_kernel<DEG, CAM, BULK>, blocks, nt, smem, stream, P, C, shs, in, out, limit);                 \
+        cudaFuncSetAttribute(sh_fwd_kernel<DEG, CAM, BULK, FC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); \
+        launch(sh_fwd_kernel<DEG, CAM, BULK, FC>, blocks, nt, smem, stream, P, C, shs, in, out, limit);                 \
     } else {                                                                                                        \
-        cudaFuncSetAttribute(sh_bwd_kernel<DEG, CAM, BULK>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); \
-        launch(sh_bwd_kernel<DEG, CAM, BULK>, blocks, nt, smem, stream, P, C, shs, in, dval, out, ddirs, limit);    \
+        cudaFuncSetAttribute(sh_bwd_kernel<DEG, CAM, BULK, FC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); \
+        launch(sh_bwd_kernel<DEG, CAM, BULK, FC>, blocks, nt, smem, stream, P, C, shs, in, dval, out, ddirs, limit);    \
     }
     if (in.xyz) {
         MSPLAT_SH_GO(true)
@@ -292,6 +304,22 @@ void sh_go(bool backward, int blocks, int nt, size_t smem, int P, int C, const f
         MSPLAT_SH_GO(false)
     }
 #undef MSPLAT_SH_GO
+}
+
+// Three channels (colour) at degree >= 4 take kernels with the count fixed
+// at compile time: the bulk ones at even degrees (C * D odd), the
+// thread-loop ones at odd degrees.
+template <int DEG, bool BULK>
+void sh_go_c(bool backward, int blocks, int nt, size_t smem, int P, int C, const float *shs, const ShDirs &in,
+             const float *dval, float *out, float *ddirs, cudaStream_t stream) {
+    constexpr bool odd_d = (((DEG + 1) * (DEG + 1)) & 1) != 0;
+    if constexpr (DEG >= 4 && MSPLAT_SH_FIXED_C3 && BULK == odd_d) {
+        if (C == 3) {
+            sh_go<DEG, BULK, 3>(backward, blocks, nt, smem, P, C, shs, in, dval, out, ddirs, stream);
+            return;
+        }
+    }
+    sh_go<DEG, BULK, 0>(backward, blocks, nt, smem, P, C, shs, in, dval, out, ddirs, stream);
 }
 
 template <int DEG>
@@ -302,10 +330,10 @@ int sh_launch(bool backward, int P, int C, const float *shs, const ShDirs &in, c
     if constexpr ((D & 1) != 0 && MSPLAT_SH_BULK) {
         const bool aligned = ((uintptr_t)shs & 15) == 0 && (!backward || ((uintptr_t)out & 15) == 0);
         if ((C & 1) && aligned) {
-            const int nt = sh_bulk_block_points(CD);
+            const int nt = sh_bulk_block_points(CD, backward ? MSPLAT_SH_BULK_KB_BWD : MSPLAT_SH_BULK_KB_FWD);
             const size_t smem = (size_t)((nt * CD + 1) & ~1) * sizeof(float) + sizeof(uint64_t);
             if (smem <= 200 * 1024) {
-                sh_go<DEG, true>(backward, ceil_div(P, nt), nt, smem, P, C, shs, in, dval, out, ddirs, stream);
+                sh_go_c<DEG, true>(backward, ceil_div(P, nt), nt, smem, P, C, shs, in, dval, out, ddirs, stream);
                 return check_launch(backward ? "compute_sh_backward" : "compute_sh_forward");
             }
         }
@@ -314,7 +342,7 @@ int sh_launch(bool backward, int P, int C, const float *shs, const ShDirs &in, c
     const size_t smem = (size_t)nt * (CD | 1) * sizeof(float);
     if (smem > 200 * 1024)
         return set_error(MSPLAT_ERR_UNSUPPORTED, "compute_sh: C*D = %d too large", CD);
-    sh_go<DEG, false>(backward, ceil_div(P, nt), nt, smem, P, C, shs, in, dval, out, ddirs, stream);
+    sh_go_c<DEG, false>(backward, ceil_div(P, nt), nt, smem, P, C, shs, in, dval, out, ddirs, stream);
     return check_launch(backward ? "compute_sh_backward" : "compute_sh_forward");
 }
 

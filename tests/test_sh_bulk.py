@@ -1,8 +1,13 @@
 """The SH kernels' two ways of staging coefficient rows: one bulk copy per
 block (rows of an odd number of floats, 16-byte aligned arrays) and the
 padded thread loop (everything else).  Both run the same arithmetic on the
-same rows, so their results must agree bit for bit; a coefficient array
-that starts 4 bytes past a 16-byte boundary takes the thread loop.  The
+same rows, so their results must agree bit for bit where both use the
+same kernel code; a coefficient array that starts 4 bytes past a 16-byte
+boundary takes the thread loop.  Three channels at degree >= 4 on the bulk
+path run kernels with the channel count fixed at compile time, whose
+multiply-adds the compiler may contract differently from the general
+kernels' (the misaligned thread loop at even degree): those two agree to
+1e-6 of the largest value.  The
 point counts leave every remainder of the last block's row count modulo 4
 (the floats the bulk copy cannot move), and the oracle checks the values.
 The bounded wait for a bulk copy is made to run out (a poll limit of 0) and
@@ -62,8 +67,12 @@ def test_bulk_equals_thread_loop(lib, deg, C, P):
     shs, d, vis, w = sh_case(P, C, deg, seed=P * 31 + deg * 7 + C)
     a = run_sh(torch.from_numpy(shs).to(DEV), d, vis, w)
     b = run_sh(misaligned(shs), d, vis, w)
+    same_code = not (C == 3 and deg >= 4)
     for x, y in zip(a, b):
-        assert torch.equal(x, y)
+        if same_code:
+            assert torch.equal(x, y)
+        else:
+            assert (x - y).abs().max().item() <= 1e-6 * max(y.abs().max().item(), 1e-30)
     oval = oracle.compute_sh_forward(shs, d, vis)
     scale = max(np.abs(oval).max(), 1e-30)
     assert np.abs(a[0].cpu().numpy() - oval).max() <= 1e-5 * scale
@@ -92,8 +101,8 @@ def test_bulk_camera_mode(lib):
         g = torch.from_numpy(np.random.default_rng(9).normal(size=(P, 3)).astype(np.float32)).to(DEV)
         (color * g).sum().backward()
         outs.append((color.detach(), sh_t.grad, xyz.grad))
-    for x, y in zip(*outs):
-        assert torch.equal(x, y)
+    for x, y in zip(*outs):  # fixed-C kernels (bulk) against the general ones (thread loop)
+        assert (x - y).abs().max().item() <= 1e-6 * max(y.abs().max().item(), 1e-30)
 
 
 def test_bulk_wait_that_runs_out_reports_timeout(lib):
@@ -114,5 +123,5 @@ def test_bulk_wait_that_runs_out_reports_timeout(lib):
     a = run_sh(torch.from_numpy(shs).to(DEV), d, vis, w)
     b = run_sh(misaligned(shs), d, vis, w)
     for x, y in zip(a, b):
-        assert torch.equal(x, y)
+        assert (x - y).abs().max().item() <= 1e-6 * max(y.abs().max().item(), 1e-30)
     assert lib.msplat_wait_error(0, ctypes.byref(err), _lib.stream()) == 0
