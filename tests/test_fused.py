@@ -87,11 +87,25 @@ def test_rasterization_fused_matches_composite(bg):
         rel_close(p[k].grad, q[k].grad, 1e-5, f"dL/d{k}")
 
 
-@pytest.mark.parametrize("deg", [0, 3, 6])
-def test_rasterization_sh_matches_compute_sh_on_view_directions(deg):
+def misaligned_copy(t):
+    """A leaf copy of `t` whose data starts 4 bytes past a 16-byte boundary."""
+    flat = torch.empty(t.numel() + 4, dtype=t.dtype, device=t.device)
+    m = flat[1:1 + t.numel()].view(t.shape)
+    m.copy_(t.detach())
+    assert m.data_ptr() % 16 == 4
+    return m.requires_grad_()
+
+
+# degrees 1 and 3 with 3 channels take the register-row kernels
+# (preprocess_sh3_*), 0 and 2 the staged ones, 6 the two-kernel path; a
+# misaligned coefficient array takes the staged kernels at degree 3
+@pytest.mark.parametrize("deg,misaligned", [(0, False), (1, False), (2, False), (3, False), (3, True), (6, False)])
+def test_rasterization_sh_matches_compute_sh_on_view_directions(deg, misaligned):
     import msplat_gb300 as ms
     W, H = 320, 240
     p = make(20000, W, H, 7 + deg, sh_deg=deg)
+    if misaligned:
+        p["shs"] = misaligned_copy(p["shs"])
     q = {k: v.detach().clone().requires_grad_() for k, v in p.items()}
     img = ms.rasterization_sh(p["xyz"], p["scale"], p["rot"], p["opacity"], p["shs"], p["intr"], p["extr"], W, H,
                               0.1)
