@@ -27,7 +27,8 @@
 // (cp.async.bulk, completing on an mbarrier) and the backward's gradient
 // rows leave as one: the whole chunk (24-36 KB) is in flight at once.
 // Otherwise the rows are padded to an odd stride and moved by a coalesced
-// thread loop.
+// thread loop; rows longer than 32 of them fit in about 200 KB go to the
+// channel-sliced kernels of compute_sh_sliced.cu.
 #include <algorithm>
 
 #include "sh_basis.cuh"
@@ -127,27 +128,6 @@ __device__ __forceinline__ void unstage_rows_bulk(float *__restrict__ dst, const
         asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");  // shared memory stays until it is read
     }
     for (int e = nv + threadIdx.x; e < total; e += blockDim.x) __stcs(dst + e, src[e]);
-}
-
-// Direction of point p and whether it is visible; n = |x - c| in camera mode.
-template <bool CAM>
-__device__ __forceinline__ bool sh_direction(const ShDirs &in, int p, const float (&cc)[3], float (&d)[3],
-                                             float &n) {
-    if (CAM) {
-        if (in.depth[p] == 0.0f) return false;
-        const float dx = in.xyz[3 * p] - cc[0], dy = in.xyz[3 * p + 1] - cc[1], dz = in.xyz[3 * p + 2] - cc[2];
-        n = sqrtf(dx * dx + dy * dy + dz * dz);
-        d[0] = dx / n;
-        d[1] = dy / n;
-        d[2] = dz / n;
-        return true;
-    }
-    if (in.visible && !in.visible[p]) return false;
-    d[0] = in.dirs[3 * p];
-    d[1] = in.dirs[3 * p + 1];
-    d[2] = in.dirs[3 * p + 2];
-    n = 1.0f;
-    return true;
 }
 
 // FC > 0: the channel count, fixed at compile time (C is then FC).
@@ -340,8 +320,13 @@ int sh_launch(bool backward, int P, int C, const float *shs, const ShDirs &in, c
     }
     const int nt = sh_block_points(CD);
     const size_t smem = (size_t)nt * (CD | 1) * sizeof(float);
-    if (smem > 200 * 1024)
-        return set_error(MSPLAT_ERR_UNSUPPORTED, "compute_sh: C*D = %d too large", CD);
+    if (smem > 200 * 1024) {  // rows longer than a block holds: slices of CC channels
+        const size_t per_ch = (size_t)kShSlicedPoints * D * sizeof(float);
+        const int CC = std::max<int>(kShChanBlock, (int)((96 * 1024) / per_ch) & ~(kShChanBlock - 1));
+        const size_t sm = (size_t)kShSlicedPoints * ((CC * D) | 1) * sizeof(float);
+        sh_go_sliced<DEG>(backward, CC, sm, P, C, shs, in, dval, out, ddirs, stream);
+        return check_launch(backward ? "compute_sh_backward" : "compute_sh_forward");
+    }
     sh_go_c<DEG, false>(backward, ceil_div(P, nt), nt, smem, P, C, shs, in, dval, out, ddirs, stream);
     return check_launch(backward ? "compute_sh_backward" : "compute_sh_forward");
 }

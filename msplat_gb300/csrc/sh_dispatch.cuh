@@ -3,6 +3,7 @@
 #pragma once
 
 #include "camgrad.cuh"
+#include "sh_basis.cuh"
 
 namespace msplat {
 
@@ -27,5 +28,34 @@ struct ShDirs {
 // dL/ddirs; in camera mode dL/dxyz goes to in.dxyz.
 int sh_dispatch(bool backward, int P, int C, int D, const float *shs, const ShDirs &in, const float *dval,
                 float *out, float *ddirs, cudaStream_t stream);
+
+// Direction of point p and whether it is visible; n = |x - c| in camera mode.
+template <bool CAM>
+__device__ __forceinline__ bool sh_direction(const ShDirs &in, int p, const float (&cc)[3], float (&d)[3],
+                                             float &n) {
+    if (CAM) {
+        if (in.depth[p] == 0.0f) return false;
+        const float dx = in.xyz[3 * p] - cc[0], dy = in.xyz[3 * p + 1] - cc[1], dz = in.xyz[3 * p + 2] - cc[2];
+        n = sqrtf(dx * dx + dy * dy + dz * dz);
+        d[0] = dx / n;
+        d[1] = dy / n;
+        d[2] = dz / n;
+        return true;
+    }
+    if (in.visible && !in.visible[p]) return false;
+    d[0] = in.dirs[3 * p];
+    d[1] = in.dirs[3 * p + 1];
+    d[2] = in.dirs[3 * p + 2];
+    n = 1.0f;
+    return true;
+}
+
+// The SH kernels for rows longer than a block's shared memory holds
+// (compute_sh_sliced.cu): blocks of kShSlicedPoints Gaussians, their rows
+// staged CC channels at a time into `smem` bytes.
+constexpr int kShSlicedPoints = 32;
+template <int DEG>
+void sh_go_sliced(bool backward, int CC, size_t smem, int P, int C, const float *shs, const ShDirs &in,
+                  const float *dval, float *out, float *ddirs, cudaStream_t stream);
 
 }  // namespace msplat

@@ -125,3 +125,48 @@ def test_bulk_wait_that_runs_out_reports_timeout(lib):
     for x, y in zip(a, b):
         assert (x - y).abs().max().item() <= 1e-6 * max(y.abs().max().item(), 1e-30)
     assert lib.msplat_wait_error(0, ctypes.byref(err), _lib.stream()) == 0
+
+
+# Rows longer than a block's shared memory holds: even C * D beyond 1,600
+# floats take the channel-sliced kernels (16 channels at degree 10, 20 at
+# degree 9, 120 at degree 3), odd ones the bulk path with blocks of 4
+# Gaussians (17 channels at degree 10).  The reference evaluates any
+# channel count (one thread per Gaussian looping over the channels).
+@pytest.mark.parametrize("deg,C", [(10, 16), (9, 20), (3, 120), (10, 17)])
+def test_many_channels_against_the_oracle(lib, deg, C):
+    P = 301
+    shs, d, vis, w = sh_case(P, C, deg, seed=deg * 100 + C)
+    val, dsh, ddir = run_sh(torch.from_numpy(shs).to(DEV), d, vis, w)
+    oval = oracle.compute_sh_forward(shs, d, vis)
+    assert np.abs(val.cpu().numpy() - oval).max() <= 1e-5 * max(np.abs(oval).max(), 1e-30)
+    odsh, oddir = oracle.compute_sh_backward(shs, d, vis, w)
+    assert np.abs(dsh.cpu().numpy() - odsh).max() <= 1e-5 * max(np.abs(odsh).max(), 1e-30)
+    assert np.abs(ddir.cpu().numpy() - oddir).max() <= 1e-4 * max(np.abs(oddir).max(), 1e-30)
+
+
+def test_many_channels_camera_mode(lib):
+    """The fused preprocess's view-direction SH with 16 channels at degree
+    10 (sliced kernels in camera mode) against compute_sh on the same
+    directions computed in PyTorch, forward and backward."""
+    import msplat_gb300 as ms
+    from _scenes import scene, sphere_camera
+    P, W, H, C = 2003, 320, 240, 16
+    s = scene(P, 21, C=3)
+    shs = torch.from_numpy(np.random.default_rng(8).normal(scale=0.1, size=(P, C, 121)).astype(np.float32)).to(DEV)
+    intr = torch.tensor([300.0, 300.0, W / 2, H / 2], device=DEV)
+    extr = torch.tensor(sphere_camera(np.random.default_rng(6)), device=DEV)
+    xyz = s["xyz"].to(DEV).contiguous()
+    g = torch.from_numpy(np.random.default_rng(10).normal(size=(P, C)).astype(np.float32)).to(DEV)
+    a = shs.clone().requires_grad_()
+    _, depth, _, _, _, color = ms.preprocess(xyz, s["scale"].to(DEV).contiguous(), s["rot"].to(DEV).contiguous(),
+                                             intr, extr, W, H, shs=a)
+    (color * g).sum().backward()
+    R, t = extr[:, :3], extr[:, 3]
+    v = xyz + R.transpose(0, 1) @ t
+    dirs = v / v.norm(dim=-1, keepdim=True)
+    b = shs.clone().requires_grad_()
+    ref = ms.compute_sh(b, dirs, (depth != 0).view(-1))
+    (ref * g).sum().backward()
+    scale = ref.abs().max().item()
+    assert (color.detach() - ref.detach()).abs().max().item() <= 1e-5 * scale
+    assert (a.grad - b.grad).abs().max().item() <= 1e-5 * b.grad.abs().max().item()
