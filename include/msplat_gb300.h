@@ -406,7 +406,9 @@ MSPLAT_API int msplat_rasterize_preprocess_backward(int P, const float *xyz, con
  * camera-major: uv [B,P,2], depth [B,P,1], conic [B,P,3], radius [B,P],
  * tiles [B,P], color [B,P,C] (when shs [P,C,D] is given; C = 0 otherwise);
  * each camera's slice equals msplat_rasterize_preprocess_forward for that
- * camera bit for bit.  Each Gaussian and its SH rows are read once. */
+ * camera bit for bit.  Each Gaussian and its SH rows are read once.
+ * Rows of at most 1,599 floats (C * D; the adjoint: 795), else
+ * MSPLAT_ERR_UNSUPPORTED. */
 MSPLAT_API int msplat_batch_preprocess_forward(int P, int B, const float *xyz, const float *scales,
                                   const float *uquats, const float *cams, const int32_t *dims,
                                   float nearest, float extent, int C, int D, const float *shs,

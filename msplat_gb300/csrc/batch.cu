@@ -294,6 +294,11 @@ batch_preprocess_bwd_kernel(int P, int B, int C, const float *__restrict__ xyz, 
 
 // Gaussians per block: the forward stages one row per Gaussian, the
 // backward two; both stay under ~96 KB of shared memory.
+// The longest coefficient rows (C * D floats) the batched backward stages:
+// 32 Gaussians' rows and gradient rows and the camera-gradient slots in
+// 200 KB of shared memory (the forward, rows alone, takes up to 1,599).
+constexpr int kBatchMaxCD = 795;
+
 inline int batch_block_points(int CD, bool backward) {
     const size_t row = (size_t)(CD | 1) * sizeof(float) * (backward ? 2 : 1);
     int nt = 256;
@@ -321,6 +326,8 @@ int batch_fwd_launch(int P, int B, int C, const float *xyz, const float *scales,
     const int CD = C * (DEG + 1) * (DEG + 1);
     const int nt = batch_block_points(CD, false);
     const size_t smem = C > 0 ? (size_t)nt * (CD | 1) * sizeof(float) : 0;
+    if (smem > 200 * 1024)
+        return set_error(MSPLAT_ERR_UNSUPPORTED, "batch_preprocess_forward: C*D = %d too large (at most 1599)", CD);
     cudaFuncSetAttribute(batch_preprocess_fwd_kernel<DEG>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     launch(batch_preprocess_fwd_kernel<DEG>, ceil_div(P, nt), nt, smem, stream, P, B, C, xyz, scales,
            (const float4 *)uquats, shs, cams, dims, nearest, extent, (float2 *)uv, depth, conic, radius, tiles, color);
@@ -339,6 +346,9 @@ int batch_bwd_launch(int P, int B, int C, const float *xyz, const float *scales,
     const bool cam = dL_dcams != nullptr;
     const size_t smem = (C > 0 ? (size_t)2 * nt * (CD | 1) * sizeof(float) : 0) +
                         (cam ? (size_t)kCamChunk * (nt / 32) * kCamGradVals * sizeof(float) : 0);
+    if (smem > 200 * 1024)
+        return set_error(MSPLAT_ERR_UNSUPPORTED, "batch_preprocess_backward: C*D = %d too large (at most %d)", CD,
+                         kBatchMaxCD);
     cudaFuncSetAttribute(batch_preprocess_bwd_kernel<DEG>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     launch(batch_preprocess_bwd_kernel<DEG>, blocks, nt, smem, stream, P, B, C, xyz, scales, (const float4 *)uquats,
            shs, cams, depth, radius, (const float2 *)dL_duv, dL_dconic, dL_dcolor, dL_dop_cam, dL_dxyz, dL_dscales,

@@ -158,3 +158,16 @@ def test_batch_capacity_too_small_reports_status():
     torch.cuda.synchronize()
     assert int(status.item()) == 0
     assert torch.equal(imgs[1], ref)
+
+
+def test_batch_rows_too_long_are_refused():
+    """The batched preprocess stages each Gaussian's coefficient row in
+    shared memory: rows longer than it takes (C * D beyond 1,599 floats
+    forward) are refused with MSPLAT_ERR_UNSUPPORTED, not launched."""
+    import msplat_gb300 as ms
+    s = scene(500, 6, C=3)
+    intrs, extrs = cameras([(64, 64)], 2)
+    shs = torch.zeros(500, 16, 121, device=DEV)
+    with pytest.raises(RuntimeError, match="too large"):
+        ms.rasterization_sh_batch(s["xyz"].to(DEV), s["scale"].to(DEV), s["rot"].to(DEV), s["opacity"].to(DEV), shs,
+                                  intrs.to(DEV), extrs.to(DEV), [(64, 64)])
