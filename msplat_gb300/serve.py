@@ -154,7 +154,7 @@ class Server:
                 raise RuntimeError(f"a request needs {need[id(r)]} bytes, more than the budget {self.budget}")
         jobs: queue.Queue = queue.Queue()
         errors: list = []
-        state = {"idle": self.n_workers}
+        state = {"idle": self.n_workers, "finished": 0}  # (finished: requests done, kept by the workers)
         base_alloc, base_res = self._device_memory()
         self.peak_allocated = self.peak_reserved = 0
         t0 = time.perf_counter()
@@ -179,12 +179,15 @@ class Server:
                         r.done = now
                         if on_done is not None:
                             on_done(r)
+                    done = len(job)
                 except Exception as e:  # re-raised by serve()
                     errors.append(e)
+                    done = 0
                 finally:
                     with self._cv:
                         self._free += sum(need[id(r)] for r in job)
                         state["idle"] += 1
+                        state["finished"] += done
                         self._cv.notify_all()
 
         threads = [threading.Thread(target=worker, daemon=True) for _ in range(self.n_workers)]
@@ -219,7 +222,7 @@ class Server:
                     if time.perf_counter() - t0 > timeout:
                         errors.append(RuntimeError(f"serving did not finish within {timeout} s"))
                         break
-                    finished = sum(1 for r in order if r.done is not None)
+                    finished = state["finished"]
                     if not dispatched and finished < len(order):
                         wait = 0.002 if nxt >= len(order) else min(0.002, max(0.0, order[nxt].arrival - now))
                         self._cv.wait(timeout=wait)
