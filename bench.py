@@ -934,7 +934,8 @@ def run_serve(args):
     from msplat_gb300.serve import Server, serve_one_by_one
     scenes, reqs = serve_workload(args.rate, args.duration)
     budget = 120 << 30
-    srv = Server(scenes, hbm_budget=budget, streams=args.streams, max_batch=16, max_backward=8)
+    srv = Server(scenes, hbm_budget=budget, streams=args.streams, max_batch=args.max_batch,
+                 max_backward=args.max_backward)
 
     def drop(r):
         r.image = None
@@ -974,8 +975,8 @@ def run_serve(args):
         "vs_baseline": None, "dtype": "f32", "data": DATA_DESC + "; Poisson arrivals)",
         "config": {"workload": f"{len(scenes)} resident scenes (N = {sizes}), SH deg 3, Poisson {args.rate} req/s "
                                f"for {args.duration} s, sizes {SERVE_SIZES}, 80% fwd / 20% fwd+bwd, "
-                               f"120 GB budget, {args.streams} streams, forward jobs up to 16 cameras of any "
-                               f"scenes, backward jobs up to 8 requests",
+                               f"120 GB budget, {args.streams} streams, forward jobs up to {args.max_batch} cameras "
+                               f"of any scenes, backward jobs up to {args.max_backward} requests",
                    "requests": len(reqs), "backward_requests": sum(r.backward for r in reqs)},
         "served": served, "one_by_one": single,
         "throughput_ratio": round(served["renders_per_s"] / single["renders_per_s"], 3),
@@ -1017,7 +1018,7 @@ def sub_results(args, device):
         torch.cuda.empty_cache()
     try:
         sv = _ap.Namespace(**vars(args))
-        sv.rate, sv.duration, sv.streams = 2000.0, 10.0, 4
+        sv.rate, sv.duration, sv.streams, sv.max_batch, sv.max_backward = 2000.0, 10.0, 4, 16, 8
         r = run_serve(sv)
         out["serve"] = {k: r[k] for k in ("metric", "value", "unit", "served", "one_by_one", "throughput_ratio",
                                           "saturation", "memory", "config")}
@@ -1054,6 +1055,8 @@ def main():
     ap.add_argument("--rate", type=float, default=2000.0, help="serve: Poisson arrival rate (requests/s)")
     ap.add_argument("--duration", type=float, default=10.0, help="serve: seconds of arrivals")
     ap.add_argument("--streams", type=int, default=4, help="serve: worker streams")
+    ap.add_argument("--max-batch", type=int, default=16, help="serve: forward requests per job at most")
+    ap.add_argument("--max-backward", type=int, default=8, help="serve: forward + backward requests per job at most")
     args = ap.parse_args()
     set_workload(args.gaussians, args.width, args.height)
     world = int(os.environ.get("WORLD_SIZE", "1"))
